@@ -1,0 +1,83 @@
+/*
+ * isoext_gb300.h -- C ABI of libisoext_gb300.so (GB300 / sm_103a iso-surface
+ * extraction).
+ *
+ * The library replaces the compute behind isoext's Python extension module
+ * (src/isoext_ext.cu in the isoext project, NB_MODULE(isoext_ext) at :93-384).
+ * Each entry point below names the binding function it stands in for.
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers (cudaMalloc / torch CUDA memory),
+ *     C-contiguous, except aabb_min / aabb_max which are HOST float[3].
+ *   - Every call is asynchronous on `stream` (a cudaStream_t passed as void*;
+ *     NULL = legacy default stream).  Sizes are known once the stream has
+ *     reached the end of the call: read `counts` then.
+ *   - Return value: 0 on success, otherwise an IsoStatus code for argument or
+ *     launch errors; iso_last_error() gives the message (thread-local).
+ *   - Errors found on the device are written to `*status` (device int, which
+ *     the caller zeroes before the call): 3 = a bounded device wait ran out,
+ *     4 = internal vertex lookup failure, 6 = output capacity exceeded (counts
+ *     still hold the exact sizes, so the caller can retry with bigger buffers).
+ *   - Grid values are float32 [nx, ny, nz] (z fastest); `nx, ny, nz` are POINTS
+ *     per axis, as isoext's UniformGrid shape.  The value buffer must be 16-byte
+ *     aligned and readable up to the next 16-byte boundary (true for any
+ *     cudaMalloc / torch allocation).
+ */
+#ifndef ISOEXT_GB300_H
+#define ISOEXT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define ISO_OK 0
+#define ISO_ERR_ARG 1
+#define ISO_ERR_CUDA 2
+#define ISO_ERR_TIMEOUT 3
+#define ISO_ERR_LOOKUP 4
+#define ISO_ERR_WORKSPACE 5
+#define ISO_ERR_OVERFLOW 6
+
+/* Message of the last failed call on this thread. */
+const char *iso_last_error(void);
+
+/* ABI version of this library (1). */
+int iso_abi_version(void);
+
+/* Tiling used by iso_mc_dense: point rows per tile, shared-memory slab ring
+ * depth and threads per CTA.  Process-wide; the autotuner sets it.  No
+ * counterpart in the reference (it has no tunables). */
+int iso_mc_set_config(int rows, int slabs, int threads);
+int iso_mc_get_config(int *rows, int *slabs, int *threads);
+
+/* Upper bound on the z extent of a tile (multiple of 32; 0 = as large as shared
+ * memory allows).  Grids whose rows do not fit in shared memory are split along
+ * z automatically; this forces it for testing.  No counterpart in the reference. */
+int iso_mc_set_zchunk(int zchunk);
+
+/* Workspace bytes iso_mc_dense needs for a grid and output capacities. */
+size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
+                                   long long face_capacity);
+
+/* Marching cubes on a dense grid.
+ * Replaces isoext_ext.marching_cubes(grid: UniformGrid, level, method)
+ * (src/isoext_ext.cu:95-109 -> mc::marching_cubes, src/mc/mc.cu:17-68).
+ *   method: 0 = "nagae" (default in isoext), 1 = "lorensen".
+ *   vertices: float32 [vertex_capacity, 3]; faces: int32 [face_capacity, 3].
+ *   counts: device int64[2] <- (V, F).  Faces come in the reference's order
+ *   (ascending cell id, table slot order); vertices in ascending edge-key order.
+ *   Unknown method -> ISO_ERR_ARG (isoext raises "Unknown method: ...").
+ *   More than 2^31-1 points -> ISO_ERR_ARG (isoext: src/grid/uniform.cu:13-16). */
+int iso_mc_dense(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                 const float *aabb_max, float level, int method, float *vertices,
+                 long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
+                 size_t workspace_bytes, long long *counts, int *status, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ISOEXT_GB300_H */

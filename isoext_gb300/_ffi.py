@@ -1,0 +1,82 @@
+"""ctypes binding of libisoext_gb300.so (the C ABI in include/isoext_gb300.h).
+
+The library is the product's only compute path: if it cannot be loaded the
+import of the extraction functions fails loudly -- there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import _build
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+ISO_OK = 0
+ISO_ERR_ARG = 1
+ISO_ERR_CUDA = 2
+ISO_ERR_TIMEOUT = 3
+ISO_ERR_LOOKUP = 4
+ISO_ERR_WORKSPACE = 5
+ISO_ERR_OVERFLOW = 6
+
+_vp = C.c_void_p
+_i = C.c_int
+_ll = C.c_longlong
+_f = C.c_float
+_fa = C.POINTER(C.c_float)
+
+
+def _declare(lib: C.CDLL) -> None:
+    lib.iso_last_error.restype = C.c_char_p
+    lib.iso_abi_version.restype = _i
+    lib.iso_mc_set_config.argtypes = [_i, _i, _i]
+    lib.iso_mc_get_config.argtypes = [C.POINTER(_i)] * 3
+    lib.iso_mc_set_zchunk.argtypes = [_i]
+    lib.iso_mc_dense_workspace_size.argtypes = [_i, _i, _i, _ll, _ll]
+    lib.iso_mc_dense_workspace_size.restype = C.c_size_t
+    lib.iso_mc_dense.argtypes = [_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp,
+                                 C.c_size_t, _vp, _vp, _vp]
+    for name, args in _EXTRA.items():
+        fn = getattr(lib, name, None)
+        if fn is not None:
+            fn.argtypes = args[0]
+            if args[1] is not None:
+                fn.restype = args[1]
+
+
+# Declarations of further entry points (added by the modules that use them).
+_EXTRA: dict[str, tuple[list, object]] = {}
+
+
+def lib() -> C.CDLL:
+    """Load (building first if the sources are newer) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            handle = C.CDLL(str(path))
+            _declare(handle)
+            _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    return lib().iso_last_error().decode(errors="replace")
+
+
+def check(rc: int) -> None:
+    if rc == ISO_OK:
+        return
+    msg = last_error()
+    if rc == ISO_ERR_ARG:
+        raise RuntimeError(msg)
+    raise RuntimeError(f"isoext_gb300 error {rc}: {msg}")
+
+
+def fvec3(xs) -> C.Array:
+    return (C.c_float * 3)(*[float(x) for x in xs])

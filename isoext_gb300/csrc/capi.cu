@@ -1,0 +1,130 @@
+// C ABI of libisoext_gb300.so (declared in include/isoext_gb300.h).
+//
+// Every entry point takes raw device pointers, sizes and a cudaStream_t, runs
+// asynchronously on that stream, and returns an IsoStatus for argument / launch
+// errors.  Errors found on the device (bounded waits that ran out, output
+// capacity exceeded) are written to the caller's device status word.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "mc_dense.cuh"
+
+namespace {
+thread_local std::string g_err;
+std::mutex g_cfg_mu;
+int g_rows = 8, g_slabs = 4, g_threads = 256, g_zchunk = 0;
+
+int fail(int code, const char* msg) {
+    g_err = msg;
+    return code;
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+    return n;
+}
+
+int plan(int nx, int ny, int nz, McTiles* t) {
+    int rows, slabs, threads, zchunk;
+    {
+        std::lock_guard<std::mutex> lk(g_cfg_mu);
+        rows = g_rows; slabs = g_slabs; threads = g_threads; zchunk = g_zchunk;
+    }
+    return mc_plan_tiles(nx, ny, nz, rows, slabs, threads, zchunk, sm_count(), t);
+}
+
+bool grid_ok(int nx, int ny, int nz) {
+    if (nx < 0 || ny < 0 || nz < 0) return false;
+    return (long long)nx * ny * nz <= 0x7fffffffll;
+}
+}  // namespace
+
+extern "C" {
+
+const char* iso_last_error(void) { return g_err.c_str(); }
+
+int iso_abi_version(void) { return 1; }
+
+int iso_mc_set_config(int rows, int slabs, int threads) {
+    if (rows < 1 || rows > 64 || slabs < 4 || slabs > 8 || (threads != 256 && threads != 512))
+        return fail(ISO_ERR_ARG, "iso_mc_set_config: rows in [1,64], slabs in [4,8], threads 256|512");
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    g_rows = rows; g_slabs = slabs; g_threads = threads;
+    return ISO_OK;
+}
+
+int iso_mc_set_zchunk(int zchunk) {
+    if (zchunk < 0) return fail(ISO_ERR_ARG, "iso_mc_set_zchunk: zchunk >= 0");
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    g_zchunk = zchunk;
+    return ISO_OK;
+}
+
+int iso_mc_get_config(int* rows, int* slabs, int* threads) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (rows) *rows = g_rows;
+    if (slabs) *slabs = g_slabs;
+    if (threads) *threads = g_threads;
+    return ISO_OK;
+}
+
+size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
+                                   long long face_capacity) {
+    if (!grid_ok(nx, ny, nz) || nx < 2 || ny < 2 || nz < 2) return 256;
+    McTiles t;
+    if (plan(nx, ny, nz, &t)) return 0;
+    return mc_workspace_bytes(t, vertex_capacity, face_capacity);
+}
+
+int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                 const float* aabb_max, float level, int method, float* vertices,
+                 long long vertex_capacity, int* faces, long long face_capacity, void* workspace,
+                 size_t workspace_bytes, long long* counts, int* status, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (!grid_ok(nx, ny, nz))
+        return fail(ISO_ERR_ARG, "Number of points exceeds maximum value 2147483647 (max int)");
+    if (method != 0 && method != 1) return fail(ISO_ERR_ARG, "method must be 0 (nagae) or 1 (lorensen)");
+    if (!counts || !status || !aabb_min || !aabb_max)
+        return fail(ISO_ERR_ARG, "counts, status and the bounding box are required");
+    if (vertex_capacity < 0 || face_capacity < 0) return fail(ISO_ERR_ARG, "negative capacity");
+    if (nx < 2 || ny < 2 || nz < 2) {
+        // no cells: empty mesh
+        if (cudaMemsetAsync(counts, 0, 2 * sizeof(long long), st) != cudaSuccess)
+            return fail(ISO_ERR_CUDA, "cudaMemsetAsync failed");
+        return ISO_OK;
+    }
+    if (!values) return fail(ISO_ERR_ARG, "values is null");
+    if (reinterpret_cast<uintptr_t>(values) & 15u)
+        return fail(ISO_ERR_ARG, "values must be 16-byte aligned");
+    if ((vertex_capacity && !vertices) || (face_capacity && !faces))
+        return fail(ISO_ERR_ARG, "output buffers are null");
+    McParams p{};
+    if (plan(nx, ny, nz, &p.t)) return fail(ISO_ERR_ARG, "grid too large for the tile planner");
+    p.vals = values;
+    for (int i = 0; i < 3; ++i) {
+        p.amin[i] = aabb_min[i];
+        p.asize[i] = aabb_max[i] - aabb_min[i];  // FP32, as aabb_max - aabb_min in the reference
+    }
+    p.level = level;
+    p.method = method;
+    p.status = status;
+    p.vout = vertices;
+    p.fout = faces;
+    p.capV = vertex_capacity;
+    p.capF = face_capacity;
+    p.counts = counts;
+    int rc = mc_launch(p, workspace, workspace_bytes, st);
+    if (rc == ISO_ERR_WORKSPACE) return fail(rc, "workspace too small");
+    if (rc) {
+        g_err = std::string("launch failed: ") + cudaGetErrorString(cudaGetLastError());
+        return rc;
+    }
+    return ISO_OK;
+}
+
+}  // extern "C"

@@ -152,11 +152,13 @@ def render() -> str:
         lines = []
         for i in range(0, len(vals), per_line):
             lines.append("    " + ", ".join(str(v) for v in vals[i:i + per_line]) + ",")
-        return f"static const {ctype} {name}[{len(vals)}] = {{\n" + "\n".join(lines) + "\n};\n"
+        return f"ISO_LUT_DECL {ctype} {name}[{len(vals)}] = {{\n" + "\n".join(lines) + "\n};\n"
 
     parts = [
         "/* Generated by gen_luts.py: do not edit. */\n",
         "#ifndef ISO_LUTS_H\n#define ISO_LUTS_H\n\n",
+        "/* Storage class of the tables; CUDA sources define it as static __constant__ const. */\n",
+        "#ifndef ISO_LUT_DECL\n#define ISO_LUT_DECL static const\n#endif\n\n",
         "/* Corner v = 4x + 2y + z.  Edge i joins ISO_EDGE_CORNERS[2i] < ISO_EDGE_CORNERS[2i+1]. */\n",
         arr("ISO_EDGE_CORNERS", "signed char", [c for p in EDGE_PAIRS for c in p], 8),
         "\n/* Bit e set when edge e carries a vertex for the case (same for both tables). */\n",

@@ -1,0 +1,65 @@
+"""Test helpers: reference-exact grid coordinates, synthetic fields, mesh comparison."""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def axis_coords(n: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+    """lo + (i / (float)(n - 1)) * (hi - lo), each step rounded in FP32."""
+    i = np.arange(n, dtype=np.float32)
+    size = np.float32(hi) - np.float32(lo)
+    return (np.float32(lo) + (i / np.float32(n - 1)) * size).astype(np.float32)
+
+
+def grid_points(shape, lo=(-1, -1, -1), hi=(1, 1, 1)) -> np.ndarray:
+    ax = [axis_coords(shape[k], lo[k], hi[k]) for k in range(3)]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    return np.stack([X, Y, Z], axis=-1)
+
+
+def sphere(shape, r, lo=(-1, -1, -1), hi=(1, 1, 1), center=(0, 0, 0)) -> np.ndarray:
+    p = grid_points(shape, lo, hi) - np.asarray(center, np.float32)
+    return (np.sqrt((p * p).sum(-1)) - np.float32(r)).astype(np.float32)
+
+
+def torus(shape, R, r) -> np.ndarray:
+    p = grid_points(shape)
+    q = np.sqrt(p[..., 0] ** 2 + p[..., 1] ** 2) - np.float32(R)
+    return (np.sqrt(q * q + p[..., 2] ** 2) - np.float32(r)).astype(np.float32)
+
+
+def noise(shape, seed: int, zero_frac: float = 0.0) -> np.ndarray:
+    """Uniform noise in [-1, 1] with a fraction of exact zeros (exercises vertices
+    that round onto grid points and degenerate triangles)."""
+    g = np.random.default_rng(seed)
+    v = g.uniform(-1, 1, size=shape).astype(np.float32)
+    if zero_frac:
+        v[g.random(shape) < zero_frac] = 0.0
+    return v
+
+
+def assert_same_mesh(v, f, vo, fo, what: str = "") -> None:
+    """Bit-exact equality up to vertex order: every vertex position must appear in
+    the other mesh with identical float bits, and the face index sequences must be
+    identical after relabelling (same faces, same order, same corner order)."""
+    v = np.asarray(v, np.float32).reshape(-1, 3)
+    vo = np.asarray(vo, np.float32).reshape(-1, 3)
+    f = np.asarray(f, np.int64).reshape(-1, 3)
+    fo = np.asarray(fo, np.int64).reshape(-1, 3)
+    assert v.shape == vo.shape, f"{what}: V {v.shape[0]} vs {vo.shape[0]}"
+    assert f.shape == fo.shape, f"{what}: F {f.shape[0]} vs {fo.shape[0]}"
+    if len(v) == 0:
+        return
+    vb = np.ascontiguousarray(v).view(np.dtype((np.void, 12))).ravel()
+    vob = np.ascontiguousarray(vo).view(np.dtype((np.void, 12))).ravel()
+    order = np.argsort(vob)
+    pos = np.searchsorted(vob[order], vb)
+    pos = np.clip(pos, 0, len(vo) - 1)
+    found = vob[order][pos] == vb
+    assert found.all(), f"{what}: {int((~found).sum())} vertices not in the other mesh"
+    perm = order[pos]
+    assert len(np.unique(perm)) == len(perm), f"{what}: vertex map is not a bijection"
+    mapped = perm[f]
+    bad = np.nonzero((mapped != fo).any(axis=1))[0]
+    assert len(bad) == 0, f"{what}: {len(bad)} faces differ, first at {bad[:5]}"

@@ -1,0 +1,49 @@
+"""The C-ABI library loads and exports every entry point its header declares
+(no compute calls: this runs without a GPU)."""
+
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(iso_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_header_symbols():
+    from isoext_gb300 import _build
+
+    lib = ctypes.CDLL(str(_build.build()))
+    names = _declared()
+    assert "iso_mc_dense" in names
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_library_reports_abi_and_config():
+    from isoext_gb300 import _ffi
+
+    lib = _ffi.lib()
+    assert lib.iso_abi_version() == 1
+    r, s, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.iso_mc_get_config(ctypes.byref(r), ctypes.byref(s), ctypes.byref(t))
+    assert r.value >= 1 and s.value >= 4 and t.value in (256, 512)
+    assert lib.iso_mc_set_config(0, 4, 256) == 1  # bad rows -> ISO_ERR_ARG
+    assert "rows" in _ffi.last_error()
+
+
+def test_unknown_method_message():
+    import isoext_gb300 as iso
+
+    import pytest
+
+    with pytest.raises(RuntimeError, match="Unknown method: foo"):
+        iso.mc.method_id("foo")

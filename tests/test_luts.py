@@ -1,0 +1,43 @@
+"""The committed lookup tables are the generator's output."""
+
+import os
+import re
+import sys
+
+import pytest
+
+CSRC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "isoext_gb300", "csrc")
+sys.path.insert(0, CSRC)
+import gen_luts  # noqa: E402
+
+
+def test_luts_header_is_current():
+    with open(os.path.join(CSRC, "luts.h")) as fh:
+        assert fh.read() == gen_luts.render()
+
+
+def test_luts_counts():
+    nag = gen_luts.expand(gen_luts.NAGAE, reflect=False)
+    lor = gen_luts.expand(gen_luts.LORENSEN, reflect=True)
+    assert max(len(t) for t in nag) == 5 and max(len(t) for t in lor) == 4
+    st = gen_luts.edge_status(nag)
+    assert st[0] == 0 and st[255] == 0 and all(st[i] for i in range(1, 255))
+
+
+def _ref_table(path, name):
+    s = open(path).read()
+    i = s.index(name)
+    body = re.sub(r"//.*", "", s[s.index("{", i) + 1: s.index("}", i)])
+    return [int(x, 0) for x in re.findall(r"-?0b[01]+|-?\d+", body)]
+
+
+def test_luts_equal_reference_tables():
+    ref = os.environ.get("ISOEXT_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "include")):
+        pytest.skip("isoext sources not present")
+    nag = gen_luts.flat(gen_luts.expand(gen_luts.NAGAE, False), 15)
+    lor = gen_luts.flat(gen_luts.expand(gen_luts.LORENSEN, True), 12)
+    assert nag == _ref_table(os.path.join(ref, "include/mc/nagae.cuh"), "tri_table[]")
+    assert lor == _ref_table(os.path.join(ref, "include/mc/lorensen.cuh"), "tri_table[]")
+    st = gen_luts.edge_status(gen_luts.expand(gen_luts.NAGAE, False))
+    assert st == _ref_table(os.path.join(ref, "src/shared_luts.cu"), "edge_status_table[edge_table_size]")

@@ -1,0 +1,156 @@
+"""Marching cubes on the GPU against the oracle and the reference's fixtures.
+
+Parity bar: bit-exact.  Every vertex position must equal a reference vertex to
+the last bit and the face sequence must be identical after relabelling vertex
+indices (faces in the same order with the same corner order).  Only the order of
+the vertex list differs (isoext sorts vertices by position; this path keeps
+them in edge-key order).
+"""
+
+import glob
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import isoext_gb300 as iso
+from helpers import assert_same_mesh, noise, sphere, torus
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+DENSE = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+               if not os.path.basename(p).startswith(("sparse", "cuboid")))
+
+
+def run_mc(values, level=0.0, method="nagae", lo=(-1, -1, -1), hi=(1, 1, 1)):
+    g = iso.UniformGrid(values.shape, lo, hi)
+    g.set_values(torch.from_numpy(np.ascontiguousarray(values)).cuda())
+    v, f = iso.marching_cubes(g, level=level, method=method)
+    if v is None:
+        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+    assert v.dtype == torch.float32 and f.dtype == torch.int32 and v.is_cuda and f.is_cuda
+    return v.cpu().numpy(), f.cpu().numpy()
+
+
+def check(oracle, values, level=0.0, method="nagae", lo=(-1, -1, -1), hi=(1, 1, 1), what=""):
+    v, f = run_mc(values, level, method, lo, hi)
+    vo, fo, _ = oracle.mc_dense(values, lo, hi, level, method)
+    assert_same_mesh(v, f, vo, fo, what)
+    return v, f
+
+
+@pytest.fixture(autouse=True)
+def _default_config():
+    lib = iso._ffi.lib()
+    lib.iso_mc_set_config(8, 4, 256)
+    lib.iso_mc_set_zchunk(0)
+    yield
+    lib.iso_mc_set_config(8, 4, 256)
+    lib.iso_mc_set_zchunk(0)
+
+
+@pytest.mark.parametrize("path", DENSE, ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("method", ["nagae", "lorensen"])
+def test_mc_matches_reference_fixture(path, method):
+    g = np.load(path)
+    v, f = run_mc(g["values"], float(g["level"]), method)
+    assert_same_mesh(v, f, g[f"mc_{method}_v"], g[f"mc_{method}_f"], os.path.basename(path))
+
+
+@pytest.mark.parametrize("n,r", [(32, 0.5), (64, 0.7), (128, 0.8), (97, 0.45)])
+@pytest.mark.parametrize("method", ["nagae", "lorensen"])
+def test_mc_sphere(oracle, n, r, method):
+    check(oracle, sphere((n, n, n), r), method=method, what=f"sphere{n}")
+
+
+def test_mc_config1_counts(oracle):
+    v, f = check(oracle, sphere((128,) * 3, 0.8), what="config1")
+    assert (len(v), len(f)) == (48576, 97148)
+
+
+@pytest.mark.parametrize("shape", [(16, 32, 48), (8, 64, 16), (33, 7, 130), (2, 2, 2), (3, 50, 5),
+                                   (40, 3, 2), (5, 5, 1000)])
+def test_mc_anisotropic(oracle, shape):
+    check(oracle, sphere(shape, 0.6), what=str(shape))
+    check(oracle, sphere(shape, 0.6, center=(0.1, -0.2, 0.05)), level=0.05, what=str(shape))
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("method", ["nagae", "lorensen"])
+def test_mc_noise_with_exact_zeros(oracle, seed, method):
+    # many vertices land exactly on grid points: exercises snapping,
+    # degenerate triangles and corner-keyed vertices
+    check(oracle, noise((23, 19, 37), seed=seed, zero_frac=0.3), method=method, what=f"noise{seed}")
+
+
+def test_mc_levels_and_box(oracle):
+    vals = torus((40, 40, 40), 0.5, 0.2)
+    for lvl in [-0.1, 0.0, 0.07]:
+        check(oracle, vals, level=lvl, what=f"torus level {lvl}")
+    check(oracle, vals, lo=(-0.5, -2.0, 0.0), hi=(1.5, 1.0, 0.25), what="torus box")
+
+
+def test_mc_flt_max_default(oracle):
+    # UniformGrid's default value is FLT_MAX; crossings towards it round onto
+    # the finite corner
+    vals = sphere((30, 30, 30), 0.5)
+    vals[:, :, 20:] = np.finfo(np.float32).max
+    check(oracle, vals, what="fltmax")
+    g = iso.UniformGrid([12, 12, 12])
+    v, f = iso.marching_cubes(g)
+    assert v is None and f is None
+
+
+def test_mc_empty_and_full():
+    assert run_mc(np.ones((10, 10, 10), np.float32))[0].shape == (0, 3)
+    assert run_mc(-np.ones((10, 10, 10), np.float32))[0].shape == (0, 3)
+    g = iso.UniformGrid([1, 5, 5])
+    assert iso.marching_cubes(g) == (None, None)
+
+
+@pytest.mark.parametrize("rows,slabs,threads", [(1, 4, 256), (2, 5, 256), (3, 4, 512), (8, 6, 512),
+                                                (16, 4, 256)])
+def test_mc_tilings(oracle, rows, slabs, threads):
+    lib = iso._ffi.lib()
+    assert lib.iso_mc_set_config(rows, slabs, threads) == 0
+    for shape in [(31, 45, 29), (64, 64, 64)]:
+        check(oracle, sphere(shape, 0.7), what=f"{shape} R{rows}")
+        check(oracle, noise(shape, seed=7, zero_frac=0.1), method="lorensen", what=f"noise {shape}")
+
+
+@pytest.mark.parametrize("zc", [32, 64, 96])
+def test_mc_z_chunks(oracle, zc):
+    lib = iso._ffi.lib()
+    assert lib.iso_mc_set_zchunk(zc) == 0
+    check(oracle, sphere((20, 24, 150), 0.8), what=f"zchunk {zc}")
+    check(oracle, noise((9, 10, 101), seed=3, zero_frac=0.2), what=f"zchunk noise {zc}")
+
+
+def test_mc_unknown_method():
+    g = iso.UniformGrid([8, 8, 8])
+    with pytest.raises(RuntimeError, match="Unknown method: foo"):
+        iso.marching_cubes(g, method="foo")
+
+
+def test_mc_512_properties(oracle):
+    # full benchmark size: counts equal the oracle's and the mesh is closed
+    vals = sphere((512,) * 3, 0.8)
+    v, f = run_mc(vals)
+    vo, fo, _ = oracle.mc_dense(vals)
+    assert_same_mesh(v, f, vo, fo, "512")
+    assert (len(v), len(f)) == (787464, 1574924)
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    _, cnt = np.unique(e[:, 0].astype(np.int64) * len(v) + e[:, 1], return_counts=True)
+    assert (cnt == 2).all()
+    assert len(v) - len(cnt) + len(f) == 2  # Euler characteristic of a sphere
+
+
+def test_mc_repeat_is_deterministic():
+    vals = torch.from_numpy(noise((40, 41, 42), seed=11, zero_frac=0.05)).cuda()
+    g = iso.UniformGrid(vals.shape)
+    g.set_values(vals)
+    a = iso.marching_cubes(g)
+    b = iso.marching_cubes(g)
+    assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
