@@ -1,0 +1,317 @@
+"""Benchmark: dense 512^3 FP32 marching cubes (sphere |p| - 0.8) in Gcells/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload mc512|mc128|dc256]
+
+One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
+  value  device-timed throughput with the grid resident in HBM (C ABI call with
+         device buffers; CUDA events on the launching stream).
+  e2e    the same through the public API with host buffers: pinned host values
+         -> device, UniformGrid.set_values, marching_cubes, result -> host.
+  roofline  of the dominant kernel (mc_extract): algorithmic bytes
+         4*N^3 + 12*V + 12*F per launch over its event-timed duration, against
+         the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's C restatement of the reference's algorithm on the
+         host cores (rank 0 only).
+--impl reference runs the reference's algorithm on the CPU (the oracle port:
+the isoext sources are not available on the GPU host) and prints the same line.
+Multi-GPU runs are independent replicas (the path has no exchange step).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+WORKLOADS = {
+    "mc512": dict(kind="mc", n=512, r=0.8, desc="mc_dense_512_sphere_r0.8"),
+    "mc128": dict(kind="mc", n=128, r=0.8, desc="mc_dense_128_sphere_r0.8"),
+    "dc256": dict(kind="dc", n=256, r=0.8, desc="dc_dense_256_sphere_r0.8"),
+}
+METRIC = "MC/DC Gcells/s @512^3 fp32"
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def sphere_values(n: int, r: float) -> np.ndarray:
+    from helpers import sphere
+
+    return sphere((n, n, n), r)
+
+
+# ---------------------------------------------------------------------------
+
+def run_ours(args, wl, rank, world) -> dict | None:
+    import torch
+
+    import isoext_gb300 as iso
+    from isoext_gb300 import _ffi
+    from isoext_gb300.mc import mc_dense_into, workspace_bytes
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = wl["n"]
+    vals_np = sphere_values(n, wl["r"])
+    vals = torch.from_numpy(vals_np).to(dev)
+    cells = (n - 1) ** 3
+    lib = _ffi.lib()
+    stream = torch.cuda.current_stream(dev)
+
+    if wl["kind"] == "mc":
+        # size outputs with one call, then time K back-to-back calls
+        grid = iso.UniformGrid([n] * 3, device=dev)
+        grid.set_values(vals)
+        v, f = iso.marching_cubes(grid)
+        nv, nf = len(v), len(f)
+        capv, capf = nv + 1024, nf + 1024
+        vout = torch.empty((capv, 3), dtype=torch.float32, device=dev)
+        fout = torch.empty((capf, 3), dtype=torch.int32, device=dev)
+        ws = torch.empty(workspace_bytes([n] * 3, capv, capf), dtype=torch.uint8, device=dev)
+        small = torch.zeros(4, dtype=torch.int64, device=dev)
+        amin, amax = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+
+        def step():
+            _ffi.check(mc_dense_into(vals, amin, amax, 0.0, 0, vout, fout, ws, small,
+                                     stream.cuda_stream))
+        algo_bytes = 4 * n ** 3 + 12 * nv + 12 * nf
+        kernels = ["mc_extract", "mc_tile_scan", "mc_resolve"]
+    else:
+        raise SystemExit(f"workload {args.workload} not available yet")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    lib.iso_profile_reset()
+    lib.iso_profile_enable(1)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    host = small.cpu()
+    assert int(host[2] & 0xffffffff) == 0, f"device status {int(host[2])}"
+    assert (int(host[0]), int(host[1])) == (nv, nf)
+    kt = {k: _ffi.profile_read(k) for k in kernels}
+    launches = sum(c for c, _ in kt.values())
+    ext_n, ext_ms = kt[kernels[0]]
+    ext_avg = ext_ms / max(ext_n, 1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # e2e through the public API with host buffers
+    pinned = torch.from_numpy(vals_np).pin_memory()
+    grid = iso.UniformGrid([n] * 3, device=dev)
+    e2e_times = []
+    h2d = pinned.numel() * 4
+    d2h = 0
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        grid.set_values(pinned.to(dev, non_blocking=True))
+        v, f = iso.marching_cubes(grid)
+        vh, fh = v.cpu(), f.cpu()
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append(t1 - t0)
+        d2h = vh.numel() * 4 + fh.numel() * 4 + 32
+    e2e_ms = 1e3 * statistics.mean(e2e_times)
+
+    if rank != 0:
+        return None
+    pk = peaks()
+    achieved = algo_bytes / (ext_avg * 1e-3) / 1e9
+    pipeline = algo_bytes / (ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": round(world * cells / (ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
+        "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae",
+                   "vertices": nv, "faces": nf, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (values 537 MB > 129 MB L2)"},
+        "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "mc_extract", "achieved": round(achieved, 1),
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                     "peak_source": pk["source"], "algorithmic_bytes": algo_bytes,
+                     "kernel_ms": round(ext_avg, 4), "traffic": None,
+                     "pipeline": {"achieved": round(pipeline, 1),
+                                  "frac": round(pipeline / pk["hbm_gbs"], 4)}},
+        "kernel_ms": {k: round(t / max(c, 1), 4) for k, (c, t) in kt.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(vals_np, cells, repeats=1)
+    return out
+
+
+def cpu_baseline(vals_np, cells, repeats=1) -> dict:
+    from oracle import Oracle
+
+    ora = Oracle()
+    t = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        ora.mc_dense(vals_np)
+        t.append(time.perf_counter() - t0)
+    sec = min(t)
+    return {"value": round(cells / sec / 1e9, 5), "unit": "Gcells/s", "cores": 1, "kind": "port",
+            "sample": f"one full extraction of the same grid ({cells} cells), oracle C port, "
+                      f"1 thread, {sec:.2f} s"}
+
+
+def run_reference(args, wl, rank) -> dict | None:
+    if rank != 0:
+        return None
+    from oracle import Oracle
+
+    n = wl["n"]
+    vals_np = sphere_values(n, wl["r"])
+    cells = (n - 1) ** 3
+    ora = Oracle()
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        if wl["kind"] == "mc":
+            ora.mc_dense(vals_np)
+        else:
+            ora.dc_dense(vals_np)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    sec = statistics.mean(times)
+    val = round(cells / sec / 1e9, 5)
+    return {
+        "metric": METRIC, "impl": "reference", "value": val, "unit": "Gcells/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
+        "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae"},
+        "cpu_baseline": {"value": val, "unit": "Gcells/s", "cores": 1, "kind": "port",
+                         "sample": "full extraction per step; the reference's algorithm restated in "
+                                   "C (oracle/iso_oracle.c); isoext's sources are not on the GPU host"},
+        "e2e": {"value": val, "unit": "Gcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        args.steps = min(args.steps, 3)
+        args.warmup = min(args.warmup, 1)
+    wl = WORKLOADS[args.workload]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        out = run_reference(args, wl, rank)
+    else:
+        out = run_ours(args, wl, rank, world)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -58,6 +58,15 @@ int iso_mc_get_config(int *rows, int *slabs, int *threads);
  * z automatically; this forces it for testing.  No counterpart in the reference. */
 int iso_mc_set_zchunk(int zchunk);
 
+/* Kernel timing for benchmarks (no counterpart in the reference).  While
+ * enabled, each kernel the library launches is bracketed by CUDA events on its
+ * stream.  iso_profile_read synchronises on the recorded events and returns the
+ * number of launches and their total device time in ms for one kernel name
+ * ("mc_extract", "mc_tile_scan", "mc_resolve", ...; NULL = all). */
+int iso_profile_enable(int on);
+void iso_profile_reset(void);
+int iso_profile_read(const char *kernel, long long *launches, double *total_ms);
+
 /* Workspace bytes iso_mc_dense needs for a grid and output capacities. */
 size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
                                    long long face_capacity);

@@ -35,6 +35,9 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_mc_set_config.argtypes = [_i, _i, _i]
     lib.iso_mc_get_config.argtypes = [C.POINTER(_i)] * 3
     lib.iso_mc_set_zchunk.argtypes = [_i]
+    lib.iso_profile_enable.argtypes = [_i]
+    lib.iso_profile_reset.restype = None
+    lib.iso_profile_read.argtypes = [C.c_char_p, C.POINTER(_ll), C.POINTER(C.c_double)]
     lib.iso_mc_dense_workspace_size.argtypes = [_i, _i, _i, _ll, _ll]
     lib.iso_mc_dense_workspace_size.restype = C.c_size_t
     lib.iso_mc_dense.argtypes = [_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp,
@@ -80,3 +83,10 @@ def check(rc: int) -> None:
 
 def fvec3(xs) -> C.Array:
     return (C.c_float * 3)(*[float(x) for x in xs])
+
+
+def profile_read(kernel: str | None) -> tuple[int, float]:
+    """(launches, total ms) recorded for a kernel since the last reset."""
+    n, t = _ll(), C.c_double()
+    check(lib().iso_profile_read(kernel.encode() if kernel else None, C.byref(n), C.byref(t)))
+    return n.value, t.value
