@@ -112,6 +112,10 @@ int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
     }
     p.level = level;
     p.method = method;
+    {
+        const int n[3] = {nx, ny, nz};
+        p.snapTau = mc_snap_tau(aabb_min, aabb_max, n);
+    }
     p.status = status;
     p.vout = vertices;
     p.fout = faces;

@@ -74,6 +74,52 @@ __device__ __forceinline__ uint32_t range_mask(int w, int lo, int hi) {
 }
 
 // ---------------------------------------------------------------------------
+// Warp-cooperative iteration over the set bits of a sequence of words.
+//
+// The warp takes 32 words at a time (one per lane), counts their set bits,
+// and hands the bits out 32 at a time, so sparse bits are processed with all
+// lanes busy instead of one lane per word.  get(i) returns word i (0 for
+// i >= n); f(i, b) runs once per set bit b of word i, on some lane.  scratch
+// points to 64 words of warp-private shared memory.
+template <class Get, class F>
+__device__ __forceinline__ void warp_foreach_bit(int first, int n, int stride, uint32_t* scratch,
+                                                 Get get, F f) {
+    const int lane = threadIdx.x & 31;
+    for (int base = first; base < n; base += stride) {
+        const int i = base + lane;
+        const uint32_t m = i < n ? get(i) : 0u;
+        const uint32_t cnt = __popc(m);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t x = __shfl_up_sync(~0u, incl, d);
+            if (lane >= d) incl += x;
+        }
+        const uint32_t total = __shfl_sync(~0u, incl, 31);
+        if (total == 0) continue;
+        scratch[lane] = m;
+        scratch[32 + lane] = incl;
+        __syncwarp();
+        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            if (k < total) {
+                // owner lane: first lane whose inclusive count exceeds k
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (scratch[32 + mid] > k) hi = mid; else lo = mid + 1;
+                }
+                uint32_t mm = scratch[lo];
+                const uint32_t before = scratch[32 + lo] - __popc(mm);
+                for (uint32_t j = k - before; j; --j) mm &= mm - 1;  // drop the lower set bits
+                f(base + lo, __ffs(mm) - 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // TMA bulk copies (cp.async.bulk, global -> shared) completing on an mbarrier.
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {

@@ -24,6 +24,7 @@
 // key order (the reference sorts them by position instead; same mesh after
 // relabelling).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "common.cuh"
@@ -34,13 +35,13 @@
 
 namespace {
 
-constexpr int NB = 10;  // bitmaps kept per plane
-enum { B_SGN = 0, B_CRX, B_CRY, B_CRZ, B_LOX, B_LOY, B_LOZ, B_HIX, B_HIY, B_HIZ };
+constexpr int NB = 7;  // bitmaps kept per plane
+enum { B_SGN = 0, B_LOX, B_LOY, B_LOZ, B_HIX, B_HIY, B_HIZ };
 constexpr int RING = 3;  // planes P-1, P, P+1
 
 struct Layout {
-    size_t bm, act, fre, snp, du, ex, vcnt, fcnt, tbl, gx, gy, gz, zval, ecol, ocol, ocell, estat,
-        tri, ntri, misc, total;
+    size_t bm, cr, act, fre, snp, du, ex, vcnt, fcnt, tbl, rowoff, gx, gy, gz, zval, ecol, ocol, ocell,
+        scratch, estat, tri, ntri, misc, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -49,26 +50,29 @@ __host__ __device__ inline Layout make_layout(const McTiles& t) {
     Layout L;
     size_t o = 0;
     const size_t rw = size_t(t.RY) * t.NW;  // words per bitmap
-    L.bm = o;    o = al16(o + size_t(RING) * NB * rw * 4);
-    L.act = o;   o = al16(o + 2 * rw * 4);
-    L.fre = o;   o = al16(o + 2 * rw * 4);
-    L.snp = o;   o = al16(o + 2 * rw * 4);
-    L.du = o;    o = al16(o + 4 * rw * 4);
-    L.ex = o;    o = al16(o + 4 * rw * 4);
-    L.vcnt = o;  o = al16(o + rw * 4);
-    L.fcnt = o;  o = al16(o + rw * 4);
-    L.tbl = o;   o = al16(o + 3 * rw * 4);
-    L.gx = o;    o = al16(o + RING * 4);
-    L.gy = o;    o = al16(o + size_t(t.RY) * 4);
-    L.gz = o;    o = al16(o + size_t(32) * t.NW * 4);
-    L.zval = o;  o = al16(o + size_t(t.NW) * 4);
-    L.ecol = o;  o = al16(o + size_t(t.NW) * 4);
-    L.ocol = o;  o = al16(o + size_t(t.NW) * 4);
-    L.ocell = o; o = al16(o + size_t(t.NW) * 4);
-    L.estat = o; o = al16(o + 256 * 2);
-    L.tri = o;   o = al16(o + 256 * 15);
-    L.ntri = o;  o = al16(o + 256);
-    L.misc = o;  o = al16(o + 64);
+    L.bm = o;      o = al16(o + size_t(RING) * NB * rw * 4);
+    L.cr = o;      o = al16(o + 3 * rw * 4);
+    L.act = o;     o = al16(o + 2 * rw * 4);
+    L.fre = o;     o = al16(o + 2 * rw * 4);
+    L.snp = o;     o = al16(o + 2 * rw * 4);
+    L.du = o;      o = al16(o + 4 * rw * 4);
+    L.ex = o;      o = al16(o + 4 * rw * 4);
+    L.vcnt = o;    o = al16(o + rw * 4);
+    L.fcnt = o;    o = al16(o + rw * 4);
+    L.tbl = o;     o = al16(o + 3 * rw * 4);
+    L.rowoff = o;  o = al16(o + size_t(t.RY) * 8);
+    L.gx = o;      o = al16(o + RING * 4);
+    L.gy = o;      o = al16(o + size_t(t.RY) * 4);
+    L.gz = o;      o = al16(o + size_t(32) * t.NW * 4);
+    L.zval = o;    o = al16(o + size_t(t.NW) * 4);
+    L.ecol = o;    o = al16(o + size_t(t.NW) * 4);
+    L.ocol = o;    o = al16(o + size_t(t.NW) * 4);
+    L.ocell = o;   o = al16(o + size_t(t.NW) * 4);
+    L.scratch = o; o = al16(o + size_t(t.threads / 32) * 64 * 4);
+    L.estat = o;   o = al16(o + 256 * 2);
+    L.tri = o;     o = al16(o + 256 * 15);
+    L.ntri = o;    o = al16(o + 256);
+    L.misc = o;    o = al16(o + 64);
     L.total = o;
     return L;
 }
@@ -80,7 +84,8 @@ using iso::prev1;
 struct Ctx {
     // shared memory
     uint32_t* bm;
-    uint32_t *act, *fre, *snp, *du, *ex, *vcnt, *fcnt, *tbl;
+    uint32_t *cr, *act, *fre, *snp, *du, *ex, *vcnt, *fcnt, *tbl;
+    long long* rowoff;
     float *gx, *gy, *gz;
     uint32_t *zval, *ecol, *ocol, *ocell;
     uint16_t* estat;
@@ -108,10 +113,13 @@ struct Ctx {
         long long y = Y0 - 1 + row, z = Z0 - 32 + col;
         return __ldg(vals + ((long long)pl * ny + y) * nz + z);
     }
+    __device__ __forceinline__ int slot_of(int rel) const {
+        return rel == 0 ? sA : (rel == 1 ? sB : sC);
+    }
 };
 
-// Corner k of the cell whose highest corner is (hy, hc) in layer L.
-//   rel = L + (k >> 2) (plane - (P - 1)), row = hy - 1 + ((k >> 1) & 1), col = hc - 1 + (k & 1)
+// Case number of the cell whose highest corner is (hy, hc) in layer L.
+// Corner k = 4dx + 2dy + dz is plane rel = L + dx, row hy - 1 + dy, col hc - 1 + dz.
 __device__ __forceinline__ uint32_t cell_case(const Ctx& c, int L, int hy, int hc) {
     const int lo = L ? c.sB : c.sA, hi = L ? c.sC : c.sB;
     uint32_t cs = 0;
@@ -135,14 +143,29 @@ __device__ __forceinline__ void cell_codes(const Ctx& c, int L, int hy, int hc, 
         const int ax = d == 4 ? 0 : (d == 2 ? 1 : 2);
         uint8_t code = uint8_t(b * 4 + ax);
         if (snap) {
-            const int rel = L + (b >> 2);
-            const int slot = rel == 0 ? c.sA : (rel == 1 ? c.sB : c.sC);
+            const int slot = c.slot_of(L + (b >> 2));
             const int row = hy - 1 + ((b >> 1) & 1), col = hc - 1 + (b & 1);
             if (c.bit(slot, B_LOX + ax, row, col)) code = uint8_t(a * 4 + 3);
             else if (c.bit(slot, B_HIX + ax, row, col)) code = uint8_t(b * 4 + 3);
         }
         ck[e] = code;
     }
+}
+
+// Number of faces a cell emits: its table count, or for a cell with snapped
+// edges the triangles whose three vertices are distinct.
+__device__ __forceinline__ uint32_t cell_nfaces(const Ctx& c, int L, int hy, int hc, bool snap) {
+    const uint32_t cs = cell_case(c, L, hy, hc);
+    if (!snap) return c.ntri[cs];
+    uint8_t ck[12];
+    cell_codes(c, L, hy, hc, c.estat[cs], true, ck);
+    const int8_t* tr = c.tri + cs * 15;
+    uint32_t nt = 0;
+    for (int k = 0; k < 15 && tr[k] >= 0; k += 3) {
+        const uint8_t k0 = ck[tr[k]], k1 = ck[tr[k + 1]], k2 = ck[tr[k + 2]];
+        nt += (k0 != k1 && k0 != k2 && k1 != k2);
+    }
+    return nt;
 }
 
 template <int BLOCK>
@@ -152,6 +175,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
     const Layout LY = make_layout(T);
     Ctx c;
     c.bm = reinterpret_cast<uint32_t*>(smem + LY.bm);
+    c.cr = reinterpret_cast<uint32_t*>(smem + LY.cr);
     c.act = reinterpret_cast<uint32_t*>(smem + LY.act);
     c.fre = reinterpret_cast<uint32_t*>(smem + LY.fre);
     c.snp = reinterpret_cast<uint32_t*>(smem + LY.snp);
@@ -160,6 +184,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
     c.vcnt = reinterpret_cast<uint32_t*>(smem + LY.vcnt);
     c.fcnt = reinterpret_cast<uint32_t*>(smem + LY.fcnt);
     c.tbl = reinterpret_cast<uint32_t*>(smem + LY.tbl);
+    c.rowoff = reinterpret_cast<long long*>(smem + LY.rowoff);
     c.gx = reinterpret_cast<float*>(smem + LY.gx);
     c.gy = reinterpret_cast<float*>(smem + LY.gy);
     c.gz = reinterpret_cast<float*>(smem + LY.gz);
@@ -174,12 +199,14 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NWARP = BLOCK / 32;
+    uint32_t* wscratch = reinterpret_cast<uint32_t*>(smem + LY.scratch) + warp * 64;
 
     c.vals = p.vals;
     c.nx = T.nx; c.ny = T.ny; c.nz = T.nz; c.level = p.level;
     c.R = T.R; c.ZC = T.ZC; c.RY = T.RY; c.NW = T.NW; c.RW = T.RY * T.NW;
     c.nRT = T.nRT; c.nZT = T.nZT;
     const int NW = c.NW, RW = c.RW;
+    const float tau = p.snapTau;
 
     // Lookup tables and the (layer/axis, row, word) decode table.
     for (int i = tid; i < 256; i += BLOCK) {
@@ -257,10 +284,15 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
             const int sp = j > 0 ? (j - 1) % RING : -1;
             if (tid == 0)
                 c.gx[slot] = iso::grid_coord(uint32_t(pl), uint32_t(c.nx), p.amin[0], p.asize[0]);
+            for (int i = tid; i < c.RY; i += BLOCK) {
+                const int y = c.Y0 - 1 + i;
+                // offset of (y, z = Z0) in the value array; -1 marks a row outside the slab
+                c.rowoff[i] = (y >= ylo && y <= yhi) ? ((long long)pl * c.ny + y) * c.nz + c.Z0 : -1ll;
+            }
+            __syncthreads();
 
             // (1) sign bits of plane pl: one warp ballot per 32 points, 4 loads in flight
             {
-                const float* base = p.vals + (long long)pl * c.ny * c.nz;
                 uint32_t* sg = c.plane(slot, B_SGN);
                 for (int r0 = warp; r0 < RW; r0 += 4 * NWARP) {
                     float v[4];
@@ -273,10 +305,9 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                         if (r < RW) {
                             const uint32_t x = c.tbl[r];
                             const int ly = (x >> 16) & 0xff, w = x & 0xffff;
-                            const int y = c.Y0 - 1 + ly;
-                            ok[u] = y >= ylo && y <= yhi && ((c.zval[w] >> lane) & 1u);
-                            if (ok[u])
-                                v[u] = __ldg(base + (long long)y * c.nz + (c.Z0 - 32 + 32 * w + lane));
+                            const long long ro = c.rowoff[ly];
+                            ok[u] = ro >= 0 && ((c.zval[w] >> lane) & 1u);
+                            if (ok[u]) v[u] = __ldg(p.vals + ro + (32 * w + lane - 32));
                         }
                     }
 #pragma unroll
@@ -289,46 +320,54 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
             }
             __syncthreads();
 
-            // (2) crossed and snapped edges whose high endpoint is in plane pl
+            // (2) crossed edges whose high endpoint is in plane pl (word-parallel)
             for (int i = tid; i < 3 * RW; i += BLOCK) {
                 const uint32_t x = c.tbl[i];
                 const int ax = x >> 24, ly = (x >> 16) & 0xff, w = x & 0xffff;
                 const int r = i - ax * RW;
-                const int y = c.Y0 - 1 + ly;
-                const bool rv = y >= ylo && y <= yhi;
+                const bool rv = c.rowoff[ly] >= 0;
                 const uint32_t* sgrow = c.plane(slot, B_SGN) + ly * NW;
                 uint32_t cr = 0;
                 if (rv) {
                     if (ax == 0) {
                         if (sp >= 0) cr = (sgrow[w] ^ c.plane(sp, B_SGN)[r]) & c.zval[w];
                     } else if (ax == 1) {
-                        if (ly >= 1 && y - 1 >= ylo) cr = (sgrow[w] ^ sgrow[w - NW]) & c.zval[w];
+                        if (ly >= 1 && c.rowoff[ly - 1] >= 0) cr = (sgrow[w] ^ sgrow[w - NW]) & c.zval[w];
                     } else {
                         cr = (sgrow[w] ^ prev1(sgrow, w)) & c.zval[w] & prev1(c.zval, w);
                     }
                 }
-                uint32_t lo = 0, hi = 0;
-                uint32_t bits = cr;
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
+                c.cr[i] = cr;
+                c.plane(slot, B_LOX + ax)[r] = 0u;
+                c.plane(slot, B_HIX + ax)[r] = 0u;
+            }
+            __syncthreads();
+
+            // (3) snapped edges: crossings whose vertex rounds onto an endpoint.
+            // Only t within tau of 0 or 1 can round onto a grid point; those get
+            // the exact test.
+            iso::warp_foreach_bit(
+                warp * 32, 3 * RW, NWARP * 32, wscratch, [&](int i) { return c.cr[i]; },
+                [&](int i, int b) {
+                    const uint32_t x = c.tbl[i];
+                    const int ax = x >> 24, ly = (x >> 16) & 0xff, w = x & 0xffff;
                     const int col = 32 * w + b;
                     const int pa = ax == 0 ? pl - 1 : pl;
                     const int ra = ax == 1 ? ly - 1 : ly;
                     const int ca = ax == 2 ? col - 1 : col;
                     const float va = c.value(pa, ra, ca), vb = c.value(pl, ly, col);
+                    const float t = iso::cross_t(c.level, va, vb);
+                    if (t >= tau && t <= 1.0f - tau) return;  // NaN falls through
                     const float xa = c.gx[ax == 0 ? sp : slot], ya = c.gy[ra], za = c.gz[ca];
                     const float xb = c.gx[slot], yb = c.gy[ly], zb = c.gz[col];
-                    const float t = iso::cross_t(c.level, va, vb);
                     const float px = iso::lerp1(t, xa, xb), py = iso::lerp1(t, ya, yb),
                                 pz = iso::lerp1(t, za, zb);
-                    if (px == xa && py == ya && pz == za) lo |= 1u << b;
-                    else if (px == xb && py == yb && pz == zb) hi |= 1u << b;
-                }
-                c.plane(slot, B_CRX + ax)[r] = cr;
-                c.plane(slot, B_LOX + ax)[r] = lo;
-                c.plane(slot, B_HIX + ax)[r] = hi;
-            }
+                    const int r = i - ax * RW;
+                    if (px == xa && py == ya && pz == za)
+                        atomicOr(&c.plane(slot, B_LOX + ax)[r], 1u << b);
+                    else if (px == xb && py == yb && pz == zb)
+                        atomicOr(&c.plane(slot, B_HIX + ax)[r], 1u << b);
+                });
             __syncthreads();
 
             // Tiles ready after this plane: P = pl - 1 and, at the grid's last
@@ -343,16 +382,14 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                 c.sC = P + 1 <= c.nx - 1 ? (P + 1 - pfirst) % RING : -1;
                 const bool L0 = P >= 1, L1 = P + 1 <= c.nx - 1;
 
-                // T12: cell masks of both layers, face counts of own cells,
-                // and per-cell vertex use for cells with snapped edges (du is
-                // clean: cleared at item start and after every tile's T3).
+                // T1: cell masks of both layers (word-parallel); cells with
+                // snapped edges mark the owned vertices their faces use.
                 for (int i = tid; i < 2 * RW; i += BLOCK) {
                     const uint32_t x = c.tbl[i];
                     const int L = x >> 24, hy = (x >> 16) & 0xff, hw = x & 0xffff;
                     uint32_t act = 0, fre = 0, snp = 0;
                     const bool lok = L ? L1 : L0;
                     const uint32_t em = (lok && hy >= hyE0 && hy <= hyE1 && hw >= 1) ? c.ecol[hw] : 0u;
-                    uint32_t faces = 0;
                     if (em) {
                         const int lo = L ? c.sB : c.sA, hi = L ? c.sC : c.sB;
                         const uint32_t* a0 = c.plane(lo, B_SGN) + (hy - 1) * NW;
@@ -366,7 +403,6 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                         act = (or8 & ~and8) & em;
                         if (act) {
                             uint32_t sn = 0;
-                            // x edges (stored in the high plane) at rows hy-1, hy; cols c-1, c
                             {
                                 const int o0 = (hy - 1) * NW;
                                 const uint32_t* xl = c.plane(hi, B_LOX);
@@ -387,57 +423,53 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                             }
                             snp = act & sn;
                             fre = act & ~sn;
-                            const uint32_t own =
-                                (L == 0 && hy >= hyO0 && hy <= hyO1) ? (act & c.ocell[hw]) : 0u;
-                            uint32_t bits = own | snp;
-                            while (bits) {
+                            uint32_t bits = snp;
+                            while (bits) {  // rare: cells with a vertex on a grid point
                                 const int b = __ffs(bits) - 1;
                                 bits &= bits - 1;
-                                // case bits: corner k = 4dx + 2dy + dz; dz = 0 reads the
-                                // prev1-shifted word (column hc - 1)
-                                const uint32_t cse =
-                                    (((w1 >> b) & 1u) << 0) | (((w0 >> b) & 1u) << 1) |
-                                    (((w3 >> b) & 1u) << 2) | (((w2 >> b) & 1u) << 3) |
-                                    (((w5 >> b) & 1u) << 4) | (((w4 >> b) & 1u) << 5) |
-                                    (((w7 >> b) & 1u) << 6) | (((w6 >> b) & 1u) << 7);
-                                uint32_t nt;
-                                if ((snp >> b) & 1u) {
-                                    const int hc = 32 * hw + b;
-                                    uint8_t ck[12];
-                                    cell_codes(c, L, hy, hc, c.estat[cse], true, ck);
-                                    const int8_t* tr = c.tri + cse * 15;
-                                    nt = 0;
-                                    for (int k = 0; k < 15 && tr[k] >= 0; k += 3) {
-                                        const uint8_t k0 = ck[tr[k]], k1 = ck[tr[k + 1]], k2 = ck[tr[k + 2]];
-                                        if (k0 == k1 || k0 == k2 || k1 == k2) continue;
-                                        ++nt;
-                                        const uint8_t kk[3] = {k0, k1, k2};
+                                const int hc = 32 * hw + b;
+                                const uint32_t cs = cell_case(c, L, hy, hc);
+                                uint8_t ck[12];
+                                cell_codes(c, L, hy, hc, c.estat[cs], true, ck);
+                                const int8_t* tr = c.tri + cs * 15;
+                                for (int k = 0; k < 15 && tr[k] >= 0; k += 3) {
+                                    const uint8_t k0 = ck[tr[k]], k1 = ck[tr[k + 1]], k2 = ck[tr[k + 2]];
+                                    if (k0 == k1 || k0 == k2 || k1 == k2) continue;
+                                    const uint8_t kk[3] = {k0, k1, k2};
 #pragma unroll
-                                        for (int m = 0; m < 3; ++m) {
-                                            const int corner = kk[m] >> 2, type = kk[m] & 3;
-                                            const int rel = L + (corner >> 2);
-                                            const int row = hy - 1 + ((corner >> 1) & 1);
-                                            const int col = hc - 1 + (corner & 1);
-                                            if (rel == 1 && row >= 1 && row <= c.Y1 - c.Y0 && col >= 32 &&
-                                                col <= c.Z1 - c.Z0 + 31)
-                                                atomicOr(&c.du[(type * c.RY + row) * NW + (col >> 5)],
-                                                         1u << (col & 31));
-                                        }
+                                    for (int m = 0; m < 3; ++m) {
+                                        const int corner = kk[m] >> 2, type = kk[m] & 3;
+                                        const int rel = L + (corner >> 2);
+                                        const int row = hy - 1 + ((corner >> 1) & 1);
+                                        const int col = hc - 1 + (corner & 1);
+                                        if (rel == 1 && row >= 1 && row <= c.Y1 - c.Y0 && col >= 32 &&
+                                            col <= c.Z1 - c.Z0 + 31)
+                                            atomicOr(&c.du[(type * c.RY + row) * NW + (col >> 5)],
+                                                     1u << (col & 31));
                                     }
-                                } else {
-                                    nt = c.ntri[cse];
                                 }
-                                if ((own >> b) & 1u) faces += nt;
                             }
                         }
                     }
                     c.act[i] = act;
                     c.fre[i] = fre;
                     c.snp[i] = snp;
-                    if (L == 0) c.fcnt[i] = faces;
+                    if (L == 0) c.fcnt[i] = 0;
                 }
                 __syncthreads();
 
+                // T2: face counts of own cells (one lane per cell)
+                iso::warp_foreach_bit(
+                    warp * 32, RW, NWARP * 32, wscratch,
+                    [&](int i) {
+                        const int hy = (c.tbl[i] >> 16) & 0xff, hw = c.tbl[i] & 0xffff;
+                        return (hy >= hyO0 && hy <= hyO1 && hw >= 1) ? (c.act[i] & c.ocell[hw]) : 0u;
+                    },
+                    [&](int i, int b) {
+                        const int hy = (c.tbl[i] >> 16) & 0xff, hw = c.tbl[i] & 0xffff;
+                        const uint32_t nt = cell_nfaces(c, 0, hy, 32 * hw + b, (c.snp[i] >> b) & 1u);
+                        if (nt) atomicAdd(&c.fcnt[i], nt);
+                    });
                 // T3: vertex existence for the owned points (plane P)
                 for (int i = tid; i < RW; i += BLOCK) {
                     const uint32_t x = c.tbl[i];
@@ -453,15 +485,20 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                                        g1n = next1(f0b, w, NW);
                         const uint32_t h0 = f1a[w], h0n = next1(f1a, w, NW), h1 = f1b[w];
                         const int sB = c.sB;
-                        uint32_t cr = c.plane(sB, B_CRX)[i];
+                        const uint32_t* sgP = c.plane(sB, B_SGN) + ly * NW;
+                        const bool rowok = c.rowoff[ly] >= 0;
+                        // crossings of the edges keyed by plane P's points
+                        const uint32_t zv = c.zval[w];
+                        const uint32_t crx = (L0 && rowok) ? (sgP[w] ^ c.plane(c.sA, B_SGN)[i]) & zv : 0u;
+                        const uint32_t cry = (rowok && ly >= 1 && c.rowoff[ly - 1] >= 0)
+                                                 ? (sgP[w] ^ sgP[w - NW]) & zv : 0u;
+                        const uint32_t crz = rowok ? (sgP[w] ^ prev1(sgP, w)) & zv & prev1(c.zval, w) : 0u;
                         uint32_t sn = c.plane(sB, B_LOX)[i] | c.plane(sB, B_HIX)[i];
-                        e0 = cr & ~sn & ((g0 | g0n | g1 | g1n) | c.du[i]) & om;
-                        cr = c.plane(sB, B_CRY)[i];
+                        e0 = crx & ~sn & ((g0 | g0n | g1 | g1n) | c.du[i]) & om;
                         sn = c.plane(sB, B_LOY)[i] | c.plane(sB, B_HIY)[i];
-                        e1 = cr & ~sn & ((g0 | g0n | h0 | h0n) | c.du[RW + i]) & om;
-                        cr = c.plane(sB, B_CRZ)[i];
+                        e1 = cry & ~sn & ((g0 | g0n | h0 | h0n) | c.du[RW + i]) & om;
                         sn = c.plane(sB, B_LOZ)[i] | c.plane(sB, B_HIZ)[i];
-                        e2 = cr & ~sn & ((g0 | g1 | h0 | h1) | c.du[2 * RW + i]) & om;
+                        e2 = crz & ~sn & ((g0 | g1 | h0 | h1) | c.du[2 * RW + i]) & om;
                         e3 = c.du[3 * RW + i] & om;
                     }
                     c.ex[i] = e0;
@@ -514,27 +551,24 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                 const bool vfit = vOff + VT <= (unsigned long long)p.capSV;
                 const bool ffit = fOff + FT <= (unsigned long long)p.capSF;
 
-                for (int i = tid; i < RW; i += BLOCK) {
-                    const uint32_t x = c.tbl[i];
-                    const int ly = (x >> 16) & 0xff, w = x & 0xffff;
-                    c.du[i] = 0;
-                    c.du[RW + i] = 0;
-                    c.du[2 * RW + i] = 0;
-                    c.du[3 * RW + i] = 0;
-                    // T5a: staged vertices, in key order
-                    const uint32_t e[4] = {c.ex[i], c.ex[RW + i], c.ex[2 * RW + i], c.ex[3 * RW + i]};
-                    uint32_t any = e[0] | e[1] | e[2] | e[3];
-                    if (any && vfit) {
-                        unsigned long long o = vOff + c.vcnt[i];
-                        const int sB = c.sB;
-                        const float bx = c.gx[sB], by = c.gy[ly];
-                        while (any) {
-                            const int b = __ffs(any) - 1;
-                            any &= any - 1;
+                // T5a: staged vertices (position + key), one lane per point, in key order
+                if (VT && vfit) {
+                    iso::warp_foreach_bit(
+                        warp * 32, RW, NWARP * 32, wscratch,
+                        [&](int i) { return c.ex[i] | c.ex[RW + i] | c.ex[2 * RW + i] | c.ex[3 * RW + i]; },
+                        [&](int i, int b) {
+                            const uint32_t x = c.tbl[i];
+                            const int ly = (x >> 16) & 0xff, w = x & 0xffff;
+                            const uint32_t e[4] = {c.ex[i], c.ex[RW + i], c.ex[2 * RW + i], c.ex[3 * RW + i]};
+                            const uint32_t below = (1u << b) - 1u;
+                            unsigned long long o = vOff + c.vcnt[i] + __popc(e[0] & below) +
+                                                   __popc(e[1] & below) + __popc(e[2] & below) +
+                                                   __popc(e[3] & below);
                             const int col = 32 * w + b;
-                            const float bz = c.gz[col];
-                            float vb = 0.0f;
-                            if ((e[0] | e[1] | e[2]) >> b & 1u) vb = c.value(P, ly, col);
+                            const int sB = c.sB;
+                            const float bx = c.gx[sB], by = c.gy[ly], bz = c.gz[col];
+                            const bool edge = ((e[0] | e[1] | e[2]) >> b) & 1u;
+                            const float vb = edge ? c.value(P, ly, col) : 0.0f;
 #pragma unroll
                             for (int type = 0; type < 4; ++type) {
                                 if (!((e[type] >> b) & 1u)) continue;
@@ -552,47 +586,62 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                                 const uint32_t key = (uint32_t((ly - 1) * c.ZC + (col - 32)) << 2) | type;
                                 p.sv[o++] = make_float4(px, py, pz, __uint_as_float(key));
                             }
-                        }
-                    }
-                    // T5b: staged faces of own cells, in cell order
-                    const int hy = ly, hw = w;
-                    if (ffit && hy >= hyO0 && hy <= hyO1 && hw >= 1) {
-                        uint32_t own = c.act[i] & c.ocell[hw];
-                        if (own) {
+                        });
+                }
+                // T5b: staged faces of own cells, one lane per cell, in cell order
+                if (FT && ffit) {
+                    iso::warp_foreach_bit(
+                        warp * 32, RW, NWARP * 32, wscratch,
+                        [&](int i) {
+                            const int hy = (c.tbl[i] >> 16) & 0xff, hw = c.tbl[i] & 0xffff;
+                            return (hy >= hyO0 && hy <= hyO1 && hw >= 1) ? (c.act[i] & c.ocell[hw]) : 0u;
+                        },
+                        [&](int i, int b) {
+                            const int hy = (c.tbl[i] >> 16) & 0xff, hw = c.tbl[i] & 0xffff;
+                            const uint32_t own = c.act[i] & c.ocell[hw];
                             const uint32_t snp = c.snp[i];
+                            // faces of the word's earlier own cells come first
                             unsigned long long o = fOff + c.fcnt[i];
-                            while (own) {
-                                const int b = __ffs(own) - 1;
-                                own &= own - 1;
-                                const int hc = 32 * hw + b;
-                                const uint32_t cs = cell_case(c, 0, hy, hc);
-                                const bool sn = (snp >> b) & 1u;
-                                uint8_t ck[12];
-                                cell_codes(c, 0, hy, hc, c.estat[cs], sn, ck);
-                                uint32_t base[8];
-#pragma unroll
-                                for (int k = 0; k < 8; ++k) {
-                                    const int rel = k >> 2;
-                                    const int row = hy - 1 + ((k >> 1) & 1);
-                                    const int col = hc - 1 + (k & 1);
-                                    const int drt = row == 0, dzt = col == 31;
-                                    const uint32_t lrow = uint32_t(row - 1 + drt * c.R);
-                                    const uint32_t lcol = uint32_t(col - 32 + dzt * c.ZC);
-                                    const uint32_t slot = uint32_t((1 - rel) * 4 + drt * 2 + dzt);
-                                    base[k] = (slot << 24) | ((lrow * uint32_t(c.ZC) + lcol) << 2);
-                                }
-                                const int8_t* tr = c.tri + cs * 15;
-                                for (int k = 0; k < 15 && tr[k] >= 0; k += 3) {
-                                    const uint8_t k0 = ck[tr[k]], k1 = ck[tr[k + 1]], k2 = ck[tr[k + 2]];
-                                    if (sn && (k0 == k1 || k0 == k2 || k1 == k2)) continue;
-                                    uint32_t* dst = p.sf + 3 * o++;
-                                    dst[0] = base[k0 >> 2] | (k0 & 3u);
-                                    dst[1] = base[k1 >> 2] | (k1 & 3u);
-                                    dst[2] = base[k2 >> 2] | (k2 & 3u);
-                                }
+                            uint32_t prior = own & ((1u << b) - 1u);
+                            while (prior) {
+                                const int b2 = __ffs(prior) - 1;
+                                prior &= prior - 1;
+                                o += cell_nfaces(c, 0, hy, 32 * hw + b2, (snp >> b2) & 1u);
                             }
-                        }
-                    }
+                            const int hc = 32 * hw + b;
+                            const uint32_t cs = cell_case(c, 0, hy, hc);
+                            const bool sn = (snp >> b) & 1u;
+                            uint8_t ck[12];
+                            cell_codes(c, 0, hy, hc, c.estat[cs], sn, ck);
+                            // owner-relative references of the 8 corner points
+                            uint32_t base[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                const int rel = k >> 2;
+                                const int row = hy - 1 + ((k >> 1) & 1);
+                                const int col = hc - 1 + (k & 1);
+                                const int drt = row == 0, dzt = col == 31;
+                                const uint32_t lrow = uint32_t(row - 1 + drt * c.R);
+                                const uint32_t lcol = uint32_t(col - 32 + dzt * c.ZC);
+                                const uint32_t slot = uint32_t((1 - rel) * 4 + drt * 2 + dzt);
+                                base[k] = (slot << 24) | ((lrow * uint32_t(c.ZC) + lcol) << 2);
+                            }
+                            const int8_t* tr = c.tri + cs * 15;
+                            for (int k = 0; k < 15 && tr[k] >= 0; k += 3) {
+                                const uint8_t k0 = ck[tr[k]], k1 = ck[tr[k + 1]], k2 = ck[tr[k + 2]];
+                                if (sn && (k0 == k1 || k0 == k2 || k1 == k2)) continue;
+                                uint32_t* dst = p.sf + 3 * o++;
+                                dst[0] = base[k0 >> 2] | (k0 & 3u);
+                                dst[1] = base[k1 >> 2] | (k1 & 3u);
+                                dst[2] = base[k2 >> 2] | (k2 & 3u);
+                            }
+                        });
+                }
+                for (int i = tid; i < RW; i += BLOCK) {
+                    c.du[i] = 0;
+                    c.du[RW + i] = 0;
+                    c.du[2 * RW + i] = 0;
+                    c.du[3 * RW + i] = 0;
                 }
                 __syncthreads();
             }
@@ -808,6 +857,23 @@ int mc_plan_tiles(int nx, int ny, int nz, int rows, int slabs, int threads, int 
     t.nItems = (long long)t.nChunks * cols;
     *out = t;
     return 0;
+}
+
+// Bound on t for an edge vertex to round onto an endpoint.  For the varying
+// coordinate, (1 - t) * a + t * b rounds to a only if t * |b - a| is within a few
+// ulps of max(|a|, |b|): t <= ~5 * 2^-24 * (|a| + |b|) / h, h the grid spacing.
+// tau = 2^-20 * (1 + max |coord| / h) keeps a 1.6x margin on that bound; the
+// same holds for 1 - t.
+float mc_snap_tau(const float amin[3], const float amax[3], const int n[3]) {
+    double r = 0;
+    for (int k = 0; k < 3; ++k) {
+        double size = double(amax[k]) - double(amin[k]);
+        double m = std::max(std::fabs(double(amin[k])), std::fabs(double(amax[k])));
+        if (size == 0.0 || !std::isfinite(size)) return 1.0f;
+        r = std::max(r, m * double(std::max(n[k] - 1, 1)) / std::fabs(size));
+    }
+    double tau = std::ldexp(1.0, -20) * (1.0 + r);
+    return tau >= 0.5 ? 1.0f : float(tau);
 }
 
 size_t mc_workspace_bytes(const McTiles& t, long long capV, long long capF) {

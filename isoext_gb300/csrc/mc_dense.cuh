@@ -45,6 +45,10 @@ struct McParams {
     float amin[3], asize[3];
     float level;
     int method;  // 0 nagae, 1 lorensen
+    // An edge vertex can round exactly onto a grid point only when its
+    // parameter t is within snapTau of 0 or 1 (set by mc_snap_tau); such
+    // edges get the exact test.
+    float snapTau;
     McTiles t;
     // workspace
     McTileRec* rec;                 // nTiles
@@ -66,4 +70,5 @@ struct McParams {
 int mc_plan_tiles(int nx, int ny, int nz, int rows, int slabs, int threads, int zchunk,
                   int sm_count, McTiles* out);
 size_t mc_workspace_bytes(const McTiles& t, long long capV, long long capF);
+float mc_snap_tau(const float amin[3], const float amax[3], const int n[3]);
 int mc_launch(const McParams& p, void* workspace, size_t ws_bytes, cudaStream_t stream);

@@ -4,6 +4,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import _ffi
@@ -61,6 +62,47 @@ def workspace_bytes(shape, cap_v: int, cap_f: int) -> int:
     return int(_ffi.lib().iso_mc_dense_workspace_size(*shape, cap_v, cap_f))
 
 
+def coarse_float_grid(shape, aabb_min, aabb_max) -> bool:
+    """True when grid spacing is within 64 ulps of the coordinates' magnitude.
+
+    Vertices are identified by grid key; isoext identifies them by exact
+    position.  The two agree while neighbouring grid coordinates are many ulps
+    apart.  On grids whose spacing approaches float resolution (e.g. a tiny box
+    far from the origin) distinct keys can share a position, and the position
+    weld of weld_by_position() is applied after extraction.
+    """
+    for n, a, b in zip(shape, aabb_min, aabb_max):
+        if n < 2:
+            continue
+        a32, b32 = np.float32(a), np.float32(b)
+        h = abs(float(b32) - float(a32)) / (n - 1)
+        ulp = float(np.spacing(np.float32(max(abs(a32), abs(b32)))))
+        if not np.isfinite(h) or h < 64.0 * ulp:
+            return True
+    return False
+
+
+def weld_by_position(v: torch.Tensor, f: torch.Tensor):
+    """Merge vertices with bit-identical positions (+0 and -0 equal), drop faces
+    that became degenerate and vertices no face uses -- the result of isoext's
+    position weld (src/utils.cu:32-59 with the degenerate test of
+    src/mc/nagae.cu:71) applied to a key-welded mesh."""
+    if v is None or len(f) == 0:
+        return v, f
+    vn = torch.where(v == 0, torch.zeros_like(v), v)
+    bits = vn.view(torch.int32)
+    uniq, inv = torch.unique(bits, dim=0, return_inverse=True)
+    f2 = inv[f.long()]
+    keep = (f2[:, 0] != f2[:, 1]) & (f2[:, 0] != f2[:, 2]) & (f2[:, 1] != f2[:, 2])
+    f2 = f2[keep]
+    if len(f2) == 0:
+        return None, None
+    used = torch.zeros(len(uniq), dtype=torch.bool, device=v.device)
+    used[f2.reshape(-1)] = True
+    remap = torch.cumsum(used.to(torch.int64), 0) - 1
+    return uniq[used].view(torch.float32).contiguous(), remap[f2].to(torch.int32).contiguous()
+
+
 def _mc_uniform(grid: UniformGrid, level: float, method: int):
     values = grid._values
     dev = values.device
@@ -87,7 +129,10 @@ def _mc_uniform(grid: UniformGrid, level: float, method: int):
             if status != 0:
                 raise RuntimeError(f"isoext_gb300: device error {status} in marching_cubes")
             _size_cache[key] = (nv, nf)
-            return _views(vout, fout, nv, nf)
+            v, f = _views(vout, fout, nv, nf)
+            if v is not None and coarse_float_grid(grid.shape, grid.aabb_min, grid.aabb_max):
+                v, f = weld_by_position(v, f)
+            return v, f
     raise RuntimeError("isoext_gb300: marching_cubes output did not fit after resizing")
 
 

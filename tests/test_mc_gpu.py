@@ -154,3 +154,23 @@ def test_mc_repeat_is_deterministic():
     a = iso.marching_cubes(g)
     b = iso.marching_cubes(g)
     assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_mc_extreme_magnitudes(oracle, seed):
+    # values spanning 1e-38 .. 1e38: many edge parameters t are tiny but not
+    # zero, so vertices round onto grid points without an exact zero value
+    g = np.random.default_rng(100 + seed)
+    shape = (21, 26, 33)
+    mag = 10.0 ** g.uniform(-38, 38, size=shape)
+    vals = (np.sign(g.uniform(-1, 1, size=shape)) * mag).astype(np.float32)
+    for m in ["nagae", "lorensen"]:
+        check(oracle, vals, method=m, what=f"extreme {seed} {m}")
+
+
+def test_mc_far_offset_box(oracle):
+    # coordinates far from the origin relative to the cell size
+    vals = noise((17, 18, 19), seed=5, zero_frac=0.2)
+    check(oracle, vals, lo=(1000.0, -500.0, 2.0), hi=(1001.0, -499.5, 2.001), what="far box")
+    check(oracle, sphere((30, 30, 30), 0.3) * 1e-3, lo=(1000.0, 1000.0, 1000.0),
+          hi=(1000.002, 1000.002, 1000.002), what="far sphere")
