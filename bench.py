@@ -150,7 +150,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
             _ffi.check(mc_dense_into(vals, amin, amax, 0.0, 0, vout, fout, ws, small,
                                      stream.cuda_stream))
         algo_bytes = 4 * n ** 3 + 12 * nv + 12 * nf
-        kernels = ["mc_extract", "mc_tile_scan", "mc_resolve"]
+        kernels = ["mc_extract", "mc_signs", "mc_tile_scan", "mc_resolve"]
     else:
         raise SystemExit(f"workload {args.workload} not available yet")
 

@@ -72,7 +72,7 @@ __host__ __device__ inline Layout make_layout(const McTiles& t) {
     L.estat = o;   o = al16(o + 256 * 2);
     L.tri = o;     o = al16(o + 256 * 15);
     L.ntri = o;    o = al16(o + 256);
-    L.misc = o;    o = al16(o + 64);
+    L.misc = o;    o = al16(o + 128);
     L.total = o;
     return L;
 }
@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
         int ly = r / NW, w = r - ly * NW;
         c.tbl[i] = (uint32_t(a) << 24) | (uint32_t(ly) << 16) | uint32_t(w);
     }
+    if (tid < 16) c.misc[tid] = 0;  // [5..8]: current staging blocks (empty)
     __syncthreads();
 
     const long long perChunk = (long long)c.nRT * c.nZT;
@@ -291,31 +292,21 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
             }
             __syncthreads();
 
-            // (1) sign bits of plane pl: one warp ballot per 32 points, 4 loads in flight
+            // (1) sign bits of plane pl, from the bitmap mc_signs wrote: tile word w
+            // covers z = Z0 - 32 + 32 w + b, i.e. bitmap word Z0 / 32 + w - 1.
             {
                 uint32_t* sg = c.plane(slot, B_SGN);
-                for (int r0 = warp; r0 < RW; r0 += 4 * NWARP) {
-                    float v[4];
-                    bool ok[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int r = r0 + u * NWARP;
-                        ok[u] = false;
-                        v[u] = 0.0f;
-                        if (r < RW) {
-                            const uint32_t x = c.tbl[r];
-                            const int ly = (x >> 16) & 0xff, w = x & 0xffff;
-                            const long long ro = c.rowoff[ly];
-                            ok[u] = ro >= 0 && ((c.zval[w] >> lane) & 1u);
-                            if (ok[u]) v[u] = __ldg(p.vals + ro + (32 * w + lane - 32));
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int r = r0 + u * NWARP;
-                        const uint32_t b = __ballot_sync(~0u, ok[u] && iso::below(v[u], c.level));
-                        if (lane == 0 && r < RW) sg[r] = b;
-                    }
+                const long long NWg = (c.nz + 31) / 32;
+                const long long w0 = c.Z0 / 32 - 1;
+                for (int r = tid; r < RW; r += BLOCK) {
+                    const uint32_t x = c.tbl[r];
+                    const int ly = (x >> 16) & 0xff, w = x & 0xffff;
+                    const int y = c.Y0 - 1 + ly;
+                    const long long gw = w0 + w;
+                    uint32_t b = 0;
+                    if (c.rowoff[ly] >= 0 && gw >= 0 && gw < NWg)
+                        b = __ldg(p.signs + ((long long)pl * c.ny + y) * NWg + gw) & c.zval[w];
+                    sg[r] = b;
                 }
             }
             __syncthreads();
@@ -530,9 +521,29 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                     }
                     const uint32_t VT = __shfl_sync(~0u, ia, 31), FT = __shfl_sync(~0u, ib, 31);
                     if (lane == 0) {
+                        // Staging is handed out in per-CTA blocks, so the global
+                        // counters see one atomic per block rather than per tile.
+                        // A tile of at least half a block gets an exact allocation;
+                        // smaller ones share blocks, abandoning a remainder smaller
+                        // than the tile (so at most half of any block is wasted).
+                        auto take = [&](uint32_t n, unsigned long long blkn, unsigned long long* ctr,
+                                        unsigned long long& cur, unsigned long long& end) {
+                            if (2ull * n >= blkn) return atomicAdd(ctr, (unsigned long long)n);
+                            if (cur + n > end) {
+                                cur = atomicAdd(ctr, blkn);
+                                end = cur + blkn;
+                            }
+                            const unsigned long long o = cur;
+                            cur += n;
+                            return o;
+                        };
                         unsigned long long vo = 0, fo = 0;
-                        if (VT) vo = atomicAdd(&p.ctr[1], (unsigned long long)VT);
-                        if (FT) fo = atomicAdd(&p.ctr[2], (unsigned long long)FT);
+                        if (VT) vo = take(VT, p.blkV, &p.ctr[1], c.misc[5], c.misc[6]);
+                        if (FT) fo = take(FT, p.blkF, &p.ctr[2], c.misc[7], c.misc[8]);
+                        if (tile / 1024 < p.nBlk) {
+                            atomicAdd(&p.blk[2 * (tile / 1024)], (unsigned long long)VT);
+                            atomicAdd(&p.blk[2 * (tile / 1024) + 1], (unsigned long long)FT);
+                        }
                         c.misc[1] = vo;
                         c.misc[2] = fo;
                         c.misc[3] = VT;
@@ -550,6 +561,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
                 const uint32_t VT = uint32_t(c.misc[3]), FT = uint32_t(c.misc[4]);
                 const bool vfit = vOff + VT <= (unsigned long long)p.capSV;
                 const bool ffit = fOff + FT <= (unsigned long long)p.capSF;
+                if (tid == 0 && (!vfit || !ffit)) atomicCAS(p.status, 0, int(ISO_ERR_OVERFLOW));
 
                 // T5a: staged vertices (position + key), one lane per point, in key order
                 if (VT && vfit) {
@@ -650,138 +662,200 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) mc_extract(const McParams
     }
 }
 
-// Exclusive prefix of per-tile counts (one CTA).
-__global__ void __launch_bounds__(1024) mc_tile_scan(const McTileRec* __restrict__ rec, uint2* pre,
-                                                     long long n, long long* counts, int* status,
-                                                     long long capV, long long capF) {
-    __shared__ unsigned long long wa[32], wb[32];
-    __shared__ unsigned long long carry[2];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) { carry[0] = 0; carry[1] = 0; }
-    __syncthreads();
-    for (long long base = 0; base < n; base += 1024) {
-        long long i = base + tid;
-        unsigned long long a = 0, b = 0;
-        if (i < n) { McTileRec r = rec[i]; a = r.vCnt; b = r.fCnt; }
-        unsigned long long ia = a, ib = b;
-        for (int d = 1; d < 32; d <<= 1) {
-            unsigned long long xa = __shfl_up_sync(~0u, ia, d), xb = __shfl_up_sync(~0u, ib, d);
-            if (lane >= d) { ia += xa; ib += xb; }
-        }
-        if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long va = wa[lane], vb = wb[lane];
-            for (int d = 1; d < 32; d <<= 1) {
-                unsigned long long xa = __shfl_up_sync(~0u, va, d), xb = __shfl_up_sync(~0u, vb, d);
-                if (lane >= d) { va += xa; vb += xb; }
+// Sign bitmap of the whole grid: bit z % 32 of word [(x * ny + y) * NWg + z / 32]
+// is (v - level < 0).  One warp per grid row, all of the row's loads in flight
+// before the ballots; lane w keeps word w so each 32 words leave in one store.
+constexpr int SIGN_BLOCK = 256;
+constexpr int SIGN_UNROLL = 16;
+
+__global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__ vals, long long rows,
+                                                       int nz, float level, uint32_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int NWg = (nz + 31) / 32;
+    const long long warps = (long long)gridDim.x * (SIGN_BLOCK / 32);
+    for (long long row = (long long)blockIdx.x * (SIGN_BLOCK / 32) + (threadIdx.x >> 5); row < rows;
+         row += warps) {
+        const float* rp = vals + row * nz;
+        uint32_t* op = out + row * NWg;
+        for (int wb = 0; wb < NWg; wb += 32) {
+            uint32_t mine = 0;
+            for (int w0 = wb; w0 < min(NWg, wb + 32); w0 += SIGN_UNROLL) {
+                float v[SIGN_UNROLL];
+#pragma unroll
+                for (int u = 0; u < SIGN_UNROLL; ++u) {
+                    const int z = 32 * (w0 + u) + lane;
+                    v[u] = (w0 + u < NWg && z < nz) ? __ldg(rp + z) : level;
+                }
+#pragma unroll
+                for (int u = 0; u < SIGN_UNROLL; ++u) {
+                    const uint32_t b = __ballot_sync(~0u, iso::below(v[u], level));
+                    if (((w0 + u) & 31) == lane) mine = b;
+                }
             }
-            wa[lane] = va;
-            wb[lane] = vb;
+            if (wb + lane < NWg) op[wb + lane] = mine;
         }
-        __syncthreads();
-        unsigned long long ea = carry[0] + (warp ? wa[warp - 1] : 0ull) + ia - a;
-        unsigned long long eb = carry[1] + (warp ? wb[warp - 1] : 0ull) + ib - b;
-        if (i < n) pre[i] = make_uint2(uint32_t(ea), uint32_t(eb));
-        __syncthreads();
-        if (tid == 0) { carry[0] += wa[31]; carry[1] += wb[31]; }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        counts[0] = (long long)carry[0];
-        counts[1] = (long long)carry[1];
-        if ((long long)carry[0] > capV || (long long)carry[1] > capF)
-            atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
     }
 }
 
-// Final vertices and faces of one tile.
-constexpr int RES_BLOCK = 128;
-constexpr int RES_KCAP = 2048;
+// Exclusive prefix of per-tile counts: CTA b scans tiles [1024 b, 1024 b + 1024)
+// and adds the totals of earlier blocks (accumulated by the extract kernel).
+__global__ void __launch_bounds__(1024) mc_tile_scan(const McTileRec* __restrict__ rec, uint2* pre,
+                                                     const unsigned long long* __restrict__ blk,
+                                                     long long n, long long nBlk, long long* counts,
+                                                     int* status, long long capV, long long capF) {
+    __shared__ unsigned long long wa[32], wb[32];
+    __shared__ unsigned long long base[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long b = blockIdx.x;
+    // prefix of earlier blocks
+    unsigned long long pa = 0, pb = 0;
+    for (long long k = tid; k < b; k += 1024) { pa += blk[2 * k]; pb += blk[2 * k + 1]; }
+    for (int d = 16; d >= 1; d >>= 1) {
+        pa += __shfl_down_sync(~0u, pa, d);
+        pb += __shfl_down_sync(~0u, pb, d);
+    }
+    if (lane == 0) { wa[warp] = pa; wb[warp] = pb; }
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long x = wa[lane], y = wb[lane];
+        for (int d = 16; d >= 1; d >>= 1) {
+            x += __shfl_down_sync(~0u, x, d);
+            y += __shfl_down_sync(~0u, y, d);
+        }
+        if (lane == 0) { base[0] = x; base[1] = y; }
+    }
+    __syncthreads();
+    const long long i = b * 1024 + tid;
+    unsigned long long a = 0, c = 0;
+    if (i < n) { const McTileRec r = rec[i]; a = r.vCnt; c = r.fCnt; }
+    unsigned long long ia = a, ic = c;
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long xa = __shfl_up_sync(~0u, ia, d), xc = __shfl_up_sync(~0u, ic, d);
+        if (lane >= d) { ia += xa; ic += xc; }
+    }
+    if (lane == 31) { wa[warp] = ia; wb[warp] = ic; }
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long va = wa[lane], vc = wb[lane];
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long xa = __shfl_up_sync(~0u, va, d), xc = __shfl_up_sync(~0u, vc, d);
+            if (lane >= d) { va += xa; vc += xc; }
+        }
+        wa[lane] = va;
+        wb[lane] = vc;
+    }
+    __syncthreads();
+    const unsigned long long ea = base[0] + (warp ? wa[warp - 1] : 0ull) + ia - a;
+    const unsigned long long ec = base[1] + (warp ? wb[warp - 1] : 0ull) + ic - c;
+    if (i < n) pre[i] = make_uint2(uint32_t(ea), uint32_t(ec));
+    if (b == nBlk - 1 && tid == 1023) {
+        const long long V = (long long)(base[0] + wa[31]), F = (long long)(base[1] + wb[31]);
+        counts[0] = V;
+        counts[1] = F;
+        if (V > capV || F > capF) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+    }
+}
+
+// Final vertices and faces; one warp per tile.  Face references are resolved by
+// binary search in the key lists of the (up to 8) tiles they can point to.
+constexpr int RES_BLOCK = 256;
+constexpr int RES_KCAP = 512;  // staged keys per warp
 
 __global__ void __launch_bounds__(RES_BLOCK) mc_resolve(const McParams p) {
     const McTiles& T = p.t;
-    const long long tile = blockIdx.x;
-    const McTileRec rec = p.rec[tile];
-    if (rec.vCnt == 0 && rec.fCnt == 0) return;
-    const uint2 pre = p.pre[tile];
-    const int tid = threadIdx.x;
-    const bool vfit = (unsigned long long)rec.vOff + rec.vCnt <= (unsigned long long)p.capSV;
-    const bool ffit = (unsigned long long)rec.fOff + rec.fCnt <= (unsigned long long)p.capSF;
-    for (uint32_t i = tid; i < rec.vCnt && vfit; i += RES_BLOCK) {
-        long long o = (long long)pre.x + i;
-        if (o >= p.capV) break;
-        float4 v = p.sv[rec.vOff + i];
-        p.vout[3 * o + 0] = v.x;
-        p.vout[3 * o + 1] = v.y;
-        p.vout[3 * o + 2] = v.z;
-    }
-    if (rec.fCnt == 0 || !ffit) return;
-
-    // Stage the key lists of the tiles faces may refer to (slot bits: plane,
-    // row group, z chunk one step back).
-    __shared__ uint32_t keys[RES_KCAP];
-    __shared__ uint32_t segOff[8], segLen[8], segBase[8], segVOff[8];
-    __shared__ int useGlobal;
-    const int zt = int(tile % T.nZT);
-    const int rt = int((tile / T.nZT) % T.nRT);
-    const int P = int(tile / ((long long)T.nZT * T.nRT));
-    if (tid == 0) {
-        uint32_t tot = 0;
-        for (int sl = 0; sl < 8; ++sl) {
-            int pp = P - (sl >> 2), rr = rt - ((sl >> 1) & 1), zz = zt - (sl & 1);
-            segOff[sl] = tot;
-            segLen[sl] = 0;
-            segBase[sl] = 0;
-            segVOff[sl] = 0;
-            if (pp < 0 || rr < 0 || zz < 0) continue;
-            long long t2 = ((long long)pp * T.nRT + rr) * T.nZT + zz;
-            McTileRec r2 = p.rec[t2];
-            // a neighbour whose staging did not fit has no keys to search (the
-            // scan already flagged the overflow; the caller retries)
-            if ((unsigned long long)r2.vOff + r2.vCnt > (unsigned long long)p.capSV) continue;
-            segLen[sl] = r2.vCnt;
-            segBase[sl] = p.pre[t2].x;
-            segVOff[sl] = r2.vOff;
-            tot += r2.vCnt;
+    __shared__ uint32_t keys_all[RES_BLOCK / 32][RES_KCAP];
+    __shared__ uint32_t seg_all[RES_BLOCK / 32][4][8];  // len, off, base, voff per slot
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* keys = keys_all[warp];
+    uint32_t(*seg)[8] = seg_all[warp];
+    const long long stride = (long long)gridDim.x * (RES_BLOCK / 32);
+    for (long long tile = (long long)blockIdx.x * (RES_BLOCK / 32) + warp; tile < T.nTiles;
+         tile += stride) {
+        const McTileRec rec = p.rec[tile];
+        if (rec.vCnt == 0 && rec.fCnt == 0) continue;
+        const uint2 pre = p.pre[tile];
+        const bool vfit = (unsigned long long)rec.vOff + rec.vCnt <= (unsigned long long)p.capSV;
+        const bool ffit = (unsigned long long)rec.fOff + rec.fCnt <= (unsigned long long)p.capSF;
+        for (uint32_t i = lane; i < rec.vCnt && vfit; i += 32) {
+            const long long o = (long long)pre.x + i;
+            if (o >= p.capV) break;
+            const float4 v = p.sv[rec.vOff + i];
+            p.vout[3 * o + 0] = v.x;
+            p.vout[3 * o + 1] = v.y;
+            p.vout[3 * o + 2] = v.z;
         }
-        useGlobal = tot > RES_KCAP;
-    }
-    __syncthreads();
-    if (!useGlobal) {
-        for (int sl = 0; sl < 8; ++sl) {
-            for (uint32_t i = tid; i < segLen[sl]; i += RES_BLOCK)
-                keys[segOff[sl] + i] = __float_as_uint(p.sv[segVOff[sl] + i].w);
+        if (rec.fCnt == 0 || !ffit) continue;
+        // neighbour key lists: lane sl < 8 reads slot sl (plane, row group,
+        // z chunk one step back per bit)
+        const int zt = int(tile % T.nZT);
+        const int rt = int((tile / T.nZT) % T.nRT);
+        const int P = int(tile / ((long long)T.nZT * T.nRT));
+        uint32_t sLen = 0, sBase = 0, sVOff = 0;
+        if (lane < 8) {
+            const int pp = P - (lane >> 2), rr = rt - ((lane >> 1) & 1), zz = zt - (lane & 1);
+            if (pp >= 0 && rr >= 0 && zz >= 0) {
+                const long long t2 = ((long long)pp * T.nRT + rr) * T.nZT + zz;
+                const McTileRec r2 = p.rec[t2];
+                if ((unsigned long long)r2.vOff + r2.vCnt <= (unsigned long long)p.capSV) {
+                    sLen = r2.vCnt;
+                    sVOff = r2.vOff;
+                    sBase = p.pre[t2].x;
+                }
+            }
         }
-    }
-    __syncthreads();
-    for (uint32_t f = tid; f < rec.fCnt; f += RES_BLOCK) {
-        long long o = (long long)pre.y + f;
-        if (o >= p.capF) break;
-        const uint32_t* src = p.sf + 3ull * (rec.fOff + f);
+        uint32_t incl = sLen;
+        for (int d = 1; d < 8; d <<= 1) {
+            const uint32_t x = __shfl_up_sync(~0u, incl, d);
+            if (lane >= d) incl += x;
+        }
+        const uint32_t total = __shfl_sync(~0u, incl, 7);
+        const uint32_t sOff = incl - sLen;
+        const bool staged = total <= RES_KCAP;
+        if (lane < 8) {
+            seg[0][lane] = sLen;
+            seg[1][lane] = sOff;
+            seg[2][lane] = sBase;
+            seg[3][lane] = sVOff;
+        }
+        if (staged) {
+            for (int sl = 0; sl < 8; ++sl) {
+                const uint32_t len = __shfl_sync(~0u, sLen, sl), off = __shfl_sync(~0u, sOff, sl);
+                const uint32_t vo = __shfl_sync(~0u, sVOff, sl);
+                for (uint32_t i = lane; i < len; i += 32) keys[off + i] = __float_as_uint(p.sv[vo + i].w);
+            }
+        }
+        __syncwarp();
+        for (uint32_t f = lane; f < rec.fCnt; f += 32) {
+            const long long o = (long long)pre.y + f;
+            if (o >= p.capF) break;
+            const uint32_t* src = p.sf + 3ull * (rec.fOff + f);
 #pragma unroll
-        for (int m = 0; m < 3; ++m) {
-            uint32_t ref = src[m];
-            uint32_t sl = ref >> 24, local = ref & 0xffffffu;
-            uint32_t lo = 0, hi = segLen[sl];
-            while (lo < hi) {
-                uint32_t mid = (lo + hi) >> 1;
-                uint32_t k = useGlobal ? __float_as_uint(p.sv[segVOff[sl] + mid].w)
-                                       : keys[segOff[sl] + mid];
-                if (k < local) lo = mid + 1; else hi = mid;
+            for (int m = 0; m < 3; ++m) {
+                const uint32_t ref = src[m];
+                const int sl = int(ref >> 24);
+                const uint32_t local = ref & 0xffffffu;
+                const uint32_t segLen = seg[0][sl], segOff = seg[1][sl];
+                const uint32_t segBase = seg[2][sl], segVOff = seg[3][sl];
+                uint32_t lo = 0, hi = segLen;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    const uint32_t k = staged ? keys[segOff + mid] : __float_as_uint(p.sv[segVOff + mid].w);
+                    if (k < local) lo = mid + 1; else hi = mid;
+                }
+                const uint32_t k = lo < segLen ? (staged ? keys[segOff + lo]
+                                                         : __float_as_uint(p.sv[segVOff + lo].w))
+                                               : 0xffffffffu;
+                int idx;
+                if (k == local) {
+                    idx = int(segBase + lo);
+                } else {
+                    atomicCAS(p.status, 0, int(ISO_ERR_LOOKUP));
+                    idx = -1;
+                }
+                p.fout[3 * o + m] = idx;
             }
-            uint32_t k = lo < segLen[sl] ? (useGlobal ? __float_as_uint(p.sv[segVOff[sl] + lo].w)
-                                                      : keys[segOff[sl] + lo])
-                                         : 0xffffffffu;
-            int idx;
-            if (k == local) {
-                idx = int(segBase[sl] + lo);
-            } else {
-                atomicCAS(p.status, 0, int(ISO_ERR_LOOKUP));
-                idx = -1;
-            }
-            p.fout[3 * o + m] = idx;
         }
+        __syncwarp();
     }
 }
 
@@ -795,6 +869,7 @@ int launch_extract(const McParams& p, cudaStream_t st) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, BLOCK, p.t.smemBytes) != cudaSuccess ||
         per < 1)
         per = 1;
+    per = std::min(per, std::max(1, p.t.ctasPerSm));  // staging slack assumes at most this many
     long long grid = (long long)sms * per;
     if (grid > p.t.nItems) grid = p.t.nItems;
     if (grid < 1) grid = 1;
@@ -845,8 +920,18 @@ int mc_plan_tiles(int nx, int ny, int nz, int rows, int slabs, int threads, int 
     if ((long long)R * ZC * 4 >= (1ll << 24)) return ISO_ERR_ARG;
     const Layout L = make_layout(t);
     t.smemBytes = L.total;
-    t.ctasPerSm = std::max(1, int((size_t(228) * 1024) / (L.total + 1024)));
-    if (t.ctasPerSm > 8) t.ctasPerSm = 8;
+    {
+        int per = 0;
+        cudaError_t e;
+        if (t.threads == 512) {
+            cudaFuncSetAttribute(mc_extract<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.total));
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_extract<512>, 512, L.total);
+        } else {
+            cudaFuncSetAttribute(mc_extract<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.total));
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_extract<256>, 256, L.total);
+        }
+        t.ctasPerSm = (e == cudaSuccess && per > 0) ? per : 1;
+    }
     // Work items: aim for several per CTA.
     long long cols = (long long)t.nRT * t.nZT;
     long long ctas = (long long)std::max(1, sm_count) * t.ctasPerSm;
@@ -876,13 +961,35 @@ float mc_snap_tau(const float amin[3], const float amax[3], const int n[3]) {
     return tau >= 0.5 ? 1.0f : float(tau);
 }
 
+// Staging blocks handed to a CTA at a time, and the slack they can leave unused.
+static void staging_blocks(const McTiles& t, long long capV, long long capF, unsigned long long* bv,
+                           unsigned long long* bf, long long* slackV, long long* slackF) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long ctas = (long long)sms * std::max(1, t.ctasPerSm);  // resident extract CTAs
+    *bv = (unsigned long long)std::min<long long>(4096, std::max<long long>(64, capV / (4 * ctas) + 1));
+    *bf = (unsigned long long)std::min<long long>(8192, std::max<long long>(64, capF / (4 * ctas) + 1));
+    // block waste is below half of the block-allocated total, plus one open
+    // block per CTA: capacity 2 * cap + ctas * block is always enough
+    *slackV = capV + ctas * (long long)*bv;
+    *slackF = capF + ctas * (long long)*bf;
+    (void)t;
+}
+
 size_t mc_workspace_bytes(const McTiles& t, long long capV, long long capF) {
+    unsigned long long bv, bf;
+    long long sv, sf;
+    staging_blocks(t, capV, capF, &bv, &bf, &sv, &sf);
+    const long long nBlk = (t.nTiles + 1023) / 1024;
     size_t o = 0;
     o = al16(o + size_t(t.nTiles) * sizeof(McTileRec));
     o = al16(o + size_t(t.nTiles) * sizeof(uint2));
-    o = al16(o + size_t(std::max<long long>(capV, 1)) * sizeof(float4));
-    o = al16(o + size_t(std::max<long long>(capF, 1)) * 3 * sizeof(uint32_t));
+    o = al16(o + size_t(std::max<long long>(capV + sv, 1)) * sizeof(float4));
+    o = al16(o + size_t(std::max<long long>(capF + sf, 1)) * 3 * sizeof(uint32_t));
+    o = al16(o + size_t(nBlk) * 2 * sizeof(unsigned long long));
     o = al16(o + 4 * sizeof(unsigned long long));
+    o = al16(o + size_t(t.nx) * t.ny * ((t.nz + 31) / 32) * sizeof(uint32_t));
     return o + 256;
 }
 
@@ -891,18 +998,37 @@ int mc_launch(const McParams& p0, void* ws, size_t ws_bytes, cudaStream_t st) {
     const McTiles& t = p.t;
     const size_t need = mc_workspace_bytes(t, p.capV, p.capF);
     if (ws_bytes < need) return ISO_ERR_WORKSPACE;
+    long long slackV, slackF;
+    staging_blocks(t, p.capV, p.capF, &p.blkV, &p.blkF, &slackV, &slackF);
+    p.nBlk = (t.nTiles + 1023) / 1024;
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     size_t o = 0;
     p.rec = reinterpret_cast<McTileRec*>(b + o); o = al16(o + size_t(t.nTiles) * sizeof(McTileRec));
     p.pre = reinterpret_cast<uint2*>(b + o);     o = al16(o + size_t(t.nTiles) * sizeof(uint2));
-    p.sv = reinterpret_cast<float4*>(b + o);     o = al16(o + size_t(std::max<long long>(p.capV, 1)) * sizeof(float4));
-    p.sf = reinterpret_cast<uint32_t*>(b + o);   o = al16(o + size_t(std::max<long long>(p.capF, 1)) * 3 * sizeof(uint32_t));
-    p.ctr = reinterpret_cast<unsigned long long*>(b + o);
-    p.capSV = p.capV;
-    p.capSF = p.capF;
+    p.capSV = p.capV + slackV;
+    p.capSF = p.capF + slackF;
+    p.sv = reinterpret_cast<float4*>(b + o);     o = al16(o + size_t(std::max<long long>(p.capSV, 1)) * sizeof(float4));
+    p.sf = reinterpret_cast<uint32_t*>(b + o);   o = al16(o + size_t(std::max<long long>(p.capSF, 1)) * 3 * sizeof(uint32_t));
+    p.blk = reinterpret_cast<unsigned long long*>(b + o); o = al16(o + size_t(p.nBlk) * 2 * sizeof(unsigned long long));
+    p.ctr = reinterpret_cast<unsigned long long*>(b + o); o = al16(o + 4 * sizeof(unsigned long long));
+    p.signs = reinterpret_cast<uint32_t*>(b + o);
+    if (cudaMemsetAsync(p.blk, 0, size_t(p.nBlk) * 2 * sizeof(unsigned long long) + 64, st) !=
+        cudaSuccess)
+        return ISO_ERR_CUDA;
     if (cudaMemsetAsync(p.ctr, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess)
         return ISO_ERR_CUDA;
     if (t.nTiles > 0x7fffffffll) return ISO_ERR_ARG;
+    {
+        iso::ProfScope ps("mc_signs", st);
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long rows = (long long)t.nx * t.ny;
+        const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
+        const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sms * 32));
+        mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(p.vals, rows, t.nz, p.level, p.signs);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
     {
         iso::ProfScope ps("mc_extract", st);
         int rc = t.threads == 512 ? launch_extract<512>(p, st) : launch_extract<256>(p, st);
@@ -910,12 +1036,18 @@ int mc_launch(const McParams& p0, void* ws, size_t ws_bytes, cudaStream_t st) {
     }
     {
         iso::ProfScope ps("mc_tile_scan", st);
-        mc_tile_scan<<<1, 1024, 0, st>>>(p.rec, p.pre, t.nTiles, p.counts, p.status, p.capV, p.capF);
+        mc_tile_scan<<<unsigned(p.nBlk), 1024, 0, st>>>(p.rec, p.pre, p.blk, t.nTiles, p.nBlk, p.counts,
+                                                       p.status, p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
         iso::ProfScope ps("mc_resolve", st);
-        mc_resolve<<<unsigned(t.nTiles), RES_BLOCK, 0, st>>>(p);
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long want = (t.nTiles + (RES_BLOCK / 32) - 1) / (RES_BLOCK / 32);
+        const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
+        mc_resolve<<<unsigned(grid), RES_BLOCK, 0, st>>>(p);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     return 0;

@@ -56,6 +56,10 @@ struct McParams {
     float4* sv;                     // staged vertices: x, y, z, key bits
     uint32_t* sf;                   // staged faces: 3 key references each
     unsigned long long* ctr;        // [0] items ticket, [1] V alloc, [2] F alloc
+    unsigned long long* blk;        // per 1024 tiles: (sum V, sum F)
+    uint32_t* signs;                // sign bitmap [nx][ny][ceil(nz / 32)]
+    long long nBlk;                 // number of 1024-tile blocks
+    unsigned long long blkV, blkF;  // staging block sizes handed to a CTA at a time
     int* status;                    // device status word
     long long capSV, capSF;         // staging capacities
     // outputs
