@@ -85,6 +85,48 @@ int iso_mc_dense(const float *values, int nx, int ny, int nz, const float *aabb_
                  long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
                  size_t workspace_bytes, long long *counts, int *status, void *stream);
 
+/* ---- dual contouring on a dense grid --------------------------------------
+ * Replaces isoext_ext.get_intersection / dual_contouring (src/isoext_ext.cu:
+ * 329-378 -> get_intersection src/its.cu:94-159, compute_intersection_normals
+ * :272-283, dual_contouring src/dc.cu:162-218).  The caller runs the steps in
+ * order on one stream and sizes buffers from the counts between them:
+ *   classify -> (A active cells, K crossings) -> intersect -> [normals] ->
+ *   solve -> quads_count -> (Q quads) -> quads_emit -> weld_count -> (V) ->
+ *   weld_write.  `ws` is one workspace of iso_dc_workspace_size bytes shared by
+ *   classify / intersect / cells / quads. */
+size_t iso_dc_workspace_size(int nx, int ny, int nz);
+/* Sign bitmap and per-word counts; counts (device int64[2]) <- (A, K). */
+int iso_dc_classify(const float *values, int nx, int ny, int nz, float level, void *ws,
+                    size_t ws_bytes, long long *counts, void *stream);
+/* Crossing points [K,3], optional normals [K,3] (NULL: none), active cell ids
+ * [A] and CSR offsets [A+1] -- isoext's Intersection arrays. */
+int iso_dc_intersect(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                     const float *aabb_max, float level, void *ws, long long A, long long K,
+                     float *points, float *normals, int *cell_ids, int *cell_offsets, void *stream);
+/* Normals of existing crossings from the grid (src/its.cu:186-268). */
+int iso_dc_normals(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                   const float *aabb_max, const float *points, const int *cell_ids,
+                   const int *cell_offsets, long long A, float *normals, void *stream);
+/* Dual vertex per active cell: QEF (src/dc.cu:14-65), pseudo-inverse with the
+ * s > svd_tol * s_max rule (src/batched_la.cu:152-178), clip (src/dc.cu:82-99). */
+int iso_dc_solve(int nx, int ny, int nz, const float *aabb_min, const float *aabb_max,
+                 const float *points, const float *normals, const int *cell_ids,
+                 const int *cell_offsets, long long A, float reg, float svd_tol, float *dual,
+                 void *stream);
+/* Active-cell masks only (an intersection computed by an earlier call). */
+int iso_dc_cells(const float *values, int nx, int ny, int nz, float level, void *ws, void *stream);
+/* Quads: count (counts[0] <- Q), then 6 dual indices per quad in isoext's
+ * order (src/grid/uniform.cu:60-83, src/dc.cu:101-157). */
+int iso_dc_quads_count(int nx, int ny, int nz, void *ws, long long *counts, void *stream);
+int iso_dc_quads_emit(int nx, int ny, int nz, void *ws, const float *dual, int *tri, void *stream);
+/* Weld dual vertices by exact position (src/utils.cu:32-59): count V
+ * (counts[0]), then write vertices [V,3] and faces [ntri/3,3]. */
+size_t iso_dc_weld_workspace_size(long long A);
+int iso_dc_weld_count(const float *dual, long long A, const int *tri, long long ntri, void *ws,
+                      size_t ws_bytes, long long *counts, int *status, void *stream);
+int iso_dc_weld_write(const float *dual, long long A, const int *tri, long long ntri, void *ws,
+                      float *vout, int *fout, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,12 +9,20 @@ The extraction functions run hand-written sm_103a kernels through the C ABI of
 ``_lib/libisoext_gb300.so`` (include/isoext_gb300.h); there is no CPU fallback.
 """
 
+from .dc import Intersection, dual_contouring, get_intersection
 from .grids import FLT_MAX, Grid, UniformGrid
 from .mc import marching_cubes
+from .utils import gaussian_smooth, make_grid, write_obj
 
 __all__ = [
     "FLT_MAX",
     "Grid",
+    "Intersection",
     "UniformGrid",
+    "dual_contouring",
+    "gaussian_smooth",
+    "get_intersection",
+    "make_grid",
     "marching_cubes",
+    "write_obj",
 ]

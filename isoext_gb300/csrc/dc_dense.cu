@@ -1,0 +1,902 @@
+// Dual contouring on a dense grid (sm_103a).
+//
+// Steps (each a C entry point; the Python layer sizes buffers between them):
+//   classify   sign bitmap (mc_signs) and, per 32-cell word, the number of
+//              active cells and crossings, summed per block of 1024 words.
+//   intersect  crossing points (lerp, the reference's arithmetic), optional
+//              normals from the cell's trilinear interpolant, active cell ids
+//              and CSR offsets -- isoext's Intersection (src/its.cu:94-283).
+//   solve      per active cell: QEF normal equations accumulated in the
+//              reference's order (src/dc.cu:14-65), a register-resident 3x3
+//              symmetric Jacobi solve in FP32 with the reference's pseudo-inverse
+//              threshold (src/batched_la.cu:152-178) refined once with an FP64
+//              residual, clipped to the cell (src/dc.cu:82-99).
+//   quads      crossed grid edges in the reference's quad order (by low
+//              endpoint, then z, y, x edge; src/grid/uniform.cu:60-83), their 4
+//              cells, orientation and diagonal split (src/dc.cu:101-157).
+//   weld       dual vertices used by faces, merged by exact position with a
+//              hash table (isoext welds by sorted position, src/utils.cu:32-59).
+#include <algorithm>
+#include <cstdint>
+
+#include "common.cuh"
+#define ISO_LUT_DECL static __constant__ const
+#include "luts.h"
+#include "profile.cuh"
+
+namespace {
+
+constexpr int DC_BLOCK = 1024;
+
+struct Grid3 {
+    int nx, ny, nz;
+    float amin[3], asize[3];
+};
+
+__device__ __forceinline__ float coord(const Grid3& g, int axis, uint32_t i) {
+    const uint32_t n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    return iso::grid_coord(i, n, g.amin[axis], g.asize[axis]);
+}
+
+// Sign words of a grid row (x, y), aligned to z = 0.
+__device__ __forceinline__ const uint32_t* srow(const uint32_t* S, const Grid3& g, int x, int y) {
+    const int NWg = (g.nz + 31) / 32;
+    return S + ((long long)x * g.ny + y) * NWg;
+}
+__device__ __forceinline__ uint32_t word_or0(const uint32_t* row, int w, int nw) {
+    return (w >= 0 && w < nw) ? row[w] : 0u;
+}
+
+// Active-cell mask of cell word (cx, cy, w): cells z in [32w, 32w+32).
+__device__ __forceinline__ uint32_t cell_act(const uint32_t* S, const Grid3& g, int cx, int cy, int w,
+                                             uint32_t* cw8) {
+    const int NWg = (g.nz + 31) / 32;
+    uint32_t and8 = ~0u, or8 = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t* r = srow(S, g, cx + (k >> 1), cy + (k & 1));
+        const uint32_t a = r[w];
+        const uint32_t b = __funnelshift_r(a, word_or0(r, w + 1, NWg), 1);  // bit z <- z + 1
+        cw8[2 * k] = a;
+        cw8[2 * k + 1] = b;
+        and8 &= a & b;
+        or8 |= a | b;
+    }
+    return (or8 & ~and8) & iso::range_mask(w, 0, g.nz - 2);  // cells z <= nz - 2
+}
+// Case bits of cell at bit b of a cell word, from the 8 corner words cw8
+// (index 2k = dz 0, 2k+1 = dz 1 for (dx, dy) = (k >> 1, k & 1)).
+__device__ __forceinline__ uint32_t case_of(const uint32_t* cw8, int b) {
+    uint32_t cs = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int dx = k >> 1, dy = k & 1;
+        cs |= ((cw8[2 * k] >> b) & 1u) << (4 * dx + 2 * dy);
+        cs |= ((cw8[2 * k + 1] >> b) & 1u) << (4 * dx + 2 * dy + 1);
+    }
+    return cs;
+}
+
+// Block-wide exclusive scan of two values per thread (DC_BLOCK threads).
+__device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea, uint32_t& eb,
+                                            uint32_t& ta, uint32_t& tb, uint32_t* sm /*66*/) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t ia = a, ib = b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(~0u, ia, d), y = __shfl_up_sync(~0u, ib, d);
+        if (lane >= d) { ia += x; ib += y; }
+    }
+    if (lane == 31) { sm[warp] = ia; sm[32 + warp] = ib; }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t x = sm[lane], y = sm[32 + lane];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(~0u, x, d), v = __shfl_up_sync(~0u, y, d);
+            if (lane >= d) { x += u; y += v; }
+        }
+        sm[lane] = x;
+        sm[32 + lane] = y;
+    }
+    __syncthreads();
+    ea = (warp ? sm[warp - 1] : 0u) + ia - a;
+    eb = (warp ? sm[32 + warp - 1] : 0u) + ib - b;
+    ta = sm[31];
+    tb = sm[63];
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// classify: per cell word, active cells and crossings; block sums.
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_cell_count(const uint32_t* __restrict__ S, Grid3 g,
+                                                          long long nwords,
+                                                          unsigned long long* __restrict__ blk) {
+    __shared__ uint32_t sm[66];
+    const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    uint32_t na = 0, nk = 0;
+    if (i < nwords) {
+        const int NWc = (g.nz - 1 + 31) / 32;
+        const int w = int(i % NWc);
+        const long long r = i / NWc;
+        const int cy = int(r % (g.ny - 1)), cx = int(r / (g.ny - 1));
+        uint32_t cw8[8];
+        uint32_t act = cell_act(S, g, cx, cy, w, cw8);
+        na = __popc(act);
+        while (act) {
+            const int b = __ffs(act) - 1;
+            act &= act - 1;
+            nk += __popc(uint32_t(ISO_EDGE_STATUS[case_of(cw8, b)]));
+        }
+    }
+    uint32_t ea, ek, ta, tk;
+    block_scan2(na, nk, ea, ek, ta, tk, sm);
+    if (threadIdx.x == 0) {
+        blk[2 * blockIdx.x] = ta;
+        blk[2 * blockIdx.x + 1] = tk;
+    }
+}
+
+// Exclusive scan of block sums (one CTA; pairs of u64).
+__global__ void __launch_bounds__(1024) dc_block_scan(unsigned long long* blk, long long nblk,
+                                                      long long* totals) {
+    __shared__ unsigned long long wa[32], wb[32], carry[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) { carry[0] = 0; carry[1] = 0; }
+    __syncthreads();
+    for (long long base = 0; base < nblk; base += 1024) {
+        const long long i = base + tid;
+        const unsigned long long a = i < nblk ? blk[2 * i] : 0ull, b = i < nblk ? blk[2 * i + 1] : 0ull;
+        unsigned long long ia = a, ib = b;
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long x = __shfl_up_sync(~0u, ia, d), y = __shfl_up_sync(~0u, ib, d);
+            if (lane >= d) { ia += x; ib += y; }
+        }
+        if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long x = wa[lane], y = wb[lane];
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long u = __shfl_up_sync(~0u, x, d), v = __shfl_up_sync(~0u, y, d);
+                if (lane >= d) { x += u; y += v; }
+            }
+            wa[lane] = x;
+            wb[lane] = y;
+        }
+        __syncthreads();
+        const unsigned long long ea = carry[0] + (warp ? wa[warp - 1] : 0ull) + ia - a;
+        const unsigned long long eb = carry[1] + (warp ? wb[warp - 1] : 0ull) + ib - b;
+        if (i < nblk) { blk[2 * i] = ea; blk[2 * i + 1] = eb; }
+        __syncthreads();
+        if (tid == 0) { carry[0] += wa[31]; carry[1] += wb[31]; }
+        __syncthreads();
+    }
+    if (tid == 0) { totals[0] = (long long)carry[0]; totals[1] = (long long)carry[1]; }
+}
+
+// ---------------------------------------------------------------------------
+// intersect: crossing points / normals, active cells, CSR offsets; also the
+// per-word active mask and exclusive active-cell prefix used by the quads.
+
+struct CellCorners {
+    float v[8];
+    float p[8][3];
+};
+
+__device__ __forceinline__ void load_cell(const float* vals, const Grid3& g, int cx, int cy, int cz,
+                                          CellCorners& cc) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int x = cx + (k >> 2), y = cy + ((k >> 1) & 1), z = cz + (k & 1);
+        cc.v[k] = __ldg(vals + ((long long)x * g.ny + y) * g.nz + z);
+        cc.p[k][0] = coord(g, 0, uint32_t(x));
+        cc.p[k][1] = coord(g, 1, uint32_t(y));
+        cc.p[k][2] = coord(g, 2, uint32_t(z));
+    }
+}
+
+// Trilinear interpolation at t in [0,1]^3 (src/its.cu:170-184).
+__device__ __forceinline__ float trilin(const float* cv, float tx, float ty, float tz) {
+    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
+    const float c00 = __fadd_rn(__fmul_rn(cv[0], oz), __fmul_rn(cv[1], tz));
+    const float c01 = __fadd_rn(__fmul_rn(cv[2], oz), __fmul_rn(cv[3], tz));
+    const float c10 = __fadd_rn(__fmul_rn(cv[4], oz), __fmul_rn(cv[5], tz));
+    const float c11 = __fadd_rn(__fmul_rn(cv[6], oz), __fmul_rn(cv[7], tz));
+    const float c0 = __fadd_rn(__fmul_rn(c00, oy), __fmul_rn(c01, ty));
+    const float c1 = __fadd_rn(__fmul_rn(c10, oy), __fmul_rn(c11, ty));
+    return __fadd_rn(__fmul_rn(c0, ox), __fmul_rn(c1, tx));
+}
+
+// Normal at crossing point p of a cell (src/its.cu:186-268).
+__device__ __forceinline__ void cell_normal(const CellCorners& cc, const float* p, float* n) {
+    float cmin[3], csz[3], t[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cmin[a] = cc.p[0][a];
+        csz[a] = __fsub_rn(cc.p[7][a], cc.p[0][a]);
+        t[a] = __fdiv_rn(__fsub_rn(p[a], cmin[a]), csz[a]);
+        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
+    }
+    const float eps = 0.02f;
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float tp[3] = {t[0], t[1], t[2]}, tm[3] = {t[0], t[1], t[2]};
+        tp[a] = fminf(__fadd_rn(t[a], eps), 0.99f);
+        tm[a] = fmaxf(__fsub_rn(t[a], eps), 0.01f);
+        const float fp = trilin(cc.v, tp[0], tp[1], tp[2]);
+        const float fm = trilin(cc.v, tm[0], tm[1], tm[2]);
+        d[a] = __fdiv_rn(__fsub_rn(fp, fm), __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]));
+    }
+    const float len =
+        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+    if (len > 1e-8f) {
+        n[0] = __fdiv_rn(d[0], len);
+        n[1] = __fdiv_rn(d[1], len);
+        n[2] = __fdiv_rn(d[2], len);
+    } else {
+        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
+    }
+}
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict__ vals,
+                                                         const uint32_t* __restrict__ S, Grid3 g,
+                                                         float level, long long nwords,
+                                                         const unsigned long long* __restrict__ blk,
+                                                         uint32_t* __restrict__ actm,
+                                                         uint32_t* __restrict__ offA, float* points,
+                                                         float* normals, uint32_t* cell_ids,
+                                                         uint32_t* cell_off, long long A, long long K) {
+    __shared__ uint32_t sm[66];
+    const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    const int NWc = (g.nz - 1 + 31) / 32;
+    uint32_t act = 0, na = 0, nk = 0;
+    uint32_t cw8[8];
+    int cx = 0, cy = 0, w = 0;
+    if (i < nwords) {
+        w = int(i % NWc);
+        const long long r = i / NWc;
+        cy = int(r % (g.ny - 1));
+        cx = int(r / (g.ny - 1));
+        act = cell_act(S, g, cx, cy, w, cw8);
+        na = __popc(act);
+        uint32_t m = act;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            nk += __popc(uint32_t(ISO_EDGE_STATUS[case_of(cw8, b)]));
+        }
+    }
+    uint32_t ea, ek, ta, tk;
+    block_scan2(na, nk, ea, ek, ta, tk, sm);
+    if (i >= nwords) return;
+    const unsigned long long a0 = blk[2 * blockIdx.x] + ea, k0 = blk[2 * blockIdx.x + 1] + ek;
+    actm[i] = act;
+    offA[i] = uint32_t(a0);
+    if (!act || !points) return;
+    unsigned long long a = a0, k = k0;
+    while (act) {
+        const int b = __ffs(act) - 1;
+        act &= act - 1;
+        const int cz = 32 * w + b;
+        const uint32_t cs = case_of(cw8, b);
+        const uint32_t est = ISO_EDGE_STATUS[cs];
+        CellCorners cc;
+        load_cell(vals, g, cx, cy, cz, cc);
+        cell_ids[a] = uint32_t(((long long)cx * (g.ny - 1) + cy) * (g.nz - 1) + cz);
+        cell_off[a] = uint32_t(k);
+        for (int e = 0; e < 12; ++e) {
+            if (!((est >> e) & 1u)) continue;
+            const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
+            const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
+            float p[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
+            points[3 * k + 0] = p[0];
+            points[3 * k + 1] = p[1];
+            points[3 * k + 2] = p[2];
+            if (normals) {
+                float n[3];
+                cell_normal(cc, p, n);
+                normals[3 * k + 0] = n[0];
+                normals[3 * k + 1] = n[1];
+                normals[3 * k + 2] = n[2];
+            }
+            ++k;
+        }
+        ++a;
+    }
+    if (a == (unsigned long long)A) cell_off[A] = uint32_t(K);
+}
+
+// Normals of an existing intersection from the grid (isoext computes them
+// when dual_contouring is given an intersection without normals).
+__global__ void dc_normals(const float* __restrict__ vals, Grid3 g, const float* __restrict__ points,
+                           const uint32_t* __restrict__ cell_ids, const uint32_t* __restrict__ cell_off,
+                           long long A, float* normals) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    const uint32_t cid = cell_ids[a];
+    const int cz = int(cid % uint32_t(g.nz - 1));
+    const uint32_t r = cid / uint32_t(g.nz - 1);
+    const int cy = int(r % uint32_t(g.ny - 1)), cx = int(r / uint32_t(g.ny - 1));
+    CellCorners cc;
+    load_cell(vals, g, cx, cy, cz, cc);
+    for (uint32_t k = cell_off[a]; k < cell_off[a + 1]; ++k) {
+        const float p[3] = {points[3 * k], points[3 * k + 1], points[3 * k + 2]};
+        float n[3];
+        cell_normal(cc, p, n);
+        normals[3 * k] = n[0];
+        normals[3 * k + 1] = n[1];
+        normals[3 * k + 2] = n[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solve
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
+// Loan, sec. 8.5), FP32.  a is destroyed; w = eigenvalues, q = eigenvectors
+// (columns).
+__device__ __forceinline__ void jacobi3f(float a[3][3], float w[3], float q[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) q[i][j] = i == j ? 1.0f : 0.0f;
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        const float off = fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]);
+        const float diag = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]);
+        if (off <= 1e-9f * diag || off == 0.0f) break;
+#pragma unroll
+        for (int pr = 0; pr < 3; ++pr) {
+            const int p = pr == 2 ? 1 : 0, r = pr == 0 ? 1 : 2;
+            const float apr = a[p][r];
+            if (apr == 0.0f) continue;
+            const float theta = (a[r][r] - a[p][p]) / (2.0f * apr);
+            const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+            const float c = rsqrtf(t * t + 1.0f), s = t * c;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float akp = a[k][p], akr = a[k][r];
+                a[k][p] = c * akp - s * akr;
+                a[k][r] = s * akp + c * akr;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float apk = a[p][k], ark = a[r][k];
+                a[p][k] = c * apk - s * ark;
+                a[r][k] = s * apk + c * ark;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float qkp = q[k][p], qkr = q[k][r];
+                q[k][p] = c * qkp - s * qkr;
+                q[k][r] = s * qkp + c * qkr;
+            }
+        }
+    }
+    w[0] = a[0][0]; w[1] = a[1][1]; w[2] = a[2][2];
+}
+
+// x += pinv(A) r with the eigen-decomposition (w, q) and the kept mask.
+__device__ __forceinline__ void apply_pinv(const float w[3], const float q[3][3], unsigned keep,
+                                           const double r[3], double x[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (!((keep >> i) & 1u)) continue;
+        const double qr = double(q[0][i]) * r[0] + double(q[1][i]) * r[1] + double(q[2][i]) * r[2];
+        const double c = qr / double(w[i]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[k] += c * double(q[k][i]);
+    }
+}
+
+__global__ void dc_solve(const float* __restrict__ points, const float* __restrict__ normals,
+                         const uint32_t* __restrict__ cell_ids, const uint32_t* __restrict__ cell_off,
+                         long long A, Grid3 g, float reg, float svd_tol, float* dual) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    // QEF, accumulated as src/dc.cu:26-62 does (each operation rounded)
+    float ata[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, atb[3] = {0, 0, 0};
+    float px = 0.0f, py = 0.0f, pz = 0.0f;
+    const uint32_t k0 = cell_off[a], k1 = cell_off[a + 1];
+    for (uint32_t k = k0; k < k1; ++k) {
+        const float nx = normals[3 * k], ny = normals[3 * k + 1], nz = normals[3 * k + 2];
+        const float qx = points[3 * k], qy = points[3 * k + 1], qz = points[3 * k + 2];
+        const float d = __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
+        px = __fadd_rn(px, qx); py = __fadd_rn(py, qy); pz = __fadd_rn(pz, qz);
+        const float n3[3] = {nx, ny, nz};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) ata[3 * i + j] = __fadd_rn(ata[3 * i + j], __fmul_rn(n3[i], n3[j]));
+        atb[0] = __fadd_rn(atb[0], __fmul_rn(nx, d));
+        atb[1] = __fadd_rn(atb[1], __fmul_rn(ny, d));
+        atb[2] = __fadd_rn(atb[2], __fmul_rn(nz, d));
+    }
+    const float cnt = __uint2float_rn(k1 - k0);
+    px = __fdiv_rn(px, cnt); py = __fdiv_rn(py, cnt); pz = __fdiv_rn(pz, cnt);
+    ata[0] = __fadd_rn(ata[0], reg); ata[4] = __fadd_rn(ata[4], reg); ata[8] = __fadd_rn(ata[8], reg);
+    atb[0] = __fadd_rn(atb[0], __fmul_rn(reg, px));
+    atb[1] = __fadd_rn(atb[1], __fmul_rn(reg, py));
+    atb[2] = __fadd_rn(atb[2], __fmul_rn(reg, pz));
+    // pseudo-inverse solve: singular values of the symmetric system are |w|
+    float m[3][3], w[3], q[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m[i][j] = ata[3 * i + j];
+    jacobi3f(m, w, q);
+    const float smax = fmaxf(fabsf(w[0]), fmaxf(fabsf(w[1]), fabsf(w[2])));
+    const float thr = svd_tol * smax;
+    unsigned keep = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) keep |= (fabsf(w[i]) > thr ? 1u : 0u) << i;
+    double x[3] = {0, 0, 0};
+    double r[3] = {atb[0], atb[1], atb[2]};
+    apply_pinv(w, q, keep, r, x);
+    // one refinement step with an FP64 residual (the FP32 eigenvectors leave
+    // an error of about cond(A) * eps; the residual recovers it)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        r[i] = double(atb[i]) - (double(ata[3 * i]) * x[0] + double(ata[3 * i + 1]) * x[1] +
+                                 double(ata[3 * i + 2]) * x[2]);
+    apply_pinv(w, q, keep, r, x);
+    // clip to the cell box (corner 0 .. corner 7)
+    const uint32_t cid = cell_ids[a];
+    const uint32_t cz = cid % uint32_t(g.nz - 1);
+    const uint32_t rr = cid / uint32_t(g.nz - 1);
+    const uint32_t cy = rr % uint32_t(g.ny - 1), cx = rr / uint32_t(g.ny - 1);
+    const uint32_t ci[3] = {cx, cy, cz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float lo = coord(g, k, ci[k]), hi = coord(g, k, ci[k] + 1);
+        dual[3 * a + k] = fminf(fmaxf(float(x[k]), lo), hi);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// quads
+
+// Crossed edges with a complete quad, per point word (points z in [32w, 32w+32)
+// of row (x, y)), as masks for the z, y and x edges leaving each point.
+__device__ __forceinline__ void quad_masks(const uint32_t* S, const Grid3& g, int x, int y, int w,
+                                           uint32_t& mz, uint32_t& my, uint32_t& mx) {
+    const int NWg = (g.nz + 31) / 32;
+    const uint32_t* r = srow(S, g, x, y);
+    const uint32_t s = r[w];
+    // z edge (z -> z+1): cells (x-1..x, y-1..y, z)
+    mz = my = mx = 0;
+    const uint32_t zin = iso::range_mask(w, 1, g.nz - 2);     // 1 <= z <= nz-2
+    const uint32_t zall = iso::range_mask(w, 0, g.nz - 2);    // z <= nz-2 (edge exists)
+    if (x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2)
+        mz = (s ^ __funnelshift_r(s, word_or0(r, w + 1, NWg), 1)) & zall;
+    // y edge (y -> y+1): cells (x-1..x, y, z-1..z)
+    if (x >= 1 && x <= g.nx - 2 && y <= g.ny - 2) my = (s ^ srow(S, g, x, y + 1)[w]) & zin;
+    // x edge (x -> x+1): cells (x, y-1..y, z-1..z)
+    if (x <= g.nx - 2 && y >= 1 && y <= g.ny - 2) mx = (s ^ srow(S, g, x + 1, y)[w]) & zin;
+}
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_quad_count(const uint32_t* __restrict__ S, Grid3 g,
+                                                          long long nwords,
+                                                          unsigned long long* __restrict__ blk) {
+    __shared__ uint32_t sm[66];
+    const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    uint32_t nq = 0;
+    if (i < nwords) {
+        const int NWg = (g.nz + 31) / 32;
+        const int w = int(i % NWg);
+        const long long r = i / NWg;
+        const int y = int(r % g.ny), x = int(r / g.ny);
+        uint32_t mz, my, mx;
+        quad_masks(S, g, x, y, w, mz, my, mx);
+        nq = __popc(mz) + __popc(my) + __popc(mx);
+    }
+    uint32_t e0, e1, t0, t1;
+    block_scan2(nq, 0u, e0, e1, t0, t1, sm);
+    if (threadIdx.x == 0) {
+        blk[2 * blockIdx.x] = t0;
+        blk[2 * blockIdx.x + 1] = 0;
+    }
+}
+
+// Active index of cell (cx, cy, cz): prefix of its word + active cells below it.
+__device__ __forceinline__ uint32_t active_index(const uint32_t* actm, const uint32_t* offA,
+                                                 const Grid3& g, int cx, int cy, int cz) {
+    const int NWc = (g.nz - 1 + 31) / 32;
+    const long long wi = ((long long)cx * (g.ny - 1) + cy) * NWc + (cz >> 5);
+    return offA[wi] + __popc(actm[wi] & ((1u << (cz & 31)) - 1u));
+}
+
+__device__ __forceinline__ float dist3(const float* a, const float* b) {
+    const float dx = __fsub_rn(a[0], b[0]), dy = __fsub_rn(a[1], b[1]), dz = __fsub_rn(a[2], b[2]);
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restrict__ S, Grid3 g,
+                                                         long long nwords,
+                                                         const unsigned long long* __restrict__ blk,
+                                                         const uint32_t* __restrict__ actm,
+                                                         const uint32_t* __restrict__ offA,
+                                                         const float* __restrict__ dual,
+                                                         int32_t* __restrict__ tri) {
+    __shared__ uint32_t sm[66];
+    const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    const int NWg = (g.nz + 31) / 32;
+    uint32_t mz = 0, my = 0, mx = 0;
+    int x = 0, y = 0, w = 0;
+    if (i < nwords) {
+        w = int(i % NWg);
+        const long long r = i / NWg;
+        y = int(r % g.ny);
+        x = int(r / g.ny);
+        quad_masks(S, g, x, y, w, mz, my, mx);
+    }
+    uint32_t eq, e1, tq, t1;
+    block_scan2(__popc(mz) + __popc(my) + __popc(mx), 0u, eq, e1, tq, t1, sm);
+    if (i >= nwords) return;
+    unsigned long long q = blk[2 * blockIdx.x] + eq;
+    const uint32_t s = srow(S, g, x, y)[w];
+    uint32_t all = mz | my | mx;
+    while (all) {
+        const int b = __ffs(all) - 1;
+        all &= all - 1;
+        const int z = 32 * w + b;
+        // is_out = v(p0) <= v(p1): for a crossed edge this holds exactly when
+        // the low endpoint p0 is below the level
+        const bool out = (s >> b) & 1u;
+#pragma unroll
+        for (int ax = 2; ax >= 0; --ax) {  // quad order for one point: z, y, x edge
+            const uint32_t m = ax == 2 ? mz : (ax == 1 ? my : mx);
+            if (!((m >> b) & 1u)) continue;
+            // edge_neighbors_table (src/shared_luts.cu:78-81): the 4 cells are p - o_i
+            int c[4][3];
+            if (ax == 0) {
+                const int o[4][3] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}};
+                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
+            } else if (ax == 1) {
+                const int o[4][3] = {{0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 0, 0}};
+                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
+            } else {
+                const int o[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
+            }
+            int32_t qi[4];
+            for (int k = 0; k < 4; ++k) qi[k] = int32_t(active_index(actm, offA, g, c[k][0], c[k][1], c[k][2]));
+            if (!out) {
+                const int32_t t0 = qi[0], t1 = qi[1];
+                qi[0] = qi[3]; qi[1] = qi[2]; qi[2] = t1; qi[3] = t0;
+            }
+            float v[4][3];
+            for (int k = 0; k < 4; ++k)
+                for (int a = 0; a < 3; ++a) v[k][a] = dual[3 * (long long)qi[k] + a];
+            int32_t* o6 = tri + 6 * q;
+            if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+                o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0];
+                o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
+            } else {
+                o6[0] = qi[2]; o6[1] = qi[0]; o6[2] = qi[1];
+                o6[3] = qi[0]; o6[4] = qi[2]; o6[5] = qi[3];
+            }
+            ++q;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// weld: exact-position dedup of the dual vertices faces use.
+
+__device__ __forceinline__ uint32_t pos_bits(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
+__device__ __forceinline__ uint32_t pos_hash(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h;
+}
+
+__global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint32_t* used) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) used[tri[i]] = 1u;
+}
+
+// Insert used vertices; a slot keeps the smallest index with its position.
+__global__ void dc_hash_insert(const float* __restrict__ dual, const uint32_t* __restrict__ used,
+                               long long A, uint32_t* table, uint32_t mask, int* status) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A || !used[a]) return;
+    const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
+    uint32_t h = pos_hash(k0, k1, k2) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const uint32_t cur = atomicCAS(&table[h], 0xffffffffu, uint32_t(a));
+        if (cur == 0xffffffffu) return;
+        const uint32_t j = cur;
+        if (pos_bits(dual[3ll * j]) == k0 && pos_bits(dual[3ll * j + 1]) == k1 &&
+            pos_bits(dual[3ll * j + 2]) == k2) {
+            atomicMin(&table[h], uint32_t(a));
+            return;
+        }
+    }
+    atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+}
+
+// rep[a] = smallest index with the same position (for used vertices).
+__global__ void dc_hash_lookup(const float* __restrict__ dual, const uint32_t* __restrict__ used,
+                               long long A, const uint32_t* __restrict__ table, uint32_t mask,
+                               uint32_t* rep) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    if (!used[a]) { rep[a] = 0xffffffffu; return; }
+    const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
+    uint32_t h = pos_hash(k0, k1, k2) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const uint32_t j = table[h];
+        if (j == 0xffffffffu) break;
+        if (pos_bits(dual[3ll * j]) == k0 && pos_bits(dual[3ll * j + 1]) == k1 &&
+            pos_bits(dual[3ll * j + 2]) == k2) {
+            rep[a] = j;
+            return;
+        }
+    }
+    rep[a] = uint32_t(a);
+}
+
+// Per block of 1024 dual vertices: number of representatives (rep[a] == a).
+__global__ void __launch_bounds__(DC_BLOCK) dc_rep_count(const uint32_t* __restrict__ rep, long long A,
+                                                         unsigned long long* blk) {
+    __shared__ uint32_t sm[66];
+    const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    const uint32_t is = (a < A && rep[a] == uint32_t(a)) ? 1u : 0u;
+    uint32_t e0, e1, t0, t1;
+    block_scan2(is, 0u, e0, e1, t0, t1, sm);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = t0; blk[2 * blockIdx.x + 1] = 0; }
+}
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_rep_write(const uint32_t* __restrict__ rep, long long A,
+                                                         const unsigned long long* __restrict__ blk,
+                                                         const float* __restrict__ dual, uint32_t* newidx,
+                                                         float* vout) {
+    __shared__ uint32_t sm[66];
+    const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    const uint32_t is = (a < A && rep[a] == uint32_t(a)) ? 1u : 0u;
+    uint32_t e0, e1, t0, t1;
+    block_scan2(is, 0u, e0, e1, t0, t1, sm);
+    if (!is) return;
+    const unsigned long long o = blk[2 * blockIdx.x] + e0;
+    newidx[a] = uint32_t(o);
+    vout[3 * o] = dual[3 * a];
+    vout[3 * o + 1] = dual[3 * a + 1];
+    vout[3 * o + 2] = dual[3 * a + 2];
+}
+
+__global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uint32_t* __restrict__ rep,
+                         const uint32_t* __restrict__ newidx, int32_t* fout) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) fout[i] = int32_t(newidx[rep[tri[i]]]);
+}
+
+Grid3 make_grid(int nx, int ny, int nz, const float* amin, const float* amax) {
+    Grid3 g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    for (int k = 0; k < 3; ++k) {
+        g.amin[k] = amin[k];
+        g.asize[k] = amax[k] - amin[k];
+    }
+    return g;
+}
+
+unsigned blocks_for(long long n, int b) { return unsigned((n + b - 1) / b); }
+
+}  // namespace
+
+// mc_signs lives in mc_dense.cu
+void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
+                     cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+size_t iso_dc_workspace_size(int nx, int ny, int nz) {
+    if (nx < 2 || ny < 2 || nz < 2) return 256;
+    const long long NWg = (nz + 31) / 32, NWc = (nz - 1 + 31) / 32;
+    const long long cwords = (long long)(nx - 1) * (ny - 1) * NWc;
+    const long long pwords = (long long)nx * ny * NWg;
+    const long long nblk = (std::max(cwords, pwords) + DC_BLOCK - 1) / DC_BLOCK;
+    size_t o = 0;
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    o = al(o + size_t(pwords) * 4);       // signs
+    o = al(o + size_t(cwords) * 4);       // active masks
+    o = al(o + size_t(cwords) * 4);       // active prefix
+    o = al(o + size_t(nblk) * 16);        // cell block sums
+    o = al(o + size_t(nblk) * 16);        // quad block sums
+    return o + 1024;
+}
+
+}  // extern "C"
+
+namespace {
+struct DcWs {
+    uint32_t *S, *actm, *offA;
+    unsigned long long *blkC, *blkQ;
+    long long cwords, pwords, nblkC, nblkQ;
+};
+DcWs carve(void* ws, int nx, int ny, int nz) {
+    DcWs w;
+    const long long NWg = (nz + 31) / 32, NWc = (nz - 1 + 31) / 32;
+    w.cwords = (long long)(nx - 1) * (ny - 1) * NWc;
+    w.pwords = (long long)nx * ny * NWg;
+    w.nblkC = (w.cwords + DC_BLOCK - 1) / DC_BLOCK;
+    w.nblkQ = (w.pwords + DC_BLOCK - 1) / DC_BLOCK;
+    const long long nblk = std::max(w.nblkC, w.nblkQ);
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    size_t o = 0;
+    w.S = reinterpret_cast<uint32_t*>(b + o);    o = al(o + size_t(w.pwords) * 4);
+    w.actm = reinterpret_cast<uint32_t*>(b + o); o = al(o + size_t(w.cwords) * 4);
+    w.offA = reinterpret_cast<uint32_t*>(b + o); o = al(o + size_t(w.cwords) * 4);
+    w.blkC = reinterpret_cast<unsigned long long*>(b + o); o = al(o + size_t(nblk) * 16);
+    w.blkQ = reinterpret_cast<unsigned long long*>(b + o);
+    return w;
+}
+}  // namespace
+
+extern "C" {
+
+int iso_dc_classify(const float* values, int nx, int ny, int nz, float level, void* ws, size_t ws_bytes,
+                    long long* counts, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (ws_bytes < iso_dc_workspace_size(nx, ny, nz)) return ISO_ERR_WORKSPACE;
+    DcWs w = carve(ws, nx, ny, nz);
+    const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
+    Grid3 g = make_grid(nx, ny, nz, amin, amax);
+    {
+        iso::ProfScope ps("mc_signs", st);
+        mc_signs_launch(values, nx, ny, nz, level, w.S, st);
+    }
+    iso::ProfScope ps("dc_classify", st);
+    dc_cell_count<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.cwords, w.blkC);
+    dc_block_scan<<<1, 1024, 0, st>>>(w.blkC, w.nblkC, counts);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                     const float* aabb_max, float level, void* ws, long long A, long long K, float* points,
+                     float* normals, int* cell_ids, int* cell_offsets, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2) return 0;
+    DcWs w = carve(ws, nx, ny, nz);
+    Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
+    iso::ProfScope ps("dc_intersect", st);
+    dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
+        values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, points, normals,
+        reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
+    if (A == 0 && cell_offsets) cudaMemsetAsync(cell_offsets, 0, 4, st);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_normals(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                   const float* aabb_max, const float* points, const int* cell_ids,
+                   const int* cell_offsets, long long A, float* normals, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (A <= 0) return 0;
+    Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
+    iso::ProfScope ps("dc_normals", st);
+    dc_normals<<<blocks_for(A, 256), 256, 0, st>>>(values, g, points,
+                                                   reinterpret_cast<const uint32_t*>(cell_ids),
+                                                   reinterpret_cast<const uint32_t*>(cell_offsets), A,
+                                                   normals);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_solve(int nx, int ny, int nz, const float* aabb_min, const float* aabb_max, const float* points,
+                 const float* normals, const int* cell_ids, const int* cell_offsets, long long A, float reg,
+                 float svd_tol, float* dual, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (A <= 0) return 0;
+    Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
+    iso::ProfScope ps("dc_solve", st);
+    dc_solve<<<blocks_for(A, 128), 128, 0, st>>>(points, normals, reinterpret_cast<const uint32_t*>(cell_ids),
+                                                 reinterpret_cast<const uint32_t*>(cell_offsets), A, g, reg,
+                                                 svd_tol, dual);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+// Active masks and prefixes only (when the intersection was made earlier).
+int iso_dc_cells(const float* values, int nx, int ny, int nz, float level, void* ws, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2) return 0;
+    DcWs w = carve(ws, nx, ny, nz);
+    const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
+    Grid3 g = make_grid(nx, ny, nz, amin, amax);
+    iso::ProfScope ps("dc_intersect", st);
+    dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
+        values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr, nullptr, nullptr, -1, 0);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_quads_count(int nx, int ny, int nz, void* ws, long long* counts, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    DcWs w = carve(ws, nx, ny, nz);
+    const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
+    Grid3 g = make_grid(nx, ny, nz, amin, amax);
+    iso::ProfScope ps("dc_quads", st);
+    dc_quad_count<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ);
+    dc_block_scan<<<1, 1024, 0, st>>>(w.blkQ, w.nblkQ, counts);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_quads_emit(int nx, int ny, int nz, void* ws, const float* dual, int* tri, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2) return 0;
+    DcWs w = carve(ws, nx, ny, nz);
+    const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
+    Grid3 g = make_grid(nx, ny, nz, amin, amax);
+    iso::ProfScope ps("dc_quads", st);
+    dc_quad_emit<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ, w.actm,
+                                                                     w.offA, dual, tri);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+size_t iso_dc_weld_workspace_size(long long A) {
+    uint32_t cap = 1024;
+    while ((long long)cap < 2 * A + 1024) cap <<= 1;
+    const long long nblk = (A + DC_BLOCK - 1) / DC_BLOCK + 1;
+    return size_t(A) * 12 + size_t(cap) * 4 + size_t(nblk) * 16 + 4096;
+}
+
+// Weld step 1: used marks, hash, representatives; counts[0] <- V.
+int iso_dc_weld_count(const float* dual, long long A, const int* tri, long long ntri, void* ws,
+                      size_t ws_bytes, long long* counts, int* status, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (ws_bytes < iso_dc_weld_workspace_size(A)) return ISO_ERR_WORKSPACE;
+    uint32_t cap = 1024;
+    while ((long long)cap < 2 * A + 1024) cap <<= 1;
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    uint32_t* used = reinterpret_cast<uint32_t*>(b);
+    uint32_t* rep = used + A;
+    uint32_t* newidx = rep + A;
+    uint32_t* table = newidx + A;
+    unsigned long long* blk = reinterpret_cast<unsigned long long*>(
+        (reinterpret_cast<uintptr_t>(table + cap) + 15) & ~uintptr_t(15));
+    const long long nblk = (A + DC_BLOCK - 1) / DC_BLOCK;
+    iso::ProfScope ps("dc_weld", st);
+    cudaMemsetAsync(used, 0, size_t(A) * 4, st);
+    cudaMemsetAsync(table, 0xff, size_t(cap) * 4, st);
+    if (ntri > 0) dc_mark_used<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, used);
+    if (A > 0) {
+        dc_hash_insert<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, status);
+        dc_hash_lookup<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, rep);
+        dc_rep_count<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk);
+        dc_block_scan<<<1, 1024, 0, st>>>(blk, nblk, counts);
+    } else {
+        cudaMemsetAsync(counts, 0, 16, st);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+// Weld step 2: write vertices [V, 3] and faces [ntri / 3, 3].
+int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long ntri, void* ws,
+                      float* vout, int* fout, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t cap = 1024;
+    while ((long long)cap < 2 * A + 1024) cap <<= 1;
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    uint32_t* used = reinterpret_cast<uint32_t*>(b);
+    uint32_t* rep = used + A;
+    uint32_t* newidx = rep + A;
+    uint32_t* table = newidx + A;
+    unsigned long long* blk = reinterpret_cast<unsigned long long*>(
+        (reinterpret_cast<uintptr_t>(table + cap) + 15) & ~uintptr_t(15));
+    const long long nblk = (A + DC_BLOCK - 1) / DC_BLOCK;
+    iso::ProfScope ps("dc_weld", st);
+    if (A > 0) dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk, dual, newidx, vout);
+    if (ntri > 0) dc_remap<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, rep, newidx, fout);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+}  // extern "C"

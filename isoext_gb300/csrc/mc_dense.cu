@@ -882,6 +882,17 @@ int launch_extract(const McParams& p, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // Host API
 
+void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
+                     cudaStream_t st) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long rows = (long long)nx * ny;
+    const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
+    const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sms * 32));
+    mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, rows, nz, level, out);
+}
+
 int mc_plan_tiles(int nx, int ny, int nz, int rows, int slabs, int threads, int zchunk,
                   int sm_count, McTiles* out) {
     McTiles t{};
@@ -1020,13 +1031,7 @@ int mc_launch(const McParams& p0, void* ws, size_t ws_bytes, cudaStream_t st) {
     if (t.nTiles > 0x7fffffffll) return ISO_ERR_ARG;
     {
         iso::ProfScope ps("mc_signs", st);
-        int dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long rows = (long long)t.nx * t.ny;
-        const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
-        const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sms * 32));
-        mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(p.vals, rows, t.nz, p.level, p.signs);
+        mc_signs_launch(p.vals, t.nx, t.ny, t.nz, p.level, p.signs, st);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
