@@ -1,18 +1,21 @@
 // Dense-grid marching cubes on sm_103a.
 //
-// Three launches on one stream:
-//   1. mc_extract  persistent CTAs; each work item is a column of tiles
+// Four launches on one stream:
+//   1. mc_signs    streams the grid once (one warp per row, 16 coalesced
+//                  128-byte loads in flight per warp) into a sign bitmap,
+//                  1 bit per point.
+//   2. mc_extract  persistent CTAs; each work item is a column of tiles
 //                  (row group, z chunk) swept along x over a chunk of planes.
-//                  Point slabs (one plane x (R+2) rows x (ZC+2) z) stream into a
-//                  shared-memory ring by TMA bulk copies, so every grid value
-//                  is read from HBM once.  Per slab: sign bits (warp ballot),
-//                  crossed-edge bitmaps and "snap" bitmaps (edge vertices that
-//                  round exactly onto a grid point).  Per tile: cell activity
-//                  by word-wide bit logic, face counts, vertex existence, and
-//                  staged vertices (position + key) and faces (key references).
-//   2. mc_tile_scan  exclusive prefix of per-tile vertex / face counts.
-//   3. mc_resolve  copies staged vertices to their final slots and turns face
-//                  key references into vertex indices.
+//                  A ring of three planes of bitmaps (signs, crossed edges,
+//                  "snap" edges whose vertex rounds exactly onto a grid point)
+//                  lives in shared memory; grid values are read only for the
+//                  crossed edges (lerp).  Per tile: cell activity by word-wide
+//                  bit logic, face counts, vertex existence, a warp scan that
+//                  takes space from per-CTA staging blocks, and staged vertices
+//                  (position + key) and faces (key references).
+//   3. mc_tile_scan  exclusive prefix of per-tile vertex / face counts.
+//   4. mc_resolve  copies staged vertices to their final slots and turns face
+//                  key references into vertex indices (one warp per tile).
 //
 // Equivalence with the reference (src/mc/mc.cu:17-68): the reference emits the
 // triangles of active cells in ascending cell id, drops triangles with two equal
