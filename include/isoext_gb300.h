@@ -85,6 +85,29 @@ int iso_mc_dense(const float *values, int nx, int ny, int nz, const float *aabb_
                  long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
                  size_t workspace_bytes, long long *counts, int *status, void *stream);
 
+/* Marching cubes with no caller workspace. This has NO counterpart in the
+ * reference: isoext allocates per call.  It is for callers that cannot give
+ * the library device memory. One example is a host with only a stream and no
+ * device allocator. Another is a frame loop that must not call cudaMalloc or
+ * cudaFree, because cudaFree synchronises the device and either call can fail
+ * mid-frame.
+ * Arguments and results are iso_mc_dense's, without workspace/workspace_bytes.
+ * The workspace is a fixed array inside the library, ISO_MC_NOALLOC_SCRATCH_BYTES
+ * (32 MiB) per device. The call allocates nothing.
+ *   - A grid plus capacities whose iso_mc_dense_workspace_size exceeds the
+ *     limit -> ISO_ERR_WORKSPACE with a message; nothing is queued. 256^3 with
+ *     capacities near its mesh size fits.
+ *   - The first call on a device does set-up: it looks up the array's address
+ *     with that device current. Make it before any stream capture.
+ *   - All calls on one device share the array. Calls not ordered on the device
+ *     (different streams or threads without events) race. Each call clears,
+ *     on its stream, what must start at zero. */
+#define ISO_MC_NOALLOC_SCRATCH_BYTES (32u << 20)
+int iso_mc_dense_noalloc(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                         const float *aabb_max, float level, int method, float *vertices,
+                         long long vertex_capacity, int *faces, long long face_capacity,
+                         long long *counts, int *status, void *stream);
+
 /* ---- dual contouring on a dense grid --------------------------------------
  * Replaces isoext_ext.get_intersection / dual_contouring (src/isoext_ext.cu:
  * 329-378 -> get_intersection src/its.cu:94-159, compute_intersection_normals

@@ -44,6 +44,11 @@ bool grid_ok(int nx, int ny, int nz) {
 }
 }  // namespace
 
+namespace iso {
+// Message iso_last_error returns on this thread (for entry points in other files).
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace iso
+
 extern "C" {
 
 const char* iso_last_error(void) { return g_err.c_str(); }
