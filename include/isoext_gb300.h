@@ -150,6 +150,57 @@ int iso_dc_weld_count(const float *dual, long long A, const int *tri, long long 
 int iso_dc_weld_write(const float *dual, long long A, const int *tri, long long ntri, void *ws,
                       float *vout, int *fout, void *stream);
 
+/* ---- sparse grids -----------------------------------------------------------
+ * Replaces isoext's SparseGrid paths (src/grid/sparse.cu:9-246 with
+ * src/mc/mc.cu:17-68, src/its.cu:94-283, src/dc.cu:162-218).  A sparse grid is
+ * `ids` (int32 [n] cell ids of an nx*ny*nz-point lattice, ascending as uint32,
+ * unique) and `vals` (float32 [n, 8], corner k = 4x + 2y + z, 16-byte aligned).
+ * `blk` is a block-sum workspace of iso_sparse_blocks_size(n) bytes; counting
+ * calls write totals to device int64 counts[2]. */
+size_t iso_sparse_blocks_size(long long n);
+/* MC: counts[0] <- F; then a triangle soup [3F, 3] in the reference's order
+ * (cell order, table slots; triangles with two equal positions dropped,
+ * src/mc/nagae.cu:71).  Weld it with iso_dc_weld_count / iso_dc_weld_write
+ * (A = 3F, tri = 0 .. 3F-1), which merges equal positions as isoext does. */
+int iso_sparse_mc_count(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                        const float *aabb_min, const float *aabb_max, float level, int method,
+                        void *blk, long long *counts, void *stream);
+int iso_sparse_mc_emit(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                       const float *aabb_min, const float *aabb_max, float level, int method,
+                       const void *blk, float *soup, void *stream);
+/* Intersection: counts <- (A, K); then points [K,3], optional normals, active
+ * cells as sparse indices [A] (isoext's Intersection.cell_indices) and as
+ * lattice ids [A] (for iso_dc_solve), offsets [A+1], and rank [n] (active
+ * index of each sparse cell, -1 if inactive). */
+int iso_sparse_its_count(const float *vals, long long n, float level, void *blk, long long *counts,
+                         void *stream);
+int iso_sparse_its_emit(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                        const float *aabb_min, const float *aabb_max, float level, const void *blk,
+                        long long A, long long K, float *points, float *normals, int *act_sparse,
+                        int *act_lattice, int *offsets, int *rank, void *stream);
+/* Normals of existing crossings (src/its.cu:186-268). */
+int iso_sparse_normals(const int *ids, const float *vals, int nx, int ny, int nz, const float *aabb_min,
+                       const float *aabb_max, const int *act_sparse, const int *offsets, long long A,
+                       const float *points, float *normals, void *stream);
+/* DC quads (src/grid/sparse.cu:181-246, src/dc.cu:101-157): counts[0] <- Q,
+ * then 6 dual indices per quad.  A quad needs its 4 cells present and active;
+ * its orientation comes from the first of them (sparse order) that crosses. */
+int iso_sparse_quads_count(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                           float level, const int *rank, void *blk, long long *counts, void *stream);
+int iso_sparse_quads_emit(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                          float level, const int *rank, const void *blk, const float *dual, int *tri,
+                          void *stream);
+/* Corner positions [m, 8, 3] of cell ids (get_points / get_points_by_cell_indices,
+ * src/grid/sparse.cu:21-43). */
+int iso_sparse_points(const int *ids, long long m, int nx, int ny, int nz, const float *aabb_min,
+                      const float *aabb_max, float *out, void *stream);
+/* filter_cell_indices (src/grid/sparse.cu:150-179): counts[0] <- kept; then the
+ * kept ids in input order. */
+int iso_sparse_filter_count(const float *vals, long long m, float level, void *blk, long long *counts,
+                            void *stream);
+int iso_sparse_filter_write(const int *ids, const float *vals, long long m, float level, const void *blk,
+                            int *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,11 @@
     grid.set_values(sdf(grid.get_points()))
     v, f = isoext.marching_cubes(grid)
 
+    sparse = isoext.SparseGrid([1024] * 3)
+    sparse.add_cells(ids)
+    sparse.set_values(sdf(sparse.get_points()))   # [N, 8]
+    v, f = isoext.dual_contouring(sparse)
+
 The extraction functions run hand-written sm_103a kernels through the C ABI of
 ``_lib/libisoext_gb300.so`` (include/isoext_gb300.h); there is no CPU fallback.
 """
@@ -12,12 +17,14 @@ The extraction functions run hand-written sm_103a kernels through the C ABI of
 from .dc import Intersection, dual_contouring, get_intersection
 from .grids import FLT_MAX, Grid, UniformGrid
 from .mc import marching_cubes
+from .sparse import SparseGrid
 from .utils import gaussian_smooth, make_grid, write_obj
 
 __all__ = [
     "FLT_MAX",
     "Grid",
     "Intersection",
+    "SparseGrid",
     "UniformGrid",
     "dual_contouring",
     "gaussian_smooth",

@@ -42,7 +42,11 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_mc_dense_workspace_size.restype = C.c_size_t
     lib.iso_mc_dense.argtypes = [_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp,
                                  C.c_size_t, _vp, _vp, _vp]
-    for name, args in _EXTRA.items():
+    _apply(lib, _EXTRA)
+
+
+def _apply(lib: C.CDLL, entries: dict) -> None:
+    for name, args in entries.items():
         fn = getattr(lib, name, None)
         if fn is not None:
             fn.argtypes = args[0]
@@ -52,6 +56,13 @@ def _declare(lib: C.CDLL) -> None:
 
 # Declarations of further entry points (added by the modules that use them).
 _EXTRA: dict[str, tuple[list, object]] = {}
+
+
+def register(entries: dict) -> None:
+    """Declare entry points {name: (argtypes, restype)}; applies at once if loaded."""
+    _EXTRA.update(entries)
+    if _lib is not None:
+        _apply(_lib, entries)
 
 
 def lib() -> C.CDLL:

@@ -697,6 +697,12 @@ void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uin
 // ---------------------------------------------------------------------------
 // C ABI
 
+// Exclusive scan of per-block (u64, u64) sums in place, totals -> totals[0..1]
+// (used by the sparse-grid kernels).
+void iso_block_scan_launch(unsigned long long* blk, long long nblk, long long* totals, cudaStream_t st) {
+    dc_block_scan<<<1, 1024, 0, st>>>(blk, nblk, totals);
+}
+
 extern "C" {
 
 size_t iso_dc_workspace_size(int nx, int ny, int nz) {

@@ -1,0 +1,623 @@
+// SparseGrid extraction on sm_103a (isoext src/grid/sparse.cu, src/mc/mc.cu).
+//
+// A sparse grid is a sorted list of cell ids over the (n-1)^3 cell lattice with
+// its own 8 corner values per cell ([N, 8], Morton corner order).  Cells share
+// no storage, so isoext welds vertices by exact position (src/utils.cu:32-59);
+// so does this path (hash weld in dc_dense.cu), which keeps it exact even when
+// two cells disagree about a shared corner's value.
+//
+//   mc_count / mc_emit   per cell: case, edge lerps, triangles whose three
+//                        positions differ (src/mc/nagae.cu:34-80), written as a
+//                        triangle soup in cell order.
+//   its_count / its_emit per active cell: crossings in edge-bit order, normals
+//                        (src/its.cu:37-90, 186-268).
+//   quads                each cell's x/y/z edges at its lowest corner, in cell
+//                        order = isoext's (p0, axis) quad order; a quad needs its
+//                        4 cells in the grid (binary search) and active.
+#include <algorithm>
+#include <cstdint>
+
+#include "common.cuh"
+#define ISO_LUT_DECL static __constant__ const
+#include "luts.h"
+#include "profile.cuh"
+
+namespace {
+
+constexpr int SP_BLOCK = 256;  // per-cell state is ~70 registers
+
+struct SpGrid {
+    int nx, ny, nz;
+    float amin[3], asize[3];
+    float level;
+    int method;
+};
+
+__device__ __forceinline__ void cell_xyz(const SpGrid& g, uint32_t id, int& x, int& y, int& z) {
+    z = int(id % uint32_t(g.nz - 1));
+    const uint32_t r = id / uint32_t(g.nz - 1);
+    y = int(r % uint32_t(g.ny - 1));
+    x = int(r / uint32_t(g.ny - 1));
+}
+
+struct Cell8 {
+    float v[8];
+    float p[8][3];
+};
+
+__device__ __forceinline__ void load_cell(const SpGrid& g, const int* ids, const float* vals, long long c,
+                                          Cell8& cc, int& x, int& y, int& z) {
+    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+    const float4* v4 = reinterpret_cast<const float4*>(vals + 8 * c);
+    const float4 a = __ldg(v4), b = __ldg(v4 + 1);
+    cc.v[0] = a.x; cc.v[1] = a.y; cc.v[2] = a.z; cc.v[3] = a.w;
+    cc.v[4] = b.x; cc.v[5] = b.y; cc.v[6] = b.z; cc.v[7] = b.w;
+    const float cx0 = iso::grid_coord(x, g.nx, g.amin[0], g.asize[0]);
+    const float cx1 = iso::grid_coord(x + 1, g.nx, g.amin[0], g.asize[0]);
+    const float cy0 = iso::grid_coord(y, g.ny, g.amin[1], g.asize[1]);
+    const float cy1 = iso::grid_coord(y + 1, g.ny, g.amin[1], g.asize[1]);
+    const float cz0 = iso::grid_coord(z, g.nz, g.amin[2], g.asize[2]);
+    const float cz1 = iso::grid_coord(z + 1, g.nz, g.amin[2], g.asize[2]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        cc.p[k][0] = (k >> 2) ? cx1 : cx0;
+        cc.p[k][1] = ((k >> 1) & 1) ? cy1 : cy0;
+        cc.p[k][2] = (k & 1) ? cz1 : cz0;
+    }
+}
+
+__device__ __forceinline__ uint32_t case_of(const Cell8& cc, float level) {
+    uint32_t cs = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cs |= (iso::below(cc.v[k], level) ? 1u : 0u) << k;
+    return cs;
+}
+
+__device__ __forceinline__ void edge_point(const Cell8& cc, int e, float level, float* p) {
+    const int a = ISO_EDGE_CORNERS[2 * e], b = ISO_EDGE_CORNERS[2 * e + 1];
+    const float t = iso::cross_t(level, cc.v[a], cc.v[b]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[a][q], cc.p[b][q]);
+}
+
+__device__ __forceinline__ bool eq3(const float* a, const float* b) {
+    return a[0] == b[0] && a[1] == b[1] && a[2] == b[2];
+}
+
+__device__ __forceinline__ const signed char* tri_row(int method, uint32_t cs, int& ml) {
+    if (method == 0) { ml = 15; return ISO_TRI_NAGAE + cs * 15; }
+    ml = 12;
+    return ISO_TRI_LORENSEN + cs * 12;
+}
+
+// Faces of one cell (positions of its crossed edges in ev).
+__device__ __forceinline__ uint32_t mc_cell(const SpGrid& g, const Cell8& cc, float (*ev)[3]) {
+    const uint32_t cs = case_of(cc, g.level);
+    if (cs == 0 || cs == 255) return 0;
+    const uint32_t est = ISO_EDGE_STATUS[cs];
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+        if ((est >> e) & 1u) edge_point(cc, e, g.level, ev[e]);
+    int ml;
+    const signed char* tr = tri_row(g.method, cs, ml);
+    uint32_t n = 0;
+    for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
+        const float* a = ev[tr[k]];
+        const float* b = ev[tr[k + 1]];
+        const float* c = ev[tr[k + 2]];
+        n += (!eq3(a, b) && !eq3(a, c) && !eq3(b, c));
+    }
+    return n;
+}
+
+__device__ __forceinline__ void block_scan1(uint32_t a, uint32_t& ea, uint32_t& ta, uint32_t* sm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t ia = a;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(~0u, ia, d);
+        if (lane >= d) ia += x;
+    }
+    if (lane == 31) sm[warp] = ia;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t x = lane < int(blockDim.x >> 5) ? sm[lane] : 0u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(~0u, x, d);
+            if (lane >= d) x += u;
+        }
+        sm[lane] = x;
+    }
+    __syncthreads();
+    ea = (warp ? sm[warp - 1] : 0u) + ia - a;
+    ta = sm[31];  // sum over all warps = block total
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_mc_count(SpGrid g, const int* __restrict__ ids,
+                                                        const float* __restrict__ vals, long long n,
+                                                        unsigned long long* blk) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t nf = 0;
+    if (c < n) {
+        Cell8 cc;
+        int x, y, z;
+        load_cell(g, ids, vals, c, cc, x, y, z);
+        float ev[12][3];
+        nf = mc_cell(g, cc, ev);
+    }
+    uint32_t e, t;
+    block_scan1(nf, e, t, sm);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = t; blk[2 * blockIdx.x + 1] = 0; }
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __restrict__ ids,
+                                                       const float* __restrict__ vals, long long n,
+                                                       const unsigned long long* __restrict__ blk,
+                                                       float* soup) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t nf = 0;
+    Cell8 cc;
+    float ev[12][3];
+    uint32_t cs = 0;
+    if (c < n) {
+        int x, y, z;
+        load_cell(g, ids, vals, c, cc, x, y, z);
+        nf = mc_cell(g, cc, ev);
+        cs = case_of(cc, g.level);
+    }
+    uint32_t e, t;
+    block_scan1(nf, e, t, sm);
+    if (!nf) return;
+    unsigned long long f = blk[2 * blockIdx.x] + e;
+    int ml;
+    const signed char* tr = tri_row(g.method, cs, ml);
+    for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
+        const float* a = ev[tr[k]];
+        const float* b = ev[tr[k + 1]];
+        const float* cpos = ev[tr[k + 2]];
+        if (eq3(a, b) || eq3(a, cpos) || eq3(b, cpos)) continue;
+        float* o = soup + 9 * f;
+        o[0] = a[0]; o[1] = a[1]; o[2] = a[2];
+        o[3] = b[0]; o[4] = b[1]; o[5] = b[2];
+        o[6] = cpos[0]; o[7] = cpos[1]; o[8] = cpos[2];
+        ++f;
+    }
+}
+
+// --- intersections -----------------------------------------------------------
+
+__device__ __forceinline__ float trilin(const float* cv, float tx, float ty, float tz) {
+    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
+    const float c00 = __fadd_rn(__fmul_rn(cv[0], oz), __fmul_rn(cv[1], tz));
+    const float c01 = __fadd_rn(__fmul_rn(cv[2], oz), __fmul_rn(cv[3], tz));
+    const float c10 = __fadd_rn(__fmul_rn(cv[4], oz), __fmul_rn(cv[5], tz));
+    const float c11 = __fadd_rn(__fmul_rn(cv[6], oz), __fmul_rn(cv[7], tz));
+    const float c0 = __fadd_rn(__fmul_rn(c00, oy), __fmul_rn(c01, ty));
+    const float c1 = __fadd_rn(__fmul_rn(c10, oy), __fmul_rn(c11, ty));
+    return __fadd_rn(__fmul_rn(c0, ox), __fmul_rn(c1, tx));
+}
+
+__device__ __forceinline__ void cell_normal(const Cell8& cc, const float* p, float* n) {
+    float csz[3], t[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        csz[a] = __fsub_rn(cc.p[7][a], cc.p[0][a]);
+        t[a] = __fdiv_rn(__fsub_rn(p[a], cc.p[0][a]), csz[a]);
+        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
+    }
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float tp[3] = {t[0], t[1], t[2]}, tm[3] = {t[0], t[1], t[2]};
+        tp[a] = fminf(__fadd_rn(t[a], 0.02f), 0.99f);
+        tm[a] = fmaxf(__fsub_rn(t[a], 0.02f), 0.01f);
+        d[a] = __fdiv_rn(__fsub_rn(trilin(cc.v, tp[0], tp[1], tp[2]), trilin(cc.v, tm[0], tm[1], tm[2])),
+                         __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]));
+    }
+    const float len =
+        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+    if (len > 1e-8f) {
+        n[0] = __fdiv_rn(d[0], len); n[1] = __fdiv_rn(d[1], len); n[2] = __fdiv_rn(d[2], len);
+    } else {
+        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
+    }
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_its_count(SpGrid g, const float* __restrict__ vals,
+                                                         long long n, unsigned long long* blk) {
+    __shared__ uint32_t sm[33];
+    __shared__ uint32_t sk[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t na = 0, nk = 0;
+    if (c < n) {
+        uint32_t cs = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cs |= (iso::below(vals[8 * c + k], g.level) ? 1u : 0u) << k;
+        nk = __popc(uint32_t(ISO_EDGE_STATUS[cs]));
+        na = nk ? 1u : 0u;
+    }
+    uint32_t e, ta, tk;
+    block_scan1(na, e, ta, sm);
+    block_scan1(nk, e, tk, sk);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = ta; blk[2 * blockIdx.x + 1] = tk; }
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_its_emit(SpGrid g, const int* __restrict__ ids,
+                                                        const float* __restrict__ vals, long long n,
+                                                        const unsigned long long* __restrict__ blk,
+                                                        float* points, float* normals, int* act_sparse,
+                                                        int* act_uniform, int* offsets, uint32_t* rank,
+                                                        long long A, long long K) {
+    __shared__ uint32_t sm[33];
+    __shared__ uint32_t sk[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t na = 0, nk = 0, est = 0;
+    if (c < n) {
+        uint32_t cs = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cs |= (iso::below(vals[8 * c + k], g.level) ? 1u : 0u) << k;
+        est = ISO_EDGE_STATUS[cs];
+        nk = __popc(est);
+        na = nk ? 1u : 0u;
+    }
+    uint32_t ea, ek, ta, tk;
+    block_scan1(na, ea, ta, sm);
+    block_scan1(nk, ek, tk, sk);
+    if (c >= n) return;
+    const unsigned long long a = blk[2 * blockIdx.x] + ea;
+    rank[c] = na ? uint32_t(a) : 0xffffffffu;
+    if (!na) return;
+    unsigned long long k = blk[2 * blockIdx.x + 1] + ek;
+    Cell8 cc;
+    int x, y, z;
+    load_cell(g, ids, vals, c, cc, x, y, z);
+    act_sparse[a] = int(c);
+    act_uniform[a] = ids[c];
+    offsets[a] = int(k);
+    for (int e = 0; e < 12; ++e) {
+        if (!((est >> e) & 1u)) continue;
+        float p[3];
+        edge_point(cc, e, g.level, p);
+        points[3 * k] = p[0]; points[3 * k + 1] = p[1]; points[3 * k + 2] = p[2];
+        if (normals) {
+            float nn[3];
+            cell_normal(cc, p, nn);
+            normals[3 * k] = nn[0]; normals[3 * k + 1] = nn[1]; normals[3 * k + 2] = nn[2];
+        }
+        ++k;
+    }
+    if (a + 1 == (unsigned long long)A) offsets[A] = int(K);
+}
+
+// Normals of an existing sparse intersection.
+__global__ void sp_normals(SpGrid g, const int* __restrict__ ids, const float* __restrict__ vals,
+                           const int* __restrict__ act_sparse, const int* __restrict__ offsets, long long A,
+                           const float* __restrict__ points, float* normals) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    Cell8 cc;
+    int x, y, z;
+    load_cell(g, ids, vals, act_sparse[a], cc, x, y, z);
+    for (int k = offsets[a]; k < offsets[a + 1]; ++k) {
+        const float p[3] = {points[3 * k], points[3 * k + 1], points[3 * k + 2]};
+        float nn[3];
+        cell_normal(cc, p, nn);
+        normals[3 * k] = nn[0]; normals[3 * k + 1] = nn[1]; normals[3 * k + 2] = nn[2];
+    }
+}
+
+// --- quads ---------------------------------------------------------------------
+
+__device__ __forceinline__ long long find_cell(const int* ids, long long n, uint32_t id) {
+    long long lo = 0, hi = n;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (uint32_t(ids[mid]) < id) lo = mid + 1; else hi = mid;
+    }
+    return (lo < n && uint32_t(ids[lo]) == id) ? lo : -1;
+}
+
+// Edge (corner a -> corner b of cell s) crossed according to sparse cell s.
+__device__ __forceinline__ int edge_sign(const float* vals, long long s, int a, int b, float level) {
+    const bool ba = iso::below(vals[8 * s + a], level), bb = iso::below(vals[8 * s + b], level);
+    return ba == bb ? -1 : (ba ? 1 : 0);  // -1 not crossed; else is_out = low endpoint below
+}
+
+// For cell c's edge along `ax` at its lowest corner: the quad's 4 sparse cells
+// and its orientation; false when it has no quad.
+__device__ bool cell_quad(const SpGrid& g, const int* ids, const float* vals, long long n, long long c, int ax,
+                          long long* q, bool& out) {
+    int x, y, z;
+    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+    // edge_neighbors_table (src/shared_luts.cu:78-81): cells p - o_i
+    const int o[3][4][3] = {{{0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}},
+                            {{0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 0, 0}},
+                            {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}}};
+    // the edge, as corners of a neighbour cell whose offset is (dx, dy, dz):
+    // its low corner is at (dx, dy, dz) relative to that cell
+    const int step = ax == 0 ? 4 : (ax == 1 ? 2 : 1);
+    int crossed = -1;
+    long long first = -1;
+    for (int i = 0; i < 4; ++i) {
+        const int cx = x - o[ax][i][0], cy = y - o[ax][i][1], cz = z - o[ax][i][2];
+        if (cx < 0 || cy < 0 || cz < 0 || cx > g.nx - 2 || cy > g.ny - 2 || cz > g.nz - 2) return false;
+        const uint32_t id = (uint32_t(cx) * uint32_t(g.ny - 1) + uint32_t(cy)) * uint32_t(g.nz - 1) + uint32_t(cz);
+        q[i] = find_cell(ids, n, id);
+        if (q[i] < 0) return false;
+    }
+    // crossing status: isoext keeps an edge if any cell reports it crossed; its
+    // orientation comes from the first such cell in sparse order
+    for (int i = 0; i < 4; ++i) {
+        const int ca = 4 * o[ax][i][0] + 2 * o[ax][i][1] + o[ax][i][2];
+        const int s = edge_sign(vals, q[i], ca, ca + step, g.level);
+        if (s >= 0 && (first < 0 || q[i] < first)) {
+            first = q[i];
+            crossed = s;
+        }
+    }
+    if (crossed < 0) return false;
+    out = crossed == 1;
+    return true;
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_quad_count(SpGrid g, const int* __restrict__ ids,
+                                                          const float* __restrict__ vals, long long n,
+                                                          const uint32_t* __restrict__ rank,
+                                                          unsigned long long* blk) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t nq = 0;
+    if (c < n) {
+        for (int ax = 2; ax >= 0; --ax) {
+            long long q[4];
+            bool out;
+            if (!cell_quad(g, ids, vals, n, c, ax, q, out)) continue;
+            bool ok = true;
+            for (int i = 0; i < 4; ++i) ok &= rank[q[i]] != 0xffffffffu;
+            nq += ok;
+        }
+    }
+    uint32_t e, t;
+    block_scan1(nq, e, t, sm);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = t; blk[2 * blockIdx.x + 1] = 0; }
+}
+
+__device__ __forceinline__ float dist3(const float* a, const float* b) {
+    const float dx = __fsub_rn(a[0], b[0]), dy = __fsub_rn(a[1], b[1]), dz = __fsub_rn(a[2], b[2]);
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_quad_emit(SpGrid g, const int* __restrict__ ids,
+                                                         const float* __restrict__ vals, long long n,
+                                                         const uint32_t* __restrict__ rank,
+                                                         const unsigned long long* __restrict__ blk,
+                                                         const float* __restrict__ dual, int* tri) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t nq = 0;
+    long long qs[3][4];
+    bool outs[3], oks[3] = {false, false, false};
+    if (c < n) {
+        for (int ax = 2; ax >= 0; --ax) {
+            if (!cell_quad(g, ids, vals, n, c, ax, qs[ax], outs[ax])) continue;
+            bool ok = true;
+            for (int i = 0; i < 4; ++i) ok &= rank[qs[ax][i]] != 0xffffffffu;
+            oks[ax] = ok;
+            nq += ok;
+        }
+    }
+    uint32_t e, t;
+    block_scan1(nq, e, t, sm);
+    if (!nq) return;
+    unsigned long long qo = blk[2 * blockIdx.x] + e;
+    for (int ax = 2; ax >= 0; --ax) {
+        if (!oks[ax]) continue;
+        int32_t qi[4];
+        for (int i = 0; i < 4; ++i) qi[i] = int32_t(rank[qs[ax][i]]);
+        if (!outs[ax]) {
+            const int32_t t0 = qi[0], t1 = qi[1];
+            qi[0] = qi[3]; qi[1] = qi[2]; qi[2] = t1; qi[3] = t0;
+        }
+        float v[4][3];
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) v[i][k] = dual[3 * (long long)qi[i] + k];
+        int* o6 = tri + 6 * qo;
+        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+            o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0]; o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
+        } else {
+            o6[0] = qi[2]; o6[1] = qi[0]; o6[2] = qi[1]; o6[3] = qi[0]; o6[4] = qi[2]; o6[5] = qi[3];
+        }
+        ++qo;
+    }
+}
+
+// --- population helpers ------------------------------------------------------
+
+// Corner positions [M, 8, 3] of cells given by linear id.
+__global__ void sp_points(SpGrid g, const int* __restrict__ ids, long long m, float* out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m * 8) return;
+    const long long c = i >> 3;
+    const int k = int(i & 7);
+    int x, y, z;
+    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+    out[3 * i] = iso::grid_coord(x + (k >> 2), g.nx, g.amin[0], g.asize[0]);
+    out[3 * i + 1] = iso::grid_coord(y + ((k >> 1) & 1), g.ny, g.amin[1], g.asize[1]);
+    out[3 * i + 2] = iso::grid_coord(z + (k & 1), g.nz, g.amin[2], g.asize[2]);
+}
+
+// Keep the ids whose 8 values straddle the level (src/grid/sparse.cu:150-179),
+// in input order.
+__global__ void __launch_bounds__(SP_BLOCK) sp_filter_count(const float* __restrict__ vals, long long m,
+                                                            float level, unsigned long long* blk) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t keep = 0;
+    if (c < m) {
+        uint32_t cs = 0;
+        for (int k = 0; k < 8; ++k) cs |= (iso::below(vals[8 * c + k], level) ? 1u : 0u) << k;
+        keep = (cs != 0 && cs != 255);
+    }
+    uint32_t e, t;
+    block_scan1(keep, e, t, sm);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = t; blk[2 * blockIdx.x + 1] = 0; }
+}
+
+__global__ void __launch_bounds__(SP_BLOCK) sp_filter_write(const int* __restrict__ ids,
+                                                            const float* __restrict__ vals, long long m,
+                                                            float level,
+                                                            const unsigned long long* __restrict__ blk,
+                                                            int* out) {
+    __shared__ uint32_t sm[33];
+    const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
+    uint32_t keep = 0;
+    if (c < m) {
+        uint32_t cs = 0;
+        for (int k = 0; k < 8; ++k) cs |= (iso::below(vals[8 * c + k], level) ? 1u : 0u) << k;
+        keep = (cs != 0 && cs != 255);
+    }
+    uint32_t e, t;
+    block_scan1(keep, e, t, sm);
+    if (keep) out[blk[2 * blockIdx.x] + e] = ids[c];
+}
+
+SpGrid mk(int nx, int ny, int nz, const float* amin, const float* amax, float level, int method) {
+    SpGrid g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    for (int k = 0; k < 3; ++k) { g.amin[k] = amin[k]; g.asize[k] = amax[k] - amin[k]; }
+    g.level = level;
+    g.method = method;
+    return g;
+}
+unsigned nb(long long n, int b) { return unsigned(std::max<long long>(1, (n + b - 1) / b)); }
+
+}  // namespace
+
+// dc_block_scan lives in dc_dense.cu
+void iso_block_scan_launch(unsigned long long* blk, long long nblk, long long* totals, cudaStream_t st);
+
+extern "C" {
+
+// Block sums workspace: 16 bytes per 1024 entries.
+size_t iso_sparse_blocks_size(long long n) { return size_t((n + SP_BLOCK - 1) / SP_BLOCK + 1) * 16 + 256; }
+
+int iso_sparse_mc_count(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
+                        const float* amin, const float* amax, float level, int method, void* blk,
+                        long long* counts, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (method != 0 && method != 1) return ISO_ERR_ARG;
+    SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
+    iso::ProfScope ps("sparse_mc", st);
+    sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)blk);
+    iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_mc_emit(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
+                       const float* amin, const float* amax, float level, int method, const void* blk,
+                       float* soup, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n <= 0) return 0;
+    SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
+    iso::ProfScope ps("sparse_mc", st);
+    sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, soup);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_its_count(const float* vals, long long n, float level, void* blk, long long* counts,
+                         void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    SpGrid g{};
+    g.level = level;
+    iso::ProfScope ps("sparse_its", st);
+    sp_its_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, vals, n, (unsigned long long*)blk);
+    iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+// Intersection arrays; act_sparse / act_uniform: sparse index / lattice id of
+// each active cell; rank[n]: active index of each sparse cell (or -1).
+int iso_sparse_its_emit(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
+                        const float* amin, const float* amax, float level, const void* blk, long long A,
+                        long long K, float* points, float* normals, int* act_sparse, int* act_uniform,
+                        int* offsets, int* rank, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (A == 0 && offsets) cudaMemsetAsync(offsets, 0, 4, st);
+    if (n <= 0) return 0;
+    SpGrid g = mk(nx, ny, nz, amin, amax, level, 0);
+    iso::ProfScope ps("sparse_its", st);
+    sp_its_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, points,
+                                                      normals, act_sparse, act_uniform, offsets,
+                                                      reinterpret_cast<uint32_t*>(rank), A, K);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_normals(const int* ids, const float* vals, int nx, int ny, int nz, const float* amin,
+                       const float* amax, const int* act_sparse, const int* offsets, long long A,
+                       const float* points, float* normals, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (A <= 0) return 0;
+    SpGrid g = mk(nx, ny, nz, amin, amax, 0.0f, 0);
+    iso::ProfScope ps("sparse_its", st);
+    sp_normals<<<nb(A, 256), 256, 0, st>>>(g, ids, vals, act_sparse, offsets, A, points, normals);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_quads_count(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
+                           float level, const int* rank, void* blk, long long* counts, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    const float z3[3] = {0, 0, 0}, o3[3] = {1, 1, 1};
+    SpGrid g = mk(nx, ny, nz, z3, o3, level, 0);
+    iso::ProfScope ps("sparse_quads", st);
+    sp_quad_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, reinterpret_cast<const uint32_t*>(rank),
+                                                        (unsigned long long*)blk);
+    iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_quads_emit(const int* ids, const float* vals, long long n, int nx, int ny, int nz, float level,
+                          const int* rank, const void* blk, const float* dual, int* tri, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n <= 0) return 0;
+    const float z3[3] = {0, 0, 0}, o3[3] = {1, 1, 1};
+    SpGrid g = mk(nx, ny, nz, z3, o3, level, 0);
+    iso::ProfScope ps("sparse_quads", st);
+    sp_quad_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, reinterpret_cast<const uint32_t*>(rank),
+                                                       (const unsigned long long*)blk, dual, tri);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_points(const int* ids, long long m, int nx, int ny, int nz, const float* amin,
+                      const float* amax, float* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (m <= 0) return 0;
+    SpGrid g = mk(nx, ny, nz, amin, amax, 0.0f, 0);
+    sp_points<<<nb(m * 8, 256), 256, 0, st>>>(g, ids, m, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_filter_count(const float* vals, long long m, float level, void* blk, long long* counts,
+                            void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (m <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    sp_filter_count<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(vals, m, level, (unsigned long long*)blk);
+    iso_block_scan_launch((unsigned long long*)blk, nb(m, SP_BLOCK), counts, st);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_sparse_filter_write(const int* ids, const float* vals, long long m, float level, const void* blk,
+                            int* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (m <= 0) return 0;
+    sp_filter_write<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(ids, vals, m, level, (const unsigned long long*)blk, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+}  // extern "C"

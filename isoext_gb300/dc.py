@@ -16,7 +16,7 @@ from .grids import SparseGridBase, UniformGrid, _check_cuda_f32
 
 _vp, _i, _ll, _f, _sz = C.c_void_p, C.c_int, C.c_longlong, C.c_float, C.c_size_t
 _fa = C.POINTER(C.c_float)
-_ffi._EXTRA.update({
+_ffi.register({
     "iso_dc_workspace_size": ([_i, _i, _i], _sz),
     "iso_dc_classify": ([_vp, _i, _i, _i, _f, _vp, _sz, _vp, _vp], _i),
     "iso_dc_intersect": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _vp], _i),

@@ -1,0 +1,278 @@
+"""SparseGrid with isoext's API (src/isoext_ext.cu:170-303, src/grid/sparse.cu:9-246)
+and its marching cubes / intersection / dual contouring on the CUDA path
+(csrc/sparse.cu).
+
+A sparse grid holds a sorted list of cell ids on the lattice of a ``shape``-point
+grid and 8 corner values per cell ([N, 8], corner k = 4x + 2y + z).  Cells do not
+share storage, so -- as in isoext -- MC vertices are welded by exact position and
+every cell uses its own 8 values.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _ffi
+from .grids import FLT_MAX, SparseGridBase, _INT_MAX, _check_cuda_f32, _shape3, _vec3
+
+_vp, _i, _ll, _f, _sz = C.c_void_p, C.c_int, C.c_longlong, C.c_float, C.c_size_t
+_fa = C.POINTER(C.c_float)
+_ffi.register({
+    "iso_sparse_blocks_size": ([_ll], _sz),
+    "iso_sparse_mc_count": ([_vp, _vp, _ll, _i, _i, _i, _fa, _fa, _f, _i, _vp, _vp, _vp], _i),
+    "iso_sparse_mc_emit": ([_vp, _vp, _ll, _i, _i, _i, _fa, _fa, _f, _i, _vp, _vp, _vp], _i),
+    "iso_sparse_its_count": ([_vp, _ll, _f, _vp, _vp, _vp], _i),
+    "iso_sparse_its_emit": ([_vp, _vp, _ll, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _ll, _vp, _vp, _vp, _vp,
+                             _vp, _vp, _vp], _i),
+    "iso_sparse_normals": ([_vp, _vp, _i, _i, _i, _fa, _fa, _vp, _vp, _ll, _vp, _vp, _vp], _i),
+    "iso_sparse_quads_count": ([_vp, _vp, _ll, _i, _i, _i, _f, _vp, _vp, _vp, _vp], _i),
+    "iso_sparse_quads_emit": ([_vp, _vp, _ll, _i, _i, _i, _f, _vp, _vp, _vp, _vp, _vp], _i),
+    "iso_sparse_points": ([_vp, _ll, _i, _i, _i, _fa, _fa, _vp, _vp], _i),
+    "iso_sparse_filter_count": ([_vp, _ll, _f, _vp, _vp, _vp], _i),
+    "iso_sparse_filter_write": ([_vp, _vp, _ll, _f, _vp, _vp, _vp], _i),
+})
+
+
+def _p(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(dev):
+    return C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+
+def _check_ids(t, what="new_cell_indices"):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{what} must be a torch.Tensor")
+    if t.dtype != torch.int32 or not t.is_cuda or not t.is_contiguous() or t.dim() != 1:
+        raise TypeError(f"{what} must be a 1D C-contiguous int32 CUDA tensor")
+
+
+def _as_uint(ids: torch.Tensor) -> torch.Tensor:
+    """int32 ids read as uint32 (isoext casts the binding's int32 to uint), int64."""
+    return ids.to(torch.int64) & 0xFFFFFFFF
+
+
+def _from_uint(u: torch.Tensor) -> torch.Tensor:
+    return torch.where(u >= 2**31, u - 2**32, u).to(torch.int32).contiguous()
+
+
+class SparseGrid(SparseGridBase):
+    """Sparse grid of cells over a ``shape``-point lattice (isoext.SparseGrid).
+
+    ``shape`` counts lattice points per axis: cell (x, y, z) has id
+    x (sy-1)(sz-1) + y (sz-1) + z and corners at points (x..x+1, y..y+1, z..z+1).
+    """
+
+    def __init__(self, shape, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0, 1.0, 1.0),
+                 default_value: float = FLT_MAX, device=None):
+        s = _shape3(shape)
+        if s[0] * s[1] * s[2] > _INT_MAX:
+            raise RuntimeError("Maximum number of points exceeds maximum value 2147483647 (max int)")
+        self.shape = s
+        self.aabb_min = _vec3(aabb_min)
+        self.aabb_max = _vec3(aabb_max)
+        self.default_value = float(np.float32(default_value))
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._ids = torch.empty(0, dtype=torch.int32, device=dev)   # ascending as uint32
+        self._values = torch.empty((0, 8), dtype=torch.float32, device=dev)
+
+    @property
+    def device(self) -> torch.device:
+        return self._ids.device
+
+    # -- container API --------------------------------------------------------------
+
+    def get_num_cells(self) -> int:
+        return int(self._ids.numel())
+
+    def get_num_points(self) -> int:
+        return 8 * int(self._ids.numel())
+
+    def get_shape(self) -> list[int]:
+        return list(self.shape)
+
+    def get_cell_indices(self) -> torch.Tensor:
+        return self._ids.clone()
+
+    def get_values(self) -> torch.Tensor:
+        return self._values.clone()
+
+    def set_values(self, new_values: torch.Tensor) -> None:
+        _check_cuda_f32(new_values, ndim=2, last=8, what="new_values")
+        if new_values.numel() != self.get_num_points():
+            raise RuntimeError("New values size does not match number of points")
+        self._values.copy_(new_values)
+
+    def get_cells(self) -> torch.Tensor:
+        """Point ids of each cell's corners in get_points() order: arange(8N).view(N, 8)."""
+        n = self.get_num_cells()
+        return torch.arange(8 * n, dtype=torch.int32, device=self.device).view(n, 8)
+
+    def _reset_values(self):
+        # isoext refills every value with the default after add/remove (src/grid/sparse.cu:94-95)
+        self._values = torch.full((self.get_num_cells(), 8), self.default_value, dtype=torch.float32,
+                                  device=self.device)
+
+    def add_cells(self, new_cell_indices: torch.Tensor) -> None:
+        """Union with new ids (sorted, unique); all values reset to default_value."""
+        _check_ids(new_cell_indices)
+        u = torch.cat([_as_uint(self._ids), _as_uint(new_cell_indices)])
+        self._ids = _from_uint(torch.unique(u, sorted=True))
+        self._reset_values()
+
+    def remove_cells(self, new_cell_indices: torch.Tensor) -> None:
+        """Set difference; all values reset to default_value."""
+        _check_ids(new_cell_indices)
+        keep = ~torch.isin(_as_uint(self._ids), _as_uint(new_cell_indices))
+        self._ids = self._ids[keep].contiguous()
+        self._reset_values()
+
+    def get_potential_cell_indices(self, chunk_size: int) -> list[torch.Tensor]:
+        """All ids 0 .. sx*sy*sz - 1 in chunks of chunk_size (src/grid/sparse.cu:128-142;
+        isoext counts sx*sy*sz ids although the lattice has (sx-1)(sy-1)(sz-1) cells)."""
+        chunk = int(chunk_size)
+        if chunk <= 0:
+            raise RuntimeError("chunk_size must be positive")
+        total = self.shape[0] * self.shape[1] * self.shape[2]
+        return [torch.arange(s, min(s + chunk, total), dtype=torch.int32, device=self.device)
+                for s in range(0, total, chunk)]
+
+    def get_points_by_cell_indices(self, cell_indices: torch.Tensor) -> torch.Tensor:
+        """Corner positions [M, 8, 3] of the given cell ids."""
+        _check_ids(cell_indices, "cell_indices")
+        return self._points_of(cell_indices)
+
+    def get_points(self) -> torch.Tensor:
+        """Corner positions [N, 8, 3] of the grid's cells."""
+        return self._points_of(self._ids)
+
+    def _points_of(self, ids: torch.Tensor) -> torch.Tensor:
+        m = int(ids.numel())
+        out = torch.empty((m, 8, 3), dtype=torch.float32, device=ids.device)
+        if m:
+            sx, sy, sz = self.shape
+            _ffi.check(_ffi.lib().iso_sparse_points(_p(ids), m, sx, sy, sz, _ffi.fvec3(self.aabb_min),
+                                                    _ffi.fvec3(self.aabb_max), _p(out), _stream(ids.device)))
+        return out
+
+    def filter_cell_indices(self, cell_indices: torch.Tensor, values: torch.Tensor,
+                            level: float = 0.0) -> torch.Tensor:
+        """Ids whose 8 values straddle ``level`` (case not 0 or 255), in input order."""
+        _check_ids(cell_indices, "cell_indices")
+        _check_cuda_f32(values, ndim=2, last=8, what="values")
+        m = int(cell_indices.numel())
+        if values.shape[0] != m:
+            raise RuntimeError("values must have one row of 8 per cell index")
+        lib = _ffi.lib()
+        dev = cell_indices.device
+        st = _stream(dev)
+        blk = torch.empty(int(lib.iso_sparse_blocks_size(m)), dtype=torch.uint8, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        _ffi.check(lib.iso_sparse_filter_count(_p(values), m, float(level), _p(blk), _p(counts), st))
+        k = int(counts[0].item())
+        out = torch.empty(k, dtype=torch.int32, device=dev)
+        if k:
+            _ffi.check(lib.iso_sparse_filter_write(_p(cell_indices), _p(values), m, float(level), _p(blk),
+                                                   _p(out), st))
+        return out
+
+    # -- extraction --------------------------------------------------------------
+
+    def _geom(self):
+        sx, sy, sz = self.shape
+        return sx, sy, sz, _ffi.fvec3(self.aabb_min), _ffi.fvec3(self.aabb_max)
+
+    def _marching_cubes(self, level: float, method: int):
+        from .dc import weld_dual
+
+        lib = _ffi.lib()
+        dev = self.device
+        n = self.get_num_cells()
+        if n == 0:
+            return None, None
+        st = _stream(dev)
+        sx, sy, sz, lo, hi = self._geom()
+        blk = torch.empty(int(lib.iso_sparse_blocks_size(n)), dtype=torch.uint8, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        _ffi.check(lib.iso_sparse_mc_count(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi,
+                                           float(level), int(method), _p(blk), _p(counts), st))
+        F = int(counts[0].item())
+        if F == 0:
+            return None, None
+        soup = torch.empty((3 * F, 3), dtype=torch.float32, device=dev)
+        _ffi.check(lib.iso_sparse_mc_emit(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi,
+                                          float(level), int(method), _p(blk), _p(soup), st))
+        tri = torch.arange(3 * F, dtype=torch.int32, device=dev)
+        return weld_dual(lib, dev, soup, 3 * F, tri, st)
+
+    def _intersect(self, level: float, compute_normals: bool):
+        from .dc import Intersection
+
+        lib = _ffi.lib()
+        dev = self.device
+        n = self.get_num_cells()
+        st = _stream(dev)
+        sx, sy, sz, lo, hi = self._geom()
+        blk = torch.empty(int(lib.iso_sparse_blocks_size(n)), dtype=torch.uint8, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        _ffi.check(lib.iso_sparse_its_count(_p(self._values), n, float(level), _p(blk), _p(counts), st))
+        A, K = (int(x) for x in counts.cpu())
+        points = torch.empty((K, 3), dtype=torch.float32, device=dev)
+        normals = torch.empty((K, 3), dtype=torch.float32, device=dev) if compute_normals else None
+        act = torch.empty(A, dtype=torch.int32, device=dev)
+        act_lattice = torch.empty(A, dtype=torch.int32, device=dev)
+        offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
+        rank = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        _ffi.check(lib.iso_sparse_its_emit(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi,
+                                           float(level), _p(blk), A, K, _p(points), _p(normals), _p(act),
+                                           _p(act_lattice), _p(offs), _p(rank), st))
+        key = (tuple(self.shape), tuple(self.aabb_min), tuple(self.aabb_max), id(self))
+        sparse = {"lattice": act_lattice, "rank": rank, "n": n}
+        return Intersection(points, normals, act, offs, level, key, sparse=sparse)
+
+    def _get_intersection(self, level: float, compute_normals: bool):
+        return self._intersect(level, compute_normals)
+
+    def _dual_contouring(self, level, its, reg, svd_tol):
+        from .dc import weld_dual
+
+        lib = _ffi.lib()
+        dev = self.device
+        st = _stream(dev)
+        sx, sy, sz, lo, hi = self._geom()
+        if its is None:
+            its = self._intersect(level, True)
+        elif its._sparse is None or its._grid_key[:3] != (tuple(self.shape), tuple(self.aabb_min),
+                                                            tuple(self.aabb_max)) \
+                or its._sparse["n"] != self.get_num_cells():
+            raise RuntimeError("intersection was computed for a different grid")
+        A = int(its._cells.numel())
+        n = self.get_num_cells()
+        normals = its._normals
+        if normals is None:
+            normals = torch.empty_like(its._points)
+            _ffi.check(lib.iso_sparse_normals(_p(self._ids), _p(self._values), sx, sy, sz, lo, hi,
+                                              _p(its._cells), _p(its._offsets), A, _p(its._points),
+                                              _p(normals), st))
+        if A == 0:
+            return None, None
+        dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
+        _ffi.check(lib.iso_dc_solve(sx, sy, sz, lo, hi, _p(its._points), _p(normals),
+                                    _p(its._sparse["lattice"]), _p(its._offsets), A, float(reg),
+                                    float(svd_tol), _p(dual), st))
+        blk = torch.empty(int(lib.iso_sparse_blocks_size(n)), dtype=torch.uint8, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        rank = its._sparse["rank"]
+        _ffi.check(lib.iso_sparse_quads_count(_p(self._ids), _p(self._values), n, sx, sy, sz,
+                                              float(its._level), _p(rank), _p(blk), _p(counts), st))
+        Q = int(counts[0].item())
+        if Q == 0:
+            return None, None
+        tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
+        _ffi.check(lib.iso_sparse_quads_emit(_p(self._ids), _p(self._values), n, sx, sy, sz,
+                                             float(its._level), _p(rank), _p(blk), _p(dual), _p(tri), st))
+        return weld_dual(lib, dev, dual, A, tri, st)

@@ -577,7 +577,7 @@ int ora_dc(const float *vals, const int32_t *cell_ids, int64_t nsparse, int spar
     for (uint32_t i = 0; i < ncell; i++) amap[i] = -1;
     for (int64_t a = 0; a < A; a++) {
         uint32_t lat = sparse ? (uint32_t)cell_ids[its->cells[a]] : its->cells[a];
-        amap[lat] = (int32_t)a;
+        if (lat < ncell) amap[lat] = (int32_t)a; /* ids past the lattice have no quads */
     }
 
     /* --- quads -> triangle soup, src/dc.cu:101-157 --- */

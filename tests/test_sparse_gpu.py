@@ -1,0 +1,242 @@
+"""SparseGrid on the GPU against the reference's fixtures and the oracle.
+
+MC: bit-exact positions, faces equal after relabelling (isoext welds by
+position; here vertices come in first-occurrence order).  Intersections:
+bit-exact.  DC: positions within 1e-4 * h of the FP64 oracle, quads as in
+test_dc_gpu.
+"""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import isoext_gb300 as iso
+from helpers import assert_same_mesh, grid_points, sphere, torus
+from test_dc_gpu import assert_dc_match, cell_h
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def sparse_from_dense(values, keep="active", extra=0, seed=0, level=0.0):
+    """(ids, vals [N, 8]) of the cells of a dense grid whose corners straddle the
+    level, plus `extra` random other cells (consistent values)."""
+    shape = values.shape
+    n = np.asarray(shape)
+    cx, cy, cz = np.meshgrid(*[np.arange(k - 1) for k in shape], indexing="ij")
+    vals = np.stack([values[cx + (k >> 2), cy + ((k >> 1) & 1), cz + (k & 1)] for k in range(8)], -1)
+    ids = ((cx * (n[1] - 1) + cy) * (n[2] - 1) + cz).astype(np.int64)
+    neg = (vals < level).sum(-1)
+    mask = (neg > 0) & (neg < 8) if keep == "active" else np.ones_like(neg, bool)
+    if extra:
+        rng = np.random.default_rng(seed)
+        flat = np.nonzero(~mask.ravel())[0]
+        pick = rng.choice(flat, size=min(extra, len(flat)), replace=False)
+        m2 = mask.ravel().copy()
+        m2[pick] = True
+        mask = m2.reshape(mask.shape)
+    sel_ids = ids[mask].astype(np.int32)
+    sel_vals = vals[mask].astype(np.float32)
+    order = np.argsort(sel_ids)
+    return sel_ids[order], np.ascontiguousarray(sel_vals[order])
+
+
+def make_sparse(shape, ids, vals, lo=(-1, -1, -1), hi=(1, 1, 1)):
+    g = iso.SparseGrid(shape, lo, hi)
+    g.add_cells(torch.from_numpy(np.asarray(ids, np.int32)).cuda())
+    g.set_values(torch.from_numpy(np.asarray(vals, np.float32)).cuda())
+    return g
+
+
+# --- fixtures from the reference's host build -----------------------------------
+
+@pytest.mark.parametrize("method", ["nagae", "lorensen"])
+def test_sparse_mc_matches_reference_fixture(method):
+    gd = np.load(os.path.join(GOLDEN, "sparse16.npz"))
+    shape = tuple(int(x) for x in gd["shape"])
+    g = make_sparse(shape, gd["cell_ids"], gd["values"])
+    v, f = iso.marching_cubes(g, method=method)
+    assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), gd[f"mc_{method}_v"], gd[f"mc_{method}_f"], method)
+
+
+def test_sparse_dc_matches_reference_fixture():
+    gd = np.load(os.path.join(GOLDEN, "sparse16.npz"))
+    shape = tuple(int(x) for x in gd["shape"])
+    g = make_sparse(shape, gd["cell_ids"], gd["values"])
+    v, f = iso.dual_contouring(g)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), gd["dc_v"], gd["dc_f"], cell_h(shape), "sparse16")
+
+
+# --- against the oracle ------------------------------------------------------------
+
+@pytest.mark.parametrize("method", ["nagae", "lorensen"])
+@pytest.mark.parametrize("extra", [0, 500])
+def test_sparse_mc_matches_oracle(oracle, method, extra):
+    vals = torus((40, 36, 44), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals, extra=extra, seed=extra)
+    g = make_sparse(vals.shape, ids, cv)
+    v, f = iso.marching_cubes(g, method=method)
+    vo, fo, _ = oracle.mc_sparse(ids, cv, vals.shape, method=method)
+    assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, f"{method} extra {extra}")
+
+
+def test_sparse_mc_inconsistent_values(oracle):
+    # independent random values per cell: shared corners disagree, so welding
+    # by exact position is all that joins cells
+    rng = np.random.default_rng(7)
+    shape = (12, 10, 14)
+    ncell = 11 * 9 * 13
+    ids = np.sort(rng.choice(ncell, size=600, replace=False)).astype(np.int32)
+    cv = rng.standard_normal((600, 8)).astype(np.float32)
+    cv[rng.random((600, 8)) < 0.05] = 0.0  # exact zeros: vertices on grid points
+    g = make_sparse(shape, ids, cv)
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, shape, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, method)
+
+
+def test_sparse_intersection_matches_oracle(oracle):
+    vals = sphere((36, 36, 36), 0.6, center=(0.02, -0.03, 0.01))
+    ids, cv = sparse_from_dense(vals, extra=300, seed=3)
+    g = make_sparse(vals.shape, ids, cv)
+    for normals in (False, True):
+        its = iso.get_intersection(g, compute_normals=normals)
+        ref = oracle.intersection_sparse(ids, cv, vals.shape, normals=normals)
+        assert np.array_equal(its.get_points().cpu().numpy(), ref["points"])
+        if normals:
+            assert np.array_equal(its.get_normals().cpu().numpy(), ref["normals"])
+        assert np.array_equal(its._cells.cpu().numpy().astype(np.uint32), ref["cell_indices"])
+        assert np.array_equal(its._offsets.cpu().numpy().astype(np.uint32), ref["cell_offsets"])
+
+
+@pytest.mark.parametrize("extra", [0, 400])
+def test_sparse_dc_matches_oracle(oracle, extra):
+    vals = sphere((40, 40, 40), 0.6, center=(0.03, 0.01, -0.02))
+    ids, cv = sparse_from_dense(vals, extra=extra, seed=11)
+    g = make_sparse(vals.shape, ids, cv)
+    v, f = iso.dual_contouring(g)
+    its = oracle.intersection_sparse(ids, cv, vals.shape)
+    vo, fo, _ = oracle.dc(its, vals.shape, values=cv, cell_ids=ids)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vo, fo, cell_h(vals.shape), f"extra {extra}")
+
+
+def test_sparse_dc_user_intersection(oracle):
+    vals = torus((36, 36, 36), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals)
+    g = make_sparse(vals.shape, ids, cv)
+    its = iso.get_intersection(g)
+    assert not its.has_normals()
+    v, f = iso.dual_contouring(g, intersection=its)  # normals computed from the grid
+    ref = oracle.intersection_sparse(ids, cv, vals.shape)
+    vo, fo, _ = oracle.dc(ref, vals.shape, values=cv, cell_ids=ids)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vo, fo, cell_h(vals.shape), "auto normals")
+    pts = its.get_points()
+    n = torch.nn.functional.normalize(pts - pts.mean(0), dim=-1).contiguous()
+    its.set_normals(n)
+    v, f = iso.dual_contouring(g, intersection=its)
+    ref["normals"] = n.cpu().numpy()
+    vo, fo, _ = oracle.dc(ref, vals.shape, values=cv, cell_ids=ids)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vo, fo, cell_h(vals.shape), "user normals")
+
+
+# --- sparse over all active cells == dense ----------------------------------------
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_sparse_equals_dense_mc(n):
+    vals = sphere((n, n, n), 0.7, center=(0.01, 0.02, -0.01))
+    ids, cv = sparse_from_dense(vals)
+    g = make_sparse(vals.shape, ids, cv)
+    d = iso.UniformGrid(vals.shape)
+    d.set_values(torch.from_numpy(vals).cuda())
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vd, fd = iso.marching_cubes(d, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vd.cpu().numpy(), fd.cpu().numpy(), method)
+
+
+def test_sparse_equals_dense_dc():
+    vals = torus((64, 64, 64), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals)
+    g = make_sparse(vals.shape, ids, cv)
+    d = iso.UniformGrid(vals.shape)
+    d.set_values(torch.from_numpy(vals).cuda())
+    v, f = iso.dual_contouring(g)
+    vd, fd = iso.dual_contouring(d)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vd.cpu().numpy(), fd.cpu().numpy(), cell_h(vals.shape))
+
+
+# --- the container API ---------------------------------------------------------------
+
+def test_sparse_container_api():
+    g = iso.SparseGrid([8, 9, 10], default_value=5.0)
+    assert g.get_num_cells() == 0 and g.get_num_points() == 0
+    g.add_cells(torch.tensor([30, 5, 30, 7], dtype=torch.int32, device="cuda"))
+    assert g.get_cell_indices().tolist() == [5, 7, 30]
+    assert g.get_num_points() == 24
+    assert torch.equal(g.get_values(), torch.full((3, 8), 5.0, device="cuda"))
+    g.set_values(torch.arange(24, dtype=torch.float32, device="cuda").view(3, 8))
+    g.add_cells(torch.tensor([6], dtype=torch.int32, device="cuda"))
+    assert g.get_cell_indices().tolist() == [5, 6, 7, 30]
+    assert (g.get_values() == 5.0).all()  # isoext resets every value on add/remove
+    g.remove_cells(torch.tensor([7, 100], dtype=torch.int32, device="cuda"))
+    assert g.get_cell_indices().tolist() == [5, 6, 30]
+    assert g.get_cells().tolist()[1] == list(range(8, 16))
+    with pytest.raises(RuntimeError, match="New values size does not match number of points"):
+        g.set_values(torch.zeros((2, 8), device="cuda"))
+    with pytest.raises(TypeError):
+        g.set_values(torch.zeros((3, 8)))
+    with pytest.raises(TypeError):
+        g.add_cells(torch.tensor([1], dtype=torch.int64, device="cuda"))
+    with pytest.raises(RuntimeError, match="max int"):
+        iso.SparseGrid([2048, 2048, 2048])
+
+
+def test_sparse_points_and_chunks():
+    shape = (17, 12, 9)
+    g = iso.SparseGrid(shape, (-1, -0.5, 0.0), (1, 0.5, 2.0))
+    ids = torch.tensor([0, 3, 57, 11 * 16 * 8 - 1], dtype=torch.int32, device="cuda")
+    g.add_cells(ids)
+    pts = g.get_points().cpu().numpy()
+    dense = grid_points(shape, (-1, -0.5, 0.0), (1, 0.5, 2.0))
+    for r, c in enumerate(ids.tolist()):
+        z = c % 8
+        y = (c // 8) % 11
+        x = c // 88
+        for k in range(8):
+            assert np.array_equal(pts[r, k], dense[x + (k >> 2), y + ((k >> 1) & 1), z + (k & 1)])
+    assert torch.equal(g.get_points_by_cell_indices(ids[1:3].contiguous()), g.get_points()[1:3])
+    chunks = g.get_potential_cell_indices(1000)
+    total = 17 * 12 * 9
+    assert len(chunks) == (total + 999) // 1000
+    assert torch.equal(torch.cat(chunks), torch.arange(total, dtype=torch.int32, device="cuda"))
+
+
+def test_sparse_population_loop_matches_dense():
+    # isoext's documented loop (doc/grids.ipynb): potential ids -> points -> SDF ->
+    # filter -> add -> set values -> extract
+    n = 48
+    g = iso.SparseGrid([n] * 3)
+    keep = []
+    for chunk in g.get_potential_cell_indices(20000):
+        p = g.get_points_by_cell_indices(chunk)
+        sdf = (p.norm(dim=-1) - 0.6).contiguous()
+        keep.append(g.filter_cell_indices(chunk, sdf))
+    g.add_cells(torch.cat(keep))
+    g.set_values((g.get_points().norm(dim=-1) - 0.6).contiguous())
+    d = iso.UniformGrid([n] * 3)
+    d.set_values((d.get_points().norm(dim=-1) - 0.6).contiguous())
+    v, f = iso.marching_cubes(g)
+    vd, fd = iso.marching_cubes(d)
+    assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vd.cpu().numpy(), fd.cpu().numpy(), "population")
+
+
+def test_sparse_empty():
+    g = iso.SparseGrid([16, 16, 16])
+    assert iso.marching_cubes(g) == (None, None)
+    assert iso.dual_contouring(g) == (None, None)
+    assert iso.get_intersection(g).get_points().shape == (0, 3)
+    g.add_cells(torch.tensor([1, 2, 3], dtype=torch.int32, device="cuda"))  # FLT_MAX values
+    assert iso.marching_cubes(g) == (None, None)
