@@ -8,11 +8,12 @@ One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
          device buffers; CUDA events on the launching stream).
   e2e    the same through the public API with host buffers: pinned host values
          -> device, UniformGrid.set_values, marching_cubes, result -> host.
-  roofline  of the dominant kernel (mc_extract): algorithmic bytes
-         4*N^3 + 12*V + 12*F per launch over its event-timed duration, against
-         the measured HBM copy bandwidth.
-  cpu_baseline  the oracle's C restatement of the reference's algorithm on the
-         host cores (rank 0 only).
+  roofline  of the kernel with the largest event-timed share: its algorithmic
+         bytes per launch over its duration, against the measured HBM copy
+         bandwidth; beside it the whole extraction's 4*N^3 + 12*V + 12*F bytes
+         over the step time.
+  cpu_baseline  the oracle's C restatement of the reference's algorithm on all
+         host cores (x slabs on threads; rank 0 only).
 --impl reference runs the reference's algorithm on the CPU (the oracle port:
 the isoext sources are not available on the GPU host) and prints the same line.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -117,6 +118,33 @@ def sphere_values(n: int, r: float) -> np.ndarray:
 
 # ---------------------------------------------------------------------------
 
+def kernel_bytes(kind: str, n: int, nv: int, nf: int) -> dict:
+    """Algorithmic bytes per launch of each kernel of the MC pipeline."""
+    pts = n ** 3
+    words = n * n * ((n + 31) // 32)
+    return {
+        "mc_signs": 4 * pts + 4 * words,           # values once, sign bitmap once
+        "mc_count": 4 * words + 4 * words,         # bitmap once, per-word entries once
+        "mc_scan": 16 * ((words + 255) // 256),    # block sums
+        "mc_emit": 8 * nv + 12 * nv + 12 * nf,     # endpoint values, vertices, faces
+        "mc_fixup": 0,                             # returns at once without snapped vertices
+    }
+
+
+def profiled_traffic(workload: str, kernel: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) recorded
+    from an ncu capture in profiles/traffic.txt ("workload kernel bytes" lines)."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for ln in fh:
+            parts = ln.split()
+            if len(parts) == 3 and parts[0] == workload and parts[1] == kernel:
+                return int(parts[2])
+    return None
+
+
 def run_ours(args, wl, rank, world) -> dict | None:
     import torch
 
@@ -133,26 +161,26 @@ def run_ours(args, wl, rank, world) -> dict | None:
     lib = _ffi.lib()
     stream = torch.cuda.current_stream(dev)
 
-    if wl["kind"] == "mc":
-        # size outputs with one call, then time K back-to-back calls
-        grid = iso.UniformGrid([n] * 3, device=dev)
-        grid.set_values(vals)
-        v, f = iso.marching_cubes(grid)
-        nv, nf = len(v), len(f)
-        capv, capf = nv + 1024, nf + 1024
-        vout = torch.empty((capv, 3), dtype=torch.float32, device=dev)
-        fout = torch.empty((capf, 3), dtype=torch.int32, device=dev)
-        ws = torch.empty(workspace_bytes([n] * 3, capv, capf), dtype=torch.uint8, device=dev)
-        small = torch.zeros(4, dtype=torch.int64, device=dev)
-        amin, amax = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
-
-        def step():
-            _ffi.check(mc_dense_into(vals, amin, amax, 0.0, 0, vout, fout, ws, small,
-                                     stream.cuda_stream))
-        algo_bytes = 4 * n ** 3 + 12 * nv + 12 * nf
-        kernels = ["mc_extract", "mc_signs", "mc_tile_scan", "mc_resolve"]
-    else:
+    if wl["kind"] != "mc":
         raise SystemExit(f"workload {args.workload} not available yet")
+    # size outputs with one call, then time K back-to-back calls
+    grid = iso.UniformGrid([n] * 3, device=dev)
+    grid.set_values(vals)
+    v, f = iso.marching_cubes(grid)
+    nv, nf = len(v), len(f)
+    capv, capf = nv + 1024, nf + 1024
+    vout = torch.empty((capv, 3), dtype=torch.float32, device=dev)
+    fout = torch.empty((capf, 3), dtype=torch.int32, device=dev)
+    ws = torch.empty(workspace_bytes([n] * 3, capv, capf), dtype=torch.uint8, device=dev)
+    small = torch.zeros(4, dtype=torch.int64, device=dev)
+    amin, amax = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+
+    def step():
+        _ffi.check(mc_dense_into(vals, amin, amax, 0.0, 0, vout, fout, ws, small, stream.cuda_stream))
+
+    algo_bytes = 4 * n ** 3 + 12 * nv + 12 * nf
+    kbytes = kernel_bytes("mc", n, nv, nf)
+    kernels = list(kbytes)
 
     for _ in range(args.warmup):
         step()
@@ -177,8 +205,8 @@ def run_ours(args, wl, rank, world) -> dict | None:
     assert (int(host[0]), int(host[1])) == (nv, nf)
     kt = {k: _ffi.profile_read(k) for k in kernels}
     launches = sum(c for c, _ in kt.values())
-    ext_n, ext_ms = kt[kernels[0]]
-    ext_avg = ext_ms / max(ext_n, 1)
+    kavg = {k: t / max(c, 1) for k, (c, t) in kt.items()}
+    top = max(kavg, key=kavg.get)
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device=dev)
@@ -206,7 +234,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
     if rank != 0:
         return None
     pk = peaks()
-    achieved = algo_bytes / (ext_avg * 1e-3) / 1e9
+    achieved = kbytes[top] / (kavg[top] * 1e-3) / 1e9
     pipeline = algo_bytes / (ms * 1e-3) / 1e9
     out = {
         "metric": METRIC, "value": round(world * cells / (ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
@@ -215,37 +243,59 @@ def run_ours(args, wl, rank, world) -> dict | None:
         "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
         "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae",
                    "vertices": nv, "faces": nf, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (values 537 MB > 129 MB L2)"},
+                   "l2": f"inputs larger than L2 (values {4 * n ** 3 / 1e6:.0f} MB > 129 MB L2)"
+                         if 4 * n ** 3 > 129e6 else "inputs smaller than L2 (not flushed)"},
         "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "mc_extract", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1),
                      "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
-                     "peak_source": pk["source"], "algorithmic_bytes": algo_bytes,
-                     "kernel_ms": round(ext_avg, 4), "traffic": None,
-                     "pipeline": {"achieved": round(pipeline, 1),
+                     "peak_source": pk["source"], "algorithmic_bytes": kbytes[top],
+                     "kernel_ms": round(kavg[top], 4), "traffic": profiled_traffic(wl["desc"], top),
+                     "pipeline": {"algorithmic_bytes": algo_bytes, "achieved": round(pipeline, 1),
                                   "frac": round(pipeline / pk["hbm_gbs"], 4)}},
-        "kernel_ms": {k: round(t / max(c, 1), 4) for k, (c, t) in kt.items()},
+        "kernel_ms": {k: round(v_, 4) for k, v_ in kavg.items()},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(vals_np, cells, repeats=1)
+        out["cpu_baseline"] = cpu_baseline(vals_np, cells)
     return out
 
 
-def cpu_baseline(vals_np, cells, repeats=1) -> dict:
+def _slabs(n: int, parts: int):
+    """x ranges [a, b] (point planes, inclusive) whose cells partition the grid's."""
+    parts = max(1, min(parts, n - 1))
+    cuts = [round(i * (n - 1) / parts) for i in range(parts + 1)]
+    return [(cuts[i], cuts[i + 1]) for i in range(parts)]
+
+
+def cpu_extract(ora, vals_np, threads: int) -> float:
+    """Seconds for one extraction of the grid by the oracle's C port, split into
+    x slabs (one point plane shared by neighbours) run on `threads` host threads.
+    ctypes releases the GIL during each call, so the slabs run in parallel.  Each
+    slab is welded on its own; its cells are the grid's cells exactly once."""
+    import concurrent.futures as cf
+
+    n = vals_np.shape[0]
+    slabs = _slabs(n, threads)
+    t0 = time.perf_counter()
+    if threads == 1:
+        ora.mc_dense(vals_np)
+    else:
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda ab: ora.mc_dense(np.ascontiguousarray(vals_np[ab[0]:ab[1] + 1])), slabs))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(vals_np, cells) -> dict:
     from oracle import Oracle
 
     ora = Oracle()
-    t = []
-    for _ in range(repeats):
-        t0 = time.perf_counter()
-        ora.mc_dense(vals_np)
-        t.append(time.perf_counter() - t0)
-    sec = min(t)
-    return {"value": round(cells / sec / 1e9, 5), "unit": "Gcells/s", "cores": 1, "kind": "port",
-            "sample": f"one full extraction of the same grid ({cells} cells), oracle C port, "
-                      f"1 thread, {sec:.2f} s"}
+    threads = os.cpu_count() or 1
+    sec = min(cpu_extract(ora, vals_np, threads) for _ in range(2))
+    return {"value": round(cells / sec / 1e9, 5), "unit": "Gcells/s", "cores": threads, "kind": "port",
+            "sample": f"one full extraction of the same grid ({cells} cells) per repeat, best of 2: "
+                      f"oracle C port over {threads} x-slabs on {threads} threads, {sec:.3f} s"}
 
 
 def run_reference(args, wl, rank) -> dict | None:
@@ -254,17 +304,15 @@ def run_reference(args, wl, rank) -> dict | None:
     from oracle import Oracle
 
     n = wl["n"]
+    if wl["kind"] != "mc":
+        return {"impl": "reference", "unavailable": f"workload {args.workload} has no reference arm yet"}
     vals_np = sphere_values(n, wl["r"])
     cells = (n - 1) ** 3
     ora = Oracle()
+    threads = os.cpu_count() or 1
     times = []
     for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        if wl["kind"] == "mc":
-            ora.mc_dense(vals_np)
-        else:
-            ora.dc_dense(vals_np)
-        dt = time.perf_counter() - t0
+        dt = cpu_extract(ora, vals_np, threads)
         if i >= args.warmup:
             times.append(dt)
     sec = statistics.mean(times)
@@ -275,9 +323,10 @@ def run_reference(args, wl, rank) -> dict | None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
         "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae"},
-        "cpu_baseline": {"value": val, "unit": "Gcells/s", "cores": 1, "kind": "port",
-                         "sample": "full extraction per step; the reference's algorithm restated in "
-                                   "C (oracle/iso_oracle.c); isoext's sources are not on the GPU host"},
+        "cpu_baseline": {"value": val, "unit": "Gcells/s", "cores": threads, "kind": "port",
+                         "sample": f"full grid per step as {threads} x-slabs on {threads} threads; the "
+                                   "reference's algorithm restated in C (oracle/iso_oracle.c); isoext's "
+                                   "sources are not on the GPU host"},
         "e2e": {"value": val, "unit": "Gcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -291,9 +340,6 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
-    if args.impl == "reference":
-        args.steps = min(args.steps, 3)
-        args.warmup = min(args.warmup, 1)
     wl = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

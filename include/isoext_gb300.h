@@ -44,25 +44,20 @@ extern "C" {
 /* Message of the last failed call on this thread. */
 const char *iso_last_error(void);
 
-/* ABI version of this library (1). */
+/* ABI version of this library (2). */
 int iso_abi_version(void);
 
-/* Tiling used by iso_mc_dense: point rows per tile, shared-memory slab ring
- * depth and threads per CTA.  Process-wide; the autotuner sets it.  No
- * counterpart in the reference (it has no tunables). */
-int iso_mc_set_config(int rows, int slabs, int threads);
-int iso_mc_get_config(int *rows, int *slabs, int *threads);
-
-/* Upper bound on the z extent of a tile (multiple of 32; 0 = as large as shared
- * memory allows).  Grids whose rows do not fit in shared memory are split along
- * z automatically; this forces it for testing.  No counterpart in the reference. */
-int iso_mc_set_zchunk(int zchunk);
+/* Threads per CTA of iso_mc_dense's emit kernel (128 or 256; default 256).
+ * Process-wide; the autotuner sets it.  No counterpart in the reference (it
+ * has no tunables). */
+int iso_mc_set_config(int threads);
+int iso_mc_get_config(int *threads);
 
 /* Kernel timing for benchmarks (no counterpart in the reference).  While
  * enabled, each kernel the library launches is bracketed by CUDA events on its
  * stream.  iso_profile_read synchronises on the recorded events and returns the
  * number of launches and their total device time in ms for one kernel name
- * ("mc_extract", "mc_tile_scan", "mc_resolve", ...; NULL = all). */
+ * ("mc_signs", "mc_count", "mc_scan", "mc_emit", "mc_fixup", ...; NULL = all). */
 int iso_profile_enable(int on);
 void iso_profile_reset(void);
 int iso_profile_read(const char *kernel, long long *launches, double *total_ms);
@@ -77,7 +72,9 @@ size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capa
  *   method: 0 = "nagae" (default in isoext), 1 = "lorensen".
  *   vertices: float32 [vertex_capacity, 3]; faces: int32 [face_capacity, 3].
  *   counts: device int64[2] <- (V, F).  Faces come in the reference's order
- *   (ascending cell id, table slot order); vertices in ascending edge-key order.
+ *   (ascending cell id, table slot order).  Vertices come in grid-edge order; they
+ *   are the same vertices as the reference's, whose order is by position.
+ *   workspace: iso_mc_dense_workspace_size bytes (any alignment).
  *   Unknown method -> ISO_ERR_ARG (isoext raises "Unknown method: ...").
  *   More than 2^31-1 points -> ISO_ERR_ARG (isoext: src/grid/uniform.cu:13-16). */
 int iso_mc_dense(const float *values, int nx, int ny, int nz, const float *aabb_min,

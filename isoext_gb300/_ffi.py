@@ -32,9 +32,8 @@ _fa = C.POINTER(C.c_float)
 def _declare(lib: C.CDLL) -> None:
     lib.iso_last_error.restype = C.c_char_p
     lib.iso_abi_version.restype = _i
-    lib.iso_mc_set_config.argtypes = [_i, _i, _i]
-    lib.iso_mc_get_config.argtypes = [C.POINTER(_i)] * 3
-    lib.iso_mc_set_zchunk.argtypes = [_i]
+    lib.iso_mc_set_config.argtypes = [_i]
+    lib.iso_mc_get_config.argtypes = [C.POINTER(_i)]
     lib.iso_profile_enable.argtypes = [_i]
     lib.iso_profile_reset.restype = None
     lib.iso_profile_read.argtypes = [C.c_char_p, C.POINTER(_ll), C.POINTER(C.c_double)]

@@ -6,7 +6,6 @@
 // capacity exceeded) are written to the caller's device status word.
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -14,28 +13,10 @@
 
 namespace {
 thread_local std::string g_err;
-std::mutex g_cfg_mu;
-int g_rows = 8, g_slabs = 4, g_threads = 256, g_zchunk = 0;
 
 int fail(int code, const char* msg) {
     g_err = msg;
     return code;
-}
-
-int sm_count() {
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
-    return n;
-}
-
-int plan(int nx, int ny, int nz, McTiles* t) {
-    int rows, slabs, threads, zchunk;
-    {
-        std::lock_guard<std::mutex> lk(g_cfg_mu);
-        rows = g_rows; slabs = g_slabs; threads = g_threads; zchunk = g_zchunk;
-    }
-    return mc_plan_tiles(nx, ny, nz, rows, slabs, threads, zchunk, sm_count(), t);
 }
 
 bool grid_ok(int nx, int ny, int nz) {
@@ -53,37 +34,23 @@ extern "C" {
 
 const char* iso_last_error(void) { return g_err.c_str(); }
 
-int iso_abi_version(void) { return 1; }
+int iso_abi_version(void) { return 2; }
 
-int iso_mc_set_config(int rows, int slabs, int threads) {
-    if (rows < 1 || rows > 64 || slabs < 4 || slabs > 8 || (threads != 256 && threads != 512))
-        return fail(ISO_ERR_ARG, "iso_mc_set_config: rows in [1,64], slabs in [4,8], threads 256|512");
-    std::lock_guard<std::mutex> lk(g_cfg_mu);
-    g_rows = rows; g_slabs = slabs; g_threads = threads;
+int iso_mc_set_config(int threads) {
+    if (mc_set_block(threads)) return fail(ISO_ERR_ARG, "iso_mc_set_config: threads must be 128 or 256");
     return ISO_OK;
 }
 
-int iso_mc_set_zchunk(int zchunk) {
-    if (zchunk < 0) return fail(ISO_ERR_ARG, "iso_mc_set_zchunk: zchunk >= 0");
-    std::lock_guard<std::mutex> lk(g_cfg_mu);
-    g_zchunk = zchunk;
-    return ISO_OK;
-}
-
-int iso_mc_get_config(int* rows, int* slabs, int* threads) {
-    std::lock_guard<std::mutex> lk(g_cfg_mu);
-    if (rows) *rows = g_rows;
-    if (slabs) *slabs = g_slabs;
-    if (threads) *threads = g_threads;
+int iso_mc_get_config(int* threads) {
+    if (threads) *threads = mc_get_block();
     return ISO_OK;
 }
 
 size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
                                    long long face_capacity) {
     if (!grid_ok(nx, ny, nz) || nx < 2 || ny < 2 || nz < 2) return 256;
-    McTiles t;
-    if (plan(nx, ny, nz, &t)) return 0;
-    return mc_workspace_bytes(t, vertex_capacity, face_capacity);
+    if (vertex_capacity < 0 || face_capacity < 0) return 0;
+    return mc_workspace_bytes(nx, ny, nz, vertex_capacity, face_capacity);
 }
 
 int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min,
@@ -109,18 +76,14 @@ int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
     if ((vertex_capacity && !vertices) || (face_capacity && !faces))
         return fail(ISO_ERR_ARG, "output buffers are null");
     McParams p{};
-    if (plan(nx, ny, nz, &p.t)) return fail(ISO_ERR_ARG, "grid too large for the tile planner");
     p.vals = values;
+    p.nx = nx; p.ny = ny; p.nz = nz;
     for (int i = 0; i < 3; ++i) {
         p.amin[i] = aabb_min[i];
         p.asize[i] = aabb_max[i] - aabb_min[i];  // FP32, as aabb_max - aabb_min in the reference
     }
     p.level = level;
     p.method = method;
-    {
-        const int n[3] = {nx, ny, nz};
-        p.snapTau = mc_snap_tau(aabb_min, aabb_max, n);
-    }
     p.status = status;
     p.vout = vertices;
     p.fout = faces;

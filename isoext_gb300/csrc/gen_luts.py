@@ -142,6 +142,10 @@ def flat(table: list[list[list[int]]], width: int) -> list[int]:
     return out
 
 
+def ntri(table: list[list[list[int]]]) -> list[int]:
+    return [len(row) for row in table]
+
+
 def render() -> str:
     nag = expand(NAGAE, reflect=False)
     lor = expand(LORENSEN, reflect=True)
@@ -169,6 +173,14 @@ def render() -> str:
         "\n/* Lorensen: up to 4 triangles per case, edge triples, -1 padded. */\n",
         "#define ISO_LORENSEN_MAX_TRI 4\n",
         arr("ISO_TRI_LORENSEN", "signed char", flat(lor, 12), 12),
+        "\n/* Triangles per case: [0, 256) Nagae, [256, 512) Lorensen. */\n",
+        arr("ISO_NTRI", "unsigned char", ntri(nag) + ntri(lor), 16),
+        "\n/* ISO_EDGE_CORNERS as a compile-time function, for fully unrolled loops. */\n",
+        "#ifdef __cplusplus\n#ifdef __CUDACC__\n#define ISO_LUT_HD __host__ __device__\n#else\n",
+        "#define ISO_LUT_HD\n#endif\n",
+        "ISO_LUT_HD constexpr int iso_edge_corner(int i) {\n    return ",
+        " : ".join(f"i == {i} ? {c}" for i, c in enumerate(c for p in EDGE_PAIRS for c in p)) + " : -1;\n}\n",
+        "#endif\n",
         "\n#endif /* ISO_LUTS_H */\n",
     ]
     return "".join(parts)

@@ -114,6 +114,7 @@ def _mc_uniform(grid: UniformGrid, level: float, method: int):
         cap_v, cap_f = _first_guess(grid.shape)
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev).cuda_stream
+        need = None  # sizes before the snap fix-up shrank them, after a retry
         for _attempt in range(2):
             vout = torch.empty((cap_v, 3), dtype=torch.float32, device=dev)
             fout = torch.empty((cap_f, 3), dtype=torch.int32, device=dev)
@@ -125,10 +126,13 @@ def _mc_uniform(grid: UniformGrid, level: float, method: int):
             nv, nf, status = int(host[0]), int(host[1]), int(host[2] & 0xffffffff)
             if status == _ffi.ISO_ERR_OVERFLOW:
                 cap_v, cap_f = nv + 1024, nf + 1024
+                need = (nv, nf)
                 continue
             if status != 0:
                 raise RuntimeError(f"isoext_gb300: device error {status} in marching_cubes")
-            _size_cache[key] = (nv, nf)
+            # counts are final sizes; output buffers must hold the sizes before
+            # snapped vertices were merged, which a retry revealed
+            _size_cache[key] = need if need is not None else (nv, nf)
             v, f = _views(vout, fout, nv, nf)
             if v is not None and coarse_float_grid(grid.shape, grid.aabb_min, grid.aabb_max):
                 v, f = weld_by_position(v, f)

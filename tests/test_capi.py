@@ -32,12 +32,12 @@ def test_library_reports_abi_and_config():
     from isoext_gb300 import _ffi
 
     lib = _ffi.lib()
-    assert lib.iso_abi_version() == 1
-    r, s, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    lib.iso_mc_get_config(ctypes.byref(r), ctypes.byref(s), ctypes.byref(t))
-    assert r.value >= 1 and s.value >= 4 and t.value in (256, 512)
-    assert lib.iso_mc_set_config(0, 4, 256) == 1  # bad rows -> ISO_ERR_ARG
-    assert "rows" in _ffi.last_error()
+    assert lib.iso_abi_version() == 2
+    t = ctypes.c_int()
+    lib.iso_mc_get_config(ctypes.byref(t))
+    assert t.value in (128, 256)
+    assert lib.iso_mc_set_config(100) == 1  # not 128 / 256 -> ISO_ERR_ARG
+    assert "threads" in _ffi.last_error()
 
 
 def test_unknown_method_message():

@@ -44,11 +44,9 @@ def check(oracle, values, level=0.0, method="nagae", lo=(-1, -1, -1), hi=(1, 1, 
 @pytest.fixture(autouse=True)
 def _default_config():
     lib = iso._ffi.lib()
-    lib.iso_mc_set_config(8, 4, 256)
-    lib.iso_mc_set_zchunk(0)
+    lib.iso_mc_set_config(256)
     yield
-    lib.iso_mc_set_config(8, 4, 256)
-    lib.iso_mc_set_zchunk(0)
+    lib.iso_mc_set_config(256)
 
 
 @pytest.mark.parametrize("path", DENSE, ids=lambda p: os.path.basename(p)[:-4])
@@ -110,22 +108,27 @@ def test_mc_empty_and_full():
     assert iso.marching_cubes(g) == (None, None)
 
 
-@pytest.mark.parametrize("rows,slabs,threads", [(1, 4, 256), (2, 5, 256), (3, 4, 512), (8, 6, 512),
-                                                (16, 4, 256)])
-def test_mc_tilings(oracle, rows, slabs, threads):
+@pytest.mark.parametrize("threads", [128, 256])
+def test_mc_block_sizes(oracle, threads):
     lib = iso._ffi.lib()
-    assert lib.iso_mc_set_config(rows, slabs, threads) == 0
-    for shape in [(31, 45, 29), (64, 64, 64)]:
-        check(oracle, sphere(shape, 0.7), what=f"{shape} R{rows}")
+    assert lib.iso_mc_set_config(threads) == 0
+    for shape in [(31, 45, 29), (64, 64, 64), (9, 10, 101)]:
+        check(oracle, sphere(shape, 0.7), what=f"{shape} T{threads}")
         check(oracle, noise(shape, seed=7, zero_frac=0.1), method="lorensen", what=f"noise {shape}")
 
 
-@pytest.mark.parametrize("zc", [32, 64, 96])
-def test_mc_z_chunks(oracle, zc):
-    lib = iso._ffi.lib()
-    assert lib.iso_mc_set_zchunk(zc) == 0
-    check(oracle, sphere((20, 24, 150), 0.8), what=f"zchunk {zc}")
-    check(oracle, noise((9, 10, 101), seed=3, zero_frac=0.2), what=f"zchunk noise {zc}")
+@pytest.mark.parametrize("nz", [31, 32, 33, 63, 64, 65, 150])
+def test_mc_word_boundaries(oracle, nz):
+    # z extents around multiples of the 32-bit word: edges and cells that span
+    # two words, partial last words
+    check(oracle, sphere((20, 24, nz), 0.8), what=f"nz {nz}")
+    check(oracle, noise((9, 10, nz), seed=nz, zero_frac=0.2), what=f"noise nz {nz}")
+
+
+def test_mc_thin_grids(oracle):
+    # fewer point words than grid coordinates (the count kernel also writes those)
+    for shape in [(2, 2, 300), (2, 300, 2), (300, 2, 2), (3, 3, 1000)]:
+        check(oracle, noise(shape, seed=5, zero_frac=0.1), what=f"thin {shape}")
 
 
 def test_mc_unknown_method():
