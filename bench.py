@@ -69,7 +69,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -122,12 +122,14 @@ def kernel_bytes(kind: str, n: int, nv: int, nf: int) -> dict:
     """Algorithmic bytes per launch of each kernel of the MC pipeline."""
     pts = n ** 3
     words = n * n * ((n + 31) // 32)
+    segs = (words + 1023) // 1024
     return {
         "mc_signs": 4 * pts + 4 * words,           # values once, sign bitmap once
         "mc_count": 4 * words + 4 * words,         # bitmap once, per-word entries once
-        "mc_scan": 16 * ((words + 255) // 256),    # block sums
-        "mc_emit": 8 * nv + 12 * nv + 12 * nf,     # endpoint values, vertices, faces
-        "mc_fixup": 0,                             # returns at once without snapped vertices
+        "mc_scan": 32 * segs,                      # segment sums read, offsets written
+        "mc_emit_vertices": 8 * nv + 8 * nv + 12 * nv,  # entries, endpoint values, vertices
+        "mc_emit_faces": 8 * nf + 12 * nf,             # cell entries (<= F), faces
+        "mc_fixup": 0,                             # returns at once without coinciding vertices
     }
 
 
@@ -185,14 +187,22 @@ def run_ours(args, wl, rank, world) -> dict | None:
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    lib.iso_profile_reset()
-    lib.iso_profile_enable(1)
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
+        # The timed region lasts milliseconds, shorter than the sampler's period:
+        # keep the GPU busy with the same step for ~0.6 s first, so the clock
+        # samples are taken under this load (they run on through the timed region).
+        t_end = time.perf_counter() + 0.6
+        while time.perf_counter() < t_end:
+            for _ in range(50):
+                step()
+            torch.cuda.synchronize()
+        lib.iso_profile_reset()
+        lib.iso_profile_enable(1)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             step()

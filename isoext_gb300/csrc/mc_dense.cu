@@ -4,19 +4,25 @@
 //   1. mc_signs   streams the grid once (one warp per row, 16 coalesced
 //                 128-byte loads in flight per warp) into a sign bitmap,
 //                 1 bit per point.  This is the only pass over all values.
-//   2. mc_count   one thread per point word, from the bitmap alone (16.8 MB at
-//                 512^3, L2-resident): crossed-edge masks along x, y and z, active
-//                 cells, face counts from the case tables; block-local vertex
-//                 offsets per word; words with vertices or faces are appended to
-//                 a list (one atomic per warp).
-//   3. mc_scan    exclusive prefix of the per-block (V, F) sums; capacity check.
-//   4. mc_emit    one thread per listed word: vertex positions at their slots
-//                 (values are read only at crossed edges), faces at the word's
-//                 face offset with vertex indices by rank.
-//   5. mc_fixup   cooperative; returns at once unless some vertex rounded exactly
-//                 onto a grid point ("snapped").  Then it merges snapped vertices
-//                 by exact position, drops faces that became degenerate and
-//                 compacts vertices and faces, keeping their order.
+//   2. mc_count   one CTA per segment of 1024 point words, from the bitmap alone
+//                 (16.8 MB at 512^3): crossed-edge masks along x, y and z, active
+//                 cells (their triangle counts spread over the lanes of a warp);
+//                 segment-local vertex offsets per word; words with vertices or
+//                 faces are appended to a list (one atomic per warp).  Words
+//                 wholly inside or outside take an early exit.
+//   3. mc_scan    segment (V, F) sums to offsets: CTAs over chunks of 4096
+//                 segments chained by decoupled look-back; totals and the
+//                 capacity check.
+//   4. mc_emit    warp-cooperative over the listed words: each lane takes one
+//                 vertex (position at its slot; values are read only at crossed
+//                 edges), then one active cell (faces at the word's face offset,
+//                 vertex indices by rank).  Vertices that can share a position
+//                 with another edge's (t within tau of 0 or 1) go through a small
+//                 hash that counts exact coincidences.
+//   5. mc_fixup   cooperative; returns at once unless the emit kernel found
+//                 coinciding vertices.  Then it merges them by exact position,
+//                 drops faces that became degenerate and compacts vertices and
+//                 faces, keeping their order.
 //
 // Equivalence with the reference (src/mc/mc.cu:17-68): the reference emits the
 // triangles of active cells in ascending cell id, drops triangles with two equal
@@ -31,6 +37,7 @@
 // Vertices come in edge order (the reference sorts them by position; the mesh
 // is the same after relabelling).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -45,21 +52,53 @@ namespace {
 // ---------------------------------------------------------------------------
 // Geometry shared by the kernels.
 
+// Unsigned 32-bit division by a divisor fixed for a launch, by multiply and
+// shift (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994): for 1 <= d < 2^31, l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (t + ((n - t) >> 1)) >> (l - 1) with
+// t = umulhi(m, n); exact for every 32-bit n.
+struct FastDiv {
+    uint32_t d, m, l;
+};
+
+FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f{d, 0u, 0u};
+    while ((1ull << f.l) < d) ++f.l;
+    if (d > 1) f.m = uint32_t(((1ull << 32) * ((1ull << f.l) - d)) / d + 1);
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> 1)) >> (f.l - 1);
+}
+
 struct McGrid {
+    FastDiv dNW, dNY;  // division by NW and by ny
     int nx, ny, nz, NW;
     long long PW;     // point words nx * ny * NW
     float level;
     int method;
     const float* gc;  // grid coordinates: x [nx], then y [ny], then z [nz]
+    // Vertices whose edge parameter t is within tau of 0 or 1 are the only ones
+    // that can share a position with a vertex of another edge (mc_snap_tau).
+    float tau;
 };
 
 // Workspace carved from one buffer (offsets 256-aligned).
 struct McWs {
     uint32_t* S;                // sign bitmap [PW]
-    uint32_t* info;             // per word: segment-local vertex offset | popc(ex) << 17 | popc(ey) << 23
+    uint32_t* info;             // per word: segment-local vertex offset | popc(ex) << 20 | popc(ey) << 26
     unsigned long long* blk;    // per segment of words: (V, F) sums, then exclusive offsets
-    uint2* list;                // words with output: (pw, segment-local face offset)
+    unsigned long long* vlist;  // vertex entries [capV]: pw | axis << 32 | bit << 34 | slot << 39
+    unsigned long long* clist;  // cell entries [capF]: pw | bit << 32 | case << 37 | face offset << 45
+    uint32_t* foff;             // per word with faces: segment-local face offset
     unsigned long long* ctr;    // [0] list size [1] snaps [2] barrier count [3] barrier gen [4] V' [5] F'
+                                // [6] unused [7] scan ticket [8] merges [9] small hash full
+                                // [10] cell entries
+    unsigned long long* state;  // look-back state per segment (follows ctr; zeroed with it)
+    uint32_t* small;            // SMALL_HC entries after the states (zeroed with them)
     float* gc;                  // grid coordinates [nx + ny + nz] (x, then y, then z)
     uint32_t* snaps;            // snapped vertex slots [capV]
     uint32_t* table;            // position hash of snapped vertices [HC]
@@ -76,6 +115,8 @@ struct McWs {
 };
 
 constexpr int FIX_BLOCK = 512;
+constexpr uint32_t SMALL_HC = 1u << 15;  // merge-detection hash of emit (entries: vertex + 1, 0 = empty)
+constexpr int NCTR = 16;
 constexpr int CNT_THREADS = 256;             // count kernel CTA size
 constexpr int WPT = 4;                       // point words per count thread
 constexpr uint32_t SEG = CNT_THREADS * WPT;  // words per segment (one scan entry)
@@ -87,6 +128,9 @@ uint32_t hash_cap(long long capV) {
     while ((long long)c < 2 * capV + 1024) c <<= 1;
     return c;
 }
+
+// Bytes cleared at the start of each call: counters, look-back states, small hash.
+inline size_t zeroed_bytes(long long nBlk) { return size_t(NCTR) * 8 + size_t(nBlk) * 8 + size_t(SMALL_HC) * 4; }
 
 McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base) {
     McWs w{};
@@ -105,8 +149,12 @@ McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base
     w.S = reinterpret_cast<uint32_t*>(take(size_t(PW) * 4));
     w.info = reinterpret_cast<uint32_t*>(take(size_t(PW) * 4));
     w.blk = reinterpret_cast<unsigned long long*>(take(size_t(w.nBlk + 1) * 16));
-    w.list = reinterpret_cast<uint2*>(take(size_t(PW) * 8));
-    w.ctr = reinterpret_cast<unsigned long long*>(take(8 * 8));
+    w.vlist = reinterpret_cast<unsigned long long*>(take(size_t(capV) * 8));
+    w.clist = reinterpret_cast<unsigned long long*>(take(size_t(capF) * 8));
+    w.foff = reinterpret_cast<uint32_t*>(take(size_t(PW) * 4));
+    w.ctr = reinterpret_cast<unsigned long long*>(take(zeroed_bytes(w.nBlk)));  // + states + small hash
+    w.state = w.ctr ? w.ctr + NCTR : nullptr;
+    w.small = w.ctr ? reinterpret_cast<uint32_t*>(w.state + w.nBlk) : nullptr;
     w.gc = reinterpret_cast<float*>(take(size_t(nx + ny + nz) * 4));
     w.snaps = reinterpret_cast<uint32_t*>(take(size_t(capV) * 4));
     w.table = reinterpret_cast<uint32_t*>(take(size_t(w.HC) * 4));
@@ -242,7 +290,20 @@ __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea
 }
 
 // ---------------------------------------------------------------------------
-// 2. count (persistent CTAs; a segment of SEG point words per iteration)
+// 2. count: persistent CTAs take segments of SEG point words in ticket order;
+// each segment's (V, F) prefix comes from a decoupled look-back over the
+// segments before it, so no separate scan pass is needed.
+
+// Segment holding point word pw.
+__device__ __forceinline__ uint32_t seg_of(uint32_t pw) { return pw / SEG; }
+
+// (x, y, w) of point word pw.
+__device__ __forceinline__ void word_xyw(const McGrid& g, uint32_t pw, int& x, int& y, int& w) {
+    const uint32_t row = fdiv(pw, g.dNW);
+    w = int(pw - row * uint32_t(g.NW));
+    x = int(fdiv(row, g.dNY));
+    y = int(row - uint32_t(x) * uint32_t(g.ny));
+}
 
 __device__ __forceinline__ void advance(const McGrid& g, int& x, int& y, int& w) {
     if (++w == g.NW) {
@@ -251,147 +312,67 @@ __device__ __forceinline__ void advance(const McGrid& g, int& x, int& y, int& w)
     }
 }
 
-__global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const float amin0, const float amin1,
-                                                        const float amin2, const float size0, const float size1,
-                                                        const float size2, const uint32_t* __restrict__ S,
-                                                        uint32_t* __restrict__ info,
-                                                        unsigned long long* __restrict__ blk,
-                                                        uint2* __restrict__ list, unsigned long long* ctr,
-                                                        float* __restrict__ gc, const uint32_t nseg) {
-    __shared__ uint8_t nt[256];
-    __shared__ uint32_t sm[64];
-    for (int c = threadIdx.x; c < 256; c += CNT_THREADS) nt[c] = ISO_NTRI[g.method * 256 + c];
-    // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
-    const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
-    for (uint32_t i = blockIdx.x * CNT_THREADS + threadIdx.x; i < ncoord; i += gridDim.x * CNT_THREADS) {
-        if (i < uint32_t(g.nx)) gc[i] = iso::grid_coord(i, g.nx, amin0, size0);
-        else if (i < uint32_t(g.nx + g.ny)) gc[i] = iso::grid_coord(i - g.nx, g.ny, amin1, size1);
-        else gc[i] = iso::grid_coord(i - g.nx - g.ny, g.nz, amin2, size2);
-    }
-    __syncthreads();
+// Look-back state of a segment: flag << 62 | V << 31 | F (V, F < 2^31).
+constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62;
+constexpr unsigned long long LB_MASK31 = 0x7fffffffull;
+
+__device__ __forceinline__ unsigned long long lb_pack(unsigned long long flag, unsigned long long v,
+                                                      unsigned long long f) {
+    return flag | (min(v, LB_MASK31) << 31) | min(f, LB_MASK31);
+}
+
+// Exclusive (V, F) prefix of segment seg; run by warp 0 after publishing the
+// segment's aggregate.  Waits are bounded: on a timeout the status is set and
+// the prefix returned is wrong (the host sees the status).
+__device__ void look_back(volatile unsigned long long* state, uint32_t seg, unsigned long long& ev,
+                          unsigned long long& ef, int* status) {
     const int lane = threadIdx.x & 31;
-    for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
-        const uint32_t pw0 = seg * SEG + threadIdx.x * WPT;
-        uint32_t nv[WPT], nf[WPT], cxy[WPT];
-        int x = 0, y = 0, w = 0;
-        if (pw0 < g.PW) {
-            const uint32_t row = pw0 / uint32_t(g.NW);
-            w = int(pw0 - row * uint32_t(g.NW));
-            x = int(row / uint32_t(g.ny));
-            y = int(row - uint32_t(x) * uint32_t(g.ny));
-        }
-#pragma unroll
-        for (int k = 0; k < WPT; ++k) {
-            nv[k] = 0; nf[k] = 0; cxy[k] = 0;
-            if (pw0 + k < g.PW) {
-                Words d;
-                load_words(g, S, pw0 + k, x, y, w, d);
-                const uint32_t zm = zmask(g, w);
-                const uint32_t ex = d.hasx ? (d.s[0][0][0] ^ d.s[1][0][0]) : 0u;
-                const uint32_t ey = d.hasy ? (d.s[0][0][0] ^ d.s[0][1][0]) : 0u;
-                const uint32_t ez = ez_of(d.s[0][0][0], d.s[0][0][1], zm);
-                nv[k] = __popc(ex) + __popc(ey) + __popc(ez);
-                cxy[k] = (uint32_t(__popc(ex)) << 17) | (uint32_t(__popc(ey)) << 23);
-                uint32_t act = active_cells(d, zm);
-                while (act) {
-                    const int b = __ffs(act) - 1;
-                    act &= act - 1;
-                    nf[k] += nt[cell_case(d, b)];
+    ev = 0;
+    ef = 0;
+    long long j = (long long)seg - 1 - lane;
+    while (true) {
+        unsigned long long st = LB_INC;  // before segment 0: inclusive zero
+        if (j >= 0) {
+            uint32_t spins = 0;
+            do {
+                st = state[j];
+                if ((st >> 62) != 0) break;
+                if (++spins > ISO_SPIN_LIMIT) {
+                    atomicCAS(status, 0, int(ISO_ERR_TIMEOUT));
+                    st = LB_INC;
+                    break;
                 }
-                advance(g, x, y, w);
-            }
+                __nanosleep(20);
+            } while (true);
         }
-        uint32_t sv = 0, sf = 0, nlive = 0;
+        const uint32_t inc = __ballot_sync(~0u, (st >> 62) == 2);
+        // lanes up to and including the nearest inclusive state contribute
+        const int stop = inc ? __ffs(inc) - 1 : 31;
+        unsigned long long v = lane <= stop ? (st >> 31) & LB_MASK31 : 0ull;
+        unsigned long long f = lane <= stop ? st & LB_MASK31 : 0ull;
 #pragma unroll
-        for (int k = 0; k < WPT; ++k) { sv += nv[k]; sf += nf[k]; nlive += (nv[k] | nf[k]) != 0; }
-        uint32_t ev, ef, tv, tf;
-        block_scan2<CNT_THREADS>(sv, sf, ev, ef, tv, tf, sm);
-        // per-word entries and the list of words with output
-        uint32_t lpos = nlive;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t u = __shfl_up_sync(~0u, lpos, d);
-            if (lane >= d) lpos += u;
+        for (int d = 16; d >= 1; d >>= 1) {
+            v += __shfl_xor_sync(~0u, v, d);
+            f += __shfl_xor_sync(~0u, f, d);
         }
-        const uint32_t wtot = __shfl_sync(~0u, lpos, 31);
-        unsigned long long lbase = 0;
-        if (lane == 31 && wtot) lbase = atomicAdd(ctr, (unsigned long long)wtot);
-        lbase = __shfl_sync(~0u, lbase, 31) + (lpos - nlive);
-#pragma unroll
-        for (int k = 0; k < WPT; ++k) {
-            if (pw0 + k < g.PW) {
-                info[pw0 + k] = ev | cxy[k];
-                if (nv[k] | nf[k]) list[lbase++] = make_uint2(pw0 + k, ef);
-            }
-            ev += nv[k];
-            ef += nf[k];
-        }
-        if (threadIdx.x == 0) {
-            blk[2 * seg] = tv;
-            blk[2 * seg + 1] = tf;
-        }
+        ev += v;
+        ef += f;
+        if (inc) break;
+        j -= 32;
     }
 }
 
-
-// ---------------------------------------------------------------------------
-// 3. scan of block sums (one CTA; each thread scans a run of blocks serially)
-
-constexpr int SCAN_THREADS = 1024;
-
-__global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk, long long nblk,
-                                                        long long* counts, int* status, long long capV,
-                                                        long long capF) {
-    __shared__ unsigned long long wa[32], wb[32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long per = (nblk + SCAN_THREADS - 1) / SCAN_THREADS;
-    const long long b0 = min(nblk, tid * per), b1 = min(nblk, b0 + per);
-    unsigned long long sa = 0, sb = 0;
-    for (long long i = b0; i < b1; ++i) { sa += blk[2 * i]; sb += blk[2 * i + 1]; }
-    unsigned long long ia = sa, ib = sb;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long x = __shfl_up_sync(~0u, ia, d), y = __shfl_up_sync(~0u, ib, d);
-        if (lane >= d) { ia += x; ib += y; }
-    }
-    if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
-    __syncthreads();
-    if (warp == 0) {
-        unsigned long long x = wa[lane], y = wb[lane];
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned long long u = __shfl_up_sync(~0u, x, d), v = __shfl_up_sync(~0u, y, d);
-            if (lane >= d) { x += u; y += v; }
-        }
-        wa[lane] = x;
-        wb[lane] = y;
-    }
-    __syncthreads();
-    unsigned long long oa = (warp ? wa[warp - 1] : 0ull) + ia - sa;
-    unsigned long long ob = (warp ? wb[warp - 1] : 0ull) + ib - sb;
-    for (long long i = b0; i < b1; ++i) {
-        const unsigned long long a = blk[2 * i], b = blk[2 * i + 1];
-        blk[2 * i] = oa;
-        blk[2 * i + 1] = ob;
-        oa += a;
-        ob += b;
-    }
-    if (tid == 0) {
-        const unsigned long long V = wa[31], F = wb[31];
-        counts[0] = (long long)V;
-        counts[1] = (long long)F;
-        if ((long long)V > capV || (long long)F > capF || V > 0x7fffffffull)
-            atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
-    }
+__device__ __forceinline__ uint32_t pbits(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
+__device__ __forceinline__ uint32_t phash(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h;
 }
-
-// ---------------------------------------------------------------------------
-// 4. emit (warp-cooperative: the set bits of 32 listed words are spread over
-// the lanes, so each lane handles one vertex, then one cell, at a time)
-
-__device__ __forceinline__ float gx(const McGrid& g, int x) { return g.gc[x]; }
-__device__ __forceinline__ float gy(const McGrid& g, int y) { return g.gc[g.nx + y]; }
-__device__ __forceinline__ float gz(const McGrid& g, int z) { return g.gc[g.nx + g.ny + z]; }
+__device__ __forceinline__ bool same_pos(const float* p, const float* q) {
+    return p[0] == q[0] && p[1] == q[1] && p[2] == q[2];
+}
 
 // Position of the k-th (from 0) set bit of m; m has more than k set bits.
 __device__ __forceinline__ int nth_set(uint32_t m, int k) {
@@ -417,204 +398,428 @@ __device__ __forceinline__ int owner_of(uint32_t incl, uint32_t j) {
     return lo;
 }
 
-struct EmitWarp {
-    uint32_t wd[8][32];   // bitmap words (dx, dy, ww) of each lane's word
-    uint32_t nb[8][32];   // vertex slot base of the 8 neighbouring words
-    uint16_t nc[8][32];   // popc(ex) | popc(ey) << 8 of those words
-    uint8_t fo[32][32];   // face offset within the word of the cell at each bit
-    uint32_t vid[12][32];
-};
-
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) mc_emit(const McGrid g, const float* __restrict__ vals,
-                                                 const uint32_t* __restrict__ S, const uint32_t* __restrict__ info,
-                                                 const unsigned long long* __restrict__ blk,
-                                                 const uint2* __restrict__ list, unsigned long long* ctr,
-                                                 uint32_t* __restrict__ snaps, float* __restrict__ vout,
-                                                 int32_t* __restrict__ fout, const long long* __restrict__ counts,
-                                                 long long capV, long long capF) {
-    constexpr int NWARP = BLOCK / 32;
-    __shared__ signed char tri[256 * 15];
-    __shared__ uint16_t est[256];
-    __shared__ uint8_t nt[256];
-    __shared__ EmitWarp ew[NWARP];
-    const int ml = g.method == 0 ? 15 : 12;
-    for (int i = threadIdx.x; i < 256 * ml; i += BLOCK) tri[i] = tri_row(g.method, 0)[i];
-    for (int i = threadIdx.x; i < 256; i += BLOCK) {
-        est[i] = ISO_EDGE_STATUS[i];
-        nt[i] = ISO_NTRI[g.method * 256 + i];
+__global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const float amin0, const float amin1,
+                                                        const float amin2, const float size0, const float size1,
+                                                        const float size2, const uint32_t* __restrict__ S,
+                                                        uint32_t* __restrict__ info,
+                                                        unsigned long long* __restrict__ blk,
+                                                        unsigned long long* __restrict__ vlist,
+                                                        unsigned long long* __restrict__ clist,
+                                                        uint32_t* __restrict__ foff, unsigned long long* ctr,
+                                                        float* __restrict__ gc, const uint32_t nseg,
+                                                        const long long capV, const long long capF) {
+    __shared__ uint32_t sm[64];
+    __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
+    // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
+    const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
+    const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
+    if (gid < ncoord) {
+        if (gid < uint32_t(g.nx)) gc[gid] = iso::grid_coord(gid, g.nx, amin0, size0);
+        else if (gid < uint32_t(g.nx + g.ny)) gc[gid] = iso::grid_coord(gid - g.nx, g.ny, amin1, size1);
+        else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2);
+    }
+    const uint32_t seg = blockIdx.x;
+    if (seg >= nseg) return;  // blocks past the segments only write coordinates
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW), syw = uint32_t(g.NW);
+    const bool vec = (g.NW & 3) == 0;  // rows start on 16-byte boundaries
+    const uint32_t pw0 = seg * SEG + threadIdx.x * WPT;
+#pragma unroll
+    for (int k = 0; k < WPT; ++k) nfs[threadIdx.x * WPT + k] = 0u;
+    // bitmap words pw0 .. pw0 + 3 of the rows (x, y), (x, y+1), (x+1, y), (x+1, y+1)
+    uint32_t r[2][2][WPT];
+    int x = 0, y = 0, w = 0;
+    if (pw0 < g.PW) word_xyw(g, pw0, x, y, w);
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            const uint32_t q = pw0 + dx * sxw + dy * syw;
+            if (vec && pw0 + WPT <= g.PW && q + WPT <= g.PW) {
+                const uint4 v4 = __ldg(reinterpret_cast<const uint4*>(S + q));
+                r[dx][dy][0] = v4.x; r[dx][dy][1] = v4.y; r[dx][dy][2] = v4.z; r[dx][dy][3] = v4.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < WPT; ++k) r[dx][dy][k] = (q + k < g.PW) ? __ldg(S + q + k) : 0u;
+            }
+        }
+    // word pw0 + 4 of each row: the next lane's first word, or a load
+    uint32_t nx4[2][2];
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            nx4[dx][dy] = __shfl_down_sync(~0u, r[dx][dy][0], 1);
+            if (lane == 31) {
+                const uint32_t q = pw0 + WPT + dx * sxw + dy * syw;
+                nx4[dx][dy] = q < g.PW ? __ldg(S + q) : 0u;
+            }
+        }
+    uint32_t nv[WPT], cxy[WPT], act[WPT];
+#pragma unroll
+    for (int k = 0; k < WPT; ++k) {
+        nv[k] = 0; cxy[k] = 0; act[k] = 0;
+        if (pw0 + k < g.PW) {
+            Words d;
+            d.x = x; d.y = y; d.w = w;
+            d.hasx = x < g.nx - 1;
+            d.hasy = y < g.ny - 1;
+            const bool nxt = w + 1 < g.NW;
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+                for (int dy = 0; dy < 2; ++dy) {
+                    const bool ok = (dx == 0 || d.hasx) && (dy == 0 || d.hasy);
+                    d.s[dx][dy][0] = ok ? r[dx][dy][k] : 0u;
+                    d.s[dx][dy][1] = (ok && nxt) ? (k + 1 < WPT ? r[dx][dy][(k + 1) % WPT] : nx4[dx][dy]) : 0u;
+                }
+            // most words lie wholly inside or outside: all their grid
+            // neighbours' words are 0 or all ~0 alike, and nothing crosses
+            const uint32_t u = d.s[0][0][0];
+            bool quiet = u == 0u || u == ~0u;
+#pragma unroll
+            for (int q = 1; q < 8; ++q) {
+                const int dx = q >> 2, dy = (q >> 1) & 1, ww = q & 1;
+                const bool valid = (dx == 0 || d.hasx) && (dy == 0 || d.hasy) && (ww == 0 || nxt);
+                quiet = quiet && (!valid || d.s[dx][dy][ww] == u);
+            }
+            if (!quiet) {
+                const uint32_t zm = zmask(g, w);
+                const uint32_t ex = d.hasx ? (d.s[0][0][0] ^ d.s[1][0][0]) : 0u;
+                const uint32_t ey = d.hasy ? (d.s[0][0][0] ^ d.s[0][1][0]) : 0u;
+                const uint32_t ez = ez_of(d.s[0][0][0], d.s[0][0][1], zm);
+                nv[k] = __popc(ex) + __popc(ey) + __popc(ez);
+                cxy[k] = (uint32_t(__popc(ex)) << 20) | (uint32_t(__popc(ey)) << 26);
+                act[k] = active_cells(d, zm);
+            }
+            advance(g, x, y, w);
+        }
+    }
+    __syncthreads();  // nfs cleared
+    // active cells, one per lane of the warp: triangle counts, and a cell entry
+    // with the cell's face offset within its word (cells of a word come in bit
+    // order: a segmented scan over the lanes plus the word's faces of earlier rounds)
+    {
+        const uint32_t na = __popc(act[0]) + __popc(act[1]) + __popc(act[2]) + __popc(act[3]);
+        uint32_t incl = na;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const uint32_t t = __shfl_up_sync(~0u, incl, dd);
+            if (lane >= dd) incl += t;
+        }
+        const uint32_t total = __shfl_sync(~0u, incl, 31);
+        for (uint32_t rr = 0; rr < total; rr += 32) {
+            const uint32_t j = rr + lane;
+            const int o = owner_of(incl, j);
+            const uint32_t oexcl = __shfl_sync(~0u, incl - na, o);
+            uint32_t oa[WPT];
+#pragma unroll
+            for (int k = 0; k < WPT; ++k) oa[k] = __shfl_sync(~0u, act[k], o);
+            const bool valid = j < total;
+            uint32_t wid = 0xffffffffu, ntc = 0, cs = 0, pw = 0;
+            int b = 0;
+            if (valid) {
+                int kk = int(j - oexcl), k = 0;
+                uint32_t m = oa[0];
+#pragma unroll
+                for (int q = 0; q < WPT - 1; ++q) {
+                    const int c = __popc(m);
+                    if (kk >= c) { kk -= c; m = oa[q + 1]; k = q + 1; }
+                    else break;
+                }
+                b = nth_set(m, kk);
+                wid = uint32_t(warp * 32 + o) * WPT + uint32_t(k);
+                pw = seg * SEG + wid;
+                int cx_, cy_, cw_;
+                word_xyw(g, pw, cx_, cy_, cw_);
+                Words d;
+                load_words(g, S, pw, cx_, cy_, cw_, d);
+                cs = cell_case(d, b);
+                ntc = ISO_NTRI[g.method * 256 + cs];
+            }
+            uint32_t sc = ntc;
+#pragma unroll
+            for (int dd = 1; dd < 32; dd <<= 1) {
+                const uint32_t t = __shfl_up_sync(~0u, sc, dd);
+                if (lane >= dd) sc += t;
+            }
+            const uint32_t prev_wid = __shfl_up_sync(~0u, wid, 1);
+            const uint32_t next_wid = __shfl_down_sync(~0u, wid, 1);
+            const uint32_t heads = __ballot_sync(~0u, valid && (lane == 0 || prev_wid != wid));
+            const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+            const uint32_t base = __shfl_sync(~0u, sc, start > 0 ? start - 1 : 0);
+            const uint32_t within_round = sc - ntc - (start > 0 ? base : 0u);
+            const uint32_t carry = valid ? nfs[wid] : 0u;
+            const uint32_t vm = __ballot_sync(~0u, valid);
+            unsigned long long cbase = 0;
+            if (lane == 0 && vm) cbase = atomicAdd(ctr + 10, (unsigned long long)__popc(vm));
+            cbase = __shfl_sync(~0u, cbase, 0);
+            __syncwarp();
+            if (valid) {
+                const unsigned long long ci = cbase + __popc(vm & ((1u << lane) - 1u));
+                if ((long long)ci < capF)
+                    clist[ci] = (unsigned long long)pw | ((unsigned long long)b << 32) |
+                                ((unsigned long long)cs << 37) |
+                                ((unsigned long long)(carry + within_round) << 45);
+                const bool tail = lane == 31 || next_wid != wid;
+                if (tail) nfs[wid] = carry + within_round + ntc;
+            }
+            __syncwarp();
+        }
     }
     __syncthreads();
-    if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
-    const uint32_t nlist = uint32_t(ctr[0]);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    EmitWarp& W = ew[warp];
-    const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW);
-    const long long sxv = (long long)g.ny * g.nz;
-
-    for (uint32_t c0 = (blockIdx.x * NWARP + warp) * 32u; c0 < nlist; c0 += gridDim.x * NWARP * 32u) {
-        // this lane's word
-        const uint32_t it = c0 + lane;
-        const bool have = it < nlist;
-        uint32_t pw = 0, fbase = 0, vbase = 0, ex = 0, ey = 0, ez = 0, act = 0;
-        int x = 0, y = 0, w = 0;
-        Words d{};
-        if (have) {
-            const uint2 e = list[it];
-            pw = e.x;
-            const uint32_t row = pw / uint32_t(g.NW);
-            w = int(pw - row * uint32_t(g.NW));
-            x = int(row / uint32_t(g.ny));
-            y = int(row - uint32_t(x) * uint32_t(g.ny));
-            load_words(g, S, pw, x, y, w, d);
-            const uint32_t zm = zmask(g, w);
-            ex = d.hasx ? (d.s[0][0][0] ^ d.s[1][0][0]) : 0u;
-            ey = d.hasy ? (d.s[0][0][0] ^ d.s[0][1][0]) : 0u;
-            ez = ez_of(d.s[0][0][0], d.s[0][0][1], zm);
-            act = active_cells(d, zm);
-            const uint32_t sg = pw / SEG;
-            vbase = uint32_t(blk[2 * sg]) + (info[pw] & 0x1ffffu);
-            fbase = uint32_t(blk[2 * sg + 1]) + e.y;
-        }
-
-        // vertices: slot vbase + k for the k-th set bit of (ex, ey, ez)
-        {
-            const uint32_t nvl = __popc(ex) + __popc(ey) + __popc(ez);
-            uint32_t incl = nvl;
+    uint32_t nf[WPT], sv = 0, sf = 0;
 #pragma unroll
-            for (int dd = 1; dd < 32; dd <<= 1) {
-                const uint32_t u = __shfl_up_sync(~0u, incl, dd);
-                if (lane >= dd) incl += u;
-            }
-            const uint32_t total = __shfl_sync(~0u, incl, 31);
-            for (uint32_t r = 0; r < total; r += 32) {
-                const uint32_t j = r + lane;
-                const int o = owner_of(incl, j);
-                const uint32_t oex = __shfl_sync(~0u, ex, o), oey = __shfl_sync(~0u, ey, o),
-                               oez = __shfl_sync(~0u, ez, o);
-                const uint32_t oexcl = __shfl_sync(~0u, incl - nvl, o);
-                const uint32_t ovb = __shfl_sync(~0u, vbase, o);
-                const int ox = __shfl_sync(~0u, x, o), oy = __shfl_sync(~0u, y, o), ow = __shfl_sync(~0u, w, o);
-                if (j >= total) continue;
-                const int k = int(j - oexcl);
-                const int cx = __popc(oex), cy = __popc(oey);
-                int ax, b;
-                if (k < cx) { ax = 0; b = nth_set(oex, k); }
-                else if (k < cx + cy) { ax = 1; b = nth_set(oey, k - cx); }
-                else { ax = 2; b = nth_set(oez, k - cx - cy); }
-                const int z = 32 * ow + b;
-                const long long ia = ((long long)ox * g.ny + oy) * g.nz + z;
-                const long long step = ax == 0 ? sxv : (ax == 1 ? (long long)g.nz : 1ll);
-                const float va = __ldg(vals + ia), vb = __ldg(vals + ia + step);
-                const float t = iso::cross_t(g.level, va, vb);
-                const float xa = gx(g, ox), ya = gy(g, oy), za = gz(g, z);
-                const float xb = ax == 0 ? gx(g, ox + 1) : xa;
-                const float yb = ax == 1 ? gy(g, oy + 1) : ya;
-                const float zb = ax == 2 ? gz(g, z + 1) : za;
-                const float px = iso::lerp1(t, xa, xb), py = iso::lerp1(t, ya, yb), pz = iso::lerp1(t, za, zb);
-                const uint32_t vi = ovb + uint32_t(k);
-                float* vo = vout + 3ll * vi;
-                vo[0] = px;
-                vo[1] = py;
-                vo[2] = pz;
-                if ((px == xa && py == ya && pz == za) || (px == xb && py == yb && pz == zb)) {
-                    const unsigned long long sidx = atomicAdd(ctr + 1, 1ull);
-                    if ((long long)sidx < capV) snaps[sidx] = vi;
-                }
-            }
-        }
-
-        // per-word tables for the faces: words, neighbour slot bases, face offsets
-        if (act) {
+    for (int k = 0; k < WPT; ++k) {
+        nf[k] = nfs[threadIdx.x * WPT + k];
+        sv += nv[k];
+        sf += nf[k];
+    }
+    uint32_t ev, ef, tv, tf;
+    block_scan2<CNT_THREADS>(sv, sf, ev, ef, tv, tf, sm);
+    // vertex entries, their slots in order: x edges, then y, then z edges of each word
+    uint32_t vpos = sv;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int dx = q >> 2, dy = (q >> 1) & 1, ww = q & 1;
-                W.wd[q][lane] = d.s[dx][dy][ww];
-                uint32_t bse = 0, cc = 0;
-                if (ww == 0 || w + 1 < g.NW) {
-                    const uint32_t qw = pw + uint32_t(dx) * sxw + uint32_t(dy) * uint32_t(g.NW) + uint32_t(ww);
-                    const uint32_t inf = info[qw];
-                    bse = uint32_t(blk[2 * (qw / SEG)]) + (inf & 0x1ffffu);
-                    cc = ((inf >> 17) & 63u) | (((inf >> 23) & 63u) << 8);
-                }
-                W.nb[q][lane] = bse;
-                W.nc[q][lane] = uint16_t(cc);
-            }
-            uint32_t m = act, run = 0;
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1;
-                W.fo[lane][b] = uint8_t(run);
-                run += nt[cell_case(d, b)];
-            }
-        }
-        __syncwarp();
-
-        // faces: one active cell per lane
-        {
-            const uint32_t na = __popc(act);
-            uint32_t incl = na;
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(~0u, vpos, d);
+        if (lane >= d) vpos += t;
+    }
+    const uint32_t vtot = __shfl_sync(~0u, vpos, 31);
+    unsigned long long vb = 0;
+    if (lane == 31 && vtot) vb = atomicAdd(ctr, (unsigned long long)vtot);
+    vb = __shfl_sync(~0u, vb, 31) + (vpos - sv);
+    if (vec && pw0 + WPT <= g.PW) {
+        *reinterpret_cast<uint4*>(info + pw0) =
+            make_uint4(ev | cxy[0], (ev + nv[0]) | cxy[1], (ev + nv[0] + nv[1]) | cxy[2],
+                       (ev + nv[0] + nv[1] + nv[2]) | cxy[3]);
+    }
 #pragma unroll
-            for (int dd = 1; dd < 32; dd <<= 1) {
-                const uint32_t u = __shfl_up_sync(~0u, incl, dd);
-                if (lane >= dd) incl += u;
-            }
-            const uint32_t total = __shfl_sync(~0u, incl, 31);
-            for (uint32_t r = 0; r < total; r += 32) {
-                const uint32_t j = r + lane;
-                const int o = owner_of(incl, j);
-                const uint32_t oact = __shfl_sync(~0u, act, o);
-                const uint32_t oexcl = __shfl_sync(~0u, incl - na, o);
-                const uint32_t ofb = __shfl_sync(~0u, fbase, o);
-                const int ow = __shfl_sync(~0u, w, o);
-                if (j >= total) continue;
-                const int b = nth_set(oact, int(j - oexcl));
-                Words c;
+    for (int k = 0; k < WPT; ++k) {
+        const uint32_t pw = pw0 + k;
+        if (pw < g.PW) {
+            if (!(vec && pw0 + WPT <= g.PW)) info[pw] = ev | cxy[k];
+            if (nf[k]) foff[pw] = ef;
+            if (nv[k]) {
+                // masks again, from the registers
+                int xx, yy, ww;
+                word_xyw(g, pw, xx, yy, ww);
+                const bool hx = xx < g.nx - 1, hy = yy < g.ny - 1, nxt = ww + 1 < g.NW;
+                const uint32_t s00 = r[0][0][k];
+                const uint32_t s00n = nxt ? (k + 1 < WPT ? r[0][0][(k + 1) % WPT] : nx4[0][0]) : 0u;
+                const uint32_t m3[3] = {hx ? (s00 ^ r[1][0][k]) : 0u, hy ? (s00 ^ r[0][1][k]) : 0u,
+                                        ez_of(s00, s00n, zmask(g, ww))};
+                uint32_t slot = ev;
 #pragma unroll
-                for (int q = 0; q < 8; ++q) c.s[q >> 2][(q >> 1) & 1][q & 1] = W.wd[q][o];
-                const uint32_t zm = zmask(g, ow);
-                const uint32_t cs = cell_case(c, b);
-                const uint32_t es = est[cs];
-#pragma unroll
-                for (int k = 0; k < 12; ++k) {
-                    if (!((es >> k) & 1u)) continue;
-                    const int a = iso_edge_corner(2 * k), cc = iso_edge_corner(2 * k + 1);
-                    const int ax = (cc - a) == 4 ? 0 : ((cc - a) == 2 ? 1 : 2);
-                    const int adx = a >> 2, ady = (a >> 1) & 1, adz = a & 1;
-                    const int ww = adz ? ((b + 1) >> 5) : 0;
-                    const int bit = (b + adz) & 31;
-                    const int q0 = (adx * 2 + ady) * 2;  // neighbour word index with ww = 0
-                    uint32_t mm, off = ww ? W.nb[q0 + 1][o] : W.nb[q0][o];
-                    const uint32_t cxy = ww ? W.nc[q0 + 1][o] : W.nc[q0][o];
-                    if (ax == 0) {
-                        mm = ww ? (c.s[0][ady][1] ^ c.s[1][ady][1]) : (c.s[0][ady][0] ^ c.s[1][ady][0]);
-                    } else if (ax == 1) {
-                        mm = ww ? (c.s[adx][0][1] ^ c.s[adx][1][1]) : (c.s[adx][0][0] ^ c.s[adx][1][0]);
-                        off += cxy & 0xffu;
-                    } else {
-                        mm = ez_of(c.s[adx][ady][0], c.s[adx][ady][1], zm);
-                        off += (cxy & 0xffu) + (cxy >> 8);
+                for (int ax = 0; ax < 3; ++ax) {
+                    uint32_t m = m3[ax];
+                    while (m) {
+                        const int bb = __ffs(m) - 1;
+                        m &= m - 1;
+                        if ((long long)vb < capV)
+                            vlist[vb] = (unsigned long long)pw | ((unsigned long long)ax << 32) |
+                                        ((unsigned long long)bb << 34) | ((unsigned long long)slot << 39);
+                        ++vb;
+                        ++slot;
                     }
-                    W.vid[k][lane] = off + __popc(mm & ((1u << bit) - 1u));
-                }
-                unsigned long long fo = (unsigned long long)ofb + W.fo[o][b];
-                const signed char* tr = tri + cs * ml;
-                for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
-                    int32_t* f3 = fout + 3 * fo;
-                    f3[0] = int32_t(W.vid[tr[k]][lane]);
-                    f3[1] = int32_t(W.vid[tr[k + 1]][lane]);
-                    f3[2] = int32_t(W.vid[tr[k + 2]][lane]);
-                    ++fo;
                 }
             }
         }
-        __syncwarp();
+        ev += nv[k];
+        ef += nf[k];
+    }
+    if (threadIdx.x == 0) {
+        blk[2 * seg] = tv;
+        blk[2 * seg + 1] = tf;
     }
 }
 
+// ---------------------------------------------------------------------------
+// 3. scan of the per-segment (V, F) sums of mc_count into exclusive offsets:
+// CTAs take chunks of SCAN_PER * SCAN_THREADS segments in ticket order and chain
+// their totals by decoupled look-back.  The last chunk writes the totals and
+// checks the capacities.
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER = 4;
+
+__global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk, uint32_t nseg,
+                                                        unsigned long long* ctr, unsigned long long* state,
+                                                        long long* counts, int* status, long long capV,
+                                                        long long capF) {
+    __shared__ uint32_t sm[64];
+    __shared__ uint32_t chunk_s;
+    __shared__ unsigned long long pre_s[2];
+    if (threadIdx.x == 0) chunk_s = uint32_t(atomicAdd(ctr + 7, 1ull));
+    __syncthreads();
+    const uint32_t chunk = chunk_s;
+    const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
+    const uint32_t s0 = chunk * SCAN_PER * SCAN_THREADS + threadIdx.x * SCAN_PER;
+    uint32_t a[SCAN_PER], b[SCAN_PER], sa = 0, sb = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; ++k) {
+        a[k] = s0 + k < nseg ? uint32_t(blk[2 * (s0 + k)]) : 0u;
+        b[k] = s0 + k < nseg ? uint32_t(blk[2 * (s0 + k) + 1]) : 0u;
+        sa += a[k];
+        sb += b[k];
+    }
+    uint32_t ea, eb, ta, tb;
+    block_scan2<SCAN_THREADS>(sa, sb, ea, eb, ta, tb, sm);
+    if (threadIdx.x < 32) {
+        unsigned long long pv = 0, pf = 0;
+        if (chunk == 0) {
+            if (threadIdx.x == 0) atomicExch(state, lb_pack(LB_INC, ta, tb));
+        } else {
+            if (threadIdx.x == 0) atomicExch(state + chunk, lb_pack(LB_AGG, ta, tb));
+            look_back(state, chunk, pv, pf, status);
+            if (threadIdx.x == 0) atomicExch(state + chunk, lb_pack(LB_INC, pv + ta, pf + tb));
+        }
+        if (threadIdx.x == 0) {
+            pre_s[0] = pv;
+            pre_s[1] = pf;
+            if (chunk == nchunk - 1) {
+                const unsigned long long V = pv + ta, F = pf + tb;
+                counts[0] = (long long)V;
+                counts[1] = (long long)F;
+                if ((long long)V > capV || (long long)F > capF || V >= LB_MASK31 || F >= LB_MASK31)
+                    atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+            }
+        }
+    }
+    __syncthreads();
+    unsigned long long ov = pre_s[0] + ea, of = pre_s[1] + eb;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; ++k) {
+        if (s0 + k < nseg) {
+            blk[2 * (s0 + k)] = ov;
+            blk[2 * (s0 + k) + 1] = of;
+        }
+        ov += a[k];
+        of += b[k];
+    }
+}
 
 // ---------------------------------------------------------------------------
-// 5. snap fix-up (cooperative launch: all CTAs are resident)
+// 4. emit: one thread per vertex entry, then one thread per cell entry.
+
+__device__ __forceinline__ float gx(const McGrid& g, int x) { return g.gc[x]; }
+__device__ __forceinline__ float gy(const McGrid& g, int y) { return g.gc[g.nx + y]; }
+__device__ __forceinline__ float gz(const McGrid& g, int z) { return g.gc[g.nx + g.ny + z]; }
+
+template <int EMIT_THREADS>
+__global__ void __launch_bounds__(EMIT_THREADS) mc_emit_vertices(
+    const McGrid g, const float* __restrict__ vals, const unsigned long long* __restrict__ blk,
+    const unsigned long long* __restrict__ vlist, unsigned long long* ctr, uint32_t* __restrict__ snaps,
+    uint32_t* small, float* vout, const long long* __restrict__ counts, long long capV, long long capF) {
+    if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
+    const unsigned long long n = min(ctr[0], (unsigned long long)capV);
+    const long long sxv = (long long)g.ny * g.nz;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * EMIT_THREADS + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * EMIT_THREADS) {
+        const unsigned long long e = vlist[i];
+        const uint32_t pw = uint32_t(e);
+        const int ax = int((e >> 32) & 3u), b = int((e >> 34) & 31u);
+        const uint32_t vi = uint32_t(blk[2 * seg_of(pw)]) + uint32_t((e >> 39) & 0xfffffu);
+        int x, y, w;
+        word_xyw(g, pw, x, y, w);
+        const int z = 32 * w + b;
+        const long long ia = ((long long)x * g.ny + y) * g.nz + z;
+        const long long step = ax == 0 ? sxv : (ax == 1 ? (long long)g.nz : 1ll);
+        const float va = __ldg(vals + ia), vb = __ldg(vals + ia + step);
+        const float t = iso::cross_t(g.level, va, vb);
+        const float xa = gx(g, x), ya = gy(g, y), za = gz(g, z);
+        const float xb = ax == 0 ? gx(g, x + 1) : xa;
+        const float yb = ax == 1 ? gy(g, y + 1) : ya;
+        const float zb = ax == 2 ? gz(g, z + 1) : za;
+        const float px = iso::lerp1(t, xa, xb), py = iso::lerp1(t, ya, yb), pz = iso::lerp1(t, za, zb);
+        float* vo = vout + 3ll * vi;
+        vo[0] = px;
+        vo[1] = py;
+        vo[2] = pz;
+        if (!(t >= g.tau && t <= 1.0f - g.tau) || (px == xa && py == ya && pz == za) ||
+            (px == xb && py == yb && pz == zb)) {
+            // a candidate for sharing its position: list it, and look for an
+            // equal position among the candidates so far
+            const unsigned long long sidx = atomicAdd(ctr + 1, 1ull);
+            if ((long long)sidx < capV) snaps[sidx] = vi;
+            __threadfence();  // the position is visible before the hash entry
+            uint32_t h = phash(pbits(px), pbits(py), pbits(pz)) & (SMALL_HC - 1u);
+            bool placed = false;
+            for (uint32_t probe = 0; probe < SMALL_HC; ++probe, h = (h + 1) & (SMALL_HC - 1u)) {
+                const uint32_t cur = atomicCAS(&small[h], 0u, vi + 1u);
+                if (cur == 0u) { placed = true; break; }
+                if (same_pos(vo, vout + 3ll * (cur - 1u))) {
+                    atomicAdd(ctr + 8, 1ull);
+                    placed = true;
+                    break;
+                }
+            }
+            if (!placed) atomicOr(reinterpret_cast<unsigned int*>(ctr + 9), 1u);
+        }
+    }
+}
+
+template <int EMIT_THREADS>
+__global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
+    const McGrid g, const uint32_t* __restrict__ S, const uint32_t* __restrict__ info,
+    const unsigned long long* __restrict__ blk, const uint32_t* __restrict__ foff,
+    const unsigned long long* __restrict__ clist, const unsigned long long* ctr, int32_t* __restrict__ fout,
+    const long long* __restrict__ counts, long long capV, long long capF) {
+    __shared__ signed char tri[256 * 15];
+    __shared__ uint16_t est[256];
+    __shared__ uint32_t vid[12][EMIT_THREADS];
+    const int ml = g.method == 0 ? 15 : 12;
+    for (int i = threadIdx.x; i < 256 * ml; i += EMIT_THREADS) tri[i] = tri_row(g.method, 0)[i];
+    for (int i = threadIdx.x; i < 256; i += EMIT_THREADS) est[i] = ISO_EDGE_STATUS[i];
+    __syncthreads();
+    if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
+    const unsigned long long n = min(ctr[10], (unsigned long long)capF);
+    const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW);
+    const int tid = threadIdx.x;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * EMIT_THREADS + tid; i < n;
+         i += (unsigned long long)gridDim.x * EMIT_THREADS) {
+        const unsigned long long e = clist[i];
+        const uint32_t pw = uint32_t(e);
+        const int b = int((e >> 32) & 31u);
+        const uint32_t cs = uint32_t((e >> 37) & 255u);
+        int x, y, w;
+        word_xyw(g, pw, x, y, w);
+        unsigned long long fo = blk[2 * seg_of(pw) + 1] + foff[pw] + ((e >> 45) & 255u);
+        Words d;
+        load_words(g, S, pw, x, y, w, d);
+        const uint32_t zm = zmask(g, w);
+        const uint32_t es = est[cs];
+        const int hi = (b + 1) >> 5;  // the cell's z + 1 lies in word w + 1
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            if (!((es >> k) & 1u)) continue;
+            const int a = iso_edge_corner(2 * k), c = iso_edge_corner(2 * k + 1);
+            const int ax = (c - a) == 4 ? 0 : ((c - a) == 2 ? 1 : 2);
+            const int adx = a >> 2, ady = (a >> 1) & 1, adz = a & 1;
+            const int ww = adz ? hi : 0;
+            const int bit = (b + adz) & 31;
+            uint32_t m;
+            if (ax == 0) m = ww ? (d.s[0][ady][1] ^ d.s[1][ady][1]) : (d.s[0][ady][0] ^ d.s[1][ady][0]);
+            else if (ax == 1) m = ww ? (d.s[adx][0][1] ^ d.s[adx][1][1]) : (d.s[adx][0][0] ^ d.s[adx][1][0]);
+            else m = ez_of(d.s[adx][ady][0], d.s[adx][ady][1], zm);
+            const uint32_t q = pw + uint32_t(adx) * sxw + uint32_t(ady) * uint32_t(g.NW) + uint32_t(ww);
+            const uint32_t inf = info[q];
+            uint32_t off = uint32_t(blk[2 * seg_of(q)]) + (inf & 0xfffffu);
+            if (ax >= 1) off += (inf >> 20) & 63u;
+            if (ax == 2) off += (inf >> 26) & 63u;
+            vid[k][tid] = off + __popc(m & ((1u << bit) - 1u));
+        }
+        const signed char* tr = tri + cs * ml;
+        for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
+            int32_t* f3 = fout + 3 * fo;
+            f3[0] = int32_t(vid[tr[k]][tid]);
+            f3[1] = int32_t(vid[tr[k + 1]][tid]);
+            f3[2] = int32_t(vid[tr[k + 2]][tid]);
+            ++fo;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. snap fix-up (cooperative launch: all CTAs are resident)
 
 struct FixArgs {
     float* vout;
@@ -656,15 +861,6 @@ __device__ bool grid_barrier(unsigned long long* ctr, int* status) {
     return ok != 0;
 }
 
-__device__ __forceinline__ uint32_t pbits(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
-__device__ __forceinline__ uint32_t phash(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
-    h ^= h >> 15;
-    h *= 0x2C1B3C6Du;
-    h ^= h >> 12;
-    return h;
-}
-
 // Vertex with the smallest index at vertex v's position among snapped vertices, or v.
 __device__ uint32_t rep_of(const FixArgs& a, uint32_t v) {
     const float* p = a.vout + 3ll * v;
@@ -674,8 +870,7 @@ __device__ uint32_t rep_of(const FixArgs& a, uint32_t v) {
     for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
         const uint32_t j = a.w.table[h];
         if (j == 0xffffffffu) break;
-        const float* q = a.vout + 3ll * j;
-        if (pbits(q[0]) == k0 && pbits(q[1]) == k1 && pbits(q[2]) == k2) return j;
+        if (same_pos(p, a.vout + 3ll * j)) return j;
     }
     return v;
 }
@@ -753,7 +948,8 @@ __global__ void __launch_bounds__(FIX_BLOCK) mc_fixup(const FixArgs a) {
     const long long V = a.counts[0], F = a.counts[1];
     if (V > a.capV || F > a.capF || V > 0x7fffffffll) return;
     const long long nsnap = min((long long)w.ctr[1], a.capV);
-    if (nsnap == 0) return;
+    // nothing to merge unless the emit kernel found equal positions (or its hash filled up)
+    if (nsnap == 0 || (w.ctr[8] == 0 && w.ctr[9] == 0)) return;
     const long long gtid = (long long)blockIdx.x * FIX_BLOCK + threadIdx.x;
     const long long gstride = (long long)gridDim.x * FIX_BLOCK;
     const uint32_t mask = w.HC - 1;
@@ -772,8 +968,7 @@ __global__ void __launch_bounds__(FIX_BLOCK) mc_fixup(const FixArgs a) {
         for (uint32_t probe = 0; probe <= mask && !done; ++probe, h = (h + 1) & mask) {
             const uint32_t cur = atomicCAS(&w.table[h], 0xffffffffu, v);
             if (cur == 0xffffffffu) { done = true; break; }
-            const float* q = a.vout + 3ll * cur;
-            if (pbits(q[0]) == k0 && pbits(q[1]) == k1 && pbits(q[2]) == k2) {
+            if (same_pos(p, a.vout + 3ll * cur)) {
                 atomicMin(&w.table[h], v);
                 done = true;
             }
@@ -912,33 +1107,51 @@ int sm_count() {
     return sms;
 }
 
-template <int BLOCK>
+template <int EMIT_THREADS>
+int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms);
+
 int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st) {
     const int sms = sm_count();
     {
         iso::ProfScope ps("mc_count", st);
-        static int per = -1;
-        if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_count, CNT_THREADS, 0);
-        const long long grid = std::max<long long>(1, std::min<long long>(w.nBlk, (long long)sms * std::max(per, 1)));
+        const long long ncoord = (long long)p.nx + p.ny + p.nz;
+        const long long grid = std::max<long long>(w.nBlk, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
         mc_count<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0], p.asize[1],
-                                                         p.asize[2], w.S, w.info, w.blk, w.list, w.ctr, w.gc,
-                                                         uint32_t(w.nBlk));
+                                                         p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff,
+                                                         w.ctr, w.gc, uint32_t(w.nBlk), p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
         iso::ProfScope ps("mc_scan", st);
-        mc_scan<<<1, SCAN_THREADS, 0, st>>>(w.blk, w.nBlk, p.counts, p.status, p.capV, p.capF);
+        const uint32_t nseg = uint32_t(w.nBlk);
+        const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
+        mc_scan<<<nchunk, SCAN_THREADS, 0, st>>>(w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV, p.capF);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
+    const int block = mc_get_block();
+    return block == 128 ? launch_emit<128>(p, g, w, st, sms) : launch_emit<256>(p, g, w, st, sms);
+}
+
+template <int EMIT_THREADS>
+int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms) {
+    static int perv = -1, perf = -1;
+    if (perv < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perv, mc_emit_vertices<EMIT_THREADS>, EMIT_THREADS, 0);
+    if (perf < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perf, mc_emit_faces<EMIT_THREADS>, EMIT_THREADS, 0);
+    // entries are a fraction of the capacities; the loops are grid-stride
+    const auto grid_for = [&](long long cap, int per) {
+        const long long want = (cap + EMIT_THREADS - 1) / EMIT_THREADS;
+        return unsigned(std::max<long long>(1, std::min<long long>(want, (long long)sms * std::max(per, 1))));
+    };
+    {
+        iso::ProfScope ps("mc_emit_vertices", st);
+        mc_emit_vertices<EMIT_THREADS><<<grid_for(p.capV, perv), EMIT_THREADS, 0, st>>>(
+            g, p.vals, w.blk, w.vlist, w.ctr, w.snaps, w.small, p.vout, p.counts, p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
-        iso::ProfScope ps("mc_emit", st);
-        static int per = -1;
-        if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_emit<BLOCK>, BLOCK, 0);
-        // enough warps for every listed word to have a lane, up to the resident limit
-        const long long want = (w.nBlk * SEG / 32 + (BLOCK / 32) - 1) / (BLOCK / 32);
-        const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sms * std::max(per, 1)));
-        mc_emit<BLOCK><<<unsigned(grid), BLOCK, 0, st>>>(g, p.vals, w.S, w.info, w.blk, w.list, w.ctr, w.snaps,
-                                                         p.vout, p.fout, p.counts, p.capV, p.capF);
+        iso::ProfScope ps("mc_emit_faces", st);
+        mc_emit_faces<EMIT_THREADS><<<grid_for(p.capF, perf), EMIT_THREADS, 0, st>>>(
+            g, w.S, w.info, w.blk, w.foff, w.clist, w.ctr, p.fout, p.counts, p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     return 0;
@@ -966,12 +1179,31 @@ void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uin
     mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, rows, nz, level, out);
 }
 
+// Bound on t for an edge vertex to land within a few ulps of an endpoint (the
+// only place two edges' vertices can meet).  The lerp (1 - t) a + t b is off
+// by at most ~2 ulps of max(|a|, |b|) per coordinate, so a vertex comes that
+// close to an endpoint only if t * h <= 2^-22 * max|coord| (h the spacing);
+// tau = 2^-20 * (1 + max|coord| / h) keeps a factor of 4 on that, and the same
+// holds for 1 - t.
+float snap_tau(const McParams& p) {
+    const int n[3] = {p.nx, p.ny, p.nz};
+    double r = 0;
+    for (int k = 0; k < 3; ++k) {
+        const double amin = p.amin[k], amax = double(p.amin[k]) + double(p.asize[k]);
+        const double size = p.asize[k];
+        const double m = std::max(std::fabs(amin), std::fabs(amax));
+        if (size == 0.0 || !std::isfinite(size)) return 1.0f;
+        r = std::max(r, m * double(std::max(n[k] - 1, 1)) / std::fabs(size));
+    }
+    const double tau = std::ldexp(1.0, -20) * (1.0 + r);
+    return tau >= 0.5 ? 1.0f : float(tau);
+}
+
 size_t mc_workspace_bytes(int nx, int ny, int nz, long long capV, long long capF) {
     return carve(nx, ny, nz, capV, capF, nullptr).total;
 }
 
 int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
-    const int block = mc_get_block();
     const McWs w0 = carve(p.nx, p.ny, p.nz, p.capV, p.capF, nullptr);
     if (ws_bytes < w0.total) return ISO_ERR_WORKSPACE;
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
@@ -979,18 +1211,21 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     McGrid g;
     g.nx = p.nx; g.ny = p.ny; g.nz = p.nz;
     g.NW = (p.nz + 31) / 32;
+    g.dNW = make_fastdiv(uint32_t(g.NW));
+    g.dNY = make_fastdiv(uint32_t(g.ny));
     g.PW = (long long)p.nx * p.ny * g.NW;
     g.level = p.level;
     g.method = p.method;
+    g.tau = snap_tau(p);
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
-    if (cudaMemsetAsync(w.ctr, 0, 8 * 8, st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cudaMemsetAsync(w.ctr, 0, zeroed_bytes(w.nBlk), st) != cudaSuccess) return ISO_ERR_CUDA;
     {
         iso::ProfScope ps("mc_signs", st);
         mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
-    const int rc = block == 128 ? launch_count_emit<128>(p, g, w, st) : launch_count_emit<256>(p, g, w, st);
+    const int rc = launch_count_emit(p, g, w, st);
     if (rc) return rc;
     {
         iso::ProfScope ps("mc_fixup", st);

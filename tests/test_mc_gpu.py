@@ -125,6 +125,12 @@ def test_mc_word_boundaries(oracle, nz):
     check(oracle, noise((9, 10, nz), seed=nz, zero_frac=0.2), what=f"noise nz {nz}")
 
 
+def test_mc_long_rows(oracle):
+    # rows longer than 2048 words (nz > 65536) take the two-pass sign + count path
+    for shape in [(3, 3, 70001), (2, 4, 66000)]:
+        check(oracle, noise(shape, seed=11, zero_frac=0.05), what=f"long rows {shape}")
+
+
 def test_mc_thin_grids(oracle):
     # fewer point words than grid coordinates (the count kernel also writes those)
     for shape in [(2, 2, 300), (2, 300, 2), (300, 2, 2), (3, 3, 1000)]:
