@@ -142,6 +142,18 @@ def flat(table: list[list[list[int]]], width: int) -> list[int]:
     return out
 
 
+def packed(table: list[list[list[int]]]) -> list[int]:
+    out = []
+    for tris in table:
+        edges = [e for t in tris for e in t]
+        assert len(edges) <= 15
+        v = len(tris) << 60
+        for i, e in enumerate(edges):
+            v |= e << (4 * i)
+        out.append(v)
+    return out
+
+
 def ntri(table: list[list[list[int]]]) -> list[int]:
     return [len(row) for row in table]
 
@@ -175,6 +187,9 @@ def render() -> str:
         arr("ISO_TRI_LORENSEN", "signed char", flat(lor, 12), 12),
         "\n/* Triangles per case: [0, 256) Nagae, [256, 512) Lorensen. */\n",
         arr("ISO_NTRI", "unsigned char", ntri(nag) + ntri(lor), 16),
+        "\n/* Each case's triangles in one word: edge of slot i in bits 4i .. 4i+3,\n"
+        " * triangle count in bits 60 .. 63.  [0, 256) Nagae, [256, 512) Lorensen. */\n",
+        arr("ISO_TRI_PACKED", "unsigned long long", [f"{v:#x}ull" for v in packed(nag) + packed(lor)], 4),
         "\n/* ISO_EDGE_CORNERS as a compile-time function, for fully unrolled loops. */\n",
         "#ifdef __cplusplus\n#ifdef __CUDACC__\n#define ISO_LUT_HD __host__ __device__\n#else\n",
         "#define ISO_LUT_HD\n#endif\n",

@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
         else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2);
     }
     const uint32_t seg = blockIdx.x;
-    if (seg >= nseg) return;  // blocks past the segments only write coordinates
+    if (seg >= nseg) return;  // CTAs past the segments only write coordinates
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW), syw = uint32_t(g.NW);
     const bool vec = (g.NW & 3) == 0;  // rows start on 16-byte boundaries
@@ -457,33 +457,48 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
         }
     uint32_t nv[WPT], cxy[WPT], act[WPT];
 #pragma unroll
-    for (int k = 0; k < WPT; ++k) {
-        nv[k] = 0; cxy[k] = 0; act[k] = 0;
-        if (pw0 + k < g.PW) {
-            Words d;
-            d.x = x; d.y = y; d.w = w;
-            d.hasx = x < g.nx - 1;
-            d.hasy = y < g.ny - 1;
-            const bool nxt = w + 1 < g.NW;
+    for (int k = 0; k < WPT; ++k) { nv[k] = 0; cxy[k] = 0; act[k] = 0; }
+    // Most words lie wholly inside or outside the surface: the word and its
+    // grid neighbours' words are all 0 or all ~0, and nothing crosses.  A warp
+    // whose 128 words are all like that skips the rest.
+    bool quiet_all = true;
+    {
+        int qx = x, qy = y, qw = w;
 #pragma unroll
-            for (int dx = 0; dx < 2; ++dx)
+        for (int k = 0; k < WPT; ++k) {
+            if (pw0 + k < g.PW) {
+                const bool hx = qx < g.nx - 1, hy = qy < g.ny - 1, nxt = qw + 1 < g.NW;
+                const uint32_t u = r[0][0][k];
+                bool quiet = u == 0u || u == ~0u;
 #pragma unroll
-                for (int dy = 0; dy < 2; ++dy) {
-                    const bool ok = (dx == 0 || d.hasx) && (dy == 0 || d.hasy);
-                    d.s[dx][dy][0] = ok ? r[dx][dy][k] : 0u;
-                    d.s[dx][dy][1] = (ok && nxt) ? (k + 1 < WPT ? r[dx][dy][(k + 1) % WPT] : nx4[dx][dy]) : 0u;
+                for (int q = 1; q < 8; ++q) {
+                    const int dx = q >> 2, dy = (q >> 1) & 1, ww = q & 1;
+                    const bool valid = (dx == 0 || hx) && (dy == 0 || hy) && (ww == 0 || nxt);
+                    const uint32_t v = ww ? (k + 1 < WPT ? r[dx][dy][(k + 1) % WPT] : nx4[dx][dy]) : r[dx][dy][k];
+                    quiet = quiet && (!valid || v == u);
                 }
-            // most words lie wholly inside or outside: all their grid
-            // neighbours' words are 0 or all ~0 alike, and nothing crosses
-            const uint32_t u = d.s[0][0][0];
-            bool quiet = u == 0u || u == ~0u;
-#pragma unroll
-            for (int q = 1; q < 8; ++q) {
-                const int dx = q >> 2, dy = (q >> 1) & 1, ww = q & 1;
-                const bool valid = (dx == 0 || d.hasx) && (dy == 0 || d.hasy) && (ww == 0 || nxt);
-                quiet = quiet && (!valid || d.s[dx][dy][ww] == u);
+                quiet_all = quiet_all && quiet;
+                advance(g, qx, qy, qw);
             }
-            if (!quiet) {
+        }
+    }
+    if (!__all_sync(~0u, quiet_all)) {
+#pragma unroll
+        for (int k = 0; k < WPT; ++k) {
+            if (pw0 + k < g.PW) {
+                Words d;
+                d.x = x; d.y = y; d.w = w;
+                d.hasx = x < g.nx - 1;
+                d.hasy = y < g.ny - 1;
+                const bool nxt = w + 1 < g.NW;
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+                    for (int dy = 0; dy < 2; ++dy) {
+                        const bool ok = (dx == 0 || d.hasx) && (dy == 0 || d.hasy);
+                        d.s[dx][dy][0] = ok ? r[dx][dy][k] : 0u;
+                        d.s[dx][dy][1] = (ok && nxt) ? (k + 1 < WPT ? r[dx][dy][(k + 1) % WPT] : nx4[dx][dy]) : 0u;
+                    }
                 const uint32_t zm = zmask(g, w);
                 const uint32_t ex = d.hasx ? (d.s[0][0][0] ^ d.s[1][0][0]) : 0u;
                 const uint32_t ey = d.hasy ? (d.s[0][0][0] ^ d.s[0][1][0]) : 0u;
@@ -491,8 +506,8 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                 nv[k] = __popc(ex) + __popc(ey) + __popc(ez);
                 cxy[k] = (uint32_t(__popc(ex)) << 20) | (uint32_t(__popc(ey)) << 26);
                 act[k] = active_cells(d, zm);
+                advance(g, x, y, w);
             }
-            advance(g, x, y, w);
         }
     }
     __syncthreads();  // nfs cleared
@@ -763,12 +778,13 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
     const unsigned long long* __restrict__ blk, const uint32_t* __restrict__ foff,
     const unsigned long long* __restrict__ clist, const unsigned long long* ctr, int32_t* __restrict__ fout,
     const long long* __restrict__ counts, long long capV, long long capF) {
-    __shared__ signed char tri[256 * 15];
+    __shared__ unsigned long long tpk[256];  // packed triangle lists of the table
     __shared__ uint16_t est[256];
     __shared__ uint32_t vid[12][EMIT_THREADS];
-    const int ml = g.method == 0 ? 15 : 12;
-    for (int i = threadIdx.x; i < 256 * ml; i += EMIT_THREADS) tri[i] = tri_row(g.method, 0)[i];
-    for (int i = threadIdx.x; i < 256; i += EMIT_THREADS) est[i] = ISO_EDGE_STATUS[i];
+    for (int i = threadIdx.x; i < 256; i += EMIT_THREADS) {
+        tpk[i] = ISO_TRI_PACKED[g.method * 256 + i];
+        est[i] = ISO_EDGE_STATUS[i];
+    }
     __syncthreads();
     if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
     const unsigned long long n = min(ctr[10], (unsigned long long)capF);
@@ -782,7 +798,7 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
         const uint32_t cs = uint32_t((e >> 37) & 255u);
         int x, y, w;
         word_xyw(g, pw, x, y, w);
-        unsigned long long fo = blk[2 * seg_of(pw) + 1] + foff[pw] + ((e >> 45) & 255u);
+        const unsigned long long fo = blk[2 * seg_of(pw) + 1] + foff[pw] + ((e >> 45) & 255u);
         Words d;
         load_words(g, S, pw, x, y, w, d);
         const uint32_t zm = zmask(g, w);
@@ -807,13 +823,13 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
             if (ax == 2) off += (inf >> 26) & 63u;
             vid[k][tid] = off + __popc(m & ((1u << bit) - 1u));
         }
-        const signed char* tr = tri + cs * ml;
-        for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
-            int32_t* f3 = fout + 3 * fo;
-            f3[0] = int32_t(vid[tr[k]][tid]);
-            f3[1] = int32_t(vid[tr[k + 1]][tid]);
-            f3[2] = int32_t(vid[tr[k + 2]][tid]);
-            ++fo;
+        unsigned long long pk = tpk[cs];
+        const int ntc = int(pk >> 60);
+        int32_t* f3 = fout + 3 * fo;
+        for (int k = 0; k < ntc; ++k, pk >>= 12, f3 += 3) {
+            f3[0] = int32_t(vid[pk & 15u][tid]);
+            f3[1] = int32_t(vid[(pk >> 4) & 15u][tid]);
+            f3[2] = int32_t(vid[(pk >> 8) & 15u][tid]);
         }
     }
 }

@@ -41,3 +41,16 @@ def test_luts_equal_reference_tables():
     assert lor == _ref_table(os.path.join(ref, "include/mc/lorensen.cuh"), "tri_table[]")
     st = gen_luts.edge_status(gen_luts.expand(gen_luts.NAGAE, False))
     assert st == _ref_table(os.path.join(ref, "src/shared_luts.cu"), "edge_status_table[edge_table_size]")
+
+
+def test_packed_triangle_lists_match_tables():
+    for method, (table, width) in enumerate([(gen_luts.NAGAE, 15), (gen_luts.LORENSEN, 12)]):
+        cases = gen_luts.expand(table, reflect=method == 1)
+        flat = gen_luts.flat(cases, width)
+        packed = gen_luts.packed(cases)
+        for c in range(256):
+            v = packed[c]
+            n = v >> 60
+            edges = [(v >> (4 * i)) & 15 for i in range(3 * n)]
+            row = [e for e in flat[c * width:(c + 1) * width] if e >= 0]
+            assert edges == row and n == len(cases[c])
