@@ -127,9 +127,7 @@ def kernel_bytes(kind: str, n: int, nv: int, nf: int) -> dict:
         "mc_signs": 4 * pts + 4 * words,           # values once, sign bitmap once
         "mc_count": 4 * words + 4 * words,         # bitmap once, per-word entries once
         "mc_scan": 32 * segs,                      # segment sums read, offsets written
-        "mc_emit_vertices": 8 * nv + 8 * nv + 12 * nv,  # entries, endpoint values, vertices
-        "mc_emit_faces": 8 * nf + 12 * nf,             # cell entries (<= F), faces
-        "mc_fixup": 0,                             # returns at once without coinciding vertices
+        "mc_emit": 16 * nv + 12 * nv + 8 * nf + 12 * nf,  # entries and endpoint values; vertices, faces
     }
 
 

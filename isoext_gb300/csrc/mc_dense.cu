@@ -1,6 +1,6 @@
 // Dense-grid marching cubes on sm_103a.
 //
-// Five launches on one stream, nothing read back by the host:
+// Four launches on one stream, nothing read back by the host:
 //   1. mc_signs   streams the grid once (one warp per row, 16 coalesced
 //                 128-byte loads in flight per warp) into a sign bitmap,
 //                 1 bit per point.  This is the only pass over all values.
@@ -19,10 +19,9 @@
 //                 vertex indices by rank).  Vertices that can share a position
 //                 with another edge's (t within tau of 0 or 1) go through a small
 //                 hash that counts exact coincidences.
-//   5. mc_fixup   cooperative; returns at once unless the emit kernel found
-//                 coinciding vertices.  Then it merges them by exact position,
-//                 drops faces that became degenerate and compacts vertices and
-//                 faces, keeping their order.
+//   The last emit CTA to finish does the fix-up when the emit kernel found
+//   coinciding vertices: it merges them by exact position, drops faces that
+//   became degenerate and compacts vertices and faces, keeping their order.
 //
 // Equivalence with the reference (src/mc/mc.cu:17-68): the reference emits the
 // triangles of active cells in ascending cell id, drops triangles with two equal
@@ -96,7 +95,7 @@ struct McWs {
     uint32_t* foff;             // per word with faces: segment-local face offset
     unsigned long long* ctr;    // [0] list size [1] snaps [2] barrier count [3] barrier gen [4] V' [5] F'
                                 // [6] unused [7] scan ticket [8] merges [9] small hash full
-                                // [10] cell entries
+                                // [10] cell entries [11] emit CTAs done
     unsigned long long* state;  // look-back state per segment (follows ctr; zeroed with it)
     uint32_t* small;            // SMALL_HC entries after the states (zeroed with them)
     float* gc;                  // grid coordinates [nx + ny + nz] (x, then y, then z)
@@ -104,17 +103,13 @@ struct McWs {
     uint32_t* table;            // position hash of snapped vertices [HC]
     uint32_t* used;             // vertex used bits [capV / 32 + 1]
     uint32_t* newidx;           // compacted vertex index [capV]
-    unsigned long long* chunkF; // per chunk of faces: kept count -> offset
-    unsigned long long* chunkV; // per chunk of vertices: used count -> offset
     int32_t* ftmp;              // compacted faces [capF, 3]
     float* vtmp;                // compacted vertices [capV, 3]
     long long nBlk;             // segments of SEG point words
-    long long nChunkF, nChunkV;
     uint32_t HC;
     size_t total;
 };
 
-constexpr int FIX_BLOCK = 512;
 constexpr uint32_t SMALL_HC = 1u << 15;  // merge-detection hash of emit (entries: vertex + 1, 0 = empty)
 constexpr int NCTR = 16;
 constexpr int CNT_THREADS = 256;             // count kernel CTA size
@@ -137,8 +132,6 @@ McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base
     const long long NW = (nz + 31) / 32;
     const long long PW = (long long)nx * ny * NW;
     w.nBlk = (PW + SEG - 1) / SEG;
-    w.nChunkF = (capF + FIX_BLOCK - 1) / FIX_BLOCK + 1;
-    w.nChunkV = (capV + FIX_BLOCK - 1) / FIX_BLOCK + 1;
     w.HC = hash_cap(capV);
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -160,8 +153,6 @@ McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base
     w.table = reinterpret_cast<uint32_t*>(take(size_t(w.HC) * 4));
     w.used = reinterpret_cast<uint32_t*>(take(size_t(capV / 32 + 1) * 4));
     w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capV) * 4));
-    w.chunkF = reinterpret_cast<unsigned long long*>(take(size_t(w.nChunkF) * 8));
-    w.chunkV = reinterpret_cast<unsigned long long*>(take(size_t(w.nChunkV) * 8));
     w.ftmp = reinterpret_cast<int32_t*>(take(size_t(capF) * 12));
     w.vtmp = reinterpret_cast<float*>(take(size_t(capV) * 12));
     w.total = o + 256;  // room to align the base
@@ -244,17 +235,6 @@ __device__ __forceinline__ uint32_t cell_case(const Words& d, int b) {
 
 __device__ __forceinline__ const signed char* tri_row(int method, uint32_t cs) {
     return method == 0 ? ISO_TRI_NAGAE + cs * 15 : ISO_TRI_LORENSEN + cs * 12;
-}
-
-// Triangle count of each case, into shared memory.
-__device__ __forceinline__ void load_ntri(int method, uint8_t* nt) {
-    const int ml = method == 0 ? 15 : 12;
-    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
-        const signed char* tr = tri_row(method, uint32_t(c));
-        int n = 0;
-        while (n * 3 < ml && tr[n * 3] >= 0) ++n;
-        nt[c] = uint8_t(n);
-    }
 }
 
 // Block-wide exclusive scan of two counts; totals in ta, tb.
@@ -410,6 +390,9 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                                                         const long long capV, const long long capF) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
+    __shared__ uint32_t wcell[CNT_THREADS / 32];
+    __shared__ unsigned long long cbase_s, vbase_s;
+    __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
     // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
@@ -426,6 +409,10 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     const uint32_t pw0 = seg * SEG + threadIdx.x * WPT;
 #pragma unroll
     for (int k = 0; k < WPT; ++k) nfs[threadIdx.x * WPT + k] = 0u;
+    if (threadIdx.x < 64) {
+        const uint8_t* t = ISO_NTRI + g.method * 256 + 4 * threadIdx.x;
+        nt4[threadIdx.x] = uint32_t(t[0]) | (uint32_t(t[1]) << 8) | (uint32_t(t[2]) << 16) | (uint32_t(t[3]) << 24);
+    }
     // bitmap words pw0 .. pw0 + 3 of the rows (x, y), (x, y+1), (x+1, y), (x+1, y+1)
     uint32_t r[2][2][WPT];
     int x = 0, y = 0, w = 0;
@@ -523,6 +510,20 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
             if (lane >= dd) incl += t;
         }
         const uint32_t total = __shfl_sync(~0u, incl, 31);
+        // the CTA's cell entries are allocated at once: warp offsets, one atomic
+        if (lane == 0) wcell[warp] = total;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int q = 0; q < CNT_THREADS / 32; ++q) {
+                const uint32_t c = wcell[q];
+                wcell[q] = run;
+                run += c;
+            }
+            cbase_s = run ? atomicAdd(ctr + 10, (unsigned long long)run) : 0ull;
+        }
+        __syncthreads();
+        const unsigned long long wbase = cbase_s + wcell[warp];
         for (uint32_t rr = 0; rr < total; rr += 32) {
             const uint32_t j = rr + lane;
             const int o = owner_of(incl, j);
@@ -550,7 +551,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                 Words d;
                 load_words(g, S, pw, cx_, cy_, cw_, d);
                 cs = cell_case(d, b);
-                ntc = ISO_NTRI[g.method * 256 + cs];
+                ntc = (nt4[cs >> 2] >> (8 * (cs & 3))) & 0xffu;
             }
             uint32_t sc = ntc;
 #pragma unroll
@@ -565,13 +566,9 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
             const uint32_t base = __shfl_sync(~0u, sc, start > 0 ? start - 1 : 0);
             const uint32_t within_round = sc - ntc - (start > 0 ? base : 0u);
             const uint32_t carry = valid ? nfs[wid] : 0u;
-            const uint32_t vm = __ballot_sync(~0u, valid);
-            unsigned long long cbase = 0;
-            if (lane == 0 && vm) cbase = atomicAdd(ctr + 10, (unsigned long long)__popc(vm));
-            cbase = __shfl_sync(~0u, cbase, 0);
             __syncwarp();
             if (valid) {
-                const unsigned long long ci = cbase + __popc(vm & ((1u << lane) - 1u));
+                const unsigned long long ci = wbase + j;
                 if ((long long)ci < capF)
                     clist[ci] = (unsigned long long)pw | ((unsigned long long)b << 32) |
                                 ((unsigned long long)cs << 37) |
@@ -592,17 +589,11 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     }
     uint32_t ev, ef, tv, tf;
     block_scan2<CNT_THREADS>(sv, sf, ev, ef, tv, tf, sm);
-    // vertex entries, their slots in order: x edges, then y, then z edges of each word
-    uint32_t vpos = sv;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(~0u, vpos, d);
-        if (lane >= d) vpos += t;
-    }
-    const uint32_t vtot = __shfl_sync(~0u, vpos, 31);
-    unsigned long long vb = 0;
-    if (lane == 31 && vtot) vb = atomicAdd(ctr, (unsigned long long)vtot);
-    vb = __shfl_sync(~0u, vb, 31) + (vpos - sv);
+    // vertex entries: the CTA's block of entries (one atomic), each entry at the
+    // block base plus its segment-local slot (x edges, then y, then z of each word)
+    if (threadIdx.x == 0) vbase_s = tv ? atomicAdd(ctr, (unsigned long long)tv) : 0ull;
+    __syncthreads();
+    const unsigned long long vb0 = vbase_s;
     if (vec && pw0 + WPT <= g.PW) {
         *reinterpret_cast<uint4*>(info + pw0) =
             make_uint4(ev | cxy[0], (ev + nv[0]) | cxy[1], (ev + nv[0] + nv[1]) | cxy[2],
@@ -630,10 +621,10 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                     while (m) {
                         const int bb = __ffs(m) - 1;
                         m &= m - 1;
+                        const unsigned long long vb = vb0 + slot;
                         if ((long long)vb < capV)
                             vlist[vb] = (unsigned long long)pw | ((unsigned long long)ax << 32) |
                                         ((unsigned long long)bb << 34) | ((unsigned long long)slot << 39);
-                        ++vb;
                         ++slot;
                     }
                 }
@@ -654,7 +645,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
 // their totals by decoupled look-back.  The last chunk writes the totals and
 // checks the capacities.
 constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_PER = 4;
+constexpr int SCAN_PER = 1;
 
 __global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk, uint32_t nseg,
                                                         unsigned long long* ctr, unsigned long long* state,
@@ -719,16 +710,41 @@ __device__ __forceinline__ float gx(const McGrid& g, int x) { return g.gc[x]; }
 __device__ __forceinline__ float gy(const McGrid& g, int y) { return g.gc[g.nx + y]; }
 __device__ __forceinline__ float gz(const McGrid& g, int z) { return g.gc[g.nx + g.ny + z]; }
 
+struct EmitArgs {
+    const float* vals;
+    const uint32_t* S;
+    const uint32_t* info;
+    const unsigned long long* blk;
+    const uint32_t* foff;
+    const unsigned long long* vlist;
+    const unsigned long long* clist;
+    unsigned long long* ctr;
+    uint32_t* snaps;
+    uint32_t* small;
+    float* vout;
+    int32_t* fout;
+    long long* counts;
+    int* status;
+    long long capV, capF;
+    unsigned nbv;  // CTAs with the vertex role; the rest emit faces
+    McWs w;        // for the fix-up
+};
+
+// Vertex role: one thread per vertex entry; CTA `bi` of `nb`.
 template <int EMIT_THREADS>
-__global__ void __launch_bounds__(EMIT_THREADS) mc_emit_vertices(
-    const McGrid g, const float* __restrict__ vals, const unsigned long long* __restrict__ blk,
-    const unsigned long long* __restrict__ vlist, unsigned long long* ctr, uint32_t* __restrict__ snaps,
-    uint32_t* small, float* vout, const long long* __restrict__ counts, long long capV, long long capF) {
-    if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
+__device__ void emit_vertices(const McGrid& g, const EmitArgs& a, unsigned bi, unsigned nb) {
+    const float* __restrict__ vals = a.vals;
+    const unsigned long long* __restrict__ blk = a.blk;
+    const unsigned long long* __restrict__ vlist = a.vlist;
+    unsigned long long* ctr = a.ctr;
+    uint32_t* __restrict__ snaps = a.snaps;
+    uint32_t* small = a.small;
+    float* vout = a.vout;
+    const long long capV = a.capV;
     const unsigned long long n = min(ctr[0], (unsigned long long)capV);
     const long long sxv = (long long)g.ny * g.nz;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * EMIT_THREADS + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * EMIT_THREADS) {
+    for (unsigned long long i = (unsigned long long)bi * EMIT_THREADS + threadIdx.x; i < n;
+         i += (unsigned long long)nb * EMIT_THREADS) {
         const unsigned long long e = vlist[i];
         const uint32_t pw = uint32_t(e);
         const int ax = int((e >> 32) & 3u), b = int((e >> 34) & 31u);
@@ -772,26 +788,28 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit_vertices(
     }
 }
 
+// Face role: one thread per cell entry; CTA `bi` of `nb`.
 template <int EMIT_THREADS>
-__global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
-    const McGrid g, const uint32_t* __restrict__ S, const uint32_t* __restrict__ info,
-    const unsigned long long* __restrict__ blk, const uint32_t* __restrict__ foff,
-    const unsigned long long* __restrict__ clist, const unsigned long long* ctr, int32_t* __restrict__ fout,
-    const long long* __restrict__ counts, long long capV, long long capF) {
+__device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsigned nb) {
     __shared__ unsigned long long tpk[256];  // packed triangle lists of the table
     __shared__ uint16_t est[256];
     __shared__ uint32_t vid[12][EMIT_THREADS];
+    const uint32_t* __restrict__ S = a.S;
+    const uint32_t* __restrict__ info = a.info;
+    const unsigned long long* __restrict__ blk = a.blk;
+    const uint32_t* __restrict__ foff = a.foff;
+    const unsigned long long* __restrict__ clist = a.clist;
+    int32_t* __restrict__ fout = a.fout;
     for (int i = threadIdx.x; i < 256; i += EMIT_THREADS) {
         tpk[i] = ISO_TRI_PACKED[g.method * 256 + i];
         est[i] = ISO_EDGE_STATUS[i];
     }
     __syncthreads();
-    if (counts[0] > capV || counts[1] > capF || counts[0] > 0x7fffffffll) return;
-    const unsigned long long n = min(ctr[10], (unsigned long long)capF);
+    const unsigned long long n = min(a.ctr[10], (unsigned long long)a.capF);
     const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW);
     const int tid = threadIdx.x;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * EMIT_THREADS + tid; i < n;
-         i += (unsigned long long)gridDim.x * EMIT_THREADS) {
+    for (unsigned long long i = (unsigned long long)bi * EMIT_THREADS + tid; i < n;
+         i += (unsigned long long)nb * EMIT_THREADS) {
         const unsigned long long e = clist[i];
         const uint32_t pw = uint32_t(e);
         const int b = int((e >> 32) & 31u);
@@ -834,65 +852,42 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit_faces(
     }
 }
 
+__device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long* counts, int* status,
+                            long long capV);
+
+template <int EMIT_THREADS>
+__global__ void __launch_bounds__(EMIT_THREADS) mc_emit(const McGrid g, const EmitArgs a) {
+    __shared__ int last;
+    if (a.counts[0] > a.capV || a.counts[1] > a.capF || a.counts[0] > 0x7fffffffll) return;
+    if (blockIdx.x < a.nbv) emit_vertices<EMIT_THREADS>(g, a, blockIdx.x, a.nbv);
+    else emit_faces<EMIT_THREADS>(g, a, blockIdx.x - a.nbv, gridDim.x - a.nbv);
+    // the last CTA to finish sees every vertex and face; it does the fix-up if
+    // the emit found coinciding positions
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(a.ctr + 11, 1ull) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (a.ctr[1] == 0 || (a.ctr[8] == 0 && a.ctr[9] == 0)) return;
+    fixup_block(a.w, a.vout, a.fout, a.counts, a.status, a.capV);
+}
+
 // ---------------------------------------------------------------------------
-// 4. snap fix-up (cooperative launch: all CTAs are resident)
+// 4. fix-up: run by the last CTA of mc_emit to finish, and only when some vertex
+// positions coincide (found by the emit kernel's small hash).  It merges the
+// candidates by exact position (smallest index wins, as a sorted weld keeps the
+// first), drops faces that became degenerate and compacts vertices and faces,
+// keeping their order.  One CTA: these inputs are rare (values exactly at the
+// level on grid points, or grids near float resolution).
 
-struct FixArgs {
-    float* vout;
-    int32_t* fout;
-    long long* counts;
-    int* status;
-    long long capV, capF;
-    McWs w;
-};
-
-// Grid-wide barrier with a bounded wait; false if it ran out (status set).
-__device__ bool grid_barrier(unsigned long long* ctr, int* status) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        ok = 1;
-        volatile unsigned long long* gen = ctr + 3;
-        const unsigned long long g0 = *gen;
-        __threadfence();
-        const unsigned long long arrived = atomicAdd(ctr + 2, 1ull);
-        if (arrived == gridDim.x - 1) {
-            ctr[2] = 0;
-            __threadfence();
-            atomicAdd(ctr + 3, 1ull);
-        } else {
-            uint32_t spins = 0;
-            while (*gen == g0) {
-                if (++spins > ISO_SPIN_LIMIT) {
-                    atomicCAS(status, 0, int(ISO_ERR_TIMEOUT));
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok != 0;
+__device__ __forceinline__ bool face_keep(const int32_t* f) {
+    return f[0] != f[1] && f[0] != f[2] && f[1] != f[2];
 }
 
-// Vertex with the smallest index at vertex v's position among snapped vertices, or v.
-__device__ uint32_t rep_of(const FixArgs& a, uint32_t v) {
-    const float* p = a.vout + 3ll * v;
-    const uint32_t k0 = pbits(p[0]), k1 = pbits(p[1]), k2 = pbits(p[2]);
-    const uint32_t mask = a.w.HC - 1;
-    uint32_t h = phash(k0, k1, k2) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-        const uint32_t j = a.w.table[h];
-        if (j == 0xffffffffu) break;
-        if (same_pos(p, a.vout + 3ll * j)) return j;
-    }
-    return v;
-}
-
+// Exclusive block scan of one count; total in `total`.
 __device__ __forceinline__ uint32_t block_excl(uint32_t x, uint32_t& total, uint32_t* sm) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     uint32_t inc = x;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -902,7 +897,7 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t x, uint32_t& total, uint
     if (lane == 31) sm[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t y = lane < FIX_BLOCK / 32 ? sm[lane] : 0u;
+        uint32_t y = lane < nwarps ? sm[lane] : 0u;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t u = __shfl_up_sync(~0u, y, d);
@@ -917,161 +912,92 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t x, uint32_t& total, uint
     return ex;
 }
 
-// Exclusive scan of n counts in place (one CTA), returns the total.
-__device__ unsigned long long scan_serial(unsigned long long* c, long long n, unsigned long long* sm64) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long per = (n + FIX_BLOCK - 1) / FIX_BLOCK;
-    const long long i0 = min(n, tid * per), i1 = min(n, i0 + per);
-    unsigned long long s = 0;
-    for (long long i = i0; i < i1; ++i) s += c[i];
-    unsigned long long inc = s;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long u = __shfl_up_sync(~0u, inc, d);
-        if (lane >= d) inc += u;
-    }
-    if (lane == 31) sm64[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned long long y = lane < FIX_BLOCK / 32 ? sm64[lane] : 0ull;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned long long u = __shfl_up_sync(~0u, y, d);
-            if (lane >= d) y += u;
-        }
-        sm64[lane] = y;
-    }
-    __syncthreads();
-    unsigned long long o = (warp ? sm64[warp - 1] : 0ull) + inc - s;
-    for (long long i = i0; i < i1; ++i) {
-        const unsigned long long v = c[i];
-        c[i] = o;
-        o += v;
-    }
-    const unsigned long long total = sm64[31];
-    __syncthreads();
-    return total;
-}
-
-__device__ __forceinline__ bool face_keep(const int32_t* f) {
-    return f[0] != f[1] && f[0] != f[2] && f[1] != f[2];
-}
-
-__global__ void __launch_bounds__(FIX_BLOCK) mc_fixup(const FixArgs a) {
-    __shared__ uint32_t sm[32];
-    __shared__ unsigned long long sm64[32];
-    const McWs& w = a.w;
-    const long long V = a.counts[0], F = a.counts[1];
-    if (V > a.capV || F > a.capF || V > 0x7fffffffll) return;
-    const long long nsnap = min((long long)w.ctr[1], a.capV);
-    // nothing to merge unless the emit kernel found equal positions (or its hash filled up)
-    if (nsnap == 0 || (w.ctr[8] == 0 && w.ctr[9] == 0)) return;
-    const long long gtid = (long long)blockIdx.x * FIX_BLOCK + threadIdx.x;
-    const long long gstride = (long long)gridDim.x * FIX_BLOCK;
+// Smallest index of a snapped vertex at vertex v's position, or v.
+__device__ uint32_t rep_of(const McWs& w, const float* vout, uint32_t v) {
+    const float* p = vout + 3ll * v;
     const uint32_t mask = w.HC - 1;
+    uint32_t h = phash(pbits(p[0]), pbits(p[1]), pbits(p[2])) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const uint32_t j = w.table[h];
+        if (j == 0xffffffffu) break;
+        if (same_pos(p, vout + 3ll * j)) return j;
+    }
+    return v;
+}
 
-    for (long long i = gtid; i < w.HC; i += gstride) w.table[i] = 0xffffffffu;
-    for (long long i = gtid; i < V / 32 + 1; i += gstride) w.used[i] = 0u;
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    // snapped vertices into the position hash; smallest index wins
-    for (long long s = gtid; s < nsnap; s += gstride) {
+__device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long* counts, int* status,
+                            long long capV) {
+    __shared__ uint32_t sm[32];
+    const long long V = counts[0], F = counts[1];
+    const long long nsnap = min((long long)w.ctr[1], capV);
+    const uint32_t mask = w.HC - 1;
+    const int T = blockDim.x, tid = threadIdx.x;
+    for (long long i = tid; i < w.HC; i += T) w.table[i] = 0xffffffffu;
+    for (long long i = tid; i < V / 32 + 1; i += T) w.used[i] = 0u;
+    __syncthreads();
+    // candidates into the position hash; the smallest index wins
+    for (long long s = tid; s < nsnap; s += T) {
         const uint32_t v = w.snaps[s];
-        const float* p = a.vout + 3ll * v;
-        const uint32_t k0 = pbits(p[0]), k1 = pbits(p[1]), k2 = pbits(p[2]);
-        uint32_t h = phash(k0, k1, k2) & mask;
+        const float* p = vout + 3ll * v;
+        uint32_t h = phash(pbits(p[0]), pbits(p[1]), pbits(p[2])) & mask;
         bool done = false;
         for (uint32_t probe = 0; probe <= mask && !done; ++probe, h = (h + 1) & mask) {
             const uint32_t cur = atomicCAS(&w.table[h], 0xffffffffu, v);
             if (cur == 0xffffffffu) { done = true; break; }
-            if (same_pos(p, a.vout + 3ll * cur)) {
+            if (same_pos(p, vout + 3ll * cur)) {
                 atomicMin(&w.table[h], v);
                 done = true;
             }
         }
-        if (!done) atomicCAS(a.status, 0, int(ISO_ERR_OVERFLOW));
+        if (!done) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
     }
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    // faces: merge snapped vertices, count the non-degenerate ones per chunk
-    const long long nchF = (F + FIX_BLOCK - 1) / FIX_BLOCK;
-    for (long long c = blockIdx.x; c < nchF; c += gridDim.x) {
-        const long long f = c * FIX_BLOCK + threadIdx.x;
+    __syncthreads();
+    // faces: merge, keep the non-degenerate ones in order, mark their vertices
+    uint32_t fn = 0;
+    for (long long base = 0; base < F; base += T) {
+        const long long f = base + tid;
         uint32_t keep = 0;
+        int32_t v3[3] = {0, 0, 0};
         if (f < F) {
-            int32_t* fp = a.fout + 3 * f;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) fp[k] = int32_t(rep_of(a, uint32_t(fp[k])));
-            keep = face_keep(fp);
+            for (int k = 0; k < 3; ++k) v3[k] = int32_t(rep_of(w, vout, uint32_t(fout[3 * f + k])));
+            keep = face_keep(v3);
         }
-        uint32_t tot;
-        block_excl(keep, tot, sm);
-        if (threadIdx.x == 0) w.chunkF[c] = tot;
-    }
-    if (!grid_barrier(w.ctr, a.status)) return;
-    if (blockIdx.x == 0) {
-        const unsigned long long Fn = scan_serial(w.chunkF, nchF, sm64);
-        if (threadIdx.x == 0) w.ctr[5] = Fn;
-    }
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    // kept faces, in order, to ftmp; mark the vertices they use
-    for (long long c = blockIdx.x; c < nchF; c += gridDim.x) {
-        const long long f = c * FIX_BLOCK + threadIdx.x;
-        uint32_t keep = 0;
-        const int32_t* fp = a.fout + 3 * (f < F ? f : 0);
-        if (f < F) keep = face_keep(fp);
         uint32_t tot;
         const uint32_t ex = block_excl(keep, tot, sm);
         if (keep) {
-            int32_t* o = w.ftmp + 3 * (w.chunkF[c] + ex);
+            int32_t* o = w.ftmp + 3ll * (fn + ex);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                o[k] = fp[k];
-                atomicOr(&w.used[uint32_t(fp[k]) >> 5], 1u << (uint32_t(fp[k]) & 31u));
+                o[k] = v3[k];
+                atomicOr(&w.used[uint32_t(v3[k]) >> 5], 1u << (uint32_t(v3[k]) & 31u));
             }
         }
+        fn += tot;
     }
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    // used vertices per chunk
-    const long long nchV = (V + FIX_BLOCK - 1) / FIX_BLOCK;
-    for (long long c = blockIdx.x; c < nchV; c += gridDim.x) {
-        const long long v = c * FIX_BLOCK + threadIdx.x;
-        const uint32_t u = v < V ? (w.used[v >> 5] >> (v & 31)) & 1u : 0u;
-        uint32_t tot;
-        block_excl(u, tot, sm);
-        if (threadIdx.x == 0) w.chunkV[c] = tot;
-    }
-    if (!grid_barrier(w.ctr, a.status)) return;
-    if (blockIdx.x == 0) {
-        const unsigned long long Vn = scan_serial(w.chunkV, nchV, sm64);
-        if (threadIdx.x == 0) w.ctr[4] = Vn;
-    }
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    // compacted vertices to vtmp, new indices
-    for (long long c = blockIdx.x; c < nchV; c += gridDim.x) {
-        const long long v = c * FIX_BLOCK + threadIdx.x;
+    __syncthreads();
+    // vertices still used, in order
+    uint32_t vn = 0;
+    for (long long base = 0; base < V; base += T) {
+        const long long v = base + tid;
         const uint32_t u = v < V ? (w.used[v >> 5] >> (v & 31)) & 1u : 0u;
         uint32_t tot;
         const uint32_t ex = block_excl(u, tot, sm);
         if (u) {
-            const unsigned long long j = w.chunkV[c] + ex;
-            w.newidx[v] = uint32_t(j);
-            w.vtmp[3 * j] = a.vout[3 * v];
-            w.vtmp[3 * j + 1] = a.vout[3 * v + 1];
-            w.vtmp[3 * j + 2] = a.vout[3 * v + 2];
+            const uint32_t j = vn + ex;
+            w.newidx[v] = j;
+            w.vtmp[3ll * j] = vout[3 * v];
+            w.vtmp[3ll * j + 1] = vout[3 * v + 1];
+            w.vtmp[3ll * j + 2] = vout[3 * v + 2];
         }
+        vn += tot;
     }
-    if (!grid_barrier(w.ctr, a.status)) return;
-
-    const long long Vn = (long long)w.ctr[4], Fn = (long long)w.ctr[5];
-    for (long long j = gtid; j < 3 * Vn; j += gstride) a.vout[j] = w.vtmp[j];
-    for (long long j = gtid; j < 3 * Fn; j += gstride) a.fout[j] = int32_t(w.newidx[w.ftmp[j]]);
-    if (gtid == 0) {
-        a.counts[0] = Vn;
-        a.counts[1] = Fn;
+    __syncthreads();
+    for (long long j = tid; j < 3ll * vn; j += T) vout[j] = w.vtmp[j];
+    for (long long j = tid; j < 3ll * fn; j += T) fout[j] = int32_t(w.newidx[w.ftmp[j]]);
+    if (tid == 0) {
+        counts[0] = vn;
+        counts[1] = fn;
     }
 }
 
@@ -1124,7 +1050,25 @@ int sm_count() {
 }
 
 template <int EMIT_THREADS>
-int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms);
+int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms) {
+    static int per = -1;
+    if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_emit<EMIT_THREADS>, EMIT_THREADS, 0);
+    // entries are a fraction of the capacities; the loops are grid-stride.  The
+    // resident CTAs are split between the roles in proportion to the work
+    // (a vertex costs about half a cell).
+    const long long resident = (long long)sms * std::max(per, 1);
+    const auto want = [&](long long cap) { return std::max<long long>(1, (cap + EMIT_THREADS - 1) / EMIT_THREADS); };
+    const long long nbv = std::max<long long>(1, std::min(want(p.capV), resident / 3));
+    const long long nbf = std::max<long long>(1, std::min(want(p.capF), resident - nbv));
+    EmitArgs a{p.vals, w.S, w.info, w.blk, w.foff, w.vlist, w.clist, w.ctr, w.snaps, w.small,
+               p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w};
+    {
+        iso::ProfScope ps("mc_emit", st);
+        mc_emit<EMIT_THREADS><<<unsigned(nbv + nbf), EMIT_THREADS, 0, st>>>(g, a);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
+    return 0;
+}
 
 int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st) {
     const int sms = sm_count();
@@ -1146,31 +1090,6 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
     }
     const int block = mc_get_block();
     return block == 128 ? launch_emit<128>(p, g, w, st, sms) : launch_emit<256>(p, g, w, st, sms);
-}
-
-template <int EMIT_THREADS>
-int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms) {
-    static int perv = -1, perf = -1;
-    if (perv < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perv, mc_emit_vertices<EMIT_THREADS>, EMIT_THREADS, 0);
-    if (perf < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perf, mc_emit_faces<EMIT_THREADS>, EMIT_THREADS, 0);
-    // entries are a fraction of the capacities; the loops are grid-stride
-    const auto grid_for = [&](long long cap, int per) {
-        const long long want = (cap + EMIT_THREADS - 1) / EMIT_THREADS;
-        return unsigned(std::max<long long>(1, std::min<long long>(want, (long long)sms * std::max(per, 1))));
-    };
-    {
-        iso::ProfScope ps("mc_emit_vertices", st);
-        mc_emit_vertices<EMIT_THREADS><<<grid_for(p.capV, perv), EMIT_THREADS, 0, st>>>(
-            g, p.vals, w.blk, w.vlist, w.ctr, w.snaps, w.small, p.vout, p.counts, p.capV, p.capF);
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
-    }
-    {
-        iso::ProfScope ps("mc_emit_faces", st);
-        mc_emit_faces<EMIT_THREADS><<<grid_for(p.capF, perf), EMIT_THREADS, 0, st>>>(
-            g, w.S, w.info, w.blk, w.foff, w.clist, w.ctr, p.fout, p.counts, p.capV, p.capF);
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
-    }
-    return 0;
 }
 
 }  // namespace
@@ -1243,20 +1162,5 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     }
     const int rc = launch_count_emit(p, g, w, st);
     if (rc) return rc;
-    {
-        iso::ProfScope ps("mc_fixup", st);
-        static int per = -1;  // co-resident fix-up CTAs per SM
-        if (per < 0) {
-            int n = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mc_fixup, FIX_BLOCK, 0);
-            per = std::max(1, std::min(n, 2));
-        }
-        FixArgs fa{p.vout, p.fout, p.counts, p.status, p.capV, p.capF, w};
-        void* args[] = {&fa};
-        const unsigned grid = unsigned(sm_count() * per);
-        if (cudaLaunchCooperativeKernel((void*)mc_fixup, dim3(grid), dim3(FIX_BLOCK), args, 0, st) !=
-            cudaSuccess)
-            return ISO_ERR_CUDA;
-    }
     return 0;
 }
