@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     __shared__ uint32_t wcell[CNT_THREADS / 32];
     __shared__ unsigned long long cbase_s, vbase_s;
     __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
+    __shared__ uint32_t vmask[3 * WPT][CNT_THREADS];  // x, y, z edge masks of each thread's words
     // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
@@ -448,26 +449,21 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     // Most words lie wholly inside or outside the surface: the word and its
     // grid neighbours' words are all 0 or all ~0, and nothing crosses.  A warp
     // whose 128 words are all like that skips the rest.
-    bool quiet_all = true;
+    bool quiet_all;
     {
-        int qx = x, qy = y, qw = w;
+        // conservative: all 20 loaded words equal, and all 0 or all ~0 (words at
+        // the grid's edges may fail it and take the exact path)
+        const uint32_t u = r[0][0][0];
+        uint32_t diff = 0;
 #pragma unroll
-        for (int k = 0; k < WPT; ++k) {
-            if (pw0 + k < g.PW) {
-                const bool hx = qx < g.nx - 1, hy = qy < g.ny - 1, nxt = qw + 1 < g.NW;
-                const uint32_t u = r[0][0][k];
-                bool quiet = u == 0u || u == ~0u;
+        for (int dx = 0; dx < 2; ++dx)
 #pragma unroll
-                for (int q = 1; q < 8; ++q) {
-                    const int dx = q >> 2, dy = (q >> 1) & 1, ww = q & 1;
-                    const bool valid = (dx == 0 || hx) && (dy == 0 || hy) && (ww == 0 || nxt);
-                    const uint32_t v = ww ? (k + 1 < WPT ? r[dx][dy][(k + 1) % WPT] : nx4[dx][dy]) : r[dx][dy][k];
-                    quiet = quiet && (!valid || v == u);
-                }
-                quiet_all = quiet_all && quiet;
-                advance(g, qx, qy, qw);
+            for (int dy = 0; dy < 2; ++dy) {
+                diff |= nx4[dx][dy] ^ u;
+#pragma unroll
+                for (int k = 0; k < WPT; ++k) diff |= r[dx][dy][k] ^ u;
             }
-        }
+        quiet_all = (u == 0u || u == ~0u) && diff == 0u;
     }
     if (!__all_sync(~0u, quiet_all)) {
 #pragma unroll
@@ -493,6 +489,9 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                 nv[k] = __popc(ex) + __popc(ey) + __popc(ez);
                 cxy[k] = (uint32_t(__popc(ex)) << 20) | (uint32_t(__popc(ey)) << 26);
                 act[k] = active_cells(d, zm);
+                vmask[3 * k][threadIdx.x] = ex;
+                vmask[3 * k + 1][threadIdx.x] = ey;
+                vmask[3 * k + 2][threadIdx.x] = ez;
                 advance(g, x, y, w);
             }
         }
@@ -590,10 +589,50 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     uint32_t ev, ef, tv, tf;
     block_scan2<CNT_THREADS>(sv, sf, ev, ef, tv, tf, sm);
     // vertex entries: the CTA's block of entries (one atomic), each entry at the
-    // block base plus its segment-local slot (x edges, then y, then z of each word)
+    // block base plus its segment-local slot (x edges, then y, then z of each
+    // word); one vertex per lane of the warp, so consecutive lanes store
+    // consecutive entries
     if (threadIdx.x == 0) vbase_s = tv ? atomicAdd(ctr, (unsigned long long)tv) : 0ull;
     __syncthreads();
     const unsigned long long vb0 = vbase_s;
+    {
+        uint32_t incl = sv;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const uint32_t t = __shfl_up_sync(~0u, incl, dd);
+            if (lane >= dd) incl += t;
+        }
+        const uint32_t total = __shfl_sync(~0u, incl, 31);
+        for (uint32_t rr = 0; rr < total; rr += 32) {
+            const uint32_t j = rr + lane;
+            const int o = owner_of(incl, j);
+            const uint32_t oexcl = __shfl_sync(~0u, incl - sv, o);
+            const uint32_t oev = __shfl_sync(~0u, ev, o);
+            uint32_t onv[WPT];
+#pragma unroll
+            for (int k = 0; k < WPT; ++k) onv[k] = __shfl_sync(~0u, nv[k], o);
+            if (j < total) {
+                uint32_t kk = j - oexcl, slot = oev + kk;
+                int k = 0;
+#pragma unroll
+                for (int q = 0; q < WPT - 1; ++q) {
+                    if (k == q && kk >= onv[q]) { kk -= onv[q]; k = q + 1; }
+                }
+                const uint32_t ot = uint32_t(warp * 32 + o);
+                const uint32_t m0 = vmask[3 * k][ot], m1 = vmask[3 * k + 1][ot], m2 = vmask[3 * k + 2][ot];
+                const uint32_t c0 = __popc(m0), c1 = __popc(m1);
+                int ax, bb;
+                if (kk < c0) { ax = 0; bb = nth_set(m0, int(kk)); }
+                else if (kk < c0 + c1) { ax = 1; bb = nth_set(m1, int(kk - c0)); }
+                else { ax = 2; bb = nth_set(m2, int(kk - c0 - c1)); }
+                const uint32_t pw = seg * SEG + ot * WPT + uint32_t(k);
+                const unsigned long long vb = vb0 + slot;
+                if ((long long)vb < capV)
+                    vlist[vb] = (unsigned long long)pw | ((unsigned long long)ax << 32) |
+                                ((unsigned long long)bb << 34) | ((unsigned long long)slot << 39);
+            }
+        }
+    }
     if (vec && pw0 + WPT <= g.PW) {
         *reinterpret_cast<uint4*>(info + pw0) =
             make_uint4(ev | cxy[0], (ev + nv[0]) | cxy[1], (ev + nv[0] + nv[1]) | cxy[2],
@@ -605,30 +644,6 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
         if (pw < g.PW) {
             if (!(vec && pw0 + WPT <= g.PW)) info[pw] = ev | cxy[k];
             if (nf[k]) foff[pw] = ef;
-            if (nv[k]) {
-                // masks again, from the registers
-                int xx, yy, ww;
-                word_xyw(g, pw, xx, yy, ww);
-                const bool hx = xx < g.nx - 1, hy = yy < g.ny - 1, nxt = ww + 1 < g.NW;
-                const uint32_t s00 = r[0][0][k];
-                const uint32_t s00n = nxt ? (k + 1 < WPT ? r[0][0][(k + 1) % WPT] : nx4[0][0]) : 0u;
-                const uint32_t m3[3] = {hx ? (s00 ^ r[1][0][k]) : 0u, hy ? (s00 ^ r[0][1][k]) : 0u,
-                                        ez_of(s00, s00n, zmask(g, ww))};
-                uint32_t slot = ev;
-#pragma unroll
-                for (int ax = 0; ax < 3; ++ax) {
-                    uint32_t m = m3[ax];
-                    while (m) {
-                        const int bb = __ffs(m) - 1;
-                        m &= m - 1;
-                        const unsigned long long vb = vb0 + slot;
-                        if ((long long)vb < capV)
-                            vlist[vb] = (unsigned long long)pw | ((unsigned long long)ax << 32) |
-                                        ((unsigned long long)bb << 34) | ((unsigned long long)slot << 39);
-                        ++slot;
-                    }
-                }
-            }
         }
         ev += nv[k];
         ef += nf[k];
