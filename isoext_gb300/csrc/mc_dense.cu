@@ -394,6 +394,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     __shared__ unsigned long long cbase_s, vbase_s;
     __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
     __shared__ uint32_t vmask[3 * WPT][CNT_THREADS];  // x, y, z edge masks of each thread's words
+    __shared__ uint32_t rows[4][WPT + 1][CNT_THREADS];  // sign words of rows (dx, dy), words k = 0..4
     // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
@@ -466,6 +467,13 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
         quiet_all = (u == 0u || u == ~0u) && diff == 0u;
     }
     if (!__all_sync(~0u, quiet_all)) {
+        // the cells of these words read their corners from here
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int k = 0; k < WPT; ++k) rows[q][k][threadIdx.x] = r[q >> 1][q & 1][k];
+            rows[q][WPT][threadIdx.x] = nx4[q >> 1][q & 1];
+        }
 #pragma unroll
         for (int k = 0; k < WPT; ++k) {
             if (pw0 + k < g.PW) {
@@ -543,12 +551,17 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                     else break;
                 }
                 b = nth_set(m, kk);
-                wid = uint32_t(warp * 32 + o) * WPT + uint32_t(k);
+                const uint32_t ot = uint32_t(warp * 32 + o);
+                wid = ot * WPT + uint32_t(k);
                 pw = seg * SEG + wid;
-                int cx_, cy_, cw_;
-                word_xyw(g, pw, cx_, cy_, cw_);
+                // corners from the owner's row words (an active cell has rows
+                // x + 1 and y + 1, and z + 1 in word w + 1 only at bit 31)
                 Words d;
-                load_words(g, S, pw, cx_, cy_, cw_, d);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    d.s[q >> 1][q & 1][0] = rows[q][k][ot];
+                    d.s[q >> 1][q & 1][1] = rows[q][k + 1][ot];
+                }
                 cs = cell_case(d, b);
                 ntc = (nt4[cs >> 2] >> (8 * (cs & 3))) & 0xffu;
             }
