@@ -198,6 +198,18 @@ int iso_sparse_filter_count(const float *vals, long long m, float level, void *b
 int iso_sparse_filter_write(const int *ids, const float *vals, long long m, float level, const void *blk,
                             int *out, void *stream);
 
+/* ------------------------------------------------------------------------- */
+/* Grid values of a union of spheres and boxes, for the served request stream
+ * (no counterpart in isoext, which builds grids with torch expressions; the
+ * distances are src/isoext/sdf.py:70-116's sphere and box formulas, the point
+ * positions the grid's own, include/utils.cuh:62-80).
+ * prims: DEVICE float [1 + 7 * count]: prims[0] = count (1 .. 32), then rows of
+ * kind (0 sphere, 1 box), centre xyz, radius | half-extents xyz.  Reading them
+ * from device memory lets a captured CUDA graph evaluate each new request.
+ * out: device float [nx, ny, nz], the minimum over the primitives. */
+int iso_sdf_union_grid(const float *prims, int nx, int ny, int nz, const float *aabb_min,
+                       const float *aabb_max, float *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

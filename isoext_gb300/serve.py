@@ -1,0 +1,354 @@
+"""Served extraction: continuous batching of marching-cubes and dual-contouring
+requests on one GPU.
+
+A request names a grid (cubic, ``n`` points per axis over [-1, 1]^3) given as
+a union of spheres and boxes, and an extraction (``"mc"`` or ``"dc"``).  The
+server keeps ``slots`` workers, each with its own CUDA stream and its own
+device buffers, resident across requests.  Requests are admitted in arrival
+order as soon as a slot is free and the device-memory budget holds the
+request's worst case; the requests on different slots run concurrently on the
+GPU.  A marching-cubes request replays a CUDA graph captured for its slot and
+grid size (grid evaluation + extraction, no host work in between); dual
+contouring runs the library's stream-ordered steps on the slot's stream.
+
+Each result equals the one-call-per-grid result (``solve_plain``) bit for bit:
+the same kernels run on the same inputs, only concurrently.
+
+The scheduling (``Scheduler``) is plain host code, testable without a GPU.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import ctypes as C
+import threading
+import time
+from collections import deque
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _ffi
+
+_vp, _i, _fa = C.c_void_p, C.c_int, C.POINTER(C.c_float)
+_ffi.register({"iso_sdf_union_grid": ([_vp, _i, _i, _i, _fa, _fa, _vp, _vp], _i)})
+
+MAX_PRIMS = 32
+LO, HI = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+
+
+@dataclass
+class Request:
+    """kind "mc" or "dc"; n points per axis; prims float [k, 7] rows of
+    (kind 0 sphere / 1 box, centre xyz, radius | half-extents xyz)."""
+
+    kind: str
+    n: int
+    prims: np.ndarray
+    level: float = 0.0
+    method: str = "nagae"
+    rid: int = 0
+
+
+@dataclass
+class Result:
+    rid: int
+    vertices: np.ndarray
+    faces: np.ndarray
+    t_submit: float
+    t_start: float
+    t_done: float
+    slot: int = -1
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.t_submit
+
+
+def prims_buffer(prims: np.ndarray) -> np.ndarray:
+    """The device layout of iso_sdf_union_grid: [count, rows of 7 ...], padded."""
+    p = np.asarray(prims, np.float32).reshape(-1, 7)
+    if not 1 <= len(p) <= MAX_PRIMS:
+        raise ValueError(f"a request has 1 .. {MAX_PRIMS} primitives")
+    out = np.zeros(1 + 7 * MAX_PRIMS, np.float32)
+    out[0] = len(p)
+    out[1:1 + p.size] = p.ravel()
+    return out
+
+
+# Kernels of this library one request launches: marching cubes = grid evaluation
+# + mc_signs, mc_count, mc_scan, mc_emit; dual contouring = grid evaluation +
+# mc_signs, cell count + scan, intersect, solve, quad count + scan, quad emit,
+# weld (mark, insert, lookup, count, scan, write, remap).
+KERNELS_PER_REQUEST = {"mc": 5, "dc": 16}
+
+
+# ---------------------------------------------------------------------------
+# scheduling (host only)
+
+class Scheduler:
+    """FIFO admission of requests to `slots` workers under a byte budget.
+
+    need(req) is the request's worst-case device memory; a request starts when a
+    worker is free and the bytes of the running requests plus its own fit the
+    budget.  The head of the queue waits for room: later requests never pass it.
+    run(slot, req) performs the request and returns (vertices, faces)."""
+
+    def __init__(self, slots: int, budget_bytes: int, need, run):
+        if slots < 1:
+            raise ValueError("slots >= 1")
+        self.budget = int(budget_bytes)
+        self._need, self._run = need, run
+        self._queue: deque = deque()
+        self._cv = threading.Condition()
+        self._reserved = 0
+        self._closed = False
+        self.max_reserved = 0
+        self.max_running = 0
+        self._running = 0
+        self._threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(slots)]
+        for t in self._threads:
+            t.start()
+
+    def submit(self, req) -> cf.Future:
+        need = int(self._need(req))
+        if need > self.budget:
+            raise ValueError(f"request needs {need} bytes, more than the budget {self.budget}")
+        fut: cf.Future = cf.Future()
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("scheduler is closed")
+            self._queue.append((req, need, fut, time.perf_counter()))
+            self._cv.notify_all()
+        return fut
+
+    def _worker(self, slot: int) -> None:
+        while True:
+            with self._cv:
+                while True:
+                    if self._queue and self._reserved + self._queue[0][1] <= self.budget:
+                        req, need, fut, t_submit = self._queue.popleft()
+                        self._reserved += need
+                        self._running += 1
+                        self.max_reserved = max(self.max_reserved, self._reserved)
+                        self.max_running = max(self.max_running, self._running)
+                        break
+                    if self._closed and not self._queue:
+                        return
+                    self._cv.wait()
+            t_start = time.perf_counter()
+            try:
+                v, f = self._run(slot, req)
+                fut.set_result(Result(getattr(req, "rid", 0), v, f, t_submit, t_start, time.perf_counter(), slot))
+            except BaseException as exc:  # noqa: BLE001 - the future carries it
+                fut.set_exception(exc)
+            finally:
+                with self._cv:
+                    self._reserved -= need
+                    self._running -= 1
+                    self._cv.notify_all()
+
+    def close(self) -> None:
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+
+
+# ---------------------------------------------------------------------------
+# GPU execution
+
+def _mc_caps(n: int) -> tuple[int, int]:
+    # the faces of a closed surface inside the box stay below twice the grid's
+    # face area in cells (and the output check catches the rest)
+    f = 4 * 6 * (n - 1) ** 2 + 4096
+    return f // 2 + 4096, f
+
+
+def request_bytes(req: Request) -> int:
+    """Worst-case device bytes of a request: grid values, workspace, outputs,
+    and for dual contouring its intermediate arrays (about 64 bytes per face)."""
+    from .mc import workspace_bytes
+
+    n = req.n
+    cap_v, cap_f = _mc_caps(n)
+    values = 4 * n ** 3
+    if req.kind == "mc":
+        return values + workspace_bytes((n, n, n), cap_v, cap_f) + 12 * cap_v + 12 * cap_f + 4096
+    return values + 4 * n ** 3 // 8 * 4 + 64 * cap_f + 12 * cap_v
+
+
+class _MCSlot:
+    """A slot's buffers for one grid size, and the captured graph
+    (grid evaluation + iso_mc_dense) that fills them."""
+
+    def __init__(self, n: int, method: int, level: float, prims_dev, stream, device, use_graph: bool):
+        import torch
+
+        from .mc import mc_dense_into, workspace_bytes
+
+        self.n, self.method, self.level = n, method, level
+        self.cap_v, self.cap_f = _mc_caps(n)
+        self.values = torch.empty((n, n, n), dtype=torch.float32, device=device)
+        self.vout = torch.empty((self.cap_v, 3), dtype=torch.float32, device=device)
+        self.fout = torch.empty((self.cap_f, 3), dtype=torch.int32, device=device)
+        self.ws = torch.empty(workspace_bytes((n, n, n), self.cap_v, self.cap_f), dtype=torch.uint8, device=device)
+        self.small = torch.zeros(4, dtype=torch.int64, device=device)
+        self.small_host = torch.zeros(4, dtype=torch.int64).pin_memory()
+        self.prims_dev = prims_dev
+        self.stream = stream
+        self._mc = mc_dense_into
+        self.graph = None
+        if use_graph:
+            with torch.cuda.stream(stream):
+                self._launch()  # once outside the graph: module loading, first-use set-up
+            stream.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+                self._launch()
+            self.graph = g
+
+    def _launch(self):
+        lib = _ffi.lib()
+        s = self.stream.cuda_stream
+        self.small.zero_()
+        _ffi.check(lib.iso_sdf_union_grid(C.c_void_p(self.prims_dev.data_ptr()), self.n, self.n, self.n,
+                                          _ffi.fvec3(LO), _ffi.fvec3(HI), C.c_void_p(self.values.data_ptr()),
+                                          C.c_void_p(s)))
+        _ffi.check(self._mc(self.values, LO, HI, self.level, self.method, self.vout, self.fout, self.ws,
+                            self.small, s))
+
+    def run(self):
+        """Returns (V, F, status) after the extraction; outputs stay on the device."""
+        import torch
+
+        with torch.cuda.stream(self.stream):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._launch()
+            self.small_host.copy_(self.small, non_blocking=True)
+        self.stream.synchronize()
+        h = self.small_host
+        return int(h[0]), int(h[1]), int(h[2]) & 0xFFFFFFFF
+
+
+class Server(Scheduler):
+    """Continuous-batching server of Requests on one GPU.
+
+    slots: concurrent workers (streams).  budget_bytes: device memory admitted
+    at once (request_bytes per running request).  use_graphs: marching cubes
+    replays a captured graph per slot and grid size."""
+
+    def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, device=None, use_graphs: bool = True):
+        import torch
+
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.use_graphs = use_graphs
+        self._slot_state = [dict() for _ in range(slots)]
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self._prims_dev = [torch.zeros(1 + 7 * MAX_PRIMS, dtype=torch.float32, device=self.device)
+                           for _ in range(slots)]
+        self._prims_host = [torch.zeros(1 + 7 * MAX_PRIMS, dtype=torch.float32).pin_memory() for _ in range(slots)]
+        self._lock = threading.Lock()  # graph capture is done one at a time
+        super().__init__(slots, budget_bytes, request_bytes, self._execute)
+
+    def warmup(self, sizes, method: str = "nagae", level: float = 0.0) -> None:
+        """Builds every slot's buffers and graphs for the given grid sizes up front."""
+        from .mc import method_id
+
+        for slot in range(len(self._streams)):
+            for n in sizes:
+                self._mc_slot(slot, int(n), method_id(method), float(level))
+
+    def _mc_slot(self, slot: int, n: int, method: int, level: float) -> _MCSlot:
+        key = ("mc", n, method, level)
+        st = self._slot_state[slot]
+        if key not in st:
+            with self._lock:
+                st[key] = _MCSlot(n, method, level, self._prims_dev[slot], self._streams[slot], self.device,
+                                  self.use_graphs)
+        return st[key]
+
+    def _upload_prims(self, slot: int, prims) -> None:
+        import torch
+
+        host = self._prims_host[slot]
+        host.copy_(torch.from_numpy(prims_buffer(prims)))
+        with torch.cuda.stream(self._streams[slot]):
+            self._prims_dev[slot].copy_(host, non_blocking=True)
+
+    def _execute(self, slot: int, req: Request):
+        import torch
+
+        from .mc import method_id
+
+        stream = self._streams[slot]
+        self._upload_prims(slot, req.prims)
+        if req.kind == "mc":
+            ms = self._mc_slot(slot, req.n, method_id(req.method), float(req.level))
+            V, F, status = ms.run()
+            if status == _ffi.ISO_ERR_OVERFLOW:
+                # larger than the slot's buffers: the plain path on this stream
+                with torch.cuda.stream(stream):
+                    return _solve_on_stream(req, self._prims_dev[slot], self.device)
+            if status != 0:
+                raise RuntimeError(f"isoext_gb300: device error {status} in a served request")
+            with torch.cuda.stream(stream):
+                v = ms.vout[:V].to("cpu", non_blocking=False).numpy().copy()
+                f = ms.fout[:F].to("cpu", non_blocking=False).numpy().copy()
+            return v, f
+        with torch.cuda.stream(stream):
+            return _solve_on_stream(req, self._prims_dev[slot], self.device)
+
+
+def _solve_on_stream(req: Request, prims_dev, device):
+    """The public API on the current stream: grid from the union, then
+    marching_cubes or dual_contouring; results copied to the host."""
+    import torch
+
+    from .dc import dual_contouring
+    from .grids import UniformGrid
+    from .mc import marching_cubes
+
+    n = req.n
+    grid = UniformGrid([n] * 3, LO, HI, device=device)
+    s = torch.cuda.current_stream(device).cuda_stream
+    _ffi.check(_ffi.lib().iso_sdf_union_grid(C.c_void_p(prims_dev.data_ptr()), n, n, n, _ffi.fvec3(LO),
+                                             _ffi.fvec3(HI), C.c_void_p(grid._values.data_ptr()), C.c_void_p(s)))
+    if req.kind == "mc":
+        v, f = marching_cubes(grid, req.level, req.method)
+    else:
+        v, f = dual_contouring(grid, req.level)
+    if v is None:
+        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+    return v.cpu().numpy(), f.cpu().numpy()
+
+
+def solve_plain(req: Request, device=None):
+    """The one-call-per-grid path: one request at a time on the current stream."""
+    import torch
+
+    device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    prims_dev = torch.from_numpy(prims_buffer(req.prims)).to(device)
+    return _solve_on_stream(req, prims_dev, device)
+
+
+def random_requests(count: int, seed: int, sizes=(64, 96, 128, 192, 256), mc_share: float = 0.7):
+    """The mixed stream: grid edge uniform over `sizes`, mc with probability
+    mc_share, each grid a union of 1..16 spheres / boxes of size U[0.05, 0.4]
+    centred in U[-0.5, 0.5]^3 (seeded)."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        k = int(rng.integers(1, 17))
+        prims = np.zeros((k, 7), np.float32)
+        prims[:, 0] = rng.integers(0, 2, size=k)
+        prims[:, 1:4] = rng.uniform(-0.5, 0.5, size=(k, 3))
+        size = rng.uniform(0.05, 0.4, size=(k, 1))
+        # spheres use the first size; boxes get three half-extents around it
+        prims[:, 4:7] = np.where(prims[:, :1] == 0, size, size * rng.uniform(0.5, 1.0, size=(k, 3)))
+        kind = "mc" if rng.random() < mc_share else "dc"
+        reqs.append(Request(kind, int(rng.choice(sizes)), prims, rid=i))
+    return reqs

@@ -13,7 +13,7 @@ from helpers import assert_same_mesh, grid_points, sphere
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 DENSE = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if not os.path.basename(p).startswith(("sparse", "cuboid")))
+               if not os.path.basename(p).startswith(("sparse", "cuboid", "sdf_")))
 
 
 @pytest.mark.parametrize("path", DENSE, ids=lambda p: os.path.basename(p)[:-4])

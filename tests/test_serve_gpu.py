@@ -1,0 +1,79 @@
+"""The served loop on the GPU: grid evaluation of a union matches its FP32
+formula, and every served result equals the one-call-per-grid result, bit for
+bit, whether the request ran alone or among others."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _union_np(points, prims):
+    """The union's value at float32 points [..., 3]: sphere |p - c| - r and box
+    |max(q, 0)| + min(max q, 0), q = |p - c| - h, each operation rounded to float32."""
+    f = np.float32
+    d = np.full(points.shape[:-1], np.finfo(np.float32).max, np.float32)
+    for row in prims.astype(np.float32):
+        dx, dy, dz = (points[..., k] - row[1 + k] for k in range(3))
+        if row[0] == 0:
+            dk = np.sqrt((dx * dx + dy * dy) + dz * dz) - row[4]
+        else:
+            qx, qy, qz = np.abs(dx) - row[4], np.abs(dy) - row[5], np.abs(dz) - row[6]
+            ox, oy, oz = (np.maximum(q, f(0)) for q in (qx, qy, qz))
+            dk = np.sqrt((ox * ox + oy * oy) + oz * oz) + np.minimum(np.maximum(qx, np.maximum(qy, qz)), f(0))
+        d = np.minimum(d, dk.astype(np.float32))
+    return d
+
+
+@pytest.mark.parametrize("shape", [(33, 40, 47), (64, 64, 64)])
+def test_union_grid_matches_formula(shape):
+    import ctypes as C
+
+    from isoext_gb300 import UniformGrid, _ffi
+    from isoext_gb300.serve import HI, LO, prims_buffer, random_requests
+
+    prims = random_requests(4, seed=11)[3].prims
+    grid = UniformGrid(list(shape), LO, HI)
+    dev = torch.from_numpy(prims_buffer(prims)).cuda()
+    _ffi.check(_ffi.lib().iso_sdf_union_grid(C.c_void_p(dev.data_ptr()), *shape, _ffi.fvec3(LO), _ffi.fvec3(HI),
+                                             C.c_void_p(grid._values.data_ptr()),
+                                             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    got = grid.get_values().cpu().numpy()
+    want = _union_np(grid.get_points().cpu().numpy(), prims)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def _same(a, b):
+    return a[0].shape == b[0].shape and np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_served_results_equal_plain_results():
+    from isoext_gb300.serve import Server, random_requests, solve_plain
+
+    reqs = random_requests(24, seed=5, sizes=(32, 48, 64))
+    solo = [solve_plain(r) for r in reqs]
+    srv = Server(slots=3, budget_bytes=1 << 30)
+    srv.warmup((32, 48, 64))
+    futs = [srv.submit(r) for r in reqs]
+    served = [f.result(timeout=300) for f in futs]
+    srv.close()
+    assert srv.max_running > 1  # requests were on the device together
+    for r, s, p in zip(reqs, served, solo):
+        assert s.rid == r.rid
+        assert len(p[1]) > 0
+        assert _same((s.vertices, s.faces), p), (r.rid, r.kind, r.n)
+
+
+def test_served_overflow_reruns_with_exact_sizes(monkeypatch):
+    from isoext_gb300 import serve
+
+    reqs = [r for r in serve.random_requests(8, seed=9, sizes=(48,)) if r.kind == "mc"][:2]
+    monkeypatch.setattr(serve, "_mc_caps", lambda n: (64, 64))
+    srv = serve.Server(slots=2, budget_bytes=1 << 30)
+    out = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    srv.close()
+    for r, s in zip(reqs, out):
+        assert len(s.faces) > 64
+        assert _same((s.vertices, s.faces), serve.solve_plain(r))
