@@ -42,6 +42,7 @@ WORKLOADS = {
     "dc256": dict(kind="dc", n=256, seed=7, desc="dc_dense_256_csg_seed7"),
     "serve": dict(kind="serve", count=512, seed=2026, sizes=(64, 96, 128, 192, 256), mc_share=0.7,
                   slots=8, budget_gb=40, desc="served_mixed_512req_n64-256_mc70"),
+    "grad": dict(kind="grad", n=256, batch=8, seed=5, desc="diff_mc_dc_8x256_fourier"),
 }
 METRIC = "MC/DC Gcells/s @512^3 fp32"
 
@@ -180,6 +181,8 @@ def run_ours(args, wl, rank, world) -> dict | None:
         return run_dc(args, wl, rank, world)
     if wl["kind"] == "serve":
         return run_serve(args, wl, rank)
+    if wl["kind"] == "grad":
+        return run_grad(args, wl, rank, world)
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     n = wl["n"]
@@ -296,6 +299,161 @@ def run_ours(args, wl, rank, world) -> dict | None:
 
 
 DC_KERNELS = ["mc_signs", "dc_classify", "dc_intersect", "dc_normals", "dc_solve", "dc_quads", "dc_weld"]
+
+
+def fourier_values(n: int, seed: int, dev, k: int = 32):
+    """helpers.fourier_sphere on the n^3 grid over [-1, 1]^3, evaluated on the device
+    in FP64 (same seeded parameters), rounded to FP32."""
+    import torch
+    from helpers import axis_coords
+
+    g = np.random.default_rng(seed)
+    w = torch.from_numpy(g.normal(0.0, 3.0, size=(k, 3))).to(dev)
+    a = g.normal(0.0, 0.02, size=k)
+    phi = g.uniform(0.0, 2 * np.pi, size=k)
+    ax = torch.from_numpy(axis_coords(n).astype(np.float64)).to(dev)
+    X, Y, Z = torch.meshgrid(ax, ax, ax, indexing="ij")
+    out = torch.sqrt(X * X + Y * Y + Z * Z) - 0.6
+    for i in range(k):
+        out += a[i] * torch.sin(X * w[i, 0] + Y * w[i, 1] + Z * w[i, 2] + phi[i])
+    return out.float().contiguous()
+
+
+GRAD_KERNELS = ["mc_signs", "mc_count", "mc_scan", "mc_emit", "mc_backward", "dc_classify", "dc_intersect",
+                "dc_solve", "dc_quads", "dc_weld", "dc_backward"]
+
+
+def run_grad(args, wl, rank, world) -> dict | None:
+    """One step: for each of the batch's grids, differentiable marching cubes and
+    dual contouring, loss = mean squared distance of each mesh's vertices to the
+    unit sphere, backward to the grid values (hand-written backward kernels)."""
+    import torch
+
+    from isoext_gb300 import _ffi, diff
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n, B = wl["n"], wl["batch"]
+    lo, hi = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+    xs = [fourier_values(n, wl["seed"] + i, dev).requires_grad_(True) for i in range(B)]
+    lib = _ffi.lib()
+    stream = torch.cuda.current_stream(dev)
+    nverts = []
+
+    def loss_of(v):
+        return ((v.norm(dim=-1) - 1.0) ** 2).mean()
+
+    def step():
+        nverts.clear()
+        for x in xs:
+            x.grad = None
+            vm, _ = diff.marching_cubes(x, lo, hi)
+            vd, _ = diff.dual_contouring(x, lo, hi)
+            (loss_of(vm) + loss_of(vd)).backward()
+            nverts.append((len(vm), len(vd)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        t_end = time.perf_counter() + 0.6
+        while time.perf_counter() < t_end:
+            step()
+        torch.cuda.synchronize()
+        lib.iso_profile_reset()
+        lib.iso_profile_enable(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    kt = {k: _ffi.profile_read(k) for k in GRAD_KERNELS}
+    kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
+    launches = sum(c for c, _ in kt.values())
+    # e2e: grids from pinned host memory, gradients back to the host
+    hosts = [x.detach().cpu().pin_memory() for x in xs]
+    outs = [torch.empty_like(h).pin_memory() for h in hosts]
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for x, h in zip(xs, hosts):
+            with torch.no_grad():
+                x.copy_(h, non_blocking=True)
+        step()
+        for x, o in zip(xs, outs):
+            o.copy_(x.grad, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e_t)
+    if rank != 0:
+        return None
+    cells = B * (n - 1) ** 3
+    pk = peaks()
+    top = "mc_backward" if "mc_backward" in kavg else None
+    V = sum(a for a, _ in nverts) // B
+    bw_bytes = V * (8 + 12 + 8 + 8)  # edge key, vertex gradient, two endpoint values (read) + two atomics
+    roof = None
+    if top:
+        ach = bw_bytes / (kavg[top] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / pk["hbm_gbs"], 4), "peak_source": pk["source"], "algorithmic_bytes": bw_bytes,
+                "kernel_ms": round(kavg[top], 4), "traffic": profiled_traffic(wl["desc"], top)}
+    out = {
+        "metric": "differentiable MC+DC Gcells/s (forward + backward)", "value": round(cells / (ms * 1e-3) / 1e9, 3),
+        "unit": "Gcells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: |p| - 0.6 + 32 seeded Fourier features on [-1,1]^3",
+        "config": {"workload": wl["desc"], "batch": B, "grid": [n, n, n], "cells_per_step": cells,
+                   "loss": "mean (|v| - 1)^2 per mesh, MC + DC", "vertices_mc_dc": nverts[0],
+                   "l2": "each grid 67 MB < L2; 8 grids 537 MB > 129 MB L2, visited in turn"},
+        "e2e": {"value": round(cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s", "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": B * 4 * n ** 3, "d2h_bytes_per_step": B * 4 * n ** 3},
+        "roofline": roof,
+        "kernel_ms": {k: round(v_, 4) for k, v_ in kavg.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_grad(wl)
+    return out
+
+
+def cpu_baseline_grad(wl) -> dict:
+    """The FP64 autograd restatement (tests/grad_ref.py) of the same forward and
+    backward on a 64^3 sample of the first grid, on the host's threads."""
+    import torch
+    from grad_ref import dc_crossed, dc_duals, mc_vertices, sphere_loss
+    from helpers import axis_coords, fourier_sphere, grid_points
+
+    from oracle import Oracle
+
+    m = 64
+    ax = axis_coords(wl["n"])
+    lo, hi = (float(ax[96]),) * 3, (float(ax[96 + m - 1]),) * 3
+    vals = fourier_sphere(grid_points((m, m, m), lo, hi), wl["seed"])
+    ora = Oracle()
+    t0 = time.perf_counter()
+    _, _, e = ora.mc_dense(vals, lo, hi)
+    its = ora.intersection_dense(vals, lo, hi)
+    a, b = e[:, 0].astype(np.int64), e[:, 1].astype(np.int64)
+    low, d = np.minimum(a, b), np.abs(a - b)
+    edges = torch.from_numpy(3 * low + np.select([d == m * m, d == m], [0, 1], 2))
+    cells = torch.from_numpy(its["cell_indices"].astype(np.int64))
+    x = torch.from_numpy(vals).double().requires_grad_(True)
+    crossed = dc_crossed(x, cells)
+    loss = sphere_loss(mc_vertices(x, edges, lo, hi)) + sphere_loss(dc_duals(x, cells, crossed, lo, hi))
+    loss.backward()
+    sec = time.perf_counter() - t0
+    c = (m - 1) ** 3
+    return {"value": round(c / sec / 1e9, 6), "unit": "Gcells/s", "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"one {m}^3 crop of the first grid: oracle C port forward (topology) + FP64 torch "
+                      f"restatement forward and autograd backward, {sec:.2f} s; isoext has no backward"}
 
 
 def _digest(v, f) -> str:

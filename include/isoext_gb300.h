@@ -146,6 +146,10 @@ int iso_dc_weld_count(const float *dual, long long A, const int *tri, long long 
                       size_t ws_bytes, long long *counts, int *status, void *stream);
 int iso_dc_weld_write(const float *dual, long long A, const int *tri, long long ntri, void *ws,
                       float *vout, int *fout, void *stream);
+/* The same, and vertex_source[i] <- the dual vertex (active cell) vertex i came
+ * from (for the backward pass). */
+int iso_dc_weld_write_src(const float *dual, long long A, const int *tri, long long ntri, void *ws,
+                          float *vout, int *fout, int *vertex_source, void *stream);
 
 /* ---- sparse grids -----------------------------------------------------------
  * Replaces isoext's SparseGrid paths (src/grid/sparse.cu:9-246 with
@@ -197,6 +201,33 @@ int iso_sparse_filter_count(const float *vals, long long m, float level, void *b
                             void *stream);
 int iso_sparse_filter_write(const int *ids, const float *vals, long long m, float level, const void *blk,
                             int *out, void *stream);
+
+/* ---- backward passes ---------------------------------------------------------
+ * No counterpart in isoext (its extraction is not differentiable).  Gradients
+ * of vertex positions are sent to the grid values; topology has no gradient.
+ * grad_values [nx, ny, nz] is ACCUMULATED into (zero it first). */
+
+/* iso_mc_dense, and vertex_edges[i] <- 3 * (point id of vertex i's low edge
+ * endpoint) + axis (0 x, 1 y, 2 z); vertex_edges has vertex_capacity entries. */
+int iso_mc_dense_edges(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                       const float *aabb_max, float level, int method, float *vertices,
+                       long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
+                       size_t workspace_bytes, long long *counts, int *status,
+                       long long *vertex_edges, void *stream);
+/* Through the interpolation weights of each vertex (src/mc/nagae.cu:52-56). */
+int iso_mc_backward(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                    const float *aabb_max, float level, const long long *vertex_edges, long long V,
+                    const float *grad_vertices, float *grad_values, void *stream);
+/* Implicit differentiation of the QEF solve (src/dc.cu:14-99) per active cell:
+ * grad_dual [A, 3] is the gradient of the unclipped-then-clipped dual vertices
+ * (zero in clipped coordinates).  normals NULL: the normals were computed from
+ * the grid (iso_dc_intersect), and the gradient flows through them; otherwise
+ * the caller's normals [K, 3] were used, and grad_normals (optional) receives
+ * their gradient. */
+int iso_dc_backward(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                    const float *aabb_max, float level, const int *cell_ids, const int *cell_offsets,
+                    long long A, float reg, float svd_tol, const float *normals, const float *grad_dual,
+                    float *grad_values, float *grad_normals, void *stream);
 
 /* ------------------------------------------------------------------------- */
 /* Grid values of a union of spheres and boxes, for the served request stream

@@ -53,10 +53,14 @@ size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capa
     return mc_workspace_bytes(nx, ny, nz, vertex_capacity, face_capacity);
 }
 
-int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min,
-                 const float* aabb_max, float level, int method, float* vertices,
-                 long long vertex_capacity, int* faces, long long face_capacity, void* workspace,
-                 size_t workspace_bytes, long long* counts, int* status, void* stream) {
+}  // extern "C"
+
+namespace {
+
+int mc_dense_impl(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
+                  float level, int method, float* vertices, long long vertex_capacity, int* faces,
+                  long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts,
+                  int* status, long long* vertex_edges, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (!grid_ok(nx, ny, nz))
         return fail(ISO_ERR_ARG, "Number of points exceeds maximum value 2147483647 (max int)");
@@ -90,6 +94,7 @@ int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
     p.capV = vertex_capacity;
     p.capF = face_capacity;
     p.counts = counts;
+    p.vedge = vertex_edges;
     int rc = mc_launch(p, workspace, workspace_bytes, st);
     if (rc == ISO_ERR_WORKSPACE) return fail(rc, "workspace too small");
     if (rc) {
@@ -97,6 +102,28 @@ int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
         return rc;
     }
     return ISO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                 const float* aabb_max, float level, int method, float* vertices,
+                 long long vertex_capacity, int* faces, long long face_capacity, void* workspace,
+                 size_t workspace_bytes, long long* counts, int* status, void* stream) {
+    return mc_dense_impl(values, nx, ny, nz, aabb_min, aabb_max, level, method, vertices, vertex_capacity, faces,
+                         face_capacity, workspace, workspace_bytes, counts, status, nullptr, stream);
+}
+
+int iso_mc_dense_edges(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                       const float* aabb_max, float level, int method, float* vertices,
+                       long long vertex_capacity, int* faces, long long face_capacity, void* workspace,
+                       size_t workspace_bytes, long long* counts, int* status, long long* vertex_edges,
+                       void* stream) {
+    if (!vertex_edges && vertex_capacity) return fail(ISO_ERR_ARG, "vertex_edges is null");
+    return mc_dense_impl(values, nx, ny, nz, aabb_min, aabb_max, level, method, vertices, vertex_capacity, faces,
+                         face_capacity, workspace, workspace_bytes, counts, status, vertex_edges, stream);
 }
 
 }  // extern "C"

@@ -1,0 +1,221 @@
+// Dual-contouring arithmetic shared by the forward kernels (dc_dense.cu) and
+// the backward kernels (backward.cu): grid positions, cell corners, the
+// trilinear interpolant and its normal stencil, the 3x3 symmetric eigen-solve.
+// Every operation is rounded as in the reference's code (src/its.cu:170-268,
+// src/dc.cu:14-99), so a kernel that recomputes a forward quantity gets the
+// same bits.
+#pragma once
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace {
+
+struct Grid3 {
+    int nx, ny, nz;
+    float amin[3], asize[3];
+};
+
+__device__ __forceinline__ float coord(const Grid3& g, int axis, uint32_t i) {
+    const uint32_t n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    return iso::grid_coord(i, n, g.amin[axis], g.asize[axis]);
+}
+
+struct CellCorners {
+    float v[8];
+    float p[8][3];
+};
+
+__device__ __forceinline__ void load_cell(const float* vals, const Grid3& g, int cx, int cy, int cz,
+                                          CellCorners& cc) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int x = cx + (k >> 2), y = cy + ((k >> 1) & 1), z = cz + (k & 1);
+        cc.v[k] = __ldg(vals + ((long long)x * g.ny + y) * g.nz + z);
+        cc.p[k][0] = coord(g, 0, uint32_t(x));
+        cc.p[k][1] = coord(g, 1, uint32_t(y));
+        cc.p[k][2] = coord(g, 2, uint32_t(z));
+    }
+}
+
+// Trilinear interpolation at t in [0,1]^3 (src/its.cu:170-184).
+__device__ __forceinline__ float trilin(const float* cv, float tx, float ty, float tz) {
+    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
+    const float c00 = __fadd_rn(__fmul_rn(cv[0], oz), __fmul_rn(cv[1], tz));
+    const float c01 = __fadd_rn(__fmul_rn(cv[2], oz), __fmul_rn(cv[3], tz));
+    const float c10 = __fadd_rn(__fmul_rn(cv[4], oz), __fmul_rn(cv[5], tz));
+    const float c11 = __fadd_rn(__fmul_rn(cv[6], oz), __fmul_rn(cv[7], tz));
+    const float c0 = __fadd_rn(__fmul_rn(c00, oy), __fmul_rn(c01, ty));
+    const float c1 = __fadd_rn(__fmul_rn(c10, oy), __fmul_rn(c11, ty));
+    return __fadd_rn(__fmul_rn(c0, ox), __fmul_rn(c1, tx));
+}
+
+// Normal at crossing point p of a cell (src/its.cu:186-268).
+__device__ __forceinline__ void cell_normal(const CellCorners& cc, const float* p, float* n) {
+    float cmin[3], csz[3], t[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cmin[a] = cc.p[0][a];
+        csz[a] = __fsub_rn(cc.p[7][a], cc.p[0][a]);
+        t[a] = __fdiv_rn(__fsub_rn(p[a], cmin[a]), csz[a]);
+        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
+    }
+    const float eps = 0.02f;
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float tp[3] = {t[0], t[1], t[2]}, tm[3] = {t[0], t[1], t[2]};
+        tp[a] = fminf(__fadd_rn(t[a], eps), 0.99f);
+        tm[a] = fmaxf(__fsub_rn(t[a], eps), 0.01f);
+        const float fp = trilin(cc.v, tp[0], tp[1], tp[2]);
+        const float fm = trilin(cc.v, tm[0], tm[1], tm[2]);
+        d[a] = __fdiv_rn(__fsub_rn(fp, fm), __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]));
+    }
+    const float len =
+        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+    if (len > 1e-8f) {
+        n[0] = __fdiv_rn(d[0], len);
+        n[1] = __fdiv_rn(d[1], len);
+        n[2] = __fdiv_rn(d[2], len);
+    } else {
+        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
+    }
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
+// Loan, sec. 8.5), FP32.  a is destroyed; w = eigenvalues, q = eigenvectors
+// (columns).
+__device__ __forceinline__ void jacobi3f(float a[3][3], float w[3], float q[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) q[i][j] = i == j ? 1.0f : 0.0f;
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        const float off = fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]);
+        const float diag = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]);
+        if (off <= 1e-9f * diag || off == 0.0f) break;
+#pragma unroll
+        for (int pr = 0; pr < 3; ++pr) {
+            const int p = pr == 2 ? 1 : 0, r = pr == 0 ? 1 : 2;
+            const float apr = a[p][r];
+            if (apr == 0.0f) continue;
+            const float theta = (a[r][r] - a[p][p]) / (2.0f * apr);
+            const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+            const float c = rsqrtf(t * t + 1.0f), s = t * c;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float akp = a[k][p], akr = a[k][r];
+                a[k][p] = c * akp - s * akr;
+                a[k][r] = s * akp + c * akr;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float apk = a[p][k], ark = a[r][k];
+                a[p][k] = c * apk - s * ark;
+                a[r][k] = s * apk + c * ark;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float qkp = q[k][p], qkr = q[k][r];
+                q[k][p] = c * qkp - s * qkr;
+                q[k][r] = s * qkp + c * qkr;
+            }
+        }
+    }
+    w[0] = a[0][0]; w[1] = a[1][1]; w[2] = a[2][2];
+}
+
+// x += pinv(A) r with the eigen-decomposition (w, q) and the kept mask.
+__device__ __forceinline__ void apply_pinv(const float w[3], const float q[3][3], unsigned keep,
+                                           const double r[3], double x[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (!((keep >> i) & 1u)) continue;
+        const double qr = double(q[0][i]) * r[0] + double(q[1][i]) * r[1] + double(q[2][i]) * r[2];
+        const double c = qr / double(w[i]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[k] += c * double(q[k][i]);
+    }
+}
+
+// QEF of a cell: normal equations of the crossings' planes plus reg times the
+// distance to their mean point, accumulated as src/dc.cu:26-62 does (each
+// operation rounded); solved by the pseudo-inverse of the 3x3 system with the
+// threshold svd_tol * largest singular value (src/batched_la.cu:152-178), from
+// an FP32 eigen-decomposition refined once with an FP64 residual.
+struct Qef {
+    float ata[9], atb[3];  // the system (reg included)
+    float w[3], q[3][3];   // its eigenvalues and eigenvectors (columns)
+    unsigned keep;         // eigenvalues above the threshold
+    double x[3];           // the solution before clipping
+};
+
+__device__ __forceinline__ void qef_solve(const float* points, const float* normals, uint32_t K, float reg,
+                                          float svd_tol, Qef& Q) {
+    float* ata = Q.ata;
+    float* atb = Q.atb;
+    for (int i = 0; i < 9; ++i) ata[i] = 0.0f;
+    atb[0] = atb[1] = atb[2] = 0.0f;
+    float px = 0.0f, py = 0.0f, pz = 0.0f;
+    for (uint32_t k = 0; k < K; ++k) {
+        const float nx = normals[3 * k], ny = normals[3 * k + 1], nz = normals[3 * k + 2];
+        const float qx = points[3 * k], qy = points[3 * k + 1], qz = points[3 * k + 2];
+        const float d = __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
+        px = __fadd_rn(px, qx); py = __fadd_rn(py, qy); pz = __fadd_rn(pz, qz);
+        const float n3[3] = {nx, ny, nz};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) ata[3 * i + j] = __fadd_rn(ata[3 * i + j], __fmul_rn(n3[i], n3[j]));
+        atb[0] = __fadd_rn(atb[0], __fmul_rn(nx, d));
+        atb[1] = __fadd_rn(atb[1], __fmul_rn(ny, d));
+        atb[2] = __fadd_rn(atb[2], __fmul_rn(nz, d));
+    }
+    const float cnt = __uint2float_rn(K);
+    px = __fdiv_rn(px, cnt); py = __fdiv_rn(py, cnt); pz = __fdiv_rn(pz, cnt);
+    ata[0] = __fadd_rn(ata[0], reg); ata[4] = __fadd_rn(ata[4], reg); ata[8] = __fadd_rn(ata[8], reg);
+    atb[0] = __fadd_rn(atb[0], __fmul_rn(reg, px));
+    atb[1] = __fadd_rn(atb[1], __fmul_rn(reg, py));
+    atb[2] = __fadd_rn(atb[2], __fmul_rn(reg, pz));
+    // pseudo-inverse solve: singular values of the symmetric system are |w|
+    float m[3][3];
+    float* w = Q.w;
+    float(*q)[3] = Q.q;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m[i][j] = ata[3 * i + j];
+    jacobi3f(m, w, q);
+    const float smax = fmaxf(fabsf(w[0]), fmaxf(fabsf(w[1]), fabsf(w[2])));
+    const float thr = svd_tol * smax;
+    unsigned keep = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) keep |= (fabsf(w[i]) > thr ? 1u : 0u) << i;
+    Q.keep = keep;
+    double* x = Q.x;
+    x[0] = x[1] = x[2] = 0.0;
+    double r[3] = {atb[0], atb[1], atb[2]};
+    apply_pinv(w, q, keep, r, x);
+    // one refinement step with an FP64 residual (the FP32 eigenvectors leave
+    // an error of about cond(A) * eps; the residual recovers it)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        r[i] = double(atb[i]) - (double(ata[3 * i]) * x[0] + double(ata[3 * i + 1]) * x[1] +
+                                 double(ata[3 * i + 2]) * x[2]);
+    apply_pinv(w, q, keep, r, x);
+}
+
+Grid3 make_grid(int nx, int ny, int nz, const float* amin, const float* amax) {
+    Grid3 g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    for (int k = 0; k < 3; ++k) {
+        g.amin[k] = amin[k];
+        g.asize[k] = amax[k] - amin[k];
+    }
+    return g;
+}
+
+unsigned blocks_for(long long n, int b) { return unsigned((n + b - 1) / b); }
+
+}  // namespace

@@ -756,6 +756,7 @@ struct EmitArgs {
     long long capV, capF;
     unsigned nbv;  // CTAs with the vertex role; the rest emit faces
     McWs w;        // for the fix-up
+    long long* vedge;  // optional: each vertex's grid edge
 };
 
 // Vertex role: one thread per vertex entry; CTA `bi` of `nb`.
@@ -793,6 +794,7 @@ __device__ void emit_vertices(const McGrid& g, const EmitArgs& a, unsigned bi, u
         vo[0] = px;
         vo[1] = py;
         vo[2] = pz;
+        if (a.vedge) a.vedge[vi] = 3 * ia + ax;
         if (!(t >= g.tau && t <= 1.0f - g.tau) || (px == xa && py == ya && pz == za) ||
             (px == xb && py == yb && pz == zb)) {
             // a candidate for sharing its position: list it, and look for an
@@ -881,7 +883,7 @@ __device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsi
 }
 
 __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long* counts, int* status,
-                            long long capV);
+                            long long capV, long long* vedge);
 
 template <int EMIT_THREADS>
 __global__ void __launch_bounds__(EMIT_THREADS) mc_emit(const McGrid g, const EmitArgs a) {
@@ -898,7 +900,7 @@ __global__ void __launch_bounds__(EMIT_THREADS) mc_emit(const McGrid g, const Em
     if (!last) return;
     __threadfence();
     if (a.ctr[1] == 0 || (a.ctr[8] == 0 && a.ctr[9] == 0)) return;
-    fixup_block(a.w, a.vout, a.fout, a.counts, a.status, a.capV);
+    fixup_block(a.w, a.vout, a.fout, a.counts, a.status, a.capV, a.vedge);
 }
 
 // ---------------------------------------------------------------------------
@@ -954,7 +956,7 @@ __device__ uint32_t rep_of(const McWs& w, const float* vout, uint32_t v) {
 }
 
 __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long* counts, int* status,
-                            long long capV) {
+                            long long capV, long long* vedge) {
     __shared__ uint32_t sm[32];
     const long long V = counts[0], F = counts[1];
     const long long nsnap = min((long long)w.ctr[1], capV);
@@ -1009,10 +1011,14 @@ __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long
     for (long long base = 0; base < V; base += T) {
         const long long v = base + tid;
         const uint32_t u = v < V ? (w.used[v >> 5] >> (v & 31)) & 1u : 0u;
+        // edges move in place: every read of this window precedes the scan's
+        // barriers, and a vertex never moves to a higher index
+        const long long ev = (u && vedge) ? vedge[v] : 0;
         uint32_t tot;
         const uint32_t ex = block_excl(u, tot, sm);
         if (u) {
             const uint32_t j = vn + ex;
+            if (vedge) vedge[j] = ev;
             w.newidx[v] = j;
             w.vtmp[3ll * j] = vout[3 * v];
             w.vtmp[3ll * j + 1] = vout[3 * v + 1];
@@ -1089,7 +1095,7 @@ int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t 
     const long long nbv = std::max<long long>(1, std::min(want(p.capV), resident / 3));
     const long long nbf = std::max<long long>(1, std::min(want(p.capF), resident - nbv));
     EmitArgs a{p.vals, w.S, w.info, w.blk, w.foff, w.vlist, w.clist, w.ctr, w.snaps, w.small,
-               p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w};
+               p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w, p.vedge};
     {
         iso::ProfScope ps("mc_emit", st);
         mc_emit<EMIT_THREADS><<<unsigned(nbv + nbf), EMIT_THREADS, 0, st>>>(g, a);

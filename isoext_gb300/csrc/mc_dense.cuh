@@ -31,6 +31,7 @@ struct McParams {
     long long capV, capF;
     long long* counts;  // device [0] V, [1] F
     int* status;        // device status word
+    long long* vedge;   // optional [capV]: per vertex, 3 * (low endpoint's point id) + axis
 };
 
 // Threads per CTA of the emit kernel (128 or 256).

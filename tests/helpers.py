@@ -63,3 +63,17 @@ def assert_same_mesh(v, f, vo, fo, what: str = "") -> None:
     mapped = perm[f]
     bad = np.nonzero((mapped != fo).any(axis=1))[0]
     assert len(bad) == 0, f"{what}: {len(bad)} faces differ, first at {bad[:5]}"
+
+
+def fourier_sphere(points: np.ndarray, seed: int, k: int = 32) -> np.ndarray:
+    """|p| - 0.6 plus k random Fourier features a sin(w . p + phi), w ~ N(0, 3^2)
+    per axis, a ~ N(0, 0.02^2), phi ~ U[0, 2 pi] (seeded); FP64, rounded to FP32."""
+    g = np.random.default_rng(seed)
+    w = g.normal(0.0, 3.0, size=(k, 3))
+    a = g.normal(0.0, 0.02, size=k)
+    phi = g.uniform(0.0, 2 * np.pi, size=k)
+    p = np.asarray(points, np.float64)
+    out = np.sqrt((p * p).sum(-1)) - 0.6
+    for i in range(k):
+        out += a[i] * np.sin(p @ w[i] + phi[i])
+    return out.astype(np.float32)
