@@ -435,7 +435,7 @@ def cpu_baseline_grad(wl) -> dict:
 
     m = 64
     ax = axis_coords(wl["n"])
-    lo, hi = (float(ax[96]),) * 3, (float(ax[96 + m - 1]),) * 3
+    lo, hi = (float(ax[190]),) + (float(ax[96]),) * 2, (float(ax[190 + m - 1]),) + (float(ax[96 + m - 1]),) * 2
     vals = fourier_sphere(grid_points((m, m, m), lo, hi), wl["seed"])
     ora = Oracle()
     t0 = time.perf_counter()

@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 DENSE = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if not os.path.basename(p).startswith(("sparse", "cuboid")))
+               if not os.path.basename(p).startswith(("sparse", "cuboid", "sdf_")))
 
 
 def run_mc(values, level=0.0, method="nagae", lo=(-1, -1, -1), hi=(1, 1, 1)):
