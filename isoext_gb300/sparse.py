@@ -141,6 +141,92 @@ class SparseGrid(SparseGridBase):
         return [torch.arange(s, min(s + chunk, total), dtype=torch.int32, device=self.device)
                 for s in range(0, total, chunk)]
 
+    def populate(self, sdf, level: float = 0.0, mode: str = "brick", band: float | None = None,
+                 brick: int = 8, max_points: int = 1 << 23) -> None:
+        """Builds the grid's cells and values from an SDF on the device, replacing
+        both.  No counterpart in isoext: it stands in for the documented loop
+        get_potential_cell_indices -> get_points_by_cell_indices -> sdf ->
+        filter_cell_indices -> add_cells -> set_values (src/grid/sparse.cu:71-179),
+        which visits every lattice cell.
+
+        The lattice is tiled by bricks of brick^3 cells.  A brick is active when
+        |sdf(centre) - level| <= band + its half-diagonal; sdf must therefore be
+        1-Lipschitz (a distance or a lower bound of one).  band defaults to 2 h
+        (h the longest cell edge).  The SDF is evaluated once per lattice point of
+        each active brick ((brick + 1)^3 points) and gathered into the per-cell
+        [N, 8] layout; positions are the lattice's FP32 positions, the same as
+        get_points() gives.
+          mode "brick":   every cell of the active bricks;
+          mode "surface": only the cells whose 8 values straddle level, i.e. the
+                          cells the documented loop keeps.
+        sdf: callable on float32 CUDA points [..., 3] returning [...] distances."""
+        if mode not in ("brick", "surface"):
+            raise ValueError('mode must be "brick" or "surface"')
+        if brick < 1:
+            raise ValueError("brick must be positive")
+        dev = self.device
+        shape = self.shape
+        ncell = [max(n - 1, 0) for n in shape]
+        if min(ncell) < 1:
+            self._ids = torch.empty(0, dtype=torch.int32, device=dev)
+            self._values = torch.empty((0, 8), dtype=torch.float32, device=dev)
+            return
+        from .grids import grid_positions
+
+        size = [float(np.float32(b) - np.float32(a)) for a, b in zip(self.aabb_min, self.aabb_max)]
+        axes = [grid_positions(torch.arange(shape[k], device=dev), shape[k], self.aabb_min[k], size[k])
+                for k in range(3)]
+        h = [abs(size[k]) / (shape[k] - 1) for k in range(3)]
+        band = 2.0 * max(h) if band is None else float(band)
+        radius = 0.5 * brick * float(np.sqrt(sum(x * x for x in h)))
+        nb = [(ncell[k] + brick - 1) // brick for k in range(3)]
+        # 1. active bricks, a slab of x at a time
+        per_slab = nb[1] * nb[2]
+        step = max(1, (1 << 22) // max(per_slab, 1))
+        active = []
+        for x0 in range(0, nb[0], step):
+            bx = torch.arange(x0, min(x0 + step, nb[0]), device=dev)
+            b = torch.stack(torch.meshgrid(bx, torch.arange(nb[1], device=dev), torch.arange(nb[2], device=dev),
+                                           indexing="ij"), -1).reshape(-1, 3)
+            lo_pt = b * brick
+            hi_pt = torch.minimum(lo_pt + brick, torch.tensor(ncell, device=dev))
+            centre = torch.stack([0.5 * (axes[k][lo_pt[:, k]] + axes[k][hi_pt[:, k]]) for k in range(3)], -1)
+            d = sdf(centre)
+            keep = (d - level).abs() <= band + radius
+            active.append(b[keep])
+        bricks = torch.cat(active)
+        # 2. lattice values of the active bricks, gathered per cell
+        L = brick + 1
+        o = torch.arange(L, device=dev)
+        oc = torch.arange(brick, device=dev)
+        corner = [(j >> 2, (j >> 1) & 1, j & 1) for j in range(8)]
+        ids_parts, val_parts = [], []
+        chunk = max(1, max_points // (L ** 3))
+        for s in range(0, len(bricks), chunk):
+            bb = bricks[s:s + chunk]
+            pts_idx = [torch.clamp(bb[:, k, None] * brick + o, max=shape[k] - 1) for k in range(3)]  # [nb, L]
+            P = torch.stack(torch.broadcast_tensors(axes[0][pts_idx[0]][:, :, None, None],
+                                                    axes[1][pts_idx[1]][:, None, :, None],
+                                                    axes[2][pts_idx[2]][:, None, None, :]), -1)
+            vals = sdf(P).to(torch.float32)  # [nb, L, L, L]
+            cv = torch.stack([vals[:, dx:dx + brick, dy:dy + brick, dz:dz + brick] for dx, dy, dz in corner], -1)
+            cx, cy, cz = (bb[:, k, None] * brick + oc for k in range(3))  # [nb, brick]
+            ok = (cx[:, :, None, None] < ncell[0]) & (cy[:, None, :, None] < ncell[1]) & \
+                (cz[:, None, None, :] < ncell[2])
+            ids = (cx[:, :, None, None] * ncell[1] + cy[:, None, :, None]) * ncell[2] + cz[:, None, None, :]
+            ids, cv = ids[ok], cv[ok]
+            if mode == "surface":
+                below = (cv - level) < 0
+                straddle = below.any(-1) & ~below.all(-1)
+                ids, cv = ids[straddle], cv[straddle]
+            ids_parts.append(ids)
+            val_parts.append(cv)
+        ids = torch.cat(ids_parts) if ids_parts else torch.empty(0, dtype=torch.int64, device=dev)
+        vals = torch.cat(val_parts) if val_parts else torch.empty((0, 8), dtype=torch.float32, device=dev)
+        ids, order = torch.sort(ids)
+        self._ids = ids.to(torch.int32).contiguous()
+        self._values = vals[order].contiguous()
+
     def get_points_by_cell_indices(self, cell_indices: torch.Tensor) -> torch.Tensor:
         """Corner positions [M, 8, 3] of the given cell ids."""
         _check_ids(cell_indices, "cell_indices")

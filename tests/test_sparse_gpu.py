@@ -240,3 +240,58 @@ def test_sparse_empty():
     assert iso.get_intersection(g).get_points().shape == (0, 3)
     g.add_cells(torch.tensor([1, 2, 3], dtype=torch.int32, device="cuda"))  # FLT_MAX values
     assert iso.marching_cubes(g) == (None, None)
+
+
+# --- device-side population ---------------------------------------------------------
+
+def _spheres(count, seed, k=0.05):
+    from isoext_gb300 import sdf as S
+
+    rng = np.random.default_rng(seed)
+    prims = [S.TranslationOp(S.SphereSDF(float(r)), [float(x) for x in c])
+             for c, r in zip(rng.uniform(-0.7, 0.7, size=(count, 3)), rng.uniform(0.05, 0.25, size=count))]
+    return S.SmoothUnionOp(prims, k)
+
+
+def test_populate_surface_equals_the_documented_loop():
+    shape = (40, 33, 47)
+    f = _spheres(12, seed=4)
+    g1 = iso.SparseGrid(shape)
+    g1.populate(f, mode="surface", brick=4)
+    g2 = iso.SparseGrid(shape)
+    ncells = 39 * 32 * 46
+    for ids in g2.get_potential_cell_indices(5000):
+        ids = ids[ids < ncells].contiguous()
+        vals = f(g2.get_points_by_cell_indices(ids)).contiguous()
+        kept = g2.filter_cell_indices(ids, vals)
+        if kept.numel():
+            g2.add_cells(kept)
+    g2.set_values(f(g2.get_points()).contiguous())
+    assert g1.get_num_cells() > 1000
+    assert torch.equal(g1.get_cell_indices(), g2.get_cell_indices())
+    assert torch.equal(g1.get_values(), g2.get_values())
+    v1, f1 = iso.marching_cubes(g1)
+    v2, f2 = iso.marching_cubes(g2)
+    assert torch.equal(v1, v2) and torch.equal(f1, f2)
+
+
+def test_populate_brick_mode_keeps_whole_bricks_around_the_surface():
+    shape = (50, 50, 50)
+    f = _spheres(6, seed=8)
+    g = iso.SparseGrid(shape)
+    g.populate(f, mode="brick", brick=8)
+    s = iso.SparseGrid(shape)
+    s.populate(f, mode="surface", brick=8)
+    ids = g.get_cell_indices().long().cpu().numpy()
+    assert np.all(np.diff(ids) > 0)
+    assert np.isin(s.get_cell_indices().cpu().numpy(), ids).all()
+    n = 49
+    x, y, z = ids // (n * n), (ids // n) % n, ids % n
+    b = (x // 8) * 49 + (y // 8) * 7 + z // 8
+    counts = np.bincount(b)
+    full = [min(8, n - 8 * k) for k in range(7)]
+    for bid in np.nonzero(counts)[0]:
+        bx, by, bz = bid // 49, (bid // 7) % 7, bid % 7
+        assert counts[bid] == full[bx] * full[by] * full[bz]
+    # values are the SDF at the cells' corners, as set_values(sdf(get_points())) gives
+    assert torch.equal(g.get_values(), f(g.get_points()).contiguous())
