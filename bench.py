@@ -43,6 +43,8 @@ WORKLOADS = {
     "serve": dict(kind="serve", count=512, seed=2026, sizes=(64, 96, 128, 192, 256), mc_share=0.7,
                   slots=8, budget_gb=40, desc="served_mixed_512req_n64-256_mc70"),
     "grad": dict(kind="grad", n=256, batch=8, seed=5, desc="diff_mc_dc_8x256_fourier"),
+    "sparse1024": dict(kind="sparse", n=1024, brick=8, spheres=64, k=0.05, seed=3,
+                       desc="sparse_mc_1024_bricks8_smoothmin64"),
 }
 METRIC = "MC/DC Gcells/s @512^3 fp32"
 
@@ -183,6 +185,8 @@ def run_ours(args, wl, rank, world) -> dict | None:
         return run_serve(args, wl, rank)
     if wl["kind"] == "grad":
         return run_grad(args, wl, rank, world)
+    if wl["kind"] == "sparse":
+        return run_sparse(args, wl, rank, world)
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     n = wl["n"]
@@ -454,6 +458,134 @@ def cpu_baseline_grad(wl) -> dict:
     return {"value": round(c / sec / 1e9, 6), "unit": "Gcells/s", "cores": torch.get_num_threads(), "kind": "port",
             "sample": f"one {m}^3 crop of the first grid: oracle C port forward (topology) + FP64 torch "
                       f"restatement forward and autograd backward, {sec:.2f} s; isoext has no backward"}
+
+
+def smoothmin_spheres(wl):
+    """Smooth-min (k) union of seeded spheres: centres U[-0.7, 0.7]^3, radii U[0.05, 0.25]."""
+    from isoext_gb300 import sdf as S
+
+    rng = np.random.default_rng(wl["seed"])
+    c = rng.uniform(-0.7, 0.7, size=(wl["spheres"], 3))
+    r = rng.uniform(0.05, 0.25, size=wl["spheres"])
+    return S.SmoothUnionOp([S.TranslationOp(S.SphereSDF(float(ri)), [float(x) for x in ci]) for ci, ri in zip(c, r)],
+                           wl["k"])
+
+
+def run_sparse(args, wl, rank, world) -> dict | None:
+    """Sparse-grid marching cubes at n^3 virtual resolution: cells of the 8^3
+    bricks within 2 h of the surface (SparseGrid.populate on the device), then
+    K timed extractions."""
+    import torch
+
+    import isoext_gb300 as iso
+    from isoext_gb300 import _ffi
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = wl["n"]
+    f = smoothmin_spheres(wl)
+    grid = iso.SparseGrid([n] * 3, device=dev)
+    builds = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        grid.populate(f, mode="brick", brick=wl["brick"])
+        torch.cuda.synchronize()
+        builds.append(time.perf_counter() - t0)
+    N = grid.get_num_cells()
+    lib = _ffi.lib()
+    stream = torch.cuda.current_stream(dev)
+    v, fa = iso.marching_cubes(grid)
+    nv, nf = len(v), len(fa)
+    for _ in range(args.warmup):
+        iso.marching_cubes(grid)
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        t_end = time.perf_counter() + 0.6
+        while time.perf_counter() < t_end:
+            iso.marching_cubes(grid)
+        torch.cuda.synchronize()
+        lib.iso_profile_reset()
+        lib.iso_profile_enable(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            iso.marching_cubes(grid)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    kt = {k: _ffi.profile_read(k) for k in ("sparse_mc", "dc_weld")}
+    kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
+    launches = sum(c for c, _ in kt.values())
+    # e2e: ids and values from pinned host memory, the mesh back
+    ids_h = grid.get_cell_indices().cpu().pin_memory()
+    vals_h = grid.get_values().cpu().pin_memory()
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g2 = iso.SparseGrid([n] * 3, device=dev)
+        g2._ids = ids_h.to(dev, non_blocking=True)  # sorted ids, as add_cells leaves them
+        g2._values = vals_h.to(dev, non_blocking=True)
+        vv, ff = iso.marching_cubes(g2)
+        vh, fh = vv.cpu(), ff.cpu()
+        if i >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e_t)
+    if rank != 0:
+        return None
+    pk = peaks()
+    mc_bytes = N * (4 + 32) + 36 * nf  # ids and values read, the triangle soup written
+    top = "sparse_mc" if "sparse_mc" in kavg else None
+    roof = None
+    if top:
+        ach = mc_bytes / (kavg[top] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / pk["hbm_gbs"], 4), "peak_source": pk["source"], "algorithmic_bytes": mc_bytes,
+                "kernel_ms": round(kavg[top], 4), "traffic": profiled_traffic(wl["desc"], top)}
+    out = {
+        "metric": "sparse MC Gcells/s (active cells)", "value": round(N / (ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": f"synthetic: smooth-min (k={wl['k']}) of {wl['spheres']} seeded spheres on [-1,1]^3",
+        "config": {"workload": wl["desc"], "virtual_grid": [n, n, n], "active_cells": N,
+                   "occupancy": round(N / (n - 1) ** 3, 4), "brick": wl["brick"], "vertices": nv, "faces": nf,
+                   "virtual_gcells_s": round((n - 1) ** 3 / (ms * 1e-3) / 1e9, 2),
+                   "populate_s": round(min(builds), 3),
+                   "l2": f"values {N * 32 / 1e9:.2f} GB > 129 MB L2"},
+        "e2e": {"value": round(N / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s", "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": N * 36, "d2h_bytes_per_step": nv * 12 + nf * 12},
+        "roofline": roof,
+        "kernel_ms": {k: round(v_, 4) for k, v_ in kavg.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_sparse(grid, N)
+    return out
+
+
+def cpu_baseline_sparse(grid, N) -> dict:
+    """The oracle's sparse MC on a contiguous sample of the grid's cells (host threads, one slice each)."""
+    import concurrent.futures as cf
+
+    from oracle import Oracle
+
+    ora = Oracle()
+    m = min(N, 4_000_000)
+    ids = grid.get_cell_indices()[:m].cpu().numpy()
+    vals = grid.get_values()[:m].cpu().numpy()
+    threads = os.cpu_count() or 1
+    cuts = np.linspace(0, m, threads + 1).astype(int)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda i: ora.mc_sparse(ids[cuts[i]:cuts[i + 1]], vals[cuts[i]:cuts[i + 1]], grid.shape),
+                    range(threads)))
+    sec = time.perf_counter() - t0
+    return {"value": round(m / sec / 1e9, 5), "unit": "Gcells/s", "cores": threads, "kind": "port",
+            "sample": f"the first {m} active cells, {threads} slices on {threads} threads (each welded on its "
+                      f"own), oracle C port, {sec:.2f} s"}
 
 
 def _digest(v, f) -> str:
@@ -744,6 +876,8 @@ def run_reference(args, wl, rank) -> dict | None:
         return None
     from oracle import Oracle
 
+    if wl["kind"] in ("sparse", "grad", "serve"):
+        return run_reference_other(args, wl)
     n = wl["n"]
     if wl["kind"] == "dc":
         return run_reference_dc(args, wl)
@@ -769,6 +903,91 @@ def run_reference(args, wl, rank) -> dict | None:
                                    "reference's algorithm restated in C (oracle/iso_oracle.c); isoext's "
                                    "sources are not on the GPU host"},
         "e2e": {"value": val, "unit": "Gcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def _union_np(points, prims):
+    """iso_sdf_union_grid's formula on the host (FP32 operations)."""
+    f = np.float32
+    d = np.full(points.shape[:-1], np.finfo(np.float32).max, np.float32)
+    for row in prims.astype(np.float32):
+        dx, dy, dz = (points[..., k] - row[1 + k] for k in range(3))
+        if row[0] == 0:
+            dk = np.sqrt((dx * dx + dy * dy) + dz * dz) - row[4]
+        else:
+            q = [np.abs(dx) - row[4], np.abs(dy) - row[5], np.abs(dz) - row[6]]
+            o = [np.maximum(x, f(0)) for x in q]
+            dk = np.sqrt((o[0] * o[0] + o[1] * o[1]) + o[2] * o[2]) + np.minimum(np.maximum(q[0], np.maximum(q[1], q[2])), f(0))
+        d = np.minimum(d, dk.astype(np.float32))
+    return d
+
+
+def run_reference_other(args, wl) -> dict:
+    """The oracle port (the reference's algorithms on the host) on a bounded
+    sample of the sparse, grad or serve workload, all host threads."""
+    import concurrent.futures as cf
+
+    import torch
+    from helpers import grid_points
+
+    from oracle import Oracle
+
+    ora = Oracle()
+    threads = os.cpu_count() or 1
+    if wl["kind"] == "sparse":
+        import isoext_gb300 as iso
+
+        g = iso.SparseGrid([wl["n"]] * 3, device="cpu")
+        g.populate(smoothmin_spheres(wl), mode="brick", brick=wl["brick"])
+        m = min(g.get_num_cells(), 4_000_000)
+        ids, vals = g._ids[:m].numpy(), g._values[:m].numpy()
+        cuts = np.linspace(0, m, threads + 1).astype(int)
+
+        def one():
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                list(ex.map(lambda i: ora.mc_sparse(ids[cuts[i]:cuts[i + 1]], vals[cuts[i]:cuts[i + 1]], g.shape),
+                            range(threads)))
+        units, unit, metric = m / 1e9, "Gcells/s", "sparse MC Gcells/s (active cells)"
+        sample = f"the first {m} active cells of the populated grid per step, {threads} slices on {threads} threads"
+    elif wl["kind"] == "grad":
+        def one():
+            cpu_baseline_grad(wl)
+        units, unit, metric = 63 ** 3 / 1e9, "Gcells/s", "differentiable MC+DC Gcells/s (forward + backward)"
+        sample = "one 64^3 crop per step: oracle forward topology + FP64 torch forward and autograd backward"
+        threads = torch.get_num_threads()
+    else:
+        from isoext_gb300.serve import random_requests
+
+        reqs = random_requests(16, wl["seed"], tuple(wl["sizes"]), wl["mc_share"])
+        grids = {r.n: grid_points((r.n,) * 3) for r in reqs}
+        vals = [_union_np(grids[r.n], r.prims) for r in reqs]
+
+        def solve(i):
+            r = reqs[i]
+            if r.kind == "mc":
+                ora.mc_dense(vals[i])
+            else:
+                ora.dc_dense(vals[i])
+
+        def one():
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                list(ex.map(solve, range(len(reqs))))
+        units, unit, metric = len(reqs), "req/s", "served requests/s (mixed MC/DC stream)"
+        sample = f"the first {len(reqs)} requests of the stream per step, one per host thread"
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        one()
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    sec = statistics.mean(times)
+    val = round(units / sec, 6 if unit == "Gcells/s" else 1)
+    return {
+        "metric": metric, "impl": "reference", "value": val, "unit": unit, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": wl["desc"]},
+        "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 

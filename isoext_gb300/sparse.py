@@ -149,14 +149,15 @@ class SparseGrid(SparseGridBase):
         filter_cell_indices -> add_cells -> set_values (src/grid/sparse.cu:71-179),
         which visits every lattice cell.
 
-        The lattice is tiled by bricks of brick^3 cells.  A brick is active when
-        |sdf(centre) - level| <= band + its half-diagonal; sdf must therefore be
-        1-Lipschitz (a distance or a lower bound of one).  band defaults to 2 h
+        The lattice is tiled by bricks of brick^3 cells.  A brick is a candidate
+        when |sdf(centre) - level| <= band + its half-diagonal; sdf must therefore
+        be 1-Lipschitz (a distance or a lower bound of one).  band defaults to 2 h
         (h the longest cell edge).  The SDF is evaluated once per lattice point of
-        each active brick ((brick + 1)^3 points) and gathered into the per-cell
-        [N, 8] layout; positions are the lattice's FP32 positions, the same as
-        get_points() gives.
-          mode "brick":   every cell of the active bricks;
+        each candidate brick ((brick + 1)^3 points) and gathered into the
+        per-cell [N, 8] layout; positions are the lattice's FP32 positions, the
+        same as get_points() gives.
+          mode "brick":   every cell of the bricks with a lattice point where
+                          |sdf - level| < band;
           mode "surface": only the cells whose 8 values straddle level, i.e. the
                           cells the documented loop keeps.
         sdf: callable on float32 CUDA points [..., 3] returning [...] distances."""
@@ -209,6 +210,10 @@ class SparseGrid(SparseGridBase):
                                                     axes[1][pts_idx[1]][:, None, :, None],
                                                     axes[2][pts_idx[2]][:, None, None, :]), -1)
             vals = sdf(P).to(torch.float32)  # [nb, L, L, L]
+            if mode == "brick":
+                # the brick stays if one of its lattice points lies within the band
+                near = (vals - level).abs().amin(dim=(1, 2, 3)) < band
+                bb, vals = bb[near], vals[near]
             cv = torch.stack([vals[:, dx:dx + brick, dy:dy + brick, dz:dz + brick] for dx, dy, dz in corner], -1)
             cx, cy, cz = (bb[:, k, None] * brick + oc for k in range(3))  # [nb, brick]
             ok = (cx[:, :, None, None] < ncell[0]) & (cy[:, None, :, None] < ncell[1]) & \
