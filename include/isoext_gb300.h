@@ -123,6 +123,14 @@ int iso_dc_classify(const float *values, int nx, int ny, int nz, float level, vo
 int iso_dc_intersect(const float *values, int nx, int ny, int nz, const float *aabb_min,
                      const float *aabb_max, float level, void *ws, long long A, long long K,
                      float *points, float *normals, int *cell_ids, int *cell_offsets, void *stream);
+/* intersect + solve in one step for dual_contouring without a caller
+ * intersection: active cell ids [A], CSR offsets [A+1] and dual vertices [A, 3]
+ * (bit-equal to iso_dc_intersect with normals followed by iso_dc_solve); the
+ * crossing points and normals are not written. */
+int iso_dc_intersect_solve(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                           const float *aabb_max, float level, void *ws, long long A, long long K,
+                           int *cell_ids, int *cell_offsets, float reg, float svd_tol, float *dual,
+                           void *stream);
 /* Normals of existing crossings from the grid (src/its.cu:186-268). */
 int iso_dc_normals(const float *values, int nx, int ny, int nz, const float *aabb_min,
                    const float *aabb_max, const float *points, const int *cell_ids,

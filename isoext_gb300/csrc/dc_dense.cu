@@ -204,40 +204,60 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict
     const unsigned long long a0 = blk[2 * blockIdx.x] + ea, k0 = blk[2 * blockIdx.x + 1] + ek;
     actm[i] = act;
     offA[i] = uint32_t(a0);
-    if (!act || !points) return;
+    if (!act || !cell_ids) return;
+    // active cells of the word: id and the offset of their crossings (values are
+    // read by dc_points, one thread per active cell)
     unsigned long long a = a0, k = k0;
     while (act) {
         const int b = __ffs(act) - 1;
         act &= act - 1;
         const int cz = 32 * w + b;
-        const uint32_t cs = case_of(cw8, b);
-        const uint32_t est = ISO_EDGE_STATUS[cs];
-        CellCorners cc;
-        load_cell(vals, g, cx, cy, cz, cc);
         cell_ids[a] = uint32_t(((long long)cx * (g.ny - 1) + cy) * (g.nz - 1) + cz);
         cell_off[a] = uint32_t(k);
-        for (int e = 0; e < 12; ++e) {
-            if (!((est >> e) & 1u)) continue;
-            const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-            const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
-            float p[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
-            points[3 * k + 0] = p[0];
-            points[3 * k + 1] = p[1];
-            points[3 * k + 2] = p[2];
-            if (normals) {
-                float n[3];
-                cell_normal(cc, p, n);
-                normals[3 * k + 0] = n[0];
-                normals[3 * k + 1] = n[1];
-                normals[3 * k + 2] = n[2];
-            }
-            ++k;
-        }
+        k += __popc(uint32_t(ISO_EDGE_STATUS[case_of(cw8, b)]));
         ++a;
     }
     if (a == (unsigned long long)A) cell_off[A] = uint32_t(K);
+}
+
+// Crossing points (lerp with the reference's arithmetic) and optional normals of
+// each active cell's crossed edges, in edge order (src/its.cu:94-159, 186-268).
+__global__ void __launch_bounds__(128) dc_points(const float* __restrict__ vals, Grid3 g, float level,
+                                                 const uint32_t* __restrict__ cell_ids,
+                                                 const uint32_t* __restrict__ cell_off, long long A,
+                                                 float* __restrict__ points, float* __restrict__ normals) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    const uint32_t cid = cell_ids[a];
+    const int cz = int(cid % uint32_t(g.nz - 1));
+    const uint32_t rr = cid / uint32_t(g.nz - 1);
+    const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+    CellCorners cc;
+    load_cell(vals, g, cx, cy, cz, cc);
+    uint32_t cs = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
+    const uint32_t est = ISO_EDGE_STATUS[cs];
+    unsigned long long k = cell_off[a];
+    for (int e = 0; e < 12; ++e) {
+        if (!((est >> e) & 1u)) continue;
+        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
+        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
+        float p[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
+        points[3 * k + 0] = p[0];
+        points[3 * k + 1] = p[1];
+        points[3 * k + 2] = p[2];
+        if (normals) {
+            float n[3];
+            cell_normal(cc, p, n);
+            normals[3 * k + 0] = n[0];
+            normals[3 * k + 1] = n[1];
+            normals[3 * k + 2] = n[2];
+        }
+        ++k;
+    }
 }
 
 // Normals of an existing intersection from the grid (isoext computes them
@@ -260,6 +280,45 @@ __global__ void dc_normals(const float* __restrict__ vals, Grid3 g, const float*
         normals[3 * k] = n[0];
         normals[3 * k + 1] = n[1];
         normals[3 * k + 2] = n[2];
+    }
+}
+
+// Crossings, grid normals and the QEF solve of each active cell in one pass,
+// when nobody asked for the intersection: the same arithmetic as dc_points
+// followed by dc_solve, without writing points and normals.
+__global__ void __launch_bounds__(128) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
+                                                     const uint32_t* __restrict__ cell_ids, long long A, float reg,
+                                                     float svd_tol, float* __restrict__ dual) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    const uint32_t cid = cell_ids[a];
+    const int cz = int(cid % uint32_t(g.nz - 1));
+    const uint32_t rr = cid / uint32_t(g.nz - 1);
+    const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+    CellCorners cc;
+    load_cell(vals, g, cx, cy, cz, cc);
+    uint32_t cs = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
+    const uint32_t est = ISO_EDGE_STATUS[cs];
+    float pk[12][3], nk[12][3];
+    uint32_t K = 0;
+    for (int e = 0; e < 12; ++e) {
+        if (!((est >> e) & 1u)) continue;
+        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
+        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) pk[K][q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
+        cell_normal(cc, pk[K], nk[K]);
+        ++K;
+    }
+    Qef Q;
+    qef_solve(&pk[0][0], &nk[0][0], K, reg, svd_tol, Q);
+    const int ci[3] = {cx, cy, cz};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float lo = coord(g, q, uint32_t(ci[q])), hi = coord(g, q, uint32_t(ci[q] + 1));
+        dual[3 * a + q] = fminf(fmaxf(float(Q.x[q]), lo), hi);
     }
 }
 
@@ -602,6 +661,32 @@ int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* a
         values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, points, normals,
         reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
     if (A == 0 && cell_offsets) cudaMemsetAsync(cell_offsets, 0, 4, st);
+    if (A > 0 && points)
+        dc_points<<<blocks_for(A, 128), 128, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids),
+                                                      reinterpret_cast<uint32_t*>(cell_offsets), A, points,
+                                                      normals);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+// Active cells, their crossing offsets and the dual vertices, without writing
+// crossing points or normals (dual_contouring without a caller intersection).
+int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const float* aabb_min,
+                           const float* aabb_max, float level, void* ws, long long A, long long K,
+                           int* cell_ids, int* cell_offsets, float reg, float svd_tol, float* dual, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (nx < 2 || ny < 2 || nz < 2 || A <= 0) return 0;
+    if (!cell_ids || !cell_offsets || !dual) return ISO_ERR_ARG;
+    DcWs w = carve(ws, nx, ny, nz);
+    Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
+    {
+        iso::ProfScope ps("dc_intersect", st);
+        dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
+            values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr,
+            reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
+    }
+    iso::ProfScope ps("dc_solve", st);
+    dc_cell_solve<<<blocks_for(A, 128), 128, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
+                                                      reg, svd_tol, dual);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 

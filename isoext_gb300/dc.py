@@ -28,6 +28,8 @@ _ffi.register({
     "iso_dc_weld_workspace_size": ([_ll], _sz),
     "iso_dc_weld_count": ([_vp, _ll, _vp, _ll, _vp, _sz, _vp, _vp, _vp], _i),
     "iso_dc_weld_write": ([_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp], _i),
+    "iso_dc_weld_write_src": ([_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp], _i),
+    "iso_dc_intersect_solve": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _ll, _vp, _vp, _f, _f, _vp, _vp], _i),
 })
 
 
@@ -123,12 +125,24 @@ def _dc_uniform(grid: UniformGrid, level, its: Intersection | None, reg, svd_tol
     amin, amax = _ffi.fvec3(grid.aabb_min), _ffi.fvec3(grid.aabb_max)
     st = _stream(dev)
     if its is None:
-        its, ws = _intersect_uniform(grid, level, True)
+        # the quad count needs only the sign bitmap: it is read with (A, K); the
+        # crossings stay in registers (iso_dc_intersect_solve)
+        ws, (A, K, Q) = _classify_quads(grid, level)
+        if A == 0 or Q == 0:
+            return None, None
+        cells = torch.empty(A, dtype=torch.int32, device=dev)
+        offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
+        dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
+        _ffi.check(lib.iso_dc_intersect_solve(_p(grid._values), nx, ny, nz, amin, amax, float(level), _p(ws), A, K,
+                                              _p(cells), _p(offs), float(reg), float(svd_tol), _p(dual), st))
+        tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
+        _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
+        return weld_dual(lib, dev, dual, A, tri, st)
     else:
         if its._sparse is not None or its._grid_key[:3] != _grid_key(grid)[:3]:
             raise RuntimeError("intersection was computed for a different grid")
         # the quads follow the intersection's crossings, i.e. its level
-        ws, _, _ = _classify(grid, its._level)
+        ws, (_, _, Q) = _classify_quads(grid, its._level)
         _ffi.check(lib.iso_dc_cells(_p(grid._values), nx, ny, nz, its._level, _p(ws), st))
     A = int(its._cells.numel())
     normals = its._normals
@@ -136,39 +150,66 @@ def _dc_uniform(grid: UniformGrid, level, its: Intersection | None, reg, svd_tol
         normals = torch.empty_like(its._points)
         _ffi.check(lib.iso_dc_normals(_p(grid._values), nx, ny, nz, amin, amax, _p(its._points),
                                       _p(its._cells), _p(its._offsets), A, _p(normals), st))
-    if A == 0:
+    if A == 0 or Q == 0:
         return None, None
     dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
     _ffi.check(lib.iso_dc_solve(nx, ny, nz, amin, amax, _p(its._points), _p(normals), _p(its._cells),
                                 _p(its._offsets), A, float(reg), float(svd_tol), _p(dual), st))
-    return _quads_and_weld(lib, dev, grid.shape, ws, dual, A, st)
-
-
-def _quads_and_weld(lib, dev, shape, ws, dual, A, st):
-    nx, ny, nz = shape
-    counts = torch.zeros(4, dtype=torch.int64, device=dev)
-    _ffi.check(lib.iso_dc_quads_count(nx, ny, nz, _p(ws), _p(counts), st))
-    Q = int(counts[0].item())
-    if Q == 0:
-        return None, None
     tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
     _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
     return weld_dual(lib, dev, dual, A, tri, st)
 
 
-def weld_dual(lib, dev, dual, A, tri, st):
+def _classify_quads(grid: UniformGrid, level: float):
+    """Workspace after classify + quad count, and (A, K, Q) in one synchronisation."""
+    lib = _ffi.lib()
+    dev = grid._values.device
+    nx, ny, nz = grid.shape
+    ws = torch.empty(int(lib.iso_dc_workspace_size(nx, ny, nz)), dtype=torch.uint8, device=dev)
+    counts = torch.zeros(4, dtype=torch.int64, device=dev)
+    st = _stream(dev)
+    _ffi.check(lib.iso_dc_classify(_p(grid._values), nx, ny, nz, float(level), _p(ws), ws.numel(),
+                                   _p(counts), st))
+    _ffi.check(lib.iso_dc_quads_count(nx, ny, nz, _p(ws), C.c_void_p(counts.data_ptr() + 16), st))
+    A, K, Q, _ = (int(x) for x in counts.cpu())
+    return ws, (A, K, Q)
+
+
+def _intersect_from(grid: UniformGrid, level: float, compute_normals: bool, ws, A: int, K: int) -> Intersection:
+    lib = _ffi.lib()
+    dev = grid._values.device
+    nx, ny, nz = grid.shape
+    points = torch.empty((K, 3), dtype=torch.float32, device=dev)
+    normals = torch.empty((K, 3), dtype=torch.float32, device=dev) if compute_normals else None
+    cells = torch.empty(A, dtype=torch.int32, device=dev)
+    offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
+    _ffi.check(lib.iso_dc_intersect(_p(grid._values), nx, ny, nz, _ffi.fvec3(grid.aabb_min),
+                                    _ffi.fvec3(grid.aabb_max), float(level), _p(ws), A, K, _p(points),
+                                    _p(normals), _p(cells), _p(offs), _stream(dev)))
+    return Intersection(points, normals, cells, offs, level, _grid_key(grid))
+
+
+def weld_dual(lib, dev, dual, A, tri, st, src=None):
+    """Merge the dual vertices faces use by exact position (isoext's sorted weld,
+    src/utils.cu:32-59).  Both steps run before the one synchronisation that reads
+    V: the vertex buffer is sized A (V <= A) and trimmed after.  src (optional,
+    int32 [A]) receives each vertex's dual vertex."""
     wws = torch.empty(int(lib.iso_dc_weld_workspace_size(A)), dtype=torch.uint8, device=dev)
     small = torch.zeros(4, dtype=torch.int64, device=dev)
+    vout = torch.empty((A, 3), dtype=torch.float32, device=dev)
+    fout = torch.empty((tri.numel() // 3, 3), dtype=torch.int32, device=dev)
     _ffi.check(lib.iso_dc_weld_count(_p(dual), A, _p(tri), tri.numel(), _p(wws), wws.numel(), _p(small),
                                      C.c_void_p(small.data_ptr() + 16), st))
+    _ffi.check(lib.iso_dc_weld_write_src(_p(dual), A, _p(tri), tri.numel(), _p(wws), _p(vout), _p(fout), _p(src),
+                                         st))
     host = small.cpu()
     V, status = int(host[0]), int(host[2] & 0xffffffff)
     if status:
         raise RuntimeError(f"isoext_gb300: device error {status} in dual_contouring weld")
-    vout = torch.empty((V, 3), dtype=torch.float32, device=dev)
-    fout = torch.empty((tri.numel() // 3, 3), dtype=torch.int32, device=dev)
-    _ffi.check(lib.iso_dc_weld_write(_p(dual), A, _p(tri), tri.numel(), _p(wws), _p(vout), _p(fout), st))
-    return vout, fout
+    v = vout[:V]
+    if A > 2 * V + 65536:
+        v = v.clone()
+    return v, fout
 
 
 def dual_contouring(grid, level: float = 0.0, intersection: Intersection | None = None,

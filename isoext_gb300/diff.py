@@ -37,7 +37,6 @@ _ffi.register({
     "iso_mc_dense_edges": ([_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp, C.c_size_t, _vp, _vp, _vp,
                             _vp], _i),
     "iso_mc_backward": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _vp, _vp, _vp], _i),
-    "iso_dc_weld_write_src": ([_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp], _i),
     "iso_dc_backward": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _vp, _ll, _f, _f, _vp, _vp, _vp, _vp, _vp], _i),
 })
 
@@ -147,51 +146,40 @@ def marching_cubes(values: torch.Tensor, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(
 # ---------------------------------------------------------------------------
 # dual contouring
 
+class _Values:
+    """The attributes of a UniformGrid the dense DC steps read, over a values tensor."""
+
+    def __init__(self, values, amin, amax):
+        self._values = values
+        self.shape = list(values.shape)
+        self.aabb_min, self.aabb_max = list(amin), list(amax)
+
+
 def _dc_forward(values: torch.Tensor, amin, amax, level: float, reg: float, svd_tol: float):
     """(vertices, faces, cells, offsets, source): cells / offsets are the active
     cells and their crossings' CSR ranges; source[i] = active cell of vertex i."""
+    from . import dc
+
     lib = _ffi.lib()
     dev = values.device
     nx, ny, nz = values.shape
     st = _stream(dev)
-    fa, fb = _ffi.fvec3(amin), _ffi.fvec3(amax)
     empty = (torch.zeros((0, 3), dtype=torch.float32, device=dev), torch.zeros((0, 3), dtype=torch.int32, device=dev))
-    ws = torch.empty(int(lib.iso_dc_workspace_size(nx, ny, nz)), dtype=torch.uint8, device=dev)
-    counts = torch.zeros(2, dtype=torch.int64, device=dev)
-    _ffi.check(lib.iso_dc_classify(_p(values), nx, ny, nz, float(level), _p(ws), ws.numel(), _p(counts), st))
-    A, K = (int(x) for x in counts.cpu())
-    if A == 0:
+    g = _Values(values, amin, amax)
+    ws, (A, K, Q) = dc._classify_quads(g, level)
+    if A == 0 or Q == 0:
         return (*empty, None, None, None)
-    points = torch.empty((K, 3), dtype=torch.float32, device=dev)
-    normals = torch.empty((K, 3), dtype=torch.float32, device=dev)
     cells = torch.empty(A, dtype=torch.int32, device=dev)
     offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
-    _ffi.check(lib.iso_dc_intersect(_p(values), nx, ny, nz, fa, fb, float(level), _p(ws), A, K, _p(points),
-                                    _p(normals), _p(cells), _p(offs), st))
     dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
-    _ffi.check(lib.iso_dc_solve(nx, ny, nz, fa, fb, _p(points), _p(normals), _p(cells), _p(offs), A, float(reg),
-                                float(svd_tol), _p(dual), st))
-    qc = torch.zeros(4, dtype=torch.int64, device=dev)
-    _ffi.check(lib.iso_dc_quads_count(nx, ny, nz, _p(ws), _p(qc), st))
-    Q = int(qc[0].item())
-    if Q == 0:
-        return (*empty, None, None, None)
+    _ffi.check(lib.iso_dc_intersect_solve(_p(values), nx, ny, nz, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level),
+                                          _p(ws), A, K, _p(cells), _p(offs), float(reg), float(svd_tol), _p(dual),
+                                          st))
     tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
     _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
-    wws = torch.empty(int(lib.iso_dc_weld_workspace_size(A)), dtype=torch.uint8, device=dev)
-    small = torch.zeros(4, dtype=torch.int64, device=dev)
-    _ffi.check(lib.iso_dc_weld_count(_p(dual), A, _p(tri), tri.numel(), _p(wws), wws.numel(), _p(small),
-                                     C.c_void_p(small.data_ptr() + 16), st))
-    h = small.cpu()
-    V, status = int(h[0]), int(h[2] & 0xFFFFFFFF)
-    if status:
-        raise RuntimeError(f"isoext_gb300: device error {status} in dual_contouring weld")
-    vout = torch.empty((V, 3), dtype=torch.float32, device=dev)
-    fout = torch.empty((tri.numel() // 3, 3), dtype=torch.int32, device=dev)
-    src = torch.empty(V, dtype=torch.int32, device=dev)
-    _ffi.check(lib.iso_dc_weld_write_src(_p(dual), A, _p(tri), tri.numel(), _p(wws), _p(vout), _p(fout), _p(src),
-                                         st))
-    return vout, fout, cells, offs, src
+    src = torch.empty(A, dtype=torch.int32, device=dev)
+    v, f = dc.weld_dual(lib, dev, dual, A, tri, st, src=src)
+    return v, f, cells, offs, src[:len(v)]
 
 
 class _DualContouring(torch.autograd.Function):

@@ -186,3 +186,15 @@ def test_intersection_set_normals_checks():
         its.set_normals(torch.zeros((3, 3)))
     with pytest.raises(RuntimeError, match="different shapes"):
         its.set_normals(torch.zeros((3, 3), device="cuda"))
+
+
+@pytest.mark.parametrize("values", ["sphere", "noise"])
+def test_dc_one_pass_solve_equals_intersection_then_solve(values):
+    """dual_contouring(grid) solves each cell without writing the intersection;
+    it must give the bits of get_intersection(normals) -> dual_contouring(its)."""
+    vals = sphere((41, 37, 45), 0.55) if values == "sphere" else noise((24, 30, 33), seed=4)
+    g = make_grid(vals)
+    v0, f0 = iso.dual_contouring(g)
+    its = iso.get_intersection(g, compute_normals=True)
+    v1, f1 = iso.dual_contouring(g, intersection=its)
+    assert torch.equal(v0, v1) and torch.equal(f0, f1)
