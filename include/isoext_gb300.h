@@ -53,15 +53,6 @@ int iso_abi_version(void);
 int iso_mc_set_config(int threads);
 int iso_mc_get_config(int *threads);
 
-/* Slabs of iso_mc_dense's pipeline (1 .. 8; default 4; process-wide).  Grids
- * of more than 2^20 point words are cut into that many x slabs (at most one per
- * 2^20 words): the sign pass of each slab runs on a low-priority stream while
- * count, scan and emit of the slabs before it run on a high-priority one, both
- * joined back to the caller's stream.  1 = one stream.  The result does not
- * depend on it.  No counterpart in the reference. */
-int iso_mc_set_slabs(int slabs);
-int iso_mc_get_slabs(int *slabs);
-
 /* Kernel timing for benchmarks (no counterpart in the reference).  While
  * enabled, each kernel the library launches is bracketed by CUDA events on its
  * stream.  iso_profile_read synchronises on the recorded events and returns the

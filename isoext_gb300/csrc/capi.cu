@@ -46,16 +46,6 @@ int iso_mc_get_config(int* threads) {
     return ISO_OK;
 }
 
-int iso_mc_set_slabs(int slabs) {
-    if (mc_set_slabs(slabs)) return fail(ISO_ERR_ARG, "iso_mc_set_slabs: slabs must be 1 .. 8");
-    return ISO_OK;
-}
-
-int iso_mc_get_slabs(int* slabs) {
-    if (slabs) *slabs = mc_get_slabs();
-    return ISO_OK;
-}
-
 size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
                                    long long face_capacity) {
     if (!grid_ok(nx, ny, nz) || nx < 2 || ny < 2 || nz < 2) return 256;

@@ -96,7 +96,6 @@ struct McWs {
     unsigned long long* ctr;    // [0] list size [1] snaps [2] barrier count [3] barrier gen [4] V' [5] F'
                                 // [6] unused [7] scan ticket [8] merges [9] small hash full
                                 // [10] cell entries [11] emit CTAs done
-                                // [16 + 2i], [17 + 2i]: vertex / cell entries after slab i
     unsigned long long* state;  // look-back state per segment (follows ctr; zeroed with it)
     uint32_t* small;            // SMALL_HC entries after the states (zeroed with them)
     float* gc;                  // grid coordinates [nx + ny + nz] (x, then y, then z)
@@ -112,8 +111,7 @@ struct McWs {
 };
 
 constexpr uint32_t SMALL_HC = 1u << 15;  // merge-detection hash of emit (entries: vertex + 1, 0 = empty)
-constexpr int NCTR = 32;
-constexpr int MAX_SLABS = 8;  // pipelined slabs per call (ends at ctr[16 ..])
+constexpr int NCTR = 16;
 constexpr int CNT_THREADS = 256;             // count kernel CTA size
 constexpr int WPT = 4;                       // point words per count thread
 constexpr uint32_t SEG = CNT_THREADS * WPT;  // words per segment (one scan entry)
@@ -388,9 +386,8 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                                                         unsigned long long* __restrict__ vlist,
                                                         unsigned long long* __restrict__ clist,
                                                         uint32_t* __restrict__ foff, unsigned long long* ctr,
-                                                        float* __restrict__ gc, const uint32_t seg0,
-                                                        const uint32_t seg_end, const long long capV,
-                                                        const long long capF) {
+                                                        float* __restrict__ gc, const uint32_t nseg,
+                                                        const long long capV, const long long capF) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
     __shared__ uint32_t wcell[CNT_THREADS / 32];
@@ -401,13 +398,13 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
-    if (seg0 == 0 && gid < ncoord) {
+    if (gid < ncoord) {
         if (gid < uint32_t(g.nx)) gc[gid] = iso::grid_coord(gid, g.nx, amin0, size0);
         else if (gid < uint32_t(g.nx + g.ny)) gc[gid] = iso::grid_coord(gid - g.nx, g.ny, amin1, size1);
         else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2);
     }
-    const uint32_t seg = seg0 + blockIdx.x;
-    if (seg >= seg_end) return;  // CTAs past the segments only write coordinates
+    const uint32_t seg = blockIdx.x;
+    if (seg >= nseg) return;  // CTAs past the segments only write coordinates
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW), syw = uint32_t(g.NW);
     const bool vec = (g.NW & 3) == 0;  // rows start on 16-byte boundaries
@@ -681,15 +678,9 @@ constexpr int SCAN_PER = 1;
 __global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk, uint32_t nseg,
                                                         unsigned long long* ctr, unsigned long long* state,
                                                         long long* counts, int* status, long long capV,
-                                                        long long capF, int slab) {
+                                                        long long capF) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t chunk_s;
-    // the entry lists' sizes once slab's segments are counted (the count of the
-    // slab ran before this launch on the stream)
-    if (slab >= 0 && blockIdx.x == 0 && threadIdx.x == 0) {
-        ctr[16 + 2 * slab] = ctr[0];
-        ctr[17 + 2 * slab] = ctr[10];
-    }
     __shared__ unsigned long long pre_s[2];
     if (threadIdx.x == 0) chunk_s = uint32_t(atomicAdd(ctr + 7, 1ull));
     __syncthreads();
@@ -766,8 +757,6 @@ struct EmitArgs {
     unsigned nbv;  // CTAs with the vertex role; the rest emit faces
     McWs w;        // for the fix-up
     long long* vedge;  // optional: each vertex's grid edge
-    int slab;      // -1: the whole grid in one launch; else the slab's entries (ctr[16 ..])
-    unsigned long long ctas_total;  // emit CTAs of all launches of the call
 };
 
 // Vertex role: one thread per vertex entry; CTA `bi` of `nb`.
@@ -781,17 +770,14 @@ __device__ void emit_vertices(const McGrid& g, const EmitArgs& a, unsigned bi, u
     uint32_t* small = a.small;
     float* vout = a.vout;
     const long long capV = a.capV;
-    const unsigned long long lo = a.slab > 0 ? ctr[16 + 2 * (a.slab - 1)] : 0ull;
-    const unsigned long long hi = a.slab >= 0 ? ctr[16 + 2 * a.slab] : ctr[0];
-    const unsigned long long n = min(hi, (unsigned long long)capV);
+    const unsigned long long n = min(ctr[0], (unsigned long long)capV);
     const long long sxv = (long long)g.ny * g.nz;
-    for (unsigned long long i = lo + (unsigned long long)bi * EMIT_THREADS + threadIdx.x; i < n;
+    for (unsigned long long i = (unsigned long long)bi * EMIT_THREADS + threadIdx.x; i < n;
          i += (unsigned long long)nb * EMIT_THREADS) {
         const unsigned long long e = vlist[i];
         const uint32_t pw = uint32_t(e);
         const int ax = int((e >> 32) & 3u), b = int((e >> 34) & 31u);
         const uint32_t vi = uint32_t(blk[2 * seg_of(pw)]) + uint32_t((e >> 39) & 0xfffffu);
-        if ((long long)vi >= capV) continue;  // over capacity: the scan reports it
         int x, y, w;
         word_xyw(g, pw, x, y, w);
         const int z = 32 * w + b;
@@ -849,12 +835,10 @@ __device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsi
         est[i] = ISO_EDGE_STATUS[i];
     }
     __syncthreads();
-    const unsigned long long lo = a.slab > 0 ? a.ctr[17 + 2 * (a.slab - 1)] : 0ull;
-    const unsigned long long hi = a.slab >= 0 ? a.ctr[17 + 2 * a.slab] : a.ctr[10];
-    const unsigned long long n = min(hi, (unsigned long long)a.capF);
+    const unsigned long long n = min(a.ctr[10], (unsigned long long)a.capF);
     const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW);
     const int tid = threadIdx.x;
-    for (unsigned long long i = lo + (unsigned long long)bi * EMIT_THREADS + tid; i < n;
+    for (unsigned long long i = (unsigned long long)bi * EMIT_THREADS + tid; i < n;
          i += (unsigned long long)nb * EMIT_THREADS) {
         const unsigned long long e = clist[i];
         const uint32_t pw = uint32_t(e);
@@ -889,7 +873,6 @@ __device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsi
         }
         unsigned long long pk = tpk[cs];
         const int ntc = int(pk >> 60);
-        if ((long long)(fo + ntc) > a.capF) continue;  // over capacity: the scan reports it
         int32_t* f3 = fout + 3 * fo;
         for (int k = 0; k < ntc; ++k, pk >>= 12, f3 += 3) {
             f3[0] = int32_t(vid[pk & 15u][tid]);
@@ -905,21 +888,18 @@ __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long
 template <int EMIT_THREADS>
 __global__ void __launch_bounds__(EMIT_THREADS) mc_emit(const McGrid g, const EmitArgs a) {
     __shared__ int last;
-    // in one launch the sizes are final; per slab they are not known yet and the
-    // writes are checked one by one
-    if (a.slab < 0 && (a.counts[0] > a.capV || a.counts[1] > a.capF || a.counts[0] > 0x7fffffffll)) return;
+    if (a.counts[0] > a.capV || a.counts[1] > a.capF || a.counts[0] > 0x7fffffffll) return;
     if (blockIdx.x < a.nbv) emit_vertices<EMIT_THREADS>(g, a, blockIdx.x, a.nbv);
     else emit_faces<EMIT_THREADS>(g, a, blockIdx.x - a.nbv, gridDim.x - a.nbv);
     // the last CTA to finish sees every vertex and face; it does the fix-up if
     // the emit found coinciding positions
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(a.ctr + 11, 1ull) == a.ctas_total - 1;
+    if (threadIdx.x == 0) last = atomicAdd(a.ctr + 11, 1ull) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
     if (a.ctr[1] == 0 || (a.ctr[8] == 0 && a.ctr[9] == 0)) return;
-    if (a.counts[0] > a.capV || a.counts[1] > a.capF || a.counts[0] > 0x7fffffffll) return;
     fixup_block(a.w, a.vout, a.fout, a.counts, a.status, a.capV, a.vedge);
 }
 
@@ -1064,13 +1044,12 @@ constexpr int SIGN_UNROLL = 16;
 // Bit z % 32 of word [(x * ny + y) * NWg + z / 32] is (v - level < 0).  One warp
 // per grid row, all of the row's loads in flight before the ballots; lane w
 // keeps word w so each 32 words leave in one store.
-__global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__ vals, long long row0,
-                                                       long long row1, int nz, float level,
-                                                       uint32_t* __restrict__ out) {
+__global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__ vals, long long rows,
+                                                       int nz, float level, uint32_t* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int NWg = (nz + 31) / 32;
     const long long warps = (long long)gridDim.x * (SIGN_BLOCK / 32);
-    for (long long row = row0 + (long long)blockIdx.x * (SIGN_BLOCK / 32) + (threadIdx.x >> 5); row < row1;
+    for (long long row = (long long)blockIdx.x * (SIGN_BLOCK / 32) + (threadIdx.x >> 5); row < rows;
          row += warps) {
         const float* rp = vals + row * nz;
         uint32_t* op = out + row * NWg;
@@ -1096,7 +1075,6 @@ __global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__
 
 std::mutex g_mu;
 int g_block = 256;
-int g_slabs = 4;
 
 int sm_count() {
     int dev = 0, sms = 1;
@@ -1105,146 +1083,47 @@ int sm_count() {
     return sms;
 }
 
-// CTAs of one emit launch: entries are a fraction of the capacities and the
-// loops are grid-stride, so the resident CTAs are split between the roles in
-// proportion to the work (a vertex costs about half a cell).
 template <int EMIT_THREADS>
-void emit_grid(const McParams& p, int sms, long long& nbv, long long& nbf) {
+int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms) {
     static int per = -1;
     if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_emit<EMIT_THREADS>, EMIT_THREADS, 0);
+    // entries are a fraction of the capacities; the loops are grid-stride.  The
+    // resident CTAs are split between the roles in proportion to the work
+    // (a vertex costs about half a cell).
     const long long resident = (long long)sms * std::max(per, 1);
     const auto want = [&](long long cap) { return std::max<long long>(1, (cap + EMIT_THREADS - 1) / EMIT_THREADS); };
-    nbv = std::max<long long>(1, std::min(want(p.capV), resident / 3));
-    nbf = std::max<long long>(1, std::min(want(p.capF), resident - nbv));
-}
-
-template <int EMIT_THREADS>
-int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms, int slab,
-                unsigned long long ctas_total) {
-    long long nbv, nbf;
-    emit_grid<EMIT_THREADS>(p, sms, nbv, nbf);
+    const long long nbv = std::max<long long>(1, std::min(want(p.capV), resident / 3));
+    const long long nbf = std::max<long long>(1, std::min(want(p.capF), resident - nbv));
     EmitArgs a{p.vals, w.S, w.info, w.blk, w.foff, w.vlist, w.clist, w.ctr, w.snaps, w.small,
-               p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w, p.vedge, slab,
-               ctas_total ? ctas_total : (unsigned long long)(nbv + nbf)};
-    iso::ProfScope ps("mc_emit", st);
-    mc_emit<EMIT_THREADS><<<unsigned(nbv + nbf), EMIT_THREADS, 0, st>>>(g, a);
-    return cudaGetLastError() != cudaSuccess ? ISO_ERR_CUDA : 0;
-}
-
-int emit_ctas(const McParams& p, int sms) {
-    long long nbv, nbf;
-    if (mc_get_block() == 128) emit_grid<128>(p, sms, nbv, nbf);
-    else emit_grid<256>(p, sms, nbv, nbf);
-    return int(nbv + nbf);
-}
-
-int launch_emit_any(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, int sms, int slab,
-                    unsigned long long ctas_total) {
-    return mc_get_block() == 128 ? launch_emit<128>(p, g, w, st, sms, slab, ctas_total)
-                                 : launch_emit<256>(p, g, w, st, sms, slab, ctas_total);
-}
-
-int launch_count(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, uint32_t seg0,
-                 uint32_t seg1) {
-    iso::ProfScope ps("mc_count", st);
-    const long long ncoord = (long long)p.nx + p.ny + p.nz;
-    long long grid = seg1 - seg0;
-    if (seg0 == 0) grid = std::max<long long>(grid, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
-    if (grid <= 0) return 0;
-    mc_count<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0], p.asize[1],
-                                                     p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff,
-                                                     w.ctr, w.gc, seg0, seg1, p.capV, p.capF);
-    return cudaGetLastError() != cudaSuccess ? ISO_ERR_CUDA : 0;
-}
-
-int launch_scan(const McParams& p, const McWs& w, cudaStream_t st, uint32_t chunks, int slab) {
-    iso::ProfScope ps("mc_scan", st);
-    mc_scan<<<chunks, SCAN_THREADS, 0, st>>>(w.blk, uint32_t(w.nBlk), w.ctr, w.state, p.counts, p.status, p.capV,
-                                             p.capF, slab);
-    return cudaGetLastError() != cudaSuccess ? ISO_ERR_CUDA : 0;
+               p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w, p.vedge};
+    {
+        iso::ProfScope ps("mc_emit", st);
+        mc_emit<EMIT_THREADS><<<unsigned(nbv + nbf), EMIT_THREADS, 0, st>>>(g, a);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
+    return 0;
 }
 
 int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st) {
     const int sms = sm_count();
-    int rc = launch_count(p, g, w, st, 0, uint32_t(w.nBlk));
-    if (rc) return rc;
-    const uint32_t nchunk = uint32_t((w.nBlk + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS));
-    rc = launch_scan(p, w, st, nchunk, -1);
-    if (rc) return rc;
-    return launch_emit_any(p, g, w, st, sms, -1, 0);
-}
-
-// Streams and events of the slab pipeline, per host thread and device: signs
-// run on a low-priority stream, count / scan / emit on a high-priority one, so
-// a slab's count takes SMs as soon as they free up while the next slab's sign
-// pass keeps HBM busy.  Created on the first pipelined call of the thread.
-struct Pipe {
-    bool ok = false, tried = false;
-    cudaStream_t sig = nullptr, work = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, slab[MAX_SLABS] = {};
-};
-constexpr int MAX_DEVICES = 64;
-thread_local Pipe t_pipes[MAX_DEVICES];
-
-Pipe* get_pipe() {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return nullptr;
-    Pipe& pp = t_pipes[dev];
-    if (pp.tried) return pp.ok ? &pp : nullptr;
-    pp.tried = true;
-    int least = 0, greatest = 0;
-    bool ok = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess;
-    ok = ok && cudaStreamCreateWithPriority(&pp.sig, cudaStreamNonBlocking, least) == cudaSuccess;
-    ok = ok && cudaStreamCreateWithPriority(&pp.work, cudaStreamNonBlocking, greatest) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&pp.fork, cudaEventDisableTiming) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&pp.join, cudaEventDisableTiming) == cudaSuccess;
-    for (int i = 0; i < MAX_SLABS && ok; ++i) ok = cudaEventCreateWithFlags(&pp.slab[i], cudaEventDisableTiming) == cudaSuccess;
-    pp.ok = ok;
-    if (!ok) cudaGetLastError();  // fall back to one stream; clear the error
-    return ok ? &pp : nullptr;
-}
-
-// Slabs of scan chunks along the point-word order (x slowest).  Slab i's count
-// needs the sign words of its rows and of the rows one x plane + 1 further, so
-// its sign pass covers those too (rows shared by two slabs are written twice
-// with the same bits, in stream order).  emit(i) runs after count and scan of
-// slab i + 1: its faces use vertex slots of the next x plane.
-int launch_pipelined(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st, Pipe& pp, int slabs) {
-    const int sms = sm_count();
-    const uint32_t CH = SCAN_PER * SCAN_THREADS;
-    const uint32_t nseg = uint32_t(w.nBlk);
-    const uint32_t nchunk = (nseg + CH - 1) / CH;
-    const long long rows = (long long)p.nx * p.ny;
-    uint32_t c[MAX_SLABS + 1];
-    for (int i = 0; i <= slabs; ++i) c[i] = uint32_t((unsigned long long)nchunk * i / slabs);
-    if (cudaEventRecord(pp.fork, st) != cudaSuccess) return ISO_ERR_CUDA;
-    if (cudaStreamWaitEvent(pp.sig, pp.fork, 0) != cudaSuccess) return ISO_ERR_CUDA;
-    if (cudaStreamWaitEvent(pp.work, pp.fork, 0) != cudaSuccess) return ISO_ERR_CUDA;
-    for (int i = 0; i < slabs; ++i) {
-        const uint32_t s0 = std::min(c[i] * CH, nseg), s1 = std::min(c[i + 1] * CH, nseg);
-        const long long r0 = (long long)s0 * SEG / g.NW;
-        const long long rl = ((long long)s1 * SEG - 1) / g.NW;  // row of the slab's last word
-        const long long r1 = i + 1 == slabs ? rows : std::min(rows, rl + p.ny + 2);
-        {
-            iso::ProfScope ps("mc_signs", pp.sig);
-            mc_signs_rows(p.vals, r0, r1, p.nz, p.level, w.S, pp.sig);
-            if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
-        }
-        if (cudaEventRecord(pp.slab[i], pp.sig) != cudaSuccess) return ISO_ERR_CUDA;
+    {
+        iso::ProfScope ps("mc_count", st);
+        const long long ncoord = (long long)p.nx + p.ny + p.nz;
+        const long long grid = std::max<long long>(w.nBlk, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
+        mc_count<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0], p.asize[1],
+                                                         p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff,
+                                                         w.ctr, w.gc, uint32_t(w.nBlk), p.capV, p.capF);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
-    const unsigned long long ctas = (unsigned long long)emit_ctas(p, sms) * slabs;
-    for (int i = 0; i < slabs; ++i) {
-        const uint32_t s0 = std::min(c[i] * CH, nseg), s1 = std::min(c[i + 1] * CH, nseg);
-        if (cudaStreamWaitEvent(pp.work, pp.slab[i], 0) != cudaSuccess) return ISO_ERR_CUDA;
-        int rc = launch_count(p, g, w, pp.work, s0, s1);
-        if (!rc) rc = launch_scan(p, w, pp.work, c[i + 1] - c[i], i);
-        if (!rc && i > 0) rc = launch_emit_any(p, g, w, pp.work, sms, i - 1, ctas);
-        if (rc) return rc;
+    {
+        iso::ProfScope ps("mc_scan", st);
+        const uint32_t nseg = uint32_t(w.nBlk);
+        const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
+        mc_scan<<<nchunk, SCAN_THREADS, 0, st>>>(w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV, p.capF);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
-    int rc = launch_emit_any(p, g, w, pp.work, sms, slabs - 1, ctas);
-    if (rc) return rc;
-    if (cudaEventRecord(pp.join, pp.work) != cudaSuccess) return ISO_ERR_CUDA;
-    return cudaStreamWaitEvent(st, pp.join, 0) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    const int block = mc_get_block();
+    return block == 128 ? launch_emit<128>(p, g, w, st, sms) : launch_emit<256>(p, g, w, st, sms);
 }
 
 }  // namespace
@@ -1261,31 +1140,12 @@ int mc_get_block() {
     return g_block;
 }
 
-int mc_set_slabs(int slabs) {
-    if (slabs < 1 || slabs > MAX_SLABS) return ISO_ERR_ARG;
-    std::lock_guard<std::mutex> lk(g_mu);
-    g_slabs = slabs;
-    return 0;
-}
-
-int mc_get_slabs() {
-    std::lock_guard<std::mutex> lk(g_mu);
-    return g_slabs;
-}
-
-// Sign words of rows [row0, row1) (row = x * ny + y).
-void mc_signs_rows(const float* vals, long long row0, long long row1, int nz, float level, uint32_t* out,
-                   cudaStream_t st) {
-    const long long rows = row1 - row0;
-    if (rows <= 0) return;
-    const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
-    const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sm_count() * 32));
-    mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, row0, row1, nz, level, out);
-}
-
 void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
                      cudaStream_t st) {
-    mc_signs_rows(vals, 0, (long long)nx * ny, nz, level, out, st);
+    const long long rows = (long long)nx * ny;
+    const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
+    const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sm_count() * 32));
+    mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, rows, nz, level, out);
 }
 
 // Bound on t for an edge vertex to land within a few ulps of an endpoint (the
@@ -1329,15 +1189,12 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
     if (cudaMemsetAsync(w.ctr, 0, zeroed_bytes(w.nBlk), st) != cudaSuccess) return ISO_ERR_CUDA;
-    const uint32_t nchunk = uint32_t((w.nBlk + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS));
-    const int slabs = std::min<int>(mc_get_slabs(), std::min<uint32_t>(nchunk, MAX_SLABS));
-    if (slabs >= 2) {
-        if (Pipe* pp = get_pipe()) return launch_pipelined(p, g, w, st, *pp, slabs);
-    }
     {
         iso::ProfScope ps("mc_signs", st);
         mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
-    return launch_count_emit(p, g, w, st);
+    const int rc = launch_count_emit(p, g, w, st);
+    if (rc) return rc;
+    return 0;
 }

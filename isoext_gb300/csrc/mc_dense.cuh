@@ -37,9 +37,6 @@ struct McParams {
 // Threads per CTA of the emit kernel (128 or 256).
 int mc_set_block(int threads);
 int mc_get_block();
-// x slabs of the sign / count / scan / emit pipeline of large grids (1 = one stream).
-int mc_set_slabs(int slabs);
-int mc_get_slabs();
 
 size_t mc_workspace_bytes(int nx, int ny, int nz, long long capV, long long capF);
 int mc_launch(const McParams& p, void* workspace, size_t ws_bytes, cudaStream_t stream);
@@ -47,6 +44,3 @@ int mc_launch(const McParams& p, void* workspace, size_t ws_bytes, cudaStream_t 
 // Sign bitmap of a grid (also used by dual contouring).
 void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
                      cudaStream_t st);
-// The same for rows [row0, row1) (row = x * ny + y).
-void mc_signs_rows(const float* vals, long long row0, long long row1, int nz, float level, uint32_t* out,
-                   cudaStream_t st);

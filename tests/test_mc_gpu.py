@@ -183,55 +183,3 @@ def test_mc_far_offset_box(oracle):
     check(oracle, vals, lo=(1000.0, -500.0, 2.0), hi=(1001.0, -499.5, 2.001), what="far box")
     check(oracle, sphere((30, 30, 30), 0.3) * 1e-3, lo=(1000.0, 1000.0, 1000.0),
           hi=(1000.002, 1000.002, 1000.002), what="far sphere")
-
-
-# --- the slab pipeline of large grids --------------------------------------------------
-
-@pytest.fixture
-def mc_slabs():
-    import ctypes
-
-    from isoext_gb300 import _ffi
-
-    lib = _ffi.lib()
-    old = ctypes.c_int()
-    lib.iso_mc_get_slabs(ctypes.byref(old))
-    yield lib
-    lib.iso_mc_set_slabs(old.value)
-
-
-def _big(kind, shape):
-    nx, ny, nz = shape
-    i = torch.arange(nx, device="cuda", dtype=torch.float32).view(-1, 1, 1)
-    j = torch.arange(ny, device="cuda", dtype=torch.float32).view(1, -1, 1)
-    k = torch.arange(nz, device="cuda", dtype=torch.float32).view(1, 1, -1)
-    if kind == "planes":
-        # integer values: zeros on grid points, where edges of two axes meet at one
-        # position (merged by the fix-up)
-        return ((i - 300.0) + (j - 350.0) + 0.0 * k).contiguous()
-    p = [(t / (n - 1)) * 2.0 - 1.0 for t, n in ((i, nx), (j, ny), (k, nz))]
-    return (torch.sqrt(p[0] ** 2 + p[1] ** 2 + p[2] ** 2) - 0.8 + 0.05 * torch.sin(9 * p[0] * p[1])).contiguous()
-
-
-@pytest.mark.parametrize("kind", ["sphere", "planes"])
-def test_mc_slab_pipeline_equals_one_stream(mc_slabs, kind):
-    from isoext_gb300 import diff
-
-    shape = (600, 700, 512)  # 6.7 M point words: 7 scan chunks
-    vals = _big(kind, shape)
-    grid = iso.UniformGrid(list(shape))
-    grid.set_values(vals)
-    out = {}
-    for slabs in (1, 2, 4, 7, 8):
-        assert mc_slabs.iso_mc_set_slabs(slabs) == 0
-        out[slabs] = iso.marching_cubes(grid)
-        if slabs in (1, 4):
-            out[("e", slabs)] = diff._mc_forward(vals, (-1.0,) * 3, (1.0,) * 3, 0.0, 0)
-    v1, f1 = out[1]
-    assert len(f1) > 100000
-    for slabs in (2, 4, 7, 8):
-        v, f = out[slabs]
-        assert torch.equal(v, v1) and torch.equal(f, f1), slabs
-    for a, b in zip(out[("e", 1)], out[("e", 4)]):
-        assert torch.equal(a, b)
-    assert mc_slabs.iso_mc_set_slabs(0) == 1 and mc_slabs.iso_mc_set_slabs(9) == 1
