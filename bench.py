@@ -145,16 +145,6 @@ def sphere_values(n: int, r: float) -> np.ndarray:
 
 # ---------------------------------------------------------------------------
 
-def _slabs_config() -> int:
-    import ctypes
-
-    from isoext_gb300 import _ffi
-
-    v = ctypes.c_int()
-    _ffi.lib().iso_mc_get_slabs(ctypes.byref(v))
-    return v.value
-
-
 def kernel_bytes(kind: str, n: int, nv: int, nf: int) -> dict:
     """Algorithmic bytes per launch of each kernel of the MC pipeline."""
     pts = n ** 3
@@ -255,8 +245,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
     assert (int(host[0]), int(host[1])) == (nv, nf)
     kt = {k: _ffi.profile_read(k) for k in kernels}
     launches = sum(c for c, _ in kt.values())
-    # per extraction: the sum of the kernel's launches (large grids run each
-    # kernel once per x slab, on two streams that overlap)
+    # per extraction: the sum of the kernel's launches in one call
     kavg = {k: t / args.steps for k, (c, t) in kt.items()}
     top = max(kavg, key=kavg.get)
     if world > 1:
@@ -294,7 +283,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
         "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae",
-                   "vertices": nv, "faces": nf, "parallelism": f"replicas x{world}", "slabs": _slabs_config(),
+                   "vertices": nv, "faces": nf, "parallelism": f"replicas x{world}",
                    "l2": f"inputs larger than L2 (values {4 * n ** 3 / 1e6:.0f} MB > 129 MB L2)"
                          if 4 * n ** 3 > 129e6 else "inputs smaller than L2 (not flushed)"},
         "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
@@ -1038,7 +1027,6 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--mc-slabs", type=int, default=None, help="x slabs of the MC pipeline (1 = one stream)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1048,9 +1036,6 @@ def main() -> None:
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    if args.mc_slabs is not None and args.impl == "ours":
-        from isoext_gb300 import _ffi
-        _ffi.check(_ffi.lib().iso_mc_set_slabs(args.mc_slabs))
     if args.impl == "reference":
         out = run_reference(args, wl, rank)
     else:
