@@ -312,42 +312,6 @@ __device__ __forceinline__ void sign_row(const float* __restrict__ vals, long lo
     }
 }
 
-// Two rows at once (rb < 0: ra only): twice the loads in flight per warp.
-__device__ __forceinline__ void sign_row2(const float* __restrict__ vals, long long ra, long long rb, int nz,
-                                          float level, uint32_t* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int NWg = (nz + 31) / 32;
-    const bool two = rb >= 0;
-    const float* pa = vals + ra * nz;
-    const float* pb = vals + (two ? rb : ra) * nz;
-    for (int wb = 0; wb < NWg; wb += 32) {
-        uint32_t ma = 0, mb = 0;
-        for (int w0 = wb; w0 < min(NWg, wb + 32); w0 += SIGN_UNROLL) {
-            float va[SIGN_UNROLL], vb[SIGN_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SIGN_UNROLL; ++u) {
-                const int z = 32 * (w0 + u) + lane;
-                const bool ok = w0 + u < NWg && z < nz;
-                va[u] = ok ? __ldg(pa + z) : level;
-                vb[u] = (ok && two) ? __ldg(pb + z) : level;
-            }
-#pragma unroll
-            for (int u = 0; u < SIGN_UNROLL; ++u) {
-                const uint32_t ba = __ballot_sync(~0u, iso::below(va[u], level));
-                const uint32_t bb = __ballot_sync(~0u, iso::below(vb[u], level));
-                if (((w0 + u) & 31) == lane) {
-                    ma = ba;
-                    mb = bb;
-                }
-            }
-        }
-        if (wb + lane < NWg) {
-            out[ra * NWg + wb + lane] = ma;
-            if (two) out[rb * NWg + wb + lane] = mb;
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // 2. classify: sign words and per-segment counts in one persistent kernel.
 // each segment's (V, F) prefix comes from a decoupled look-back over the
@@ -789,7 +753,7 @@ __global__ void mc_plan(const McGrid g, uint32_t nseg, long long rows, long long
 // Persistent CTAs take work items in ticket order: a sign tile (TILE_ROWS rows,
 // HBM-bound) or the counts of a segment (instruction-bound), so both kinds run
 // side by side.  A segment waits, bounded, for the tiles of the rows it reads.
-__global__ void __launch_bounds__(CNT_THREADS, 4) mc_classify(const McGrid g, const float amin0, const float amin1,
+__global__ void __launch_bounds__(CNT_THREADS) mc_classify(const McGrid g, const float amin0, const float amin1,
                                                            const float amin2, const float size0, const float size1,
                                                            const float size2, const float* __restrict__ vals,
                                                            CountArgs c, float* __restrict__ gc,
@@ -814,9 +778,8 @@ __global__ void __launch_bounds__(CNT_THREADS, 4) mc_classify(const McGrid g, co
         if (it == INT_MIN) return;
         if (it >= 0) {
             const long long r0 = (long long)it * TILE_ROWS, r1 = min(rows, r0 + TILE_ROWS);
-            constexpr int NWARP = CNT_THREADS / 32;
-            for (long long row = r0 + (threadIdx.x >> 5); row < r1; row += 2 * NWARP)
-                sign_row2(vals, row, row + NWARP < r1 ? row + NWARP : -1, g.nz, g.level, const_cast<uint32_t*>(c.S));
+            for (long long row = r0 + (threadIdx.x >> 5); row < r1; row += CNT_THREADS / 32)
+                sign_row(vals, row, g.nz, g.level, const_cast<uint32_t*>(c.S));
             __threadfence();
             __syncthreads();
             if (threadIdx.x == 0) atomicExch(tile_done + it, 1u);
