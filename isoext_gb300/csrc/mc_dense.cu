@@ -734,17 +734,14 @@ __device__ uint32_t segs_below(const McGrid& g, uint32_t nseg, long long rows, l
 }
 
 // Work items of mc_classify in ticket order: sign tile t, then the segments
-// whose last needed row lies in tile t - lag (as -(segment + 1)); the rest
-// after the last tile.  A segment's tiles all come before it, so a CTA waiting
-// for them waits on items that running or finished CTAs hold; the lag (about
-// one item per resident CTA) makes the tiles done by then, as a rule.
-__global__ void mc_plan(const McGrid g, uint32_t nseg, long long rows, long long ntile, long long lag,
-                        int32_t* items) {
+// whose last needed row lies in tile t (as -(segment + 1)).  A segment's tiles
+// all come before it, so a CTA waiting for them waits on items that running or
+// finished CTAs hold.
+__global__ void mc_plan(const McGrid g, uint32_t nseg, long long rows, long long ntile, int32_t* items) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntile) return;
-    const long long u = t - lag;  // segments of tile u follow tile t
-    const uint32_t a = u <= 0 ? 0u : segs_below(g, nseg, rows, u * TILE_ROWS);
-    const uint32_t b = t == ntile - 1 ? nseg : (u < 0 ? 0u : segs_below(g, nseg, rows, (u + 1) * TILE_ROWS));
+    const uint32_t a = t == 0 ? 0u : segs_below(g, nseg, rows, t * TILE_ROWS);
+    const uint32_t b = t == ntile - 1 ? nseg : segs_below(g, nseg, rows, (t + 1) * TILE_ROWS);
     const long long pos = t + a;
     items[pos] = int32_t(t);
     for (uint32_t j = a; j < b; ++j) items[pos + 1 + (j - a)] = -int32_t(j) - 1;
@@ -1230,12 +1227,11 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
     const long long rows = (long long)p.nx * p.ny;
     {
         iso::ProfScope ps("mc_classify", st);
+        mc_plan<<<unsigned((w.nTile + 255) / 256), 256, 0, st>>>(g, uint32_t(w.nBlk), rows, w.nTile, w.items);
         static int per = -1;
         if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_classify, CNT_THREADS, 0);
         const long long nitems = w.nTile + w.nBlk;
         const long long grid = std::max<long long>(1, std::min<long long>(nitems, (long long)sms * std::max(per, 1)));
-        mc_plan<<<unsigned((w.nTile + 255) / 256), 256, 0, st>>>(g, uint32_t(w.nBlk), rows, w.nTile, grid,
-                                                                 w.items);
         CountArgs c{w.S, w.info, w.blk, w.vlist, w.clist, w.foff, w.ctr, p.capV, p.capF};
         mc_classify<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0],
                                                             p.asize[1], p.asize[2], p.vals, c, w.gc, w.items,
