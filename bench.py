@@ -151,7 +151,8 @@ def kernel_bytes(kind: str, n: int, nv: int, nf: int) -> dict:
     words = n * n * ((n + 31) // 32)
     segs = (words + 1023) // 1024
     return {
-        "mc_classify": 4 * pts + 4 * words + 4 * words,  # values once, bitmap written, per-word entries
+        "mc_signs": 4 * pts + 4 * words,           # values once, sign bitmap once
+        "mc_count": 4 * words + 4 * words,         # bitmap once, per-word entries once
         "mc_scan": 32 * segs,                      # segment sums read, offsets written
         "mc_emit": 16 * nv + 12 * nv + 8 * nf + 12 * nf,  # entries and endpoint values; vertices, faces
     }

@@ -94,14 +94,10 @@ struct McWs {
     unsigned long long* clist;  // cell entries [capF]: pw | bit << 32 | case << 37 | face offset << 45
     uint32_t* foff;             // per word with faces: segment-local face offset
     unsigned long long* ctr;    // [0] list size [1] snaps [2] barrier count [3] barrier gen [4] V' [5] F'
-                                // [6] classify ticket [7] scan ticket [8] merges [9] small hash full
-                                // [12] a classify wait ran out
+                                // [6] unused [7] scan ticket [8] merges [9] small hash full
                                 // [10] cell entries [11] emit CTAs done
     unsigned long long* state;  // look-back state per segment (follows ctr; zeroed with it)
     uint32_t* small;            // SMALL_HC entries after the states (zeroed with them)
-    uint32_t* tile_done;        // per sign tile: rows written (after the small hash; zeroed)
-    int32_t* items;             // classify work items in ticket order: tile t, or -(segment + 1)
-    long long nTile;            // sign tiles of TILE_ROWS rows
     float* gc;                  // grid coordinates [nx + ny + nz] (x, then y, then z)
     uint32_t* snaps;            // snapped vertex slots [capV]
     uint32_t* table;            // position hash of snapped vertices [HC]
@@ -129,20 +125,13 @@ uint32_t hash_cap(long long capV) {
 }
 
 // Bytes cleared at the start of each call: counters, look-back states, small hash.
-constexpr int TILE_ROWS = 64;  // grid rows per sign tile of the classify kernel
-
-// Bytes cleared at the start of each call: counters, look-back states, small
-// hash, tile flags.
-inline size_t zeroed_bytes(long long nBlk, long long nTile) {
-    return size_t(NCTR) * 8 + size_t(nBlk) * 8 + size_t(SMALL_HC) * 4 + size_t(nTile) * 4;
-}
+inline size_t zeroed_bytes(long long nBlk) { return size_t(NCTR) * 8 + size_t(nBlk) * 8 + size_t(SMALL_HC) * 4; }
 
 McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base) {
     McWs w{};
     const long long NW = (nz + 31) / 32;
     const long long PW = (long long)nx * ny * NW;
     w.nBlk = (PW + SEG - 1) / SEG;
-    w.nTile = ((long long)nx * ny + TILE_ROWS - 1) / TILE_ROWS;
     w.HC = hash_cap(capV);
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -156,11 +145,9 @@ McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base
     w.vlist = reinterpret_cast<unsigned long long*>(take(size_t(capV) * 8));
     w.clist = reinterpret_cast<unsigned long long*>(take(size_t(capF) * 8));
     w.foff = reinterpret_cast<uint32_t*>(take(size_t(PW) * 4));
-    w.ctr = reinterpret_cast<unsigned long long*>(take(zeroed_bytes(w.nBlk, w.nTile)));  // + states, hash, flags
+    w.ctr = reinterpret_cast<unsigned long long*>(take(zeroed_bytes(w.nBlk)));  // + states + small hash
     w.state = w.ctr ? w.ctr + NCTR : nullptr;
     w.small = w.ctr ? reinterpret_cast<uint32_t*>(w.state + w.nBlk) : nullptr;
-    w.tile_done = w.small ? w.small + SMALL_HC : nullptr;
-    w.items = reinterpret_cast<int32_t*>(take(size_t(w.nTile + w.nBlk) * 4));
     w.gc = reinterpret_cast<float*>(take(size_t(nx + ny + nz) * 4));
     w.snaps = reinterpret_cast<uint32_t*>(take(size_t(capV) * 4));
     w.table = reinterpret_cast<uint32_t*>(take(size_t(w.HC) * 4));
@@ -282,38 +269,8 @@ __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea
     __syncthreads();
 }
 
-constexpr int SIGN_UNROLL = 16;
-
-// Sign words of one grid row, by one warp: bit z % 32 of word
-// [row * NWg + z / 32] is (v - level < 0).  All of the row's loads are in
-// flight before the ballots; lane w keeps word w so 32 words leave in one store.
-__device__ __forceinline__ void sign_row(const float* __restrict__ vals, long long row, int nz, float level,
-                                         uint32_t* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int NWg = (nz + 31) / 32;
-    const float* rp = vals + row * nz;
-    uint32_t* op = out + row * NWg;
-    for (int wb = 0; wb < NWg; wb += 32) {
-        uint32_t mine = 0;
-        for (int w0 = wb; w0 < min(NWg, wb + 32); w0 += SIGN_UNROLL) {
-            float v[SIGN_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SIGN_UNROLL; ++u) {
-                const int z = 32 * (w0 + u) + lane;
-                v[u] = (w0 + u < NWg && z < nz) ? __ldg(rp + z) : level;
-            }
-#pragma unroll
-            for (int u = 0; u < SIGN_UNROLL; ++u) {
-                const uint32_t b = __ballot_sync(~0u, iso::below(v[u], level));
-                if (((w0 + u) & 31) == lane) mine = b;
-            }
-        }
-        if (wb + lane < NWg) op[wb + lane] = mine;
-    }
-}
-
 // ---------------------------------------------------------------------------
-// 2. classify: sign words and per-segment counts in one persistent kernel.
+// 2. count: persistent CTAs take segments of SEG point words in ticket order;
 // each segment's (V, F) prefix comes from a decoupled look-back over the
 // segments before it, so no separate scan pass is needed.
 
@@ -421,31 +378,16 @@ __device__ __forceinline__ int owner_of(uint32_t incl, uint32_t j) {
     return lo;
 }
 
-struct CountArgs {
-    const uint32_t* S;
-    uint32_t* info;
-    unsigned long long* blk;
-    unsigned long long* vlist;
-    unsigned long long* clist;
-    uint32_t* foff;
-    unsigned long long* ctr;
-    long long capV, capF;
-};
-
-// Counts of one segment of SEG point words, by the whole CTA: per word its
-// vertex offset within the segment and its x / y edge counts (info), the
-// segment's face offsets (foff), its (V, F) sums (blk) and its vertex and cell
-// entries.  The sign words are read through L2 (ld.global.cg): in the classify
-// kernel other CTAs write them during the same launch.
-__device__ __forceinline__ void count_segment(const McGrid& g, const CountArgs& c, const uint32_t seg) {
-    const uint32_t* __restrict__ S = c.S;
-    uint32_t* __restrict__ info = c.info;
-    unsigned long long* __restrict__ blk = c.blk;
-    unsigned long long* __restrict__ vlist = c.vlist;
-    unsigned long long* __restrict__ clist = c.clist;
-    uint32_t* __restrict__ foff = c.foff;
-    unsigned long long* ctr = c.ctr;
-    const long long capV = c.capV, capF = c.capF;
+__global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const float amin0, const float amin1,
+                                                        const float amin2, const float size0, const float size1,
+                                                        const float size2, const uint32_t* __restrict__ S,
+                                                        uint32_t* __restrict__ info,
+                                                        unsigned long long* __restrict__ blk,
+                                                        unsigned long long* __restrict__ vlist,
+                                                        unsigned long long* __restrict__ clist,
+                                                        uint32_t* __restrict__ foff, unsigned long long* ctr,
+                                                        float* __restrict__ gc, const uint32_t nseg,
+                                                        const long long capV, const long long capF) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
     __shared__ uint32_t wcell[CNT_THREADS / 32];
@@ -453,6 +395,16 @@ __device__ __forceinline__ void count_segment(const McGrid& g, const CountArgs& 
     __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
     __shared__ uint32_t vmask[3 * WPT][CNT_THREADS];  // x, y, z edge masks of each thread's words
     __shared__ uint32_t rows[4][WPT + 1][CNT_THREADS];  // sign words of rows (dx, dy), words k = 0..4
+    // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
+    const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
+    const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
+    if (gid < ncoord) {
+        if (gid < uint32_t(g.nx)) gc[gid] = iso::grid_coord(gid, g.nx, amin0, size0);
+        else if (gid < uint32_t(g.nx + g.ny)) gc[gid] = iso::grid_coord(gid - g.nx, g.ny, amin1, size1);
+        else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2);
+    }
+    const uint32_t seg = blockIdx.x;
+    if (seg >= nseg) return;  // CTAs past the segments only write coordinates
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sxw = uint32_t(g.ny) * uint32_t(g.NW), syw = uint32_t(g.NW);
     const bool vec = (g.NW & 3) == 0;  // rows start on 16-byte boundaries
@@ -473,11 +425,11 @@ __device__ __forceinline__ void count_segment(const McGrid& g, const CountArgs& 
         for (int dy = 0; dy < 2; ++dy) {
             const uint32_t q = pw0 + dx * sxw + dy * syw;
             if (vec && pw0 + WPT <= g.PW && q + WPT <= g.PW) {
-                const uint4 v4 = __ldcg(reinterpret_cast<const uint4*>(S + q));
+                const uint4 v4 = __ldg(reinterpret_cast<const uint4*>(S + q));
                 r[dx][dy][0] = v4.x; r[dx][dy][1] = v4.y; r[dx][dy][2] = v4.z; r[dx][dy][3] = v4.w;
             } else {
 #pragma unroll
-                for (int k = 0; k < WPT; ++k) r[dx][dy][k] = (q + k < g.PW) ? __ldcg(S + q + k) : 0u;
+                for (int k = 0; k < WPT; ++k) r[dx][dy][k] = (q + k < g.PW) ? __ldg(S + q + k) : 0u;
             }
         }
     // word pw0 + 4 of each row: the next lane's first word, or a load
@@ -489,7 +441,7 @@ __device__ __forceinline__ void count_segment(const McGrid& g, const CountArgs& 
             nx4[dx][dy] = __shfl_down_sync(~0u, r[dx][dy][0], 1);
             if (lane == 31) {
                 const uint32_t q = pw0 + WPT + dx * sxw + dy * syw;
-                nx4[dx][dy] = q < g.PW ? __ldcg(S + q) : 0u;
+                nx4[dx][dy] = q < g.PW ? __ldg(S + q) : 0u;
             }
         }
     uint32_t nv[WPT], cxy[WPT], act[WPT];
@@ -712,98 +664,6 @@ __device__ __forceinline__ void count_segment(const McGrid& g, const CountArgs& 
     if (threadIdx.x == 0) {
         blk[2 * seg] = tv;
         blk[2 * seg + 1] = tf;
-    }
-}
-
-// Rows the counts of segment seg read: its own words' rows up to the row one x
-// plane and one y row further (x + 1, y + 1).
-__device__ __forceinline__ long long seg_need_row(const McGrid& g, uint32_t seg, long long rows) {
-    const long long last = min((long long)(seg + 1) * SEG, g.PW) - 1;
-    return min(rows - 1, last / g.NW + g.ny + 1);
-}
-
-// Segments whose rows all lie below row lim (seg_need_row is nondecreasing).
-__device__ uint32_t segs_below(const McGrid& g, uint32_t nseg, long long rows, long long lim) {
-    uint32_t lo = 0, hi = nseg;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) / 2;
-        if (seg_need_row(g, mid, rows) < lim) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Work items of mc_classify in ticket order: sign tile t, then the segments
-// whose last needed row lies in tile t (as -(segment + 1)).  A segment's tiles
-// all come before it, so a CTA waiting for them waits on items that running or
-// finished CTAs hold.
-__global__ void mc_plan(const McGrid g, uint32_t nseg, long long rows, long long ntile, int32_t* items) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntile) return;
-    const uint32_t a = t == 0 ? 0u : segs_below(g, nseg, rows, t * TILE_ROWS);
-    const uint32_t b = t == ntile - 1 ? nseg : segs_below(g, nseg, rows, (t + 1) * TILE_ROWS);
-    const long long pos = t + a;
-    items[pos] = int32_t(t);
-    for (uint32_t j = a; j < b; ++j) items[pos + 1 + (j - a)] = -int32_t(j) - 1;
-}
-
-// Persistent CTAs take work items in ticket order: a sign tile (TILE_ROWS rows,
-// HBM-bound) or the counts of a segment (instruction-bound), so both kinds run
-// side by side.  A segment waits, bounded, for the tiles of the rows it reads.
-__global__ void __launch_bounds__(CNT_THREADS) mc_classify(const McGrid g, const float amin0, const float amin1,
-                                                           const float amin2, const float size0, const float size1,
-                                                           const float size2, const float* __restrict__ vals,
-                                                           CountArgs c, float* __restrict__ gc,
-                                                           const int32_t* __restrict__ items, uint32_t nitems,
-                                                           uint32_t* tile_done, long long rows, int* status) {
-    __shared__ int item_s;
-    // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
-    const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
-    for (uint32_t i = blockIdx.x * CNT_THREADS + threadIdx.x; i < ncoord; i += gridDim.x * CNT_THREADS) {
-        if (i < uint32_t(g.nx)) gc[i] = iso::grid_coord(i, g.nx, amin0, size0);
-        else if (i < uint32_t(g.nx + g.ny)) gc[i] = iso::grid_coord(i - g.nx, g.ny, amin1, size1);
-        else gc[i] = iso::grid_coord(i - g.nx - g.ny, g.nz, amin2, size2);
-    }
-    while (true) {
-        __syncthreads();  // the last item's shared memory is free
-        if (threadIdx.x == 0) {
-            const unsigned long long k = atomicAdd(c.ctr + 6, 1ull);
-            item_s = k < nitems ? items[k] : INT_MIN;
-        }
-        __syncthreads();
-        const int it = item_s;
-        if (it == INT_MIN) return;
-        if (it >= 0) {
-            const long long r0 = (long long)it * TILE_ROWS, r1 = min(rows, r0 + TILE_ROWS);
-            for (long long row = r0 + (threadIdx.x >> 5); row < r1; row += CNT_THREADS / 32)
-                sign_row(vals, row, g.nz, g.level, const_cast<uint32_t*>(c.S));
-            __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) atomicExch(tile_done + it, 1u);
-        } else {
-            const uint32_t seg = uint32_t(-(it + 1));
-            if (threadIdx.x == 0) {
-                const long long ta = ((long long)seg * SEG / g.NW) / TILE_ROWS;
-                const long long tb = seg_need_row(g, seg, rows) / TILE_ROWS;
-                // after one wait has run out (ctr[12] set) the others are skipped
-                volatile unsigned long long* gave_up = c.ctr + 12;
-                for (long long t = ta; t <= tb; ++t) {
-                    const volatile uint32_t* f = tile_done + t;
-                    uint32_t spins = 0;
-                    while (*f == 0u && *gave_up == 0ull) {
-                        if (++spins > ISO_SPIN_LIMIT) {
-                            atomicCAS(status, 0, int(ISO_ERR_TIMEOUT));
-                            atomicExch(const_cast<unsigned long long*>(gave_up), 1ull);
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
-                __threadfence();
-            }
-            __syncthreads();
-            count_segment(g, c, seg);
-        }
     }
 }
 
@@ -1179,16 +1039,38 @@ __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long
 // 1. sign bitmap
 
 constexpr int SIGN_BLOCK = 256;
+constexpr int SIGN_UNROLL = 16;
 
 // Bit z % 32 of word [(x * ny + y) * NWg + z / 32] is (v - level < 0).  One warp
 // per grid row, all of the row's loads in flight before the ballots; lane w
 // keeps word w so each 32 words leave in one store.
 __global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__ vals, long long rows,
                                                        int nz, float level, uint32_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int NWg = (nz + 31) / 32;
     const long long warps = (long long)gridDim.x * (SIGN_BLOCK / 32);
     for (long long row = (long long)blockIdx.x * (SIGN_BLOCK / 32) + (threadIdx.x >> 5); row < rows;
-         row += warps)
-        sign_row(vals, row, nz, level, out);
+         row += warps) {
+        const float* rp = vals + row * nz;
+        uint32_t* op = out + row * NWg;
+        for (int wb = 0; wb < NWg; wb += 32) {
+            uint32_t mine = 0;
+            for (int w0 = wb; w0 < min(NWg, wb + 32); w0 += SIGN_UNROLL) {
+                float v[SIGN_UNROLL];
+#pragma unroll
+                for (int u = 0; u < SIGN_UNROLL; ++u) {
+                    const int z = 32 * (w0 + u) + lane;
+                    v[u] = (w0 + u < NWg && z < nz) ? __ldg(rp + z) : level;
+                }
+#pragma unroll
+                for (int u = 0; u < SIGN_UNROLL; ++u) {
+                    const uint32_t b = __ballot_sync(~0u, iso::below(v[u], level));
+                    if (((w0 + u) & 31) == lane) mine = b;
+                }
+            }
+            if (wb + lane < NWg) op[wb + lane] = mine;
+        }
+    }
 }
 
 std::mutex g_mu;
@@ -1224,18 +1106,13 @@ int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t 
 
 int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t st) {
     const int sms = sm_count();
-    const long long rows = (long long)p.nx * p.ny;
     {
-        iso::ProfScope ps("mc_classify", st);
-        mc_plan<<<unsigned((w.nTile + 255) / 256), 256, 0, st>>>(g, uint32_t(w.nBlk), rows, w.nTile, w.items);
-        static int per = -1;
-        if (per < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mc_classify, CNT_THREADS, 0);
-        const long long nitems = w.nTile + w.nBlk;
-        const long long grid = std::max<long long>(1, std::min<long long>(nitems, (long long)sms * std::max(per, 1)));
-        CountArgs c{w.S, w.info, w.blk, w.vlist, w.clist, w.foff, w.ctr, p.capV, p.capF};
-        mc_classify<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0],
-                                                            p.asize[1], p.asize[2], p.vals, c, w.gc, w.items,
-                                                            uint32_t(nitems), w.tile_done, rows, p.status);
+        iso::ProfScope ps("mc_count", st);
+        const long long ncoord = (long long)p.nx + p.ny + p.nz;
+        const long long grid = std::max<long long>(w.nBlk, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
+        mc_count<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0], p.asize[1],
+                                                         p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff,
+                                                         w.ctr, w.gc, uint32_t(w.nBlk), p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
@@ -1311,7 +1188,12 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.tau = snap_tau(p);
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
-    if (cudaMemsetAsync(w.ctr, 0, zeroed_bytes(w.nBlk, w.nTile), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cudaMemsetAsync(w.ctr, 0, zeroed_bytes(w.nBlk), st) != cudaSuccess) return ISO_ERR_CUDA;
+    {
+        iso::ProfScope ps("mc_signs", st);
+        mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
     const int rc = launch_count_emit(p, g, w, st);
     if (rc) return rc;
     return 0;
