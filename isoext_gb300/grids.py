@@ -108,7 +108,17 @@ class UniformGrid(Grid):
         return self._values.clone()
 
     def set_values(self, new_values: torch.Tensor) -> None:
-        _check_cuda_f32(new_values, ndim=3, what="new_values")
+        """Copy new values [sx, sy, sz] float32 into the grid.
+
+        isoext takes a CUDA tensor only.  Here a C-contiguous float32 host
+        tensor is also accepted and copied straight into the grid's device
+        storage (one H2D copy, at full speed from pinned memory); the call
+        returns once the copy is done."""
+        if isinstance(new_values, torch.Tensor) and not new_values.is_cuda:
+            if new_values.dtype != torch.float32 or not new_values.is_contiguous() or new_values.dim() != 3:
+                raise TypeError("new_values must be a C-contiguous float32 tensor with 3 dimensions")
+        else:
+            _check_cuda_f32(new_values, ndim=3, what="new_values")
         if list(new_values.shape) != self.shape:
             raise RuntimeError("Cannot set values with different shapes")
         self._values.copy_(new_values)

@@ -183,3 +183,18 @@ def test_mc_far_offset_box(oracle):
     check(oracle, vals, lo=(1000.0, -500.0, 2.0), hi=(1001.0, -499.5, 2.001), what="far box")
     check(oracle, sphere((30, 30, 30), 0.3) * 1e-3, lo=(1000.0, 1000.0, 1000.0),
           hi=(1000.002, 1000.002, 1000.002), what="far sphere")
+
+
+def test_set_values_from_host_tensors():
+    vals = sphere((20, 21, 22), 0.6)
+    ref = iso.UniformGrid([20, 21, 22])
+    ref.set_values(torch.from_numpy(vals).cuda())
+    for host in (torch.from_numpy(vals), torch.from_numpy(vals).pin_memory()):
+        g = iso.UniformGrid([20, 21, 22])
+        g.set_values(host)
+        assert torch.equal(g.get_values(), ref.get_values())
+    g = iso.UniformGrid([20, 21, 22])
+    with pytest.raises(TypeError):
+        g.set_values(torch.from_numpy(vals).double())
+    with pytest.raises(RuntimeError, match="different shapes"):
+        g.set_values(torch.zeros((20, 21, 23)))
