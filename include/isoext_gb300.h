@@ -62,12 +62,6 @@ int iso_profile_enable(int on);
 void iso_profile_reset(void);
 int iso_profile_read(const char *kernel, long long *launches, double *total_ms);
 
-/* Copy bytes from src to dst on the stream with a kernel (no counterpart in
- * isoext).  Either side may be pinned host memory, which the GPU addresses
- * directly; reading it with the SMs is faster than one copy-engine transfer on
- * a Grace-Blackwell node.  Both addresses 16-byte aligned, or bytes <= 1 MiB. */
-int iso_copy(void *dst, const void *src, long long bytes, void *stream);
-
 /* Workspace bytes iso_mc_dense needs for a grid and output capacities. */
 size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
                                    long long face_capacity);

@@ -34,7 +34,6 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_abi_version.restype = _i
     lib.iso_mc_set_config.argtypes = [_i]
     lib.iso_mc_get_config.argtypes = [C.POINTER(_i)]
-    lib.iso_copy.argtypes = [_vp, _vp, _ll, _vp]
     lib.iso_profile_enable.argtypes = [_i]
     lib.iso_profile_reset.restype = None
     lib.iso_profile_read.argtypes = [C.c_char_p, C.POINTER(_ll), C.POINTER(C.c_double)]

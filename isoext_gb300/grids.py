@@ -49,20 +49,6 @@ def grid_positions(index: torch.Tensor, n: int, amin: float, size: float) -> tor
         torch.tensor(amin, dtype=torch.float32, device=index.device)
 
 
-def _copy_from_pinned(dst: torch.Tensor, src: torch.Tensor) -> None:
-    """dst (device) <- src (pinned host) by the SMs, which read pinned memory
-    over the CPU-GPU link faster than one copy-engine transfer; synchronous."""
-    import ctypes as C
-
-    from . import _ffi
-
-    lib = _ffi.lib()
-    st = torch.cuda.current_stream(dst.device)
-    _ffi.check(lib.iso_copy(C.c_void_p(dst.data_ptr()), C.c_void_p(src.data_ptr()), src.numel() * src.element_size(),
-                            C.c_void_p(st.cuda_stream)))
-    st.synchronize()
-
-
 class Grid:
     """Common base of UniformGrid and SparseGrid (isoext ``Grid``)."""
 
@@ -135,10 +121,7 @@ class UniformGrid(Grid):
             _check_cuda_f32(new_values, ndim=3, what="new_values")
         if list(new_values.shape) != self.shape:
             raise RuntimeError("Cannot set values with different shapes")
-        if not new_values.is_cuda and new_values.is_pinned():
-            _copy_from_pinned(self._values, new_values)
-        else:
-            self._values.copy_(new_values)
+        self._values.copy_(new_values)
 
     def get_cells(self) -> torch.Tensor:
         """8 corner point ids per cell (Morton order), [sx-1, sy-1, sz-1, 8]."""
