@@ -221,7 +221,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
         # The timed region lasts milliseconds, shorter than the sampler's period:
         # keep the GPU busy with the same step for ~0.6 s first, so the clock
         # samples are taken under this load (they run on through the timed region).
-        t_end = time.perf_counter() + 0.6
+        t_end = time.perf_counter() + (0.0 if args.quick else 0.6)
         while time.perf_counter() < t_end:
             for _ in range(50):
                 step()
@@ -374,7 +374,7 @@ def run_grad(args, wl, rank, world) -> dict | None:
         step()
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
-        t_end = time.perf_counter() + 0.6
+        t_end = time.perf_counter() + (0.0 if args.quick else 0.6)
         while time.perf_counter() < t_end:
             step()
         torch.cuda.synchronize()
@@ -515,7 +515,7 @@ def run_sparse(args, wl, rank, world) -> dict | None:
         iso.marching_cubes(grid)
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
-        t_end = time.perf_counter() + 0.6
+        t_end = time.perf_counter() + (0.0 if args.quick else 0.6)
         while time.perf_counter() < t_end:
             iso.marching_cubes(grid)
         torch.cuda.synchronize()
@@ -748,7 +748,7 @@ def run_dc(args, wl, rank, world) -> dict | None:
         step()
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
-        t_end = time.perf_counter() + 0.6
+        t_end = time.perf_counter() + (0.0 if args.quick else 0.6)
         while time.perf_counter() < t_end:
             step()
         torch.cuda.synchronize()
@@ -1040,6 +1040,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="no load phase before the timed region (for profiler runs; clocks are not sampled under load)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
