@@ -141,69 +141,108 @@ __device__ __forceinline__ void apply_pinv(const float w[3], const float q[3][3]
 
 // QEF of a cell: normal equations of the crossings' planes plus reg times the
 // distance to their mean point, accumulated as src/dc.cu:26-62 does (each
-// operation rounded); solved by the pseudo-inverse of the 3x3 system with the
-// threshold svd_tol * largest singular value (src/batched_la.cu:152-178), from
-// an FP32 eigen-decomposition refined once with an FP64 residual.
+// operation rounded, crossings in order); solved by the pseudo-inverse of the
+// 3x3 system with the threshold svd_tol * largest singular value
+// (src/batched_la.cu:152-178), from an FP32 eigen-decomposition refined once
+// with an FP64 residual.
 struct Qef {
-    float ata[9], atb[3];  // the system (reg included)
+    float ata[9], atb[3];  // the system (reg included after qef_finish)
+    float px, py, pz;      // sum of the points
     float w[3], q[3][3];   // its eigenvalues and eigenvectors (columns)
     unsigned keep;         // eigenvalues above the threshold
     double x[3];           // the solution before clipping
 };
 
-__device__ __forceinline__ void qef_solve(const float* points, const float* normals, uint32_t K, float reg,
-                                          float svd_tol, Qef& Q) {
+__device__ __forceinline__ void qef_init(Qef& Q) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Q.ata[i] = 0.0f;
+    Q.atb[0] = Q.atb[1] = Q.atb[2] = 0.0f;
+    Q.px = Q.py = Q.pz = 0.0f;
+}
+
+// One crossing: point (qx, qy, qz), normal (nx, ny, nz).
+__device__ __forceinline__ void qef_add(Qef& Q, float qx, float qy, float qz, float nx, float ny, float nz) {
+    const float d = __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
+    Q.px = __fadd_rn(Q.px, qx);
+    Q.py = __fadd_rn(Q.py, qy);
+    Q.pz = __fadd_rn(Q.pz, qz);
+    const float n3[3] = {nx, ny, nz};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Q.ata[3 * i + j] = __fadd_rn(Q.ata[3 * i + j], __fmul_rn(n3[i], n3[j]));
+    Q.atb[0] = __fadd_rn(Q.atb[0], __fmul_rn(nx, d));
+    Q.atb[1] = __fadd_rn(Q.atb[1], __fmul_rn(ny, d));
+    Q.atb[2] = __fadd_rn(Q.atb[2], __fmul_rn(nz, d));
+}
+
+// The regularisation, the eigen-decomposition and the solution of K crossings.
+__device__ __forceinline__ void qef_finish(Qef& Q, uint32_t K, float reg, float svd_tol) {
     float* ata = Q.ata;
     float* atb = Q.atb;
-    for (int i = 0; i < 9; ++i) ata[i] = 0.0f;
-    atb[0] = atb[1] = atb[2] = 0.0f;
-    float px = 0.0f, py = 0.0f, pz = 0.0f;
-    for (uint32_t k = 0; k < K; ++k) {
-        const float nx = normals[3 * k], ny = normals[3 * k + 1], nz = normals[3 * k + 2];
-        const float qx = points[3 * k], qy = points[3 * k + 1], qz = points[3 * k + 2];
-        const float d = __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
-        px = __fadd_rn(px, qx); py = __fadd_rn(py, qy); pz = __fadd_rn(pz, qz);
-        const float n3[3] = {nx, ny, nz};
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) ata[3 * i + j] = __fadd_rn(ata[3 * i + j], __fmul_rn(n3[i], n3[j]));
-        atb[0] = __fadd_rn(atb[0], __fmul_rn(nx, d));
-        atb[1] = __fadd_rn(atb[1], __fmul_rn(ny, d));
-        atb[2] = __fadd_rn(atb[2], __fmul_rn(nz, d));
-    }
     const float cnt = __uint2float_rn(K);
-    px = __fdiv_rn(px, cnt); py = __fdiv_rn(py, cnt); pz = __fdiv_rn(pz, cnt);
+    const float px = __fdiv_rn(Q.px, cnt), py = __fdiv_rn(Q.py, cnt), pz = __fdiv_rn(Q.pz, cnt);
     ata[0] = __fadd_rn(ata[0], reg); ata[4] = __fadd_rn(ata[4], reg); ata[8] = __fadd_rn(ata[8], reg);
     atb[0] = __fadd_rn(atb[0], __fmul_rn(reg, px));
     atb[1] = __fadd_rn(atb[1], __fmul_rn(reg, py));
     atb[2] = __fadd_rn(atb[2], __fmul_rn(reg, pz));
     // pseudo-inverse solve: singular values of the symmetric system are |w|
     float m[3][3];
-    float* w = Q.w;
-    float(*q)[3] = Q.q;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) m[i][j] = ata[3 * i + j];
-    jacobi3f(m, w, q);
-    const float smax = fmaxf(fabsf(w[0]), fmaxf(fabsf(w[1]), fabsf(w[2])));
+    jacobi3f(m, Q.w, Q.q);
+    const float smax = fmaxf(fabsf(Q.w[0]), fmaxf(fabsf(Q.w[1]), fabsf(Q.w[2])));
     const float thr = svd_tol * smax;
     unsigned keep = 0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) keep |= (fabsf(w[i]) > thr ? 1u : 0u) << i;
+    for (int i = 0; i < 3; ++i) keep |= (fabsf(Q.w[i]) > thr ? 1u : 0u) << i;
     Q.keep = keep;
     double* x = Q.x;
     x[0] = x[1] = x[2] = 0.0;
     double r[3] = {atb[0], atb[1], atb[2]};
-    apply_pinv(w, q, keep, r, x);
+    apply_pinv(Q.w, Q.q, keep, r, x);
     // one refinement step with an FP64 residual (the FP32 eigenvectors leave
     // an error of about cond(A) * eps; the residual recovers it)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
         r[i] = double(atb[i]) - (double(ata[3 * i]) * x[0] + double(ata[3 * i + 1]) * x[1] +
                                  double(ata[3 * i + 2]) * x[2]);
-    apply_pinv(w, q, keep, r, x);
+    apply_pinv(Q.w, Q.q, keep, r, x);
+}
+
+// The QEF of K crossings stored as points [K, 3] and normals [K, 3].
+__device__ __forceinline__ void qef_solve(const float* points, const float* normals, uint32_t K, float reg,
+                                          float svd_tol, Qef& Q) {
+    qef_init(Q);
+    for (uint32_t k = 0; k < K; ++k)
+        qef_add(Q, points[3 * k], points[3 * k + 1], points[3 * k + 2], normals[3 * k], normals[3 * k + 1],
+                normals[3 * k + 2]);
+    qef_finish(Q, K, reg, svd_tol);
+}
+
+// Crossing of edge e of a cell: t and the point (the reference's lerp).  The
+// edge's corners are selected, not indexed, so the cell stays in registers when
+// e is not a constant.
+__device__ __forceinline__ float edge_cross(const CellCorners& cc, float level, int e, float* p) {
+    const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
+    float va = cc.v[0], vb = cc.v[0], pa[3] = {cc.p[0][0], cc.p[0][1], cc.p[0][2]}, pb[3] = {pa[0], pa[1], pa[2]};
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+        if (j == ca) {
+            va = cc.v[j];
+            pa[0] = cc.p[j][0]; pa[1] = cc.p[j][1]; pa[2] = cc.p[j][2];
+        }
+        if (j == cb) {
+            vb = cc.v[j];
+            pb[0] = cc.p[j][0]; pb[1] = cc.p[j][1]; pb[2] = cc.p[j][2];
+        }
+    }
+    const float t = iso::cross_t(level, va, vb);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, pa[q], pb[q]);
+    return t;
 }
 
 Grid3 make_grid(int nx, int ny, int nz, const float* amin, const float* amax) {

@@ -20,9 +20,9 @@
 #include <cstdint>
 
 #include "common.cuh"
-#include "dc_common.cuh"
 #define ISO_LUT_DECL static __constant__ const
 #include "luts.h"
+#include "dc_common.cuh"
 #include "profile.cuh"
 
 namespace {
@@ -239,13 +239,11 @@ __global__ void __launch_bounds__(128) dc_points(const float* __restrict__ vals,
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
     const uint32_t est = ISO_EDGE_STATUS[cs];
     unsigned long long k = cell_off[a];
+#pragma unroll 1
     for (int e = 0; e < 12; ++e) {
         if (!((est >> e) & 1u)) continue;
-        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
         float p[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
+        edge_cross(cc, level, e, p);
         points[3 * k + 0] = p[0];
         points[3 * k + 1] = p[1];
         points[3 * k + 2] = p[2];
@@ -301,19 +299,19 @@ __global__ void __launch_bounds__(128) dc_cell_solve(const float* __restrict__ v
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
     const uint32_t est = ISO_EDGE_STATUS[cs];
-    float pk[12][3], nk[12][3];
+    Qef Q;
+    qef_init(Q);
     uint32_t K = 0;
+#pragma unroll 1
     for (int e = 0; e < 12; ++e) {
         if (!((est >> e) & 1u)) continue;
-        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) pk[K][q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
-        cell_normal(cc, pk[K], nk[K]);
+        float p[3], n[3];
+        edge_cross(cc, level, e, p);
+        cell_normal(cc, p, n);
+        qef_add(Q, p[0], p[1], p[2], n[0], n[1], n[2]);
         ++K;
     }
-    Qef Q;
-    qef_solve(&pk[0][0], &nk[0][0], K, reg, svd_tol, Q);
+    qef_finish(Q, K, reg, svd_tol);
     const int ci[3] = {cx, cy, cz};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {

@@ -45,13 +45,16 @@ struct Cell8 {
     float p[8][3];
 };
 
-__device__ __forceinline__ void load_cell(const SpGrid& g, const int* ids, const float* vals, long long c,
-                                          Cell8& cc, int& x, int& y, int& z) {
-    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+// The 8 values of cell c (two 16-byte loads).
+__device__ __forceinline__ void load_vals(const float* vals, long long c, Cell8& cc) {
     const float4* v4 = reinterpret_cast<const float4*>(vals + 8 * c);
     const float4 a = __ldg(v4), b = __ldg(v4 + 1);
     cc.v[0] = a.x; cc.v[1] = a.y; cc.v[2] = a.z; cc.v[3] = a.w;
     cc.v[4] = b.x; cc.v[5] = b.y; cc.v[6] = b.z; cc.v[7] = b.w;
+}
+
+// Corner positions of cell (x, y, z) (include/utils.cuh:62-80).
+__device__ __forceinline__ void set_coords(const SpGrid& g, int x, int y, int z, Cell8& cc) {
     const float cx0 = iso::grid_coord(x, g.nx, g.amin[0], g.asize[0]);
     const float cx1 = iso::grid_coord(x + 1, g.nx, g.amin[0], g.asize[0]);
     const float cy0 = iso::grid_coord(y, g.ny, g.amin[1], g.asize[1]);
@@ -64,6 +67,29 @@ __device__ __forceinline__ void load_cell(const SpGrid& g, const int* ids, const
         cc.p[k][1] = ((k >> 1) & 1) ? cy1 : cy0;
         cc.p[k][2] = (k & 1) ? cz1 : cz0;
     }
+}
+
+__device__ __forceinline__ void load_cell(const SpGrid& g, const int* ids, const float* vals, long long c,
+                                          Cell8& cc, int& x, int& y, int& z) {
+    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+    load_vals(vals, c, cc);
+    set_coords(g, x, y, z, cc);
+}
+
+// Values and case of cell c; positions only for a cell the surface crosses
+// (most cells of a band are empty).
+__device__ __forceinline__ uint32_t load_active(const SpGrid& g, const int* ids, const float* vals, long long c,
+                                                Cell8& cc) {
+    load_vals(vals, c, cc);
+    uint32_t cs = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cs |= (iso::below(cc.v[k], g.level) ? 1u : 0u) << k;
+    if (cs != 0 && cs != 255) {
+        int x, y, z;
+        cell_xyz(g, uint32_t(ids[c]), x, y, z);
+        set_coords(g, x, y, z, cc);
+    }
+    return cs;
 }
 
 __device__ __forceinline__ uint32_t case_of(const Cell8& cc, float level) {
@@ -143,10 +169,11 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_count(SpGrid g, const int* __r
     uint32_t nf = 0;
     if (c < n) {
         Cell8 cc;
-        int x, y, z;
-        load_cell(g, ids, vals, c, cc, x, y, z);
-        float ev[12][3];
-        nf = mc_cell(g, cc, ev);
+        const uint32_t cs = load_active(g, ids, vals, c, cc);
+        if (cs != 0 && cs != 255) {
+            float ev[12][3];
+            nf = mc_cell(g, cc, ev);
+        }
     }
     uint32_t e, t;
     block_scan1(nf, e, t, sm);
@@ -164,10 +191,8 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __re
     float ev[12][3];
     uint32_t cs = 0;
     if (c < n) {
-        int x, y, z;
-        load_cell(g, ids, vals, c, cc, x, y, z);
-        nf = mc_cell(g, cc, ev);
-        cs = case_of(cc, g.level);
+        cs = load_active(g, ids, vals, c, cc);
+        if (cs != 0 && cs != 255) nf = mc_cell(g, cc, ev);
     }
     uint32_t e, t;
     block_scan1(nf, e, t, sm);
