@@ -133,7 +133,7 @@ __device__ void normal_backward(const CellCorners& cc, const float* p, const flo
     for (int b = 0; b < 3; ++b) gp[b] += gt[b] * tin[b] / csz[b];
 }
 
-__global__ void __launch_bounds__(128, 4) dc_backward(const float* __restrict__ vals, Grid3 g, float level,
+__global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ vals, Grid3 g, float level,
                                                    const uint32_t* __restrict__ cell_ids,
                                                    const uint32_t* __restrict__ cell_off, long long A,
                                                    float reg, float svd_tol,
@@ -149,32 +149,35 @@ __global__ void __launch_bounds__(128, 4) dc_backward(const float* __restrict__ 
     const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
     CellCorners cc;
     load_cell(vals, g, cx, cy, cz, cc);
-    // the crossings in the forward's order (edges of the case, ascending): the
-    // QEF is accumulated as the forward does, and each crossing is recomputed
-    // (same arithmetic) on the way back
+    // the crossings in the forward's order (edges of the case, ascending)
     uint32_t cs = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
     const uint32_t est = ISO_EDGE_STATUS[cs];
-    const uint32_t k0 = cell_off[a];
-    Qef Q;
-    qef_init(Q);
-    uint32_t K = 0;
-#pragma unroll 1
+    float pk[12][3], nk[12][3], tk[12];
+    int ek[12];
+    int K = 0;
     for (int e = 0; e < 12; ++e) {
         if (!((est >> e) & 1u)) continue;
-        float p[3], n[3];
-        edge_cross(cc, level, e, p);
-        if (user_normals) {
+        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
+        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
 #pragma unroll
-            for (int q = 0; q < 3; ++q) n[q] = user_normals[3ll * (k0 + K) + q];
-        } else {
-            cell_normal(cc, p, n);
-        }
-        qef_add(Q, p[0], p[1], p[2], n[0], n[1], n[2]);
+        for (int q = 0; q < 3; ++q) pk[K][q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
+        tk[K] = t;
+        ek[K] = e;
         ++K;
     }
-    qef_finish(Q, K, reg, svd_tol);
+    const uint32_t k0 = cell_off[a];
+    for (int k = 0; k < K; ++k) {
+        if (user_normals) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) nk[k][q] = user_normals[3ll * (k0 + k) + q];
+        } else {
+            cell_normal(cc, pk[k], nk[k]);
+        }
+    }
+    Qef Q;
+    qef_solve(&pk[0][0], &nk[0][0], uint32_t(K), reg, svd_tol, Q);
     const int ci[3] = {cx, cy, cz};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -188,26 +191,16 @@ __global__ void __launch_bounds__(128, 4) dc_backward(const float* __restrict__ 
     const float l[3] = {float(lam[0]), float(lam[1]), float(lam[2])};
     const float rk = reg / float(K);
     float gc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    uint32_t k = 0;
-#pragma unroll 1
-    for (int e = 0; e < 12; ++e) {
-        if (!((est >> e) & 1u)) continue;
-        float p[3], n[3], u[3], gn[3], gp[3];
-        const float t = edge_cross(cc, level, e, p);
-        if (user_normals) {
+    for (int k = 0; k < K; ++k) {
+        float u[3], gn[3], gp[3];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) n[q] = user_normals[3ll * (k0 + k) + q];
-        } else {
-            cell_normal(cc, p, n);
-        }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) u[q] = float(double(p[q]) - Q.x[q]);
-        const float ln = l[0] * n[0] + l[1] * n[1] + l[2] * n[2];
-        const float nu = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
+        for (int q = 0; q < 3; ++q) u[q] = float(double(pk[k][q]) - Q.x[q]);
+        const float ln = l[0] * nk[k][0] + l[1] * nk[k][1] + l[2] * nk[k][2];
+        const float nu = nk[k][0] * u[0] + nk[k][1] * u[1] + nk[k][2] * u[2];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             gn[q] = l[q] * nu + u[q] * ln;
-            gp[q] = n[q] * ln + rk * l[q];
+            gp[q] = nk[k][q] * ln + rk * l[q];
         }
         if (user_normals) {
             if (gnormals) {
@@ -215,32 +208,16 @@ __global__ void __launch_bounds__(128, 4) dc_backward(const float* __restrict__ 
                 for (int q = 0; q < 3; ++q) gnormals[3ll * (k0 + k) + q] = gn[q];
             }
         } else {
-            normal_backward(cc, p, gn, gp, gc);
+            normal_backward(cc, pk[k], gn, gp, gc);
         }
-        ++k;
-        // the edge's two corners by selection (a dynamic index would put the
-        // cell's arrays in local memory)
-        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-        float va = cc.v[0], vb = cc.v[0], pa[3] = {cc.p[0][0], cc.p[0][1], cc.p[0][2]}, pb[3] = {pa[0], pa[1], pa[2]};
-#pragma unroll
-        for (int j = 1; j < 8; ++j) {
-            if (j == ca) {
-                va = cc.v[j];
-                pa[0] = cc.p[j][0]; pa[1] = cc.p[j][1]; pa[2] = cc.p[j][2];
-            }
-            if (j == cb) {
-                vb = cc.v[j];
-                pb[0] = cc.p[j][0]; pb[1] = cc.p[j][1]; pb[2] = cc.p[j][2];
-            }
-        }
-        const float d = vb - va;
+        const int ca = ISO_EDGE_CORNERS[2 * ek[k]], cb = ISO_EDGE_CORNERS[2 * ek[k] + 1];
+        const float d = cc.v[cb] - cc.v[ca];
         if (d == 0.0f) continue;
         float gt = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) gt += gp[q] * (pb[q] - pa[q]);
-        const float ga = -gt * (1.0f - t) / d, gb = -gt * t / d;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) gc[j] += (j == ca ? ga : 0.0f) + (j == cb ? gb : 0.0f);
+        for (int q = 0; q < 3; ++q) gt += gp[q] * (cc.p[cb][q] - cc.p[ca][q]);
+        gc[ca] -= gt * (1.0f - tk[k]) / d;
+        gc[cb] -= gt * tk[k] / d;
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
