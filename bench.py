@@ -213,6 +213,9 @@ def run_ours(args, wl, rank, world) -> dict | None:
     algo_bytes = 4 * n ** 3 + 12 * nv + 12 * nf
     kbytes = kernel_bytes("mc", n, nv, nf)
     kernels = list(kbytes)
+    # launch parameters for this GPU and grid (isoext_gb300.tune), before timing
+    from isoext_gb300 import tune
+    tuned = tune.autotune(grid, kinds=("mc",), repeats=10)
 
     for _ in range(args.warmup):
         step()
@@ -296,6 +299,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
         "data": "synthetic: sphere SDF |p|-0.8 on [-1,1]^3",
         "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "method": "nagae",
                    "vertices": nv, "faces": nf, "parallelism": f"replicas x{world}",
+                   "tuned": {k: v for k, v in tuned["best"].items() if k.startswith("mc.")},
                    "l2": f"inputs larger than L2 (values {4 * n ** 3 / 1e6:.0f} MB > 129 MB L2)"
                          if 4 * n ** 3 > 129e6 else "inputs smaller than L2 (not flushed)"},
         "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",

@@ -53,6 +53,15 @@ int iso_abi_version(void);
 int iso_mc_set_config(int threads);
 int iso_mc_get_config(int *threads);
 
+/* Launch parameters for the autotuner (isoext_gb300.tune; process-wide; no
+ * counterpart in the reference).  Keys and values:
+ *   "mc.emit_threads"     128 | 256   threads per CTA of the MC emit kernel
+ *   "mc.sign_ctas_per_sm" 1 .. 64     CTAs per SM of the sign pass (MC and DC)
+ *   "dc.cell_threads"     64 | 128 | 256  threads per CTA of the per-cell DC kernels
+ * Results do not depend on them. */
+int iso_tune_set(const char *key, int value);
+int iso_tune_get(const char *key, int *value);
+
 /* Kernel timing for benchmarks (no counterpart in the reference).  While
  * enabled, each kernel the library launches is bracketed by CUDA events on its
  * stream.  iso_profile_read synchronises on the recorded events and returns the

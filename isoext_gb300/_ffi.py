@@ -34,6 +34,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_abi_version.restype = _i
     lib.iso_mc_set_config.argtypes = [_i]
     lib.iso_mc_get_config.argtypes = [C.POINTER(_i)]
+    lib.iso_tune_set.argtypes = [C.c_char_p, _i]
+    lib.iso_tune_get.argtypes = [C.c_char_p, C.POINTER(_i)]
     lib.iso_profile_enable.argtypes = [_i]
     lib.iso_profile_reset.restype = None
     lib.iso_profile_read.argtypes = [C.c_char_p, C.POINTER(_ll), C.POINTER(C.c_double)]

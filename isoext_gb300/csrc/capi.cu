@@ -4,6 +4,7 @@
 // asynchronously on that stream, and returns an IsoStatus for argument / launch
 // errors.  Errors found on the device (bounded waits that ran out, output
 // capacity exceeded) are written to the caller's device status word.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -28,6 +29,11 @@ bool grid_ok(int nx, int ny, int nz) {
 namespace iso {
 // Message iso_last_error returns on this thread (for entry points in other files).
 void set_last_error(const char* msg) { g_err = msg; }
+
+// Tunables: sign-pass CTAs per SM (MC and DC sign bitmaps), threads per block of
+// the per-active-cell DC kernels.
+std::atomic<int> g_tune[TUNE_KEYS] = {{32}, {128}};
+int tune_get(int key) { return key >= 0 && key < TUNE_KEYS ? g_tune[key].load(std::memory_order_relaxed) : 0; }
 }  // namespace iso
 
 extern "C" {
@@ -43,6 +49,34 @@ int iso_mc_set_config(int threads) {
 
 int iso_mc_get_config(int* threads) {
     if (threads) *threads = mc_get_block();
+    return ISO_OK;
+}
+
+int iso_tune_set(const char* key, int value) {
+    if (!key) return fail(ISO_ERR_ARG, "iso_tune_set: key is null");
+    if (!strcmp(key, "mc.emit_threads")) {
+        if (mc_set_block(value)) return fail(ISO_ERR_ARG, "mc.emit_threads must be 128 or 256");
+        return ISO_OK;
+    }
+    if (!strcmp(key, "mc.sign_ctas_per_sm")) {
+        if (value < 1 || value > 64) return fail(ISO_ERR_ARG, "mc.sign_ctas_per_sm must be 1 .. 64");
+        iso::g_tune[iso::TUNE_MC_SIGN_CTAS] = value;
+        return ISO_OK;
+    }
+    if (!strcmp(key, "dc.cell_threads")) {
+        if (value != 64 && value != 128 && value != 256) return fail(ISO_ERR_ARG, "dc.cell_threads must be 64, 128 or 256");
+        iso::g_tune[iso::TUNE_DC_CELL_THREADS] = value;
+        return ISO_OK;
+    }
+    return fail(ISO_ERR_ARG, "iso_tune_set: unknown key");
+}
+
+int iso_tune_get(const char* key, int* value) {
+    if (!key || !value) return fail(ISO_ERR_ARG, "iso_tune_get: null argument");
+    if (!strcmp(key, "mc.emit_threads")) *value = mc_get_block();
+    else if (!strcmp(key, "mc.sign_ctas_per_sm")) *value = iso::tune_get(iso::TUNE_MC_SIGN_CTAS);
+    else if (!strcmp(key, "dc.cell_threads")) *value = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+    else return fail(ISO_ERR_ARG, "iso_tune_get: unknown key");
     return ISO_OK;
 }
 

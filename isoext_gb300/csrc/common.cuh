@@ -165,4 +165,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
+// ---------------------------------------------------------------------------
+// Launch parameters the autotuner may change (process-wide; iso_tune_set).
+
+enum TuneKey { TUNE_MC_SIGN_CTAS = 0, TUNE_DC_CELL_THREADS = 1, TUNE_KEYS = 2 };
+int tune_get(int key);
+
 }  // namespace iso

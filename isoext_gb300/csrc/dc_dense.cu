@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict
 
 // Crossing points (lerp with the reference's arithmetic) and optional normals of
 // each active cell's crossed edges, in edge order (src/its.cu:94-159, 186-268).
-__global__ void __launch_bounds__(128) dc_points(const float* __restrict__ vals, Grid3 g, float level,
+__global__ void __launch_bounds__(256) dc_points(const float* __restrict__ vals, Grid3 g, float level,
                                                  const uint32_t* __restrict__ cell_ids,
                                                  const uint32_t* __restrict__ cell_off, long long A,
                                                  float* __restrict__ points, float* __restrict__ normals) {
@@ -284,7 +284,7 @@ __global__ void dc_normals(const float* __restrict__ vals, Grid3 g, const float*
 // Crossings, grid normals and the QEF solve of each active cell in one pass,
 // when nobody asked for the intersection: the same arithmetic as dc_points
 // followed by dc_solve, without writing points and normals.
-__global__ void __launch_bounds__(128) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
+__global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
                                                      float svd_tol, float* __restrict__ dual) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -660,7 +660,8 @@ int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* a
         reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
     if (A == 0 && cell_offsets) cudaMemsetAsync(cell_offsets, 0, 4, st);
     if (A > 0 && points)
-        dc_points<<<blocks_for(A, 128), 128, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids),
+        dc_points<<<blocks_for(A, iso::tune_get(iso::TUNE_DC_CELL_THREADS)), iso::tune_get(iso::TUNE_DC_CELL_THREADS), 0,
+                    st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids),
                                                       reinterpret_cast<uint32_t*>(cell_offsets), A, points,
                                                       normals);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -683,7 +684,8 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
             reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
     }
     iso::ProfScope ps("dc_solve", st);
-    dc_cell_solve<<<blocks_for(A, 128), 128, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
+    const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+    dc_cell_solve<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
                                                       reg, svd_tol, dual);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
@@ -709,7 +711,8 @@ int iso_dc_solve(int nx, int ny, int nz, const float* aabb_min, const float* aab
     if (A <= 0) return 0;
     Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     iso::ProfScope ps("dc_solve", st);
-    dc_solve<<<blocks_for(A, 128), 128, 0, st>>>(points, normals, reinterpret_cast<const uint32_t*>(cell_ids),
+    const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+    dc_solve<<<blocks_for(A, bt), bt, 0, st>>>(points, normals, reinterpret_cast<const uint32_t*>(cell_ids),
                                                  reinterpret_cast<const uint32_t*>(cell_offsets), A, g, reg,
                                                  svd_tol, dual);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;

@@ -1144,7 +1144,8 @@ void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uin
                      cudaStream_t st) {
     const long long rows = (long long)nx * ny;
     const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
-    const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sm_count() * 32));
+    const long long per = iso::tune_get(iso::TUNE_MC_SIGN_CTAS);
+    const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sm_count() * per));
     mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, rows, nz, level, out);
 }
 

@@ -47,3 +47,21 @@ def test_unknown_method_message():
 
     with pytest.raises(RuntimeError, match="Unknown method: foo"):
         iso.mc.method_id("foo")
+
+
+def test_tunables_roundtrip_and_reject_bad_values():
+    from isoext_gb300 import _ffi, tune
+
+    lib = _ffi.lib()
+    old = tune.current()
+    assert set(old) == set(tune.KNOBS)
+    for key, values in tune.KNOBS.items():
+        for v in values:
+            tune.set(key, v)
+            assert tune.get(key) == v
+    assert lib.iso_tune_set(b"mc.emit_threads", 100) == 1
+    assert lib.iso_tune_set(b"dc.cell_threads", 96) == 1
+    assert lib.iso_tune_set(b"mc.sign_ctas_per_sm", 0) == 1
+    assert lib.iso_tune_set(b"no.such.key", 1) == 1 and "unknown" in _ffi.last_error()
+    tune.apply(old)
+    assert tune.current() == old

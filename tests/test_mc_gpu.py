@@ -198,3 +198,27 @@ def test_set_values_from_host_tensors():
         g.set_values(torch.from_numpy(vals).double())
     with pytest.raises(RuntimeError, match="different shapes"):
         g.set_values(torch.zeros((20, 21, 23)))
+
+
+def test_launch_parameters_do_not_change_results():
+    """Every value of every autotuner knob gives the same meshes (MC and DC)."""
+    from isoext_gb300 import tune
+
+    vals = sphere((70, 65, 90), 0.55) + 0.02 * noise((70, 65, 90), seed=2)
+    g = iso.UniformGrid(list(vals.shape))
+    g.set_values(torch.from_numpy(vals.astype(np.float32)).cuda())
+    old = tune.current()
+    try:
+        ref_mc, ref_dc = iso.marching_cubes(g), iso.dual_contouring(g)
+        for key, values in tune.KNOBS.items():
+            for v in values:
+                tune.set(key, v)
+                mc, dc = iso.marching_cubes(g), iso.dual_contouring(g)
+                assert torch.equal(mc[0], ref_mc[0]) and torch.equal(mc[1], ref_mc[1]), (key, v)
+                assert torch.equal(dc[0], ref_dc[0]) and torch.equal(dc[1], ref_dc[1]), (key, v)
+            tune.set(key, old[key])
+        rep = tune.autotune(g, repeats=3)
+        assert all(rep["best"][k] in tune.KNOBS[k] for k in tune.KNOBS)
+        assert tune.current() == rep["best"]
+    finally:
+        tune.apply(old)
