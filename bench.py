@@ -672,7 +672,7 @@ def run_serve(args, wl, rank) -> dict | None:
     gaps = rng.exponential(1.0, size=len(reqs))
     srv = serve.Server(slots=wl["slots"], budget_bytes=int(wl["budget_gb"] * (1 << 30)), device=dev)
     t_cap = time.perf_counter()
-    srv.warmup(sizes)
+    tuned = srv.warmup(sizes)
     t_cap = time.perf_counter() - t_cap
     for r in warm:  # first calls of each size on both paths
         serve.solve_plain(r, dev)
@@ -701,7 +701,8 @@ def run_serve(args, wl, rank) -> dict | None:
         "data": "synthetic: seeded unions of 1-16 spheres/boxes (sizes U[0.05,0.4]) on [-1,1]^3",
         "config": {"workload": wl["desc"], "requests": len(reqs), "sizes": list(sizes), "mc": n_mc,
                    "dc": len(reqs) - n_mc, "slots": wl["slots"], "budget_gb": wl["budget_gb"],
-                   "cells_per_stream": cells, "graph_capture_s": round(t_cap, 2),
+                   "cells_per_stream": cells, "warmup_s": round(t_cap, 2),
+                   "tuned": tuned["best"] if tuned else None,
                    "l2": "each request's grid is written and read once; not flushed"},
         "served": {"req_s": round(s_rate, 1), "p50_ms": _pct(served_sat[0][1], 50),
                    "p99_ms": _pct(served_sat[0][1], 99), "gcells_s": round(cells * s_rate / len(reqs) / 1e9, 3),

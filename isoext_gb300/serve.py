@@ -254,13 +254,27 @@ class Server(Scheduler):
         self._lock = threading.Lock()  # graph capture is done one at a time
         super().__init__(slots, budget_bytes, request_bytes, self._execute)
 
-    def warmup(self, sizes, method: str = "nagae", level: float = 0.0) -> None:
-        """Builds every slot's buffers and graphs for the given grid sizes up front."""
+    def warmup(self, sizes, method: str = "nagae", level: float = 0.0, tune: bool = True) -> dict | None:
+        """Builds every slot's buffers and graphs for the given grid sizes up front.
+        With tune, the launch parameters are first tuned (isoext_gb300.tune) on a
+        grid of the largest size, so the captured graphs use them; returns the
+        tuning report."""
         from .mc import method_id
 
+        import torch
+
+        report = None
+        if tune:
+            from . import tune as tuner
+
+            n = int(max(sizes))
+            req = random_requests(1, seed=0, sizes=(n,))[0]
+            prims = torch.from_numpy(prims_buffer(req.prims)).to(self.device)
+            report = _tune_on(n, prims, self.device, level, tuner)
         for slot in range(len(self._streams)):
             for n in sizes:
                 self._mc_slot(slot, int(n), method_id(method), float(level))
+        return report
 
     def _mc_slot(self, slot: int, n: int, method: int, level: float) -> _MCSlot:
         key = ("mc", n, method, level)
@@ -301,6 +315,19 @@ class Server(Scheduler):
             return v, f
         with torch.cuda.stream(stream):
             return _solve_on_stream(req, self._prims_dev[slot], self.device)
+
+
+def _tune_on(n: int, prims_dev, device, level: float, tuner) -> dict:
+    """Tunes the launch parameters on an n^3 grid of the union in prims_dev."""
+    import torch
+
+    from .grids import UniformGrid
+
+    grid = UniformGrid([n] * 3, LO, HI, device=device)
+    s = torch.cuda.current_stream(device).cuda_stream
+    _ffi.check(_ffi.lib().iso_sdf_union_grid(C.c_void_p(prims_dev.data_ptr()), n, n, n, _ffi.fvec3(LO),
+                                             _ffi.fvec3(HI), C.c_void_p(grid._values.data_ptr()), C.c_void_p(s)))
+    return tuner.autotune(grid, level, repeats=5)
 
 
 def _solve_on_stream(req: Request, prims_dev, device):
