@@ -140,6 +140,22 @@ int iso_dc_intersect_solve(const float *values, int nx, int ny, int nz, const fl
                            const float *aabb_max, float level, void *ws, long long A, long long K,
                            int *cell_ids, int *cell_offsets, float reg, float svd_tol, float *dual,
                            void *stream);
+/* Dual contouring in one call with no host synchronisation, the dense path of
+ * isoext_ext.dual_contouring(grid, level, None, reg, svd_tol) (src/dc.cu:162-218
+ * with intersections from the grid, src/its.cu:94-283).  Vertices [V, 3] and
+ * faces [F, 3] as the step-by-step entry points give them (bit for bit).
+ *   vertex_capacity bounds the active cells A (one dual vertex each, V <= A);
+ *   face_capacity the faces F = 2 Q (two per quad).
+ *   counts: device int64[5] <- (V, F, A, K, Q).  When A or F exceed the
+ *   capacities the status is 6 (ISO_ERR_OVERFLOW), nothing is written to the
+ *   outputs, and counts[2..4] give the sizes for a retry.
+ *   workspace: iso_dc_dense_workspace_size bytes.  Capturable in a CUDA graph. */
+size_t iso_dc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
+                                   long long face_capacity);
+int iso_dc_dense(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                 const float *aabb_max, float level, float reg, float svd_tol, float *vertices,
+                 long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
+                 size_t workspace_bytes, long long *counts, int *status, void *stream);
 /* Normals of existing crossings from the grid (src/its.cu:186-268). */
 int iso_dc_normals(const float *values, int nx, int ny, int nz, const float *aabb_min,
                    const float *aabb_max, const float *points, const int *cell_ids,

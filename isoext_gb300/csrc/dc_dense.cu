@@ -177,8 +177,13 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict
                                                          uint32_t* __restrict__ actm,
                                                          uint32_t* __restrict__ offA, float* points,
                                                          float* normals, uint32_t* cell_ids,
-                                                         uint32_t* cell_off, long long A, long long K) {
+                                                         uint32_t* cell_off, long long A, long long K,
+                                                         const long long* __restrict__ dn) {
     __shared__ uint32_t sm[66];
+    if (dn) {  // the sizes on the device (A, K); 0 when they exceeded the capacities
+        A = dn[0];
+        K = dn[1];
+    }
     const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
     const int NWc = (g.nz - 1 + 31) / 32;
     uint32_t act = 0, na = 0, nk = 0;
@@ -208,6 +213,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict
     // active cells of the word: id and the offset of their crossings (values are
     // read by dc_points, one thread per active cell)
     unsigned long long a = a0, k = k0;
+    if (a0 >= (unsigned long long)A) return;
     while (act) {
         const int b = __ffs(act) - 1;
         act &= act - 1;
@@ -286,8 +292,10 @@ __global__ void dc_normals(const float* __restrict__ vals, Grid3 g, const float*
 // followed by dc_solve, without writing points and normals.
 __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
-                                                     float svd_tol, float* __restrict__ dual) {
+                                                     float svd_tol, float* __restrict__ dual,
+                                                     const long long* __restrict__ dn) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dn) A = dn[0];
     if (a >= A) return;
     const uint32_t cid = cell_ids[a];
     const int cz = int(cid % uint32_t(g.nz - 1));
@@ -409,10 +417,13 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
                                                          const uint32_t* __restrict__ actm,
                                                          const uint32_t* __restrict__ offA,
                                                          const float* __restrict__ dual,
-                                                         int32_t* __restrict__ tri) {
+                                                         int32_t* __restrict__ tri,
+                                                         const long long* __restrict__ dn) {
     __shared__ uint32_t sm[66];
     const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
     const int NWg = (g.nz + 31) / 32;
+    // dn: the triangle indices the output holds (6 Q, or 0 over capacity)
+    const unsigned long long qmax = dn ? (unsigned long long)(dn[2] / 6) : ~0ull;
     uint32_t mz = 0, my = 0, mx = 0;
     int x = 0, y = 0, w = 0;
     if (i < nwords) {
@@ -426,6 +437,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
     block_scan2(__popc(mz) + __popc(my) + __popc(mx), 0u, eq, e1, tq, t1, sm);
     if (i >= nwords) return;
     unsigned long long q = blk[2 * blockIdx.x] + eq;
+    if (q + __popc(mz) + __popc(my) + __popc(mx) > qmax) return;
     const uint32_t s = srow(S, g, x, y)[w];
     uint32_t all = mz | my | mx;
     while (all) {
@@ -485,15 +497,19 @@ __device__ __forceinline__ uint32_t pos_hash(uint32_t a, uint32_t b, uint32_t c)
     return h;
 }
 
-__global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint32_t* used) {
+__global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint32_t* used,
+                             const long long* __restrict__ dn) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dn) n = dn[2];
     if (i < n) used[tri[i]] = 1u;
 }
 
 // Insert used vertices; a slot keeps the smallest index with its position.
 __global__ void dc_hash_insert(const float* __restrict__ dual, const uint32_t* __restrict__ used,
-                               long long A, uint32_t* table, uint32_t mask, int* status) {
+                               long long A, uint32_t* table, uint32_t mask, int* status,
+                               const long long* __restrict__ dn) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dn) A = dn[0];
     if (a >= A || !used[a]) return;
     const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
     uint32_t h = pos_hash(k0, k1, k2) & mask;
@@ -513,8 +529,9 @@ __global__ void dc_hash_insert(const float* __restrict__ dual, const uint32_t* _
 // rep[a] = smallest index with the same position (for used vertices).
 __global__ void dc_hash_lookup(const float* __restrict__ dual, const uint32_t* __restrict__ used,
                                long long A, const uint32_t* __restrict__ table, uint32_t mask,
-                               uint32_t* rep) {
+                               uint32_t* rep, const long long* __restrict__ dn) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dn) A = dn[0];
     if (a >= A) return;
     if (!used[a]) { rep[a] = 0xffffffffu; return; }
     const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
@@ -533,9 +550,10 @@ __global__ void dc_hash_lookup(const float* __restrict__ dual, const uint32_t* _
 
 // Per block of 1024 dual vertices: number of representatives (rep[a] == a).
 __global__ void __launch_bounds__(DC_BLOCK) dc_rep_count(const uint32_t* __restrict__ rep, long long A,
-                                                         unsigned long long* blk) {
+                                                         unsigned long long* blk, const long long* __restrict__ dn) {
     __shared__ uint32_t sm[66];
     const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    if (dn) A = dn[0];
     const uint32_t is = (a < A && rep[a] == uint32_t(a)) ? 1u : 0u;
     uint32_t e0, e1, t0, t1;
     block_scan2(is, 0u, e0, e1, t0, t1, sm);
@@ -545,9 +563,10 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_rep_count(const uint32_t* __restr
 __global__ void __launch_bounds__(DC_BLOCK) dc_rep_write(const uint32_t* __restrict__ rep, long long A,
                                                          const unsigned long long* __restrict__ blk,
                                                          const float* __restrict__ dual, uint32_t* newidx,
-                                                         float* vout, uint32_t* vsrc) {
+                                                         float* vout, uint32_t* vsrc, const long long* __restrict__ dn) {
     __shared__ uint32_t sm[66];
     const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    if (dn) A = dn[0];
     const uint32_t is = (a < A && rep[a] == uint32_t(a)) ? 1u : 0u;
     uint32_t e0, e1, t0, t1;
     block_scan2(is, 0u, e0, e1, t0, t1, sm);
@@ -561,10 +580,31 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_rep_write(const uint32_t* __restr
 }
 
 __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uint32_t* __restrict__ rep,
-                         const uint32_t* __restrict__ newidx, int32_t* fout) {
+                         const uint32_t* __restrict__ newidx, int32_t* fout, const long long* __restrict__ dn) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dn) n = dn[2];
     if (i < n) fout[i] = int32_t(newidx[rep[tri[i]]]);
 }
+
+// One-call dual contouring: the sizes found on the device, checked against the
+// capacities.  eff = (A, K, 6 Q) the later kernels use, all 0 when something
+// does not fit (the status says so; counts hold the sizes for a retry).
+__global__ void dc_dense_sizes(const long long* __restrict__ tak, const long long* __restrict__ tq,
+                               long long capA, long long capQ, long long* eff, long long* counts, int* status) {
+    const long long A = tak[0], K = tak[1], Q = tq[0];
+    const bool ok = A <= capA && Q <= capQ && A < 0x7fffffffll && 6 * Q < 0x7fffffffll && K < 0x7fffffffll;
+    if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+    eff[0] = ok ? A : 0;
+    eff[1] = ok ? K : 0;
+    eff[2] = ok ? 6 * Q : 0;
+    counts[0] = 0;
+    counts[1] = ok ? 2 * Q : 0;
+    counts[2] = A;
+    counts[3] = K;
+    counts[4] = Q;
+}
+
+__global__ void dc_dense_finish(const long long* __restrict__ vtot, long long* counts) { counts[0] = vtot[0]; }
 
 }  // namespace
 
@@ -657,7 +697,7 @@ int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* a
     iso::ProfScope ps("dc_intersect", st);
     dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
         values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, points, normals,
-        reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
+        reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K, nullptr);
     if (A == 0 && cell_offsets) cudaMemsetAsync(cell_offsets, 0, 4, st);
     if (A > 0 && points)
         dc_points<<<blocks_for(A, iso::tune_get(iso::TUNE_DC_CELL_THREADS)), iso::tune_get(iso::TUNE_DC_CELL_THREADS), 0,
@@ -681,12 +721,12 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
         iso::ProfScope ps("dc_intersect", st);
         dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
             values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr,
-            reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K);
+            reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K, nullptr);
     }
     iso::ProfScope ps("dc_solve", st);
     const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
     dc_cell_solve<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
-                                                      reg, svd_tol, dual);
+                                                      reg, svd_tol, dual, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -727,7 +767,7 @@ int iso_dc_cells(const float* values, int nx, int ny, int nz, float level, void*
     Grid3 g = make_grid(nx, ny, nz, amin, amax);
     iso::ProfScope ps("dc_intersect", st);
     dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
-        values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr, nullptr, nullptr, -1, 0);
+        values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr, nullptr, nullptr, -1, 0, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -751,7 +791,7 @@ int iso_dc_quads_emit(int nx, int ny, int nz, void* ws, const float* dual, int* 
     Grid3 g = make_grid(nx, ny, nz, amin, amax);
     iso::ProfScope ps("dc_quads", st);
     dc_quad_emit<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ, w.actm,
-                                                                     w.offA, dual, tri);
+                                                                     w.offA, dual, tri, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -780,11 +820,11 @@ int iso_dc_weld_count(const float* dual, long long A, const int* tri, long long 
     iso::ProfScope ps("dc_weld", st);
     cudaMemsetAsync(used, 0, size_t(A) * 4, st);
     cudaMemsetAsync(table, 0xff, size_t(cap) * 4, st);
-    if (ntri > 0) dc_mark_used<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, used);
+    if (ntri > 0) dc_mark_used<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, used, nullptr);
     if (A > 0) {
-        dc_hash_insert<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, status);
-        dc_hash_lookup<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, rep);
-        dc_rep_count<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk);
+        dc_hash_insert<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, status, nullptr);
+        dc_hash_lookup<<<blocks_for(A, 256), 256, 0, st>>>(dual, used, A, table, cap - 1, rep, nullptr);
+        dc_rep_count<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk, nullptr);
         dc_block_scan<<<1, 1024, 0, st>>>(blk, nblk, counts);
     } else {
         cudaMemsetAsync(counts, 0, 16, st);
@@ -810,14 +850,139 @@ int iso_dc_weld_write_src(const float* dual, long long A, const int* tri, long l
     iso::ProfScope ps("dc_weld", st);
     if (A > 0)
         dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk, dual, newidx, vout,
-                                                           reinterpret_cast<uint32_t*>(vertex_source));
-    if (ntri > 0) dc_remap<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, rep, newidx, fout);
+                                                           reinterpret_cast<uint32_t*>(vertex_source), nullptr);
+    if (ntri > 0) dc_remap<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, rep, newidx, fout, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
 int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long ntri, void* ws,
                       float* vout, int* fout, void* stream) {
     return iso_dc_weld_write_src(dual, A, tri, ntri, ws, vout, fout, nullptr, stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// One call, no host synchronisation: for stream capture and for callers that
+// size their buffers once.  Capacities: vertex_capacity bounds the active cells
+// (dual vertices before the weld, A >= V), face_capacity the faces (2 per quad).
+
+namespace {
+struct DcDenseWs {
+    DcWs d;
+    long long* tot;  // [0..1] A, K  [2..3] Q, 0  [4..6] eff  [8..9] V, 0
+    uint32_t *cells, *offs, *used, *rep, *newidx, *table;
+    float* dual;
+    int32_t* tri;
+    unsigned long long* wblk;
+    uint32_t hcap;
+    long long nwblk;
+    size_t total;
+};
+
+DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA, long long capQ) {
+    DcDenseWs w{};
+    const size_t base = iso_dc_workspace_size(nx, ny, nz);
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    if (ws) w.d = carve(b, nx, ny, nz);
+    size_t o = (base + 255) & ~size_t(255);
+    auto take = [&](size_t bytes) {
+        uint8_t* p = ws ? b + o : nullptr;
+        o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        return p;
+    };
+    w.hcap = 1024;
+    while ((long long)w.hcap < 2 * capA + 1024) w.hcap <<= 1;
+    w.nwblk = (capA + DC_BLOCK - 1) / DC_BLOCK + 1;
+    w.tot = reinterpret_cast<long long*>(take(16 * 8));
+    w.cells = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.offs = reinterpret_cast<uint32_t*>(take(size_t(capA + 1) * 4));
+    w.dual = reinterpret_cast<float*>(take(size_t(capA) * 12));
+    w.tri = reinterpret_cast<int32_t*>(take(size_t(capQ) * 24));
+    w.used = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.rep = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
+    w.wblk = reinterpret_cast<unsigned long long*>(take(size_t(w.nwblk) * 16));
+    w.total = o + 256;
+    return w;
+}
+}  // namespace
+
+extern "C" {
+
+size_t iso_dc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity, long long face_capacity) {
+    if (nx < 2 || ny < 2 || nz < 2) return 256;
+    if (vertex_capacity < 0 || face_capacity < 0) return 0;
+    return carve_dense(nullptr, nx, ny, nz, vertex_capacity, face_capacity / 2).total;
+}
+
+int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
+                 float level, float reg, float svd_tol, float* vertices, long long vertex_capacity, int* faces,
+                 long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
+                 void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (!counts || !status || !aabb_min || !aabb_max || vertex_capacity < 0 || face_capacity < 0) return ISO_ERR_ARG;
+    if ((long long)nx * ny * nz > 0x7fffffffll) return ISO_ERR_ARG;
+    if (nx < 2 || ny < 2 || nz < 2)
+        return cudaMemsetAsync(counts, 0, 5 * sizeof(long long), st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (!values || (vertex_capacity && !vertices) || (face_capacity && !faces)) return ISO_ERR_ARG;
+    const long long capA = vertex_capacity, capQ = face_capacity / 2;
+    if (workspace_bytes < iso_dc_dense_workspace_size(nx, ny, nz, vertex_capacity, face_capacity))
+        return ISO_ERR_WORKSPACE;
+    const DcDenseWs w = carve_dense(workspace, nx, ny, nz, capA, capQ);
+    const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
+    long long* eff = w.tot + 4;
+    {
+        iso::ProfScope ps("mc_signs", st);
+        mc_signs_launch(values, nx, ny, nz, level, w.d.S, st);
+    }
+    {
+        iso::ProfScope ps("dc_classify", st);
+        dc_cell_count<<<blocks_for(w.d.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.cwords, w.d.blkC);
+        dc_block_scan<<<1, 1024, 0, st>>>(w.d.blkC, w.d.nblkC, w.tot);
+        dc_quad_count<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ);
+        dc_block_scan<<<1, 1024, 0, st>>>(w.d.blkQ, w.d.nblkQ, w.tot + 2);
+        dc_dense_sizes<<<1, 1, 0, st>>>(w.tot, w.tot + 2, capA, capQ, eff, counts, status);
+    }
+    {
+        iso::ProfScope ps("dc_intersect", st);
+        dc_intersect<<<blocks_for(w.d.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
+            values, w.d.S, g, level, w.d.cwords, w.d.blkC, w.d.actm, w.d.offA, nullptr, nullptr, w.cells, w.offs, 0, 0,
+            eff);
+    }
+    if (capA > 0) {
+        iso::ProfScope ps("dc_solve", st);
+        const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+        dc_cell_solve<<<blocks_for(capA, bt), bt, 0, st>>>(values, g, level, w.cells, capA, reg, svd_tol, w.dual,
+                                                           eff);
+    }
+    {
+        iso::ProfScope ps("dc_quads", st);
+        dc_quad_emit<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ, w.d.actm,
+                                                                           w.d.offA, w.dual, w.tri, eff);
+    }
+    {
+        iso::ProfScope ps("dc_weld", st);
+        cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
+        cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
+        if (capQ > 0) dc_mark_used<<<blocks_for(6 * capQ, 256), 256, 0, st>>>(w.tri, 6 * capQ, w.used, eff);
+        if (capA > 0) {
+            dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(w.dual, w.used, capA, w.table, w.hcap - 1, status, eff);
+            dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(w.dual, w.used, capA, w.table, w.hcap - 1, w.rep, eff);
+        }
+        const long long nblk = (capA + DC_BLOCK - 1) / DC_BLOCK;
+        if (nblk > 0) {
+            dc_rep_count<<<unsigned(nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.wblk, eff);
+            dc_block_scan<<<1, 1024, 0, st>>>(w.wblk, nblk, w.tot + 8);
+            dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.wblk, w.dual, w.newidx, vertices, nullptr,
+                                                              eff);
+            dc_dense_finish<<<1, 1, 0, st>>>(w.tot + 8, counts);
+        }
+        if (capQ > 0)
+            dc_remap<<<blocks_for(6 * capQ, 256), 256, 0, st>>>(w.tri, 6 * capQ, w.rep, w.newidx, faces, eff);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -30,7 +30,13 @@ _ffi.register({
     "iso_dc_weld_write": ([_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp], _i),
     "iso_dc_weld_write_src": ([_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp], _i),
     "iso_dc_intersect_solve": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _ll, _vp, _vp, _f, _f, _vp, _vp], _i),
+    "iso_dc_dense_workspace_size": ([_i, _i, _i, _ll, _ll], _sz),
+    "iso_dc_dense": ([_vp, _i, _i, _i, _fa, _fa, _f, _f, _f, _vp, _ll, _vp, _ll, _vp, _sz, _vp, _vp, _vp], _i),
 })
+
+# Last seen (active cells, quads) per (shape, level, box): the next call sizes its
+# buffers from them (10% + a margin), so steady-state calls run once.
+_dc_sizes: dict[tuple, tuple[int, int]] = {}
 
 
 def _p(t):
@@ -125,19 +131,7 @@ def _dc_uniform(grid: UniformGrid, level, its: Intersection | None, reg, svd_tol
     amin, amax = _ffi.fvec3(grid.aabb_min), _ffi.fvec3(grid.aabb_max)
     st = _stream(dev)
     if its is None:
-        # the quad count needs only the sign bitmap: it is read with (A, K); the
-        # crossings stay in registers (iso_dc_intersect_solve)
-        ws, (A, K, Q) = _classify_quads(grid, level)
-        if A == 0 or Q == 0:
-            return None, None
-        cells = torch.empty(A, dtype=torch.int32, device=dev)
-        offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
-        dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
-        _ffi.check(lib.iso_dc_intersect_solve(_p(grid._values), nx, ny, nz, amin, amax, float(level), _p(ws), A, K,
-                                              _p(cells), _p(offs), float(reg), float(svd_tol), _p(dual), st))
-        tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
-        _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
-        return weld_dual(lib, dev, dual, A, tri, st)
+        return _dc_one_call(grid, level, reg, svd_tol)
     else:
         if its._sparse is not None or its._grid_key[:3] != _grid_key(grid)[:3]:
             raise RuntimeError("intersection was computed for a different grid")
@@ -158,6 +152,54 @@ def _dc_uniform(grid: UniformGrid, level, its: Intersection | None, reg, svd_tol
     tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
     _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
     return weld_dual(lib, dev, dual, A, tri, st)
+
+
+def dc_dense_into(values: torch.Tensor, aabb_min, aabb_max, level: float, reg: float, svd_tol: float,
+                  vout: torch.Tensor, fout: torch.Tensor, ws: torch.Tensor, small: torch.Tensor, stream: int) -> int:
+    """Launch iso_dc_dense into caller-provided buffers (no synchronisation).
+    small: int64[8] device tensor; [0:5] receives (V, F, A, K, Q), [6] the status word."""
+    nx, ny, nz = values.shape
+    return _ffi.lib().iso_dc_dense(_p(values), nx, ny, nz, _ffi.fvec3(aabb_min), _ffi.fvec3(aabb_max),
+                                   float(level), float(reg), float(svd_tol), _p(vout), vout.shape[0], _p(fout),
+                                   fout.shape[0], _p(ws), ws.numel(), _p(small), C.c_void_p(small.data_ptr() + 48),
+                                   C.c_void_p(stream))
+
+
+def dc_workspace_bytes(shape, cap_v: int, cap_f: int) -> int:
+    return int(_ffi.lib().iso_dc_dense_workspace_size(*shape, cap_v, cap_f))
+
+
+def _dc_one_call(grid: UniformGrid, level, reg, svd_tol):
+    """dual_contouring without a caller intersection: iso_dc_dense, one
+    synchronisation to read the sizes (a retry with exact capacities if the
+    buffers were too small)."""
+    from .mc import _first_guess, _views
+
+    dev = grid._values.device
+    key = (tuple(grid.shape), float(level), tuple(grid.aabb_min), tuple(grid.aabb_max))
+    if key in _dc_sizes:
+        a, q = _dc_sizes[key]
+        cap_v, cap_f = a + a // 10 + 1024, 2 * q + (2 * q) // 10 + 1024
+    else:
+        cap_v, cap_f = _first_guess(grid.shape)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    for _ in range(2):
+        vout = torch.empty((cap_v, 3), dtype=torch.float32, device=dev)
+        fout = torch.empty((cap_f, 3), dtype=torch.int32, device=dev)
+        ws = torch.empty(dc_workspace_bytes(grid.shape, cap_v, cap_f), dtype=torch.uint8, device=dev)
+        small = torch.zeros(8, dtype=torch.int64, device=dev)
+        _ffi.check(dc_dense_into(grid._values, grid.aabb_min, grid.aabb_max, level, reg, svd_tol, vout, fout, ws,
+                                 small, st))
+        h = small.cpu()
+        V, F, A, Q, status = int(h[0]), int(h[1]), int(h[2]), int(h[4]), int(h[6] & 0xFFFFFFFF)
+        _dc_sizes[key] = (A, Q)
+        if status == _ffi.ISO_ERR_OVERFLOW:
+            cap_v, cap_f = A + 1024, 2 * Q + 1024
+            continue
+        if status:
+            raise RuntimeError(f"isoext_gb300: device error {status} in dual_contouring")
+        return _views(vout, fout, V, F)
+    raise RuntimeError("isoext_gb300: dual_contouring output did not fit after resizing")
 
 
 def _classify_quads(grid: UniformGrid, level: float):

@@ -7,9 +7,10 @@ server keeps ``slots`` workers, each with its own CUDA stream and its own
 device buffers, resident across requests.  Requests are admitted in arrival
 order as soon as a slot is free and the device-memory budget holds the
 request's worst case; the requests on different slots run concurrently on the
-GPU.  A marching-cubes request replays a CUDA graph captured for its slot and
-grid size (grid evaluation + extraction, no host work in between); dual
-contouring runs the library's stream-ordered steps on the slot's stream.
+GPU.  A request replays a CUDA graph captured for its slot, kind and grid size:
+grid evaluation + extraction, no host work in between (iso_mc_dense for
+marching cubes, iso_dc_dense for dual contouring).  A mesh larger than the
+slot's buffers reruns through the plain path.
 
 Each result equals the one-call-per-grid result (``solve_plain``) bit for bit:
 the same kernels run on the same inputs, only concurrently.
@@ -34,6 +35,7 @@ _vp, _i, _fa = C.c_void_p, C.c_int, C.POINTER(C.c_float)
 _ffi.register({"iso_sdf_union_grid": ([_vp, _i, _i, _i, _fa, _fa, _vp, _vp], _i)})
 
 MAX_PRIMS = 32
+DC_REG, DC_SVD_TOL = 1e-2, 1e-6  # dual_contouring's defaults (isoext)
 LO, HI = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
 
 
@@ -78,9 +80,9 @@ def prims_buffer(prims: np.ndarray) -> np.ndarray:
 
 # Kernels of this library one request launches: marching cubes = grid evaluation
 # + mc_signs, mc_count, mc_scan, mc_emit; dual contouring = grid evaluation +
-# mc_signs, cell count + scan, intersect, solve, quad count + scan, quad emit,
-# weld (mark, insert, lookup, count, scan, write, remap).
-KERNELS_PER_REQUEST = {"mc": 5, "dc": 16}
+# mc_signs, cell count + scan, quad count + scan, sizes, intersect, solve, quad
+# emit, weld (mark, insert, lookup, count, scan, write, finish, remap).
+KERNELS_PER_REQUEST = {"mc": 5, "dc": 18}
 
 
 # ---------------------------------------------------------------------------
@@ -167,38 +169,38 @@ def _mc_caps(n: int) -> tuple[int, int]:
 
 
 def request_bytes(req: Request) -> int:
-    """Worst-case device bytes of a request: grid values, workspace, outputs,
-    and for dual contouring its intermediate arrays (about 64 bytes per face)."""
+    """Worst-case device bytes of a request: grid values, workspace and outputs
+    at the capacity bound."""
+    from .dc import dc_workspace_bytes
     from .mc import workspace_bytes
 
     n = req.n
     cap_v, cap_f = _mc_caps(n)
-    values = 4 * n ** 3
-    if req.kind == "mc":
-        return values + workspace_bytes((n, n, n), cap_v, cap_f) + 12 * cap_v + 12 * cap_f + 4096
-    return values + 4 * n ** 3 // 8 * 4 + 64 * cap_f + 12 * cap_v
+    ws = (workspace_bytes if req.kind == "mc" else dc_workspace_bytes)((n, n, n), cap_v, cap_f)
+    return 4 * n ** 3 + ws + 12 * cap_v + 12 * cap_f + 4096
 
 
-class _MCSlot:
-    """A slot's buffers for one grid size, and the captured graph
-    (grid evaluation + iso_mc_dense) that fills them."""
+class _GraphSlot:
+    """A slot's buffers for one kind and grid size, and the captured graph
+    (grid evaluation + iso_mc_dense or iso_dc_dense) that fills them."""
 
-    def __init__(self, n: int, method: int, level: float, prims_dev, stream, device, use_graph: bool):
+    def __init__(self, kind: str, n: int, method: int, level: float, prims_dev, stream, device, use_graph: bool):
         import torch
 
-        from .mc import mc_dense_into, workspace_bytes
+        from .dc import dc_workspace_bytes
+        from .mc import workspace_bytes
 
-        self.n, self.method, self.level = n, method, level
+        self.kind, self.n, self.method, self.level = kind, n, method, level
         self.cap_v, self.cap_f = _mc_caps(n)
+        wsb = (workspace_bytes if kind == "mc" else dc_workspace_bytes)((n, n, n), self.cap_v, self.cap_f)
         self.values = torch.empty((n, n, n), dtype=torch.float32, device=device)
         self.vout = torch.empty((self.cap_v, 3), dtype=torch.float32, device=device)
         self.fout = torch.empty((self.cap_f, 3), dtype=torch.int32, device=device)
-        self.ws = torch.empty(workspace_bytes((n, n, n), self.cap_v, self.cap_f), dtype=torch.uint8, device=device)
-        self.small = torch.zeros(4, dtype=torch.int64, device=device)
-        self.small_host = torch.zeros(4, dtype=torch.int64).pin_memory()
+        self.ws = torch.empty(wsb, dtype=torch.uint8, device=device)
+        self.small = torch.zeros(8, dtype=torch.int64, device=device)
+        self.small_host = torch.zeros(8, dtype=torch.int64).pin_memory()
         self.prims_dev = prims_dev
         self.stream = stream
-        self._mc = mc_dense_into
         self.graph = None
         if use_graph:
             with torch.cuda.stream(stream):
@@ -210,14 +212,21 @@ class _MCSlot:
             self.graph = g
 
     def _launch(self):
+        from .dc import dc_dense_into
+        from .mc import mc_dense_into
+
         lib = _ffi.lib()
         s = self.stream.cuda_stream
         self.small.zero_()
         _ffi.check(lib.iso_sdf_union_grid(C.c_void_p(self.prims_dev.data_ptr()), self.n, self.n, self.n,
                                           _ffi.fvec3(LO), _ffi.fvec3(HI), C.c_void_p(self.values.data_ptr()),
                                           C.c_void_p(s)))
-        _ffi.check(self._mc(self.values, LO, HI, self.level, self.method, self.vout, self.fout, self.ws,
-                            self.small, s))
+        if self.kind == "mc":
+            _ffi.check(mc_dense_into(self.values, LO, HI, self.level, self.method, self.vout, self.fout, self.ws,
+                                     self.small, s))
+        else:
+            _ffi.check(dc_dense_into(self.values, LO, HI, self.level, DC_REG, DC_SVD_TOL, self.vout, self.fout,
+                                     self.ws, self.small, s))
 
     def run(self):
         """Returns (V, F, status) after the extraction; outputs stay on the device."""
@@ -231,7 +240,8 @@ class _MCSlot:
             self.small_host.copy_(self.small, non_blocking=True)
         self.stream.synchronize()
         h = self.small_host
-        return int(h[0]), int(h[1]), int(h[2]) & 0xFFFFFFFF
+        status = int(h[2] if self.kind == "mc" else h[6]) & 0xFFFFFFFF
+        return int(h[0]), int(h[1]), status
 
 
 class Server(Scheduler):
@@ -254,14 +264,15 @@ class Server(Scheduler):
         self._lock = threading.Lock()  # graph capture is done one at a time
         super().__init__(slots, budget_bytes, request_bytes, self._execute)
 
-    def warmup(self, sizes, method: str = "nagae", level: float = 0.0, tune: bool = True) -> dict | None:
+    def warmup(self, sizes, method: str = "nagae", level: float = 0.0, tune: bool = True,
+               kinds=("mc", "dc")) -> dict | None:
         """Builds every slot's buffers and graphs for the given grid sizes up front.
         With tune, the launch parameters are first tuned (isoext_gb300.tune) on a
         grid of the largest size, so the captured graphs use them; returns the
         tuning report."""
-        from .mc import method_id
-
         import torch
+
+        from .mc import method_id
 
         report = None
         if tune:
@@ -273,16 +284,17 @@ class Server(Scheduler):
             report = _tune_on(n, prims, self.device, level, tuner)
         for slot in range(len(self._streams)):
             for n in sizes:
-                self._mc_slot(slot, int(n), method_id(method), float(level))
+                for kind in kinds:
+                    self._slot(slot, kind, int(n), method_id(method), float(level))
         return report
 
-    def _mc_slot(self, slot: int, n: int, method: int, level: float) -> _MCSlot:
-        key = ("mc", n, method, level)
+    def _slot(self, slot: int, kind: str, n: int, method: int, level: float) -> _GraphSlot:
+        key = (kind, n, method if kind == "mc" else 0, level)
         st = self._slot_state[slot]
         if key not in st:
             with self._lock:
-                st[key] = _MCSlot(n, method, level, self._prims_dev[slot], self._streams[slot], self.device,
-                                  self.use_graphs)
+                st[key] = _GraphSlot(kind, n, method, level, self._prims_dev[slot], self._streams[slot], self.device,
+                                     self.use_graphs)
         return st[key]
 
     def _upload_prims(self, slot: int, prims) -> None:
@@ -300,21 +312,20 @@ class Server(Scheduler):
 
         stream = self._streams[slot]
         self._upload_prims(slot, req.prims)
-        if req.kind == "mc":
-            ms = self._mc_slot(slot, req.n, method_id(req.method), float(req.level))
-            V, F, status = ms.run()
-            if status == _ffi.ISO_ERR_OVERFLOW:
-                # larger than the slot's buffers: the plain path on this stream
-                with torch.cuda.stream(stream):
-                    return _solve_on_stream(req, self._prims_dev[slot], self.device)
-            if status != 0:
-                raise RuntimeError(f"isoext_gb300: device error {status} in a served request")
+        gs = self._slot(slot, req.kind, req.n, method_id(req.method), float(req.level))
+        V, F, status = gs.run()
+        if status == _ffi.ISO_ERR_OVERFLOW:
+            # larger than the slot's buffers: the plain path on this stream
             with torch.cuda.stream(stream):
-                v = ms.vout[:V].to("cpu", non_blocking=False).numpy().copy()
-                f = ms.fout[:F].to("cpu", non_blocking=False).numpy().copy()
-            return v, f
+                return _solve_on_stream(req, self._prims_dev[slot], self.device)
+        if status != 0:
+            raise RuntimeError(f"isoext_gb300: device error {status} in a served request")
+        if V == 0 or F == 0:
+            return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
         with torch.cuda.stream(stream):
-            return _solve_on_stream(req, self._prims_dev[slot], self.device)
+            v = gs.vout[:V].to("cpu").numpy().copy()
+            f = gs.fout[:F].to("cpu").numpy().copy()
+        return v, f
 
 
 def _tune_on(n: int, prims_dev, device, level: float, tuner) -> dict:
@@ -332,7 +343,7 @@ def _tune_on(n: int, prims_dev, device, level: float, tuner) -> dict:
 
 def _solve_on_stream(req: Request, prims_dev, device):
     """The public API on the current stream: grid from the union, then
-    marching_cubes or dual_contouring; results copied to the host."""
+    marching_cubes or dual_contouring (isoext's defaults); results copied to the host."""
     import torch
 
     from .dc import dual_contouring
@@ -347,7 +358,7 @@ def _solve_on_stream(req: Request, prims_dev, device):
     if req.kind == "mc":
         v, f = marching_cubes(grid, req.level, req.method)
     else:
-        v, f = dual_contouring(grid, req.level)
+        v, f = dual_contouring(grid, req.level, reg=DC_REG, svd_tol=DC_SVD_TOL)
     if v is None:
         return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
     return v.cpu().numpy(), f.cpu().numpy()

@@ -198,3 +198,18 @@ def test_dc_one_pass_solve_equals_intersection_then_solve(values):
     its = iso.get_intersection(g, compute_normals=True)
     v1, f1 = iso.dual_contouring(g, intersection=its)
     assert torch.equal(v0, v1) and torch.equal(f0, f1)
+
+
+def test_dc_one_call_retries_when_buffers_are_small():
+    """dual_contouring sizes its buffers from the last call; when they are too
+    small the device reports the sizes and the call reruns with them."""
+    from isoext_gb300 import dc
+
+    vals = sphere((48, 50, 52), 0.7)
+    g = make_grid(vals)
+    v0, f0 = iso.dual_contouring(g)
+    key = (tuple(g.shape), 0.0, tuple(g.aabb_min), tuple(g.aabb_max))
+    dc._dc_sizes[key] = (8, 8)
+    v1, f1 = iso.dual_contouring(g)
+    assert torch.equal(v0, v1) and torch.equal(f0, f1)
+    assert dc._dc_sizes[key][0] >= len(v0)

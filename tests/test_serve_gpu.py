@@ -69,10 +69,11 @@ def test_served_results_equal_plain_results():
 def test_served_overflow_reruns_with_exact_sizes(monkeypatch):
     from isoext_gb300 import serve
 
-    reqs = [r for r in serve.random_requests(16, seed=9, sizes=(48,)) if r.kind == "mc"]
+    reqs = serve.random_requests(24, seed=9, sizes=(48,))
     plain = [serve.solve_plain(r) for r in reqs]
-    big = [(r, p) for r, p in zip(reqs, plain) if len(p[1]) > 64][:2]
-    assert len(big) == 2
+    big = [(r, p) for r, p in zip(reqs, plain) if len(p[1]) > 64 and r.kind == "mc"][:2]
+    big += [(r, p) for r, p in zip(reqs, plain) if len(p[1]) > 64 and r.kind == "dc"][:2]
+    assert len(big) == 4
     monkeypatch.setattr(serve, "_mc_caps", lambda n: (64, 64))
     srv = serve.Server(slots=2, budget_bytes=1 << 30)
     out = [f.result(timeout=300) for f in [srv.submit(r) for r, _ in big]]
