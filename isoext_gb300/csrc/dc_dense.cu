@@ -609,8 +609,7 @@ __global__ void dc_dense_finish(const long long* __restrict__ vtot, long long* c
 }  // namespace
 
 // mc_signs lives in mc_dense.cu
-void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
-                     cudaStream_t st);
+#include "mc_dense.cuh"
 
 // ---------------------------------------------------------------------------
 // C ABI

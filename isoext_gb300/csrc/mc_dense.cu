@@ -395,6 +395,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
     __shared__ uint32_t vmask[3 * WPT][CNT_THREADS];  // x, y, z edge masks of each thread's words
     __shared__ uint32_t rows[4][WPT + 1][CNT_THREADS];  // sign words of rows (dx, dy), words k = 0..4
+    iso::grid_wait();
     // grid coordinates (include/utils.cuh:62-80), read by the emit kernel
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
@@ -682,6 +683,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk,
     __shared__ uint32_t sm[64];
     __shared__ uint32_t chunk_s;
     __shared__ unsigned long long pre_s[2];
+    iso::grid_wait();
     if (threadIdx.x == 0) chunk_s = uint32_t(atomicAdd(ctr + 7, 1ull));
     __syncthreads();
     const uint32_t chunk = chunk_s;
@@ -888,6 +890,7 @@ __device__ void fixup_block(const McWs& w, float* vout, int32_t* fout, long long
 template <int EMIT_THREADS>
 __global__ void __launch_bounds__(EMIT_THREADS) mc_emit(const McGrid g, const EmitArgs a) {
     __shared__ int last;
+    iso::grid_wait();
     if (a.counts[0] > a.capV || a.counts[1] > a.capF || a.counts[0] > 0x7fffffffll) return;
     if (blockIdx.x < a.nbv) emit_vertices<EMIT_THREADS>(g, a, blockIdx.x, a.nbv);
     else emit_faces<EMIT_THREADS>(g, a, blockIdx.x - a.nbv, gridDim.x - a.nbv);
@@ -1045,7 +1048,13 @@ constexpr int SIGN_UNROLL = 16;
 // per grid row, all of the row's loads in flight before the ballots; lane w
 // keeps word w so each 32 words leave in one store.
 __global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__ vals, long long rows,
-                                                       int nz, float level, uint32_t* __restrict__ out) {
+                                                       int nz, float level, uint32_t* __restrict__ out,
+                                                       unsigned long long* __restrict__ zero, long long nzero) {
+    iso::grid_wait();
+    // counters, look-back states and the small hash of the call start at zero
+    for (long long i = (long long)blockIdx.x * SIGN_BLOCK + threadIdx.x; i < nzero;
+         i += (long long)gridDim.x * SIGN_BLOCK)
+        zero[i] = 0ull;
     const int lane = threadIdx.x & 31;
     const int NWg = (nz + 31) / 32;
     const long long warps = (long long)gridDim.x * (SIGN_BLOCK / 32);
@@ -1098,7 +1107,7 @@ int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t 
                p.vout, p.fout, p.counts, p.status, p.capV, p.capF, unsigned(nbv), w, p.vedge};
     {
         iso::ProfScope ps("mc_emit", st);
-        mc_emit<EMIT_THREADS><<<unsigned(nbv + nbf), EMIT_THREADS, 0, st>>>(g, a);
+        iso::launch_pdl(mc_emit<EMIT_THREADS>, unsigned(nbv + nbf), EMIT_THREADS, st, g, a);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     return 0;
@@ -1110,16 +1119,17 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
         iso::ProfScope ps("mc_count", st);
         const long long ncoord = (long long)p.nx + p.ny + p.nz;
         const long long grid = std::max<long long>(w.nBlk, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
-        mc_count<<<unsigned(grid), CNT_THREADS, 0, st>>>(g, p.amin[0], p.amin[1], p.amin[2], p.asize[0], p.asize[1],
-                                                         p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff,
-                                                         w.ctr, w.gc, uint32_t(w.nBlk), p.capV, p.capF);
+        iso::launch_pdl(mc_count, unsigned(grid), CNT_THREADS, st, g, p.amin[0], p.amin[1], p.amin[2], p.asize[0],
+                   p.asize[1], p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff, w.ctr, w.gc,
+                   uint32_t(w.nBlk), p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
         iso::ProfScope ps("mc_scan", st);
         const uint32_t nseg = uint32_t(w.nBlk);
         const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
-        mc_scan<<<nchunk, SCAN_THREADS, 0, st>>>(w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV, p.capF);
+        iso::launch_pdl(mc_scan, nchunk, SCAN_THREADS, st, w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV,
+                   p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     const int block = mc_get_block();
@@ -1141,12 +1151,12 @@ int mc_get_block() {
 }
 
 void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
-                     cudaStream_t st) {
+                     cudaStream_t st, unsigned long long* zero, long long nzero) {
     const long long rows = (long long)nx * ny;
     const long long want = (rows + (SIGN_BLOCK / 32) - 1) / (SIGN_BLOCK / 32);
     const long long per = iso::tune_get(iso::TUNE_MC_SIGN_CTAS);
     const long long grid = std::max<long long>(1, std::min<long long>(want, (long long)sm_count() * per));
-    mc_signs<<<unsigned(grid), SIGN_BLOCK, 0, st>>>(vals, rows, nz, level, out);
+    iso::launch_pdl(mc_signs, unsigned(grid), SIGN_BLOCK, st, vals, rows, nz, level, out, zero, nzero);
 }
 
 // Bound on t for an edge vertex to land within a few ulps of an endpoint (the
@@ -1189,10 +1199,9 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.tau = snap_tau(p);
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
-    if (cudaMemsetAsync(w.ctr, 0, zeroed_bytes(w.nBlk), st) != cudaSuccess) return ISO_ERR_CUDA;
     {
         iso::ProfScope ps("mc_signs", st);
-        mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st);
+        mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st, w.ctr, (long long)(zeroed_bytes(w.nBlk) / 8));
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     const int rc = launch_count_emit(p, g, w, st);

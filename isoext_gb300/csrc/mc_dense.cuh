@@ -42,5 +42,7 @@ size_t mc_workspace_bytes(int nx, int ny, int nz, long long capV, long long capF
 int mc_launch(const McParams& p, void* workspace, size_t ws_bytes, cudaStream_t stream);
 
 // Sign bitmap of a grid (also used by dual contouring).
+// zero / nzero: 8-byte words to clear before the pass's end (the MC call's
+// counters), or nullptr / 0.
 void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
-                     cudaStream_t st);
+                     cudaStream_t st, unsigned long long* zero = nullptr, long long nzero = 0);
