@@ -229,8 +229,6 @@ def run_ours(args, wl, rank, world) -> dict | None:
             for _ in range(50):
                 step()
             torch.cuda.synchronize()
-        lib.iso_profile_reset()
-        lib.iso_profile_enable(1)
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
@@ -241,8 +239,15 @@ def run_ours(args, wl, rank, world) -> dict | None:
             step()
         e1.record(stream)
         torch.cuda.synchronize()
-    lib.iso_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    # per-kernel times in a separate pass: the timing hooks put events between
+    # the kernels, which the timed region above does not have
+    lib.iso_profile_reset()
+    lib.iso_profile_enable(1)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
     host = small.cpu()
     assert int(host[2] & 0xffffffff) == 0, f"device status {int(host[2])}"
     assert (int(host[0]), int(host[1])) == (nv, nf)
@@ -382,17 +387,19 @@ def run_grad(args, wl, rank, world) -> dict | None:
         while time.perf_counter() < t_end:
             step()
         torch.cuda.synchronize()
-        lib.iso_profile_reset()
-        lib.iso_profile_enable(1)
-        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             step()
         e1.record(stream)
         torch.cuda.synchronize()
-    lib.iso_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    lib.iso_profile_reset()  # per-kernel times in a separate pass (events between kernels)
+    lib.iso_profile_enable(1)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in GRAD_KERNELS}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
     launches = sum(c for c, _ in kt.values())
@@ -523,16 +530,19 @@ def run_sparse(args, wl, rank, world) -> dict | None:
         while time.perf_counter() < t_end:
             iso.marching_cubes(grid)
         torch.cuda.synchronize()
-        lib.iso_profile_reset()
-        lib.iso_profile_enable(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             iso.marching_cubes(grid)
         e1.record(stream)
         torch.cuda.synchronize()
-    lib.iso_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    lib.iso_profile_reset()  # per-kernel times in a separate pass (events between kernels)
+    lib.iso_profile_enable(1)
+    for _ in range(args.steps):
+        iso.marching_cubes(grid)
+    torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in ("sparse_mc", "dc_weld")}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
     launches = sum(c for c, _ in kt.values())
@@ -757,8 +767,6 @@ def run_dc(args, wl, rank, world) -> dict | None:
         while time.perf_counter() < t_end:
             step()
         torch.cuda.synchronize()
-        lib.iso_profile_reset()
-        lib.iso_profile_enable(1)
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
@@ -769,8 +777,13 @@ def run_dc(args, wl, rank, world) -> dict | None:
             step()
         e1.record(stream)
         torch.cuda.synchronize()
-    lib.iso_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    lib.iso_profile_reset()  # per-kernel times in a separate pass (events between kernels)
+    lib.iso_profile_enable(1)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in DC_KERNELS}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
     launches = sum(c for c, _ in kt.values())
