@@ -224,6 +224,16 @@ int iso_sparse_quads_count(const int *ids, const float *vals, long long n, int n
 int iso_sparse_quads_emit(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
                           float level, const int *rank, const void *blk, const float *dual, int *tri,
                           void *stream);
+/* Sparse MC in one call with no host synchronisation: the soup of
+ * iso_sparse_mc_count/emit welded as iso_dc_weld_* does, into vertices
+ * [vertex_capacity, 3] and faces [face_capacity, 3].  counts (device
+ * int64[3]) <- (V, F, F needed); status 6 when F or V exceed the capacities
+ * (the outputs are then incomplete; retry with the sizes from counts). */
+size_t iso_sparse_mc_workspace_size(long long n, long long vertex_capacity, long long face_capacity);
+int iso_sparse_mc(const int *ids, const float *vals, long long n, int nx, int ny, int nz,
+                  const float *aabb_min, const float *aabb_max, float level, int method, float *vertices,
+                  long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
+                  size_t workspace_bytes, long long *counts, int *status, void *stream);
 /* Corner positions [m, 8, 3] of cell ids (get_points / get_points_by_cell_indices,
  * src/grid/sparse.cu:21-43). */
 int iso_sparse_points(const int *ids, long long m, int nx, int ny, int nz, const float *aabb_min,

@@ -501,7 +501,7 @@ __global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint3
                              const long long* __restrict__ dn) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) n = dn[2];
-    if (i < n) used[tri[i]] = 1u;
+    if (i < n) used[tri ? tri[i] : int32_t(i)] = 1u;  // tri == nullptr: triangle i is point i
 }
 
 // Insert used vertices; a slot keeps the smallest index with its position.
@@ -573,6 +573,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_rep_write(const uint32_t* __restr
     if (!is) return;
     const unsigned long long o = blk[2 * blockIdx.x] + e0;
     newidx[a] = uint32_t(o);
+    if (dn && (long long)o >= dn[3]) return;  // past the vertex capacity: the caller sees V and retries
     if (vsrc) vsrc[o] = uint32_t(a);
     vout[3 * o] = dual[3 * a];
     vout[3 * o + 1] = dual[3 * a + 1];
@@ -583,7 +584,7 @@ __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uin
                          const uint32_t* __restrict__ newidx, int32_t* fout, const long long* __restrict__ dn) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) n = dn[2];
-    if (i < n) fout[i] = int32_t(newidx[rep[tri[i]]]);
+    if (i < n) fout[i] = int32_t(newidx[rep[tri ? tri[i] : int32_t(i)]]);
 }
 
 // One-call dual contouring: the sizes found on the device, checked against the
@@ -597,6 +598,7 @@ __global__ void dc_dense_sizes(const long long* __restrict__ tak, const long lon
     eff[0] = ok ? A : 0;
     eff[1] = ok ? K : 0;
     eff[2] = ok ? 6 * Q : 0;
+    eff[3] = capA;  // V <= A <= capA
     counts[0] = 0;
     counts[1] = ok ? 2 * Q : 0;
     counts[2] = A;
@@ -607,6 +609,62 @@ __global__ void dc_dense_sizes(const long long* __restrict__ tak, const long lon
 __global__ void dc_dense_finish(const long long* __restrict__ vtot, long long* counts) { counts[0] = vtot[0]; }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Exact-position weld with device-side sizes, for the one-call paths: eff[0] =
+// points, eff[2] = triangle indices (tri == nullptr: index i is point i),
+// eff[3] = vertex capacity of vout.  vtot[0] <- V.  Grids are sized by the
+// capacities capA / capT.
+
+struct WeldDev {
+    uint32_t *used, *rep, *newidx, *table;
+    unsigned long long* blk;
+    uint32_t hcap;
+    long long nblk;
+    size_t total;
+};
+
+WeldDev weld_dev_carve(void* ws, long long capA) {
+    WeldDev w{};
+    w.hcap = 1024;
+    while ((long long)w.hcap < 2 * capA + 1024) w.hcap <<= 1;
+    w.nblk = (capA + DC_BLOCK - 1) / DC_BLOCK;
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        uint8_t* p = ws ? b + o : nullptr;
+        o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        return p;
+    };
+    w.used = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.rep = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
+    w.blk = reinterpret_cast<unsigned long long*>(take(size_t(w.nblk + 1) * 16));
+    w.total = o + 256;
+    return w;
+}
+
+size_t weld_dev_workspace(long long capA) { return weld_dev_carve(nullptr, capA).total; }
+
+void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
+                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st) {
+    const WeldDev w = weld_dev_carve(ws, capA);
+    iso::ProfScope ps("dc_weld", st);
+    cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
+    cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
+    if (capT > 0) dc_mark_used<<<blocks_for(capT, 256), 256, 0, st>>>(tri, capT, w.used, eff);
+    if (capA > 0) {
+        dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(pts, w.used, capA, w.table, w.hcap - 1, status, eff);
+        dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(pts, w.used, capA, w.table, w.hcap - 1, w.rep, eff);
+        dc_rep_count<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, eff);
+        dc_block_scan<<<1, 1024, 0, st>>>(w.blk, w.nblk, vtot);
+        dc_rep_write<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, pts, w.newidx, vout, nullptr, eff);
+    } else {
+        cudaMemsetAsync(vtot, 0, 16, st);
+    }
+    if (capT > 0) dc_remap<<<blocks_for(capT, 256), 256, 0, st>>>(tri, capT, w.rep, w.newidx, fout, eff);
+}
 
 // mc_signs lives in mc_dense.cu
 #include "mc_dense.cuh"
@@ -869,13 +927,11 @@ int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long 
 namespace {
 struct DcDenseWs {
     DcWs d;
-    long long* tot;  // [0..1] A, K  [2..3] Q, 0  [4..6] eff  [8..9] V, 0
-    uint32_t *cells, *offs, *used, *rep, *newidx, *table;
+    long long* tot;  // [0..1] A, K  [2..3] Q, 0  [4..7] eff  [8..9] V, 0
+    uint32_t *cells, *offs;
     float* dual;
     int32_t* tri;
-    unsigned long long* wblk;
-    uint32_t hcap;
-    long long nwblk;
+    void* weld;  // weld_dev_workspace(capA) bytes
     size_t total;
 };
 
@@ -890,19 +946,12 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA, long lon
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.hcap = 1024;
-    while ((long long)w.hcap < 2 * capA + 1024) w.hcap <<= 1;
-    w.nwblk = (capA + DC_BLOCK - 1) / DC_BLOCK + 1;
     w.tot = reinterpret_cast<long long*>(take(16 * 8));
     w.cells = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.offs = reinterpret_cast<uint32_t*>(take(size_t(capA + 1) * 4));
     w.dual = reinterpret_cast<float*>(take(size_t(capA) * 12));
     w.tri = reinterpret_cast<int32_t*>(take(size_t(capQ) * 24));
-    w.used = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.rep = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
-    w.wblk = reinterpret_cast<unsigned long long*>(take(size_t(w.nwblk) * 16));
+    w.weld = take(weld_dev_workspace(capA));
     w.total = o + 256;
     return w;
 }
@@ -961,26 +1010,8 @@ int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
         dc_quad_emit<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ, w.d.actm,
                                                                            w.d.offA, w.dual, w.tri, eff);
     }
-    {
-        iso::ProfScope ps("dc_weld", st);
-        cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
-        cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
-        if (capQ > 0) dc_mark_used<<<blocks_for(6 * capQ, 256), 256, 0, st>>>(w.tri, 6 * capQ, w.used, eff);
-        if (capA > 0) {
-            dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(w.dual, w.used, capA, w.table, w.hcap - 1, status, eff);
-            dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(w.dual, w.used, capA, w.table, w.hcap - 1, w.rep, eff);
-        }
-        const long long nblk = (capA + DC_BLOCK - 1) / DC_BLOCK;
-        if (nblk > 0) {
-            dc_rep_count<<<unsigned(nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.wblk, eff);
-            dc_block_scan<<<1, 1024, 0, st>>>(w.wblk, nblk, w.tot + 8);
-            dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.wblk, w.dual, w.newidx, vertices, nullptr,
-                                                              eff);
-            dc_dense_finish<<<1, 1, 0, st>>>(w.tot + 8, counts);
-        }
-        if (capQ > 0)
-            dc_remap<<<blocks_for(6 * capQ, 256), 256, 0, st>>>(w.tri, 6 * capQ, w.rep, w.newidx, faces, eff);
-    }
+    weld_dev_launch(w.dual, capA, w.tri, 6 * capQ, eff, w.weld, vertices, faces, w.tot + 8, status, st);
+    dc_dense_finish<<<1, 1, 0, st>>>(w.tot + 8, counts);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 

@@ -183,8 +183,9 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_count(SpGrid g, const int* __r
 __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __restrict__ ids,
                                                        const float* __restrict__ vals, long long n,
                                                        const unsigned long long* __restrict__ blk,
-                                                       float* soup) {
+                                                       float* soup, const long long* __restrict__ dn) {
     __shared__ uint32_t sm[33];
+    if (dn && dn[0] == 0) return;  // over capacity (or nothing to write): the sizes say so
     const long long c = (long long)blockIdx.x * SP_BLOCK + threadIdx.x;
     uint32_t nf = 0;
     Cell8 cc;
@@ -524,6 +525,60 @@ unsigned nb(long long n, int b) { return unsigned(std::max<long long>(1, (n + b 
 
 // dc_block_scan lives in dc_dense.cu
 void iso_block_scan_launch(unsigned long long* blk, long long nblk, long long* totals, cudaStream_t st);
+// dc_dense.cu: exact-position weld with device-side sizes
+size_t weld_dev_workspace(long long capA);
+void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
+                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st);
+
+namespace {
+
+// One-call sparse MC: the soup's size against the capacities; eff = (3 F, 0,
+// 3 F, vertex capacity) for the weld, all 0 when the soup does not fit.
+__global__ void sp_mc_sizes(const long long* __restrict__ tf, long long capF, long long capV, long long* eff,
+                            long long* counts, int* status) {
+    const long long F = tf[0];
+    const bool ok = F <= capF && 3 * F < 0x7fffffffll;
+    if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+    eff[0] = ok ? 3 * F : 0;
+    eff[1] = 0;
+    eff[2] = ok ? 3 * F : 0;
+    eff[3] = capV;
+    counts[1] = ok ? F : 0;
+    counts[2] = F;
+}
+
+__global__ void sp_mc_finish(const long long* __restrict__ vtot, long long capV, long long* counts, int* status) {
+    const long long V = vtot[0];
+    counts[0] = V;
+    if (V > capV) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+}
+
+struct SpMcWs {
+    void* blk;
+    long long* tot;  // [0..1] F, 0  [4..7] eff  [8..9] V, 0
+    float* soup;
+    void* weld;
+    size_t total;
+};
+
+SpMcWs sp_mc_carve(void* ws, long long n, long long capF) {
+    SpMcWs w{};
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        uint8_t* p = ws ? b + o : nullptr;
+        o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        return p;
+    };
+    w.blk = take(size_t((n + SP_BLOCK - 1) / SP_BLOCK + 1) * 16);
+    w.tot = reinterpret_cast<long long*>(take(16 * 8));
+    w.soup = reinterpret_cast<float*>(take(size_t(3 * capF) * 12));
+    w.weld = take(weld_dev_workspace(3 * capF));
+    w.total = o + 256;
+    return w;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -550,7 +605,7 @@ int iso_sparse_mc_emit(const int* ids, const float* vals, long long n, int nx, i
     if (n <= 0) return 0;
     SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     iso::ProfScope ps("sparse_mc", st);
-    sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, soup);
+    sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, soup, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -642,6 +697,42 @@ int iso_sparse_filter_write(const int* ids, const float* vals, long long m, floa
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (m <= 0) return 0;
     sp_filter_write<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(ids, vals, m, level, (const unsigned long long*)blk, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+// Sparse marching cubes in one call with no host synchronisation: the triangle
+// soup and its exact-position weld (isoext's sparse MC, src/grid/sparse.cu with
+// src/mc/mc.cu:17-68).  counts (device int64[3]) <- (V, F, F needed); status 6
+// when F > face_capacity or V > vertex_capacity, and a retry sizes from counts.
+size_t iso_sparse_mc_workspace_size(long long n, long long vertex_capacity, long long face_capacity) {
+    if (n < 0 || vertex_capacity < 0 || face_capacity < 0) return 0;
+    return sp_mc_carve(nullptr, n, face_capacity).total;
+}
+
+int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny, int nz, const float* amin,
+                  const float* amax, float level, int method, float* vertices, long long vertex_capacity, int* faces,
+                  long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
+                  void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (!counts || !status || !amin || !amax || n < 0 || vertex_capacity < 0 || face_capacity < 0) return ISO_ERR_ARG;
+    if (method != 0 && method != 1) return ISO_ERR_ARG;
+    if (n == 0) return cudaMemsetAsync(counts, 0, 24, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (!ids || !vals || (vertex_capacity && !vertices) || (face_capacity && !faces)) return ISO_ERR_ARG;
+    if (workspace_bytes < iso_sparse_mc_workspace_size(n, vertex_capacity, face_capacity)) return ISO_ERR_WORKSPACE;
+    const SpMcWs w = sp_mc_carve(workspace, n, face_capacity);
+    const SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
+    long long* eff = w.tot + 4;
+    {
+        iso::ProfScope ps("sparse_mc", st);
+        sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk);
+        iso_block_scan_launch((unsigned long long*)w.blk, nb(n, SP_BLOCK), w.tot, st);
+        sp_mc_sizes<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
+        sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.soup,
+                                                         eff);
+    }
+    weld_dev_launch(w.soup, 3 * face_capacity, nullptr, 3 * face_capacity, eff, w.weld, vertices, faces, w.tot + 8,
+                    status, st);
+    sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 

@@ -33,6 +33,8 @@ _ffi.register({
     "iso_sparse_points": ([_vp, _ll, _i, _i, _i, _fa, _fa, _vp, _vp], _i),
     "iso_sparse_filter_count": ([_vp, _ll, _f, _vp, _vp, _vp], _i),
     "iso_sparse_filter_write": ([_vp, _vp, _ll, _f, _vp, _vp, _vp], _i),
+    "iso_sparse_mc_workspace_size": ([_ll, _ll, _ll], _sz),
+    "iso_sparse_mc": ([_vp, _vp, _ll, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp, _sz, _vp, _vp, _vp], _i),
 })
 
 
@@ -278,7 +280,9 @@ class SparseGrid(SparseGridBase):
         return sx, sy, sz, _ffi.fvec3(self.aabb_min), _ffi.fvec3(self.aabb_max)
 
     def _marching_cubes(self, level: float, method: int):
-        from .dc import weld_dual
+        """iso_sparse_mc in one call, sized from the last call on this grid (one
+        synchronisation; a retry with exact capacities when they were small)."""
+        from .mc import _views
 
         lib = _ffi.lib()
         dev = self.device
@@ -287,18 +291,34 @@ class SparseGrid(SparseGridBase):
             return None, None
         st = _stream(dev)
         sx, sy, sz, lo, hi = self._geom()
-        blk = torch.empty(int(lib.iso_sparse_blocks_size(n)), dtype=torch.uint8, device=dev)
-        counts = torch.zeros(2, dtype=torch.int64, device=dev)
-        _ffi.check(lib.iso_sparse_mc_count(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi,
-                                           float(level), int(method), _p(blk), _p(counts), st))
-        F = int(counts[0].item())
-        if F == 0:
-            return None, None
-        soup = torch.empty((3 * F, 3), dtype=torch.float32, device=dev)
-        _ffi.check(lib.iso_sparse_mc_emit(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi,
-                                          float(level), int(method), _p(blk), _p(soup), st))
-        tri = torch.arange(3 * F, dtype=torch.int32, device=dev)
-        return weld_dual(lib, dev, soup, 3 * F, tri, st)
+        key = (n, float(level), int(method))
+        if getattr(self, "_mc_sizes", None) and key in self._mc_sizes:
+            v, f = self._mc_sizes[key]
+            cap_v, cap_f = v + v // 10 + 1024, f + f // 10 + 1024
+        else:
+            cap_f = 2 * n + 1024
+            cap_v = cap_f
+        for _ in range(2):
+            vout = torch.empty((cap_v, 3), dtype=torch.float32, device=dev)
+            fout = torch.empty((cap_f, 3), dtype=torch.int32, device=dev)
+            ws = torch.empty(int(lib.iso_sparse_mc_workspace_size(n, cap_v, cap_f)), dtype=torch.uint8, device=dev)
+            small = torch.zeros(4, dtype=torch.int64, device=dev)
+            _ffi.check(lib.iso_sparse_mc(_p(self._ids), _p(self._values), n, sx, sy, sz, lo, hi, float(level),
+                                         int(method), _p(vout), cap_v, _p(fout), cap_f, _p(ws), ws.numel(),
+                                         _p(small), C.c_void_p(small.data_ptr() + 24), st))
+            h = small.cpu()
+            V, F, Fneed, status = int(h[0]), int(h[1]), int(h[2]), int(h[3] & 0xFFFFFFFF)
+            if not getattr(self, "_mc_sizes", None):
+                self._mc_sizes = {}
+            self._mc_sizes[key] = (max(V, 1), max(Fneed, 1))
+            if status == _ffi.ISO_ERR_OVERFLOW:
+                cap_f = Fneed + 1024
+                cap_v = max(V, 3 * Fneed if V == 0 else V) + 1024
+                continue
+            if status:
+                raise RuntimeError(f"isoext_gb300: device error {status} in marching_cubes")
+            return _views(vout, fout, V, F)
+        raise RuntimeError("isoext_gb300: marching_cubes output did not fit after resizing")
 
     def _intersect(self, level: float, compute_normals: bool):
         from .dc import Intersection

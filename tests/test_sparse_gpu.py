@@ -295,3 +295,16 @@ def test_populate_brick_mode_keeps_whole_bricks_around_the_surface():
         assert counts[bid] == full[bx] * full[by] * full[bz]
     # values are the SDF at the cells' corners, as set_values(sdf(get_points())) gives
     assert torch.equal(g.get_values(), f(g.get_points()).contiguous())
+
+
+def test_sparse_mc_retries_when_buffers_are_small():
+    vals = sphere((40, 40, 40), 0.6)
+    ids, cv = sparse_from_dense(vals, extra=200, seed=1)
+    g = make_sparse((40, 40, 40), ids, cv)
+    v0, f0 = iso.marching_cubes(g)
+    g._mc_sizes = {(g.get_num_cells(), 0.0, 0): (4, 4)}
+    v1, f1 = iso.marching_cubes(g)
+    assert torch.equal(v0, v1) and torch.equal(f0, f1)
+    g._mc_sizes = {(g.get_num_cells(), 0.0, 0): (4, len(f0))}  # faces fit, vertices do not
+    v2, f2 = iso.marching_cubes(g)
+    assert torch.equal(v0, v2) and torch.equal(f0, f2)
