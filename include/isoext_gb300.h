@@ -62,6 +62,13 @@ int iso_mc_get_config(int *threads);
 int iso_tune_set(const char *key, int value);
 int iso_tune_get(const char *key, int *value);
 
+/* Test hook of the bounded device waits (no counterpart in the reference):
+ * the scan's decoupled look-back over states that are never published
+ * (state: device, >= 32 zeroed u64) gives up after spin_limit polls
+ * (<= 2^20) and writes ISO_ERR_TIMEOUT to *status; out (device u64[2]). */
+int iso_test_wait_timeout(unsigned spin_limit, unsigned long long *state, int *status,
+                          unsigned long long *out, void *stream);
+
 /* Kernel timing for benchmarks (no counterpart in the reference).  While
  * enabled, each kernel the library launches is bracketed by CUDA events on its
  * stream.  iso_profile_read synchronises on the recorded events and returns the

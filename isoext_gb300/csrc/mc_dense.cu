@@ -305,7 +305,7 @@ __device__ __forceinline__ unsigned long long lb_pack(unsigned long long flag, u
 // segment's aggregate.  Waits are bounded: on a timeout the status is set and
 // the prefix returned is wrong (the host sees the status).
 __device__ void look_back(volatile unsigned long long* state, uint32_t seg, unsigned long long& ev,
-                          unsigned long long& ef, int* status) {
+                          unsigned long long& ef, int* status, uint32_t limit = ISO_SPIN_LIMIT) {
     const int lane = threadIdx.x & 31;
     ev = 0;
     ef = 0;
@@ -317,7 +317,7 @@ __device__ void look_back(volatile unsigned long long* state, uint32_t seg, unsi
             do {
                 st = state[j];
                 if ((st >> 62) != 0) break;
-                if (++spins > ISO_SPIN_LIMIT) {
+                if (++spins > limit) {
                     atomicCAS(status, 0, int(ISO_ERR_TIMEOUT));
                     st = LB_INC;
                     break;
@@ -730,6 +730,18 @@ __global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk,
         }
         ov += a[k];
         of += b[k];
+    }
+}
+
+// The scan's look-back for chunk `seg` over states nobody publishes: it must
+// give up after `limit` polls and set the status (a test of the bounded wait).
+__global__ void lookback_probe(unsigned long long* state, uint32_t seg, uint32_t limit, int* status,
+                               unsigned long long* out) {
+    unsigned long long ev = 0, ef = 0;
+    look_back(state, seg, ev, ef, status, limit);
+    if (threadIdx.x == 0) {
+        out[0] = ev;
+        out[1] = ef;
     }
 }
 
@@ -1207,4 +1219,15 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     const int rc = launch_count_emit(p, g, w, st);
     if (rc) return rc;
     return 0;
+}
+
+// Test hook of the bounded waits (no counterpart in isoext): runs the scan's
+// look-back for chunk 32 over `state` (device, >= 32 zeroed u64, never
+// published) with a limit of spin_limit polls; *status (device) becomes
+// ISO_ERR_TIMEOUT and the kernel returns.  spin_limit <= 2^20.
+extern "C" int iso_test_wait_timeout(unsigned spin_limit, unsigned long long* state, int* status,
+                                     unsigned long long* out, void* stream) {
+    if (!state || !status || !out || spin_limit > (1u << 20)) return ISO_ERR_ARG;
+    lookback_probe<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>(state, 32u, spin_limit, status, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }

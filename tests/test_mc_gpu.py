@@ -222,3 +222,28 @@ def test_launch_parameters_do_not_change_results():
         assert tune.current() == rep["best"]
     finally:
         tune.apply(old)
+
+
+def test_bounded_wait_times_out_with_a_status():
+    """A look-back wait on states nobody publishes gives up after its limit and
+    reports ISO_ERR_TIMEOUT; the context stays usable."""
+    import ctypes
+
+    from isoext_gb300 import _ffi
+
+    lib = _ffi.lib()
+    lib.iso_test_wait_timeout.argtypes = [ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]
+    state = torch.zeros(64, dtype=torch.int64, device="cuda")
+    status = torch.zeros(2, dtype=torch.int32, device="cuda")
+    out = torch.zeros(2, dtype=torch.int64, device="cuda")
+    rc = lib.iso_test_wait_timeout(4096, ctypes.c_void_p(state.data_ptr()), ctypes.c_void_p(status.data_ptr()),
+                                   ctypes.c_void_p(out.data_ptr()),
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(status[0]) == _ffi.ISO_ERR_TIMEOUT
+    assert lib.iso_test_wait_timeout(1 << 21, ctypes.c_void_p(state.data_ptr()), ctypes.c_void_p(status.data_ptr()),
+                                     ctypes.c_void_p(out.data_ptr()), None) == _ffi.ISO_ERR_ARG
+    v, f = run_mc(sphere((24, 24, 24), 0.5))
+    assert len(f) > 0
