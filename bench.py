@@ -49,6 +49,23 @@ WORKLOADS = {
 METRIC = "MC/DC Gcells/s @512^3 fp32"
 
 
+def max_over_ranks(ms: float, world: int, dev=None) -> float:
+    """The slowest rank's step time (replicas: every rank times its own steps)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, ms: float, world: int) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -256,11 +273,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
     # per extraction: the sum of the kernel's launches in one call
     kavg = {k: t / args.steps for k, (c, t) in kt.items()}
     top = max(kavg, key=kavg.get)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
 
     # e2e through the public API with host buffers: pinned values copied into the
     # grid (set_values with a host tensor: one H2D copy), marching_cubes, the mesh
@@ -787,11 +800,7 @@ def run_dc(args, wl, rank, world) -> dict | None:
     kt = {k: _ffi.profile_read(k) for k in DC_KERNELS}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
     launches = sum(c for c, _ in kt.values())
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
 
     # e2e: host values -> device -> grid -> the step -> mesh to host
     host = vals.cpu().pin_memory()
