@@ -15,7 +15,8 @@ enum IsoStatus : int {
     ISO_ERR_OVERFLOW = 6,     // output capacity exceeded (counts are still exact)
 };
 
-// Bounded spin limit for mbarrier waits: about a second of polling.
+// Polls before a bounded device wait gives up (with a sleep between polls: a
+// few seconds at most).
 #define ISO_SPIN_LIMIT (1u << 26)
 
 namespace iso {
@@ -50,19 +51,6 @@ __device__ __forceinline__ bool below(float v, float level) { return __fsub_rn(v
 // ---------------------------------------------------------------------------
 // Bit helpers on rows of 32-bit words indexed by column c (bit c & 31 of word c >> 5).
 
-// Word w of the row shifted so that bit c holds the row's bit c - 1.
-__device__ __forceinline__ uint32_t prev1(const uint32_t* row, int w) {
-    uint32_t lo = w > 0 ? row[w - 1] : 0u;
-    return __funnelshift_l(lo, row[w], 1);
-}
-// Word w of the row shifted so that bit c holds the row's bit c + 1.
-__device__ __forceinline__ uint32_t next1(const uint32_t* row, int w, int nw) {
-    uint32_t hi = (w + 1 < nw) ? row[w + 1] : 0u;
-    return __funnelshift_r(row[w], hi, 1);
-}
-__device__ __forceinline__ uint32_t bit_at(const uint32_t* row, int c) {
-    return (row[c >> 5] >> (c & 31)) & 1u;
-}
 // Mask of bits [lo, hi] (inclusive, in column units) within word w.
 __device__ __forceinline__ uint32_t range_mask(int w, int lo, int hi) {
     int a = lo - 32 * w, b = hi - 32 * w;
@@ -71,98 +59,6 @@ __device__ __forceinline__ uint32_t range_mask(int w, int lo, int hi) {
     if (b > 31) b = 31;
     uint32_t top = (b == 31) ? 0xffffffffu : ((2u << b) - 1u);
     return top & ~((1u << a) - 1u);
-}
-
-// ---------------------------------------------------------------------------
-// Warp-cooperative iteration over the set bits of a sequence of words.
-//
-// The warp takes 32 words at a time (one per lane), counts their set bits,
-// and hands the bits out 32 at a time, so sparse bits are processed with all
-// lanes busy instead of one lane per word.  get(i) returns word i (0 for
-// i >= n); f(i, b) runs once per set bit b of word i, on some lane.  scratch
-// points to 64 words of warp-private shared memory.
-template <class Get, class F>
-__device__ __forceinline__ void warp_foreach_bit(int first, int n, int stride, uint32_t* scratch,
-                                                 Get get, F f) {
-    const int lane = threadIdx.x & 31;
-    for (int base = first; base < n; base += stride) {
-        const int i = base + lane;
-        const uint32_t m = i < n ? get(i) : 0u;
-        const uint32_t cnt = __popc(m);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t x = __shfl_up_sync(~0u, incl, d);
-            if (lane >= d) incl += x;
-        }
-        const uint32_t total = __shfl_sync(~0u, incl, 31);
-        if (total == 0) continue;
-        scratch[lane] = m;
-        scratch[32 + lane] = incl;
-        __syncwarp();
-        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
-            const uint32_t k = k0 + lane;
-            if (k < total) {
-                // owner lane: first lane whose inclusive count exceeds k
-                int lo = 0, hi = 31;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (scratch[32 + mid] > k) hi = mid; else lo = mid + 1;
-                }
-                uint32_t mm = scratch[lo];
-                const uint32_t before = scratch[32 + lo] - __popc(mm);
-                for (uint32_t j = k - before; j; --j) mm &= mm - 1;  // drop the lower set bits
-                f(base + lo, __ffs(mm) - 1);
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// TMA bulk copies (cp.async.bulk, global -> shared) completing on an mbarrier.
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_init_fence() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
-                                         uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-            "r"(smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait; returns false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < ISO_SPIN_LIMIT; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-    }
-    return false;
 }
 
 // ---------------------------------------------------------------------------
