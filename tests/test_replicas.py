@@ -30,7 +30,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_report_the_slowest_rank():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork: the test process may hold a CUDA context
     mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
     assert dict(out) == {0: 2.0, 1: 2.0}
 
