@@ -364,9 +364,10 @@ GRAD_KERNELS = ["mc_signs", "mc_count", "mc_scan", "mc_emit", "mc_backward", "dc
 
 
 def run_grad(args, wl, rank, world) -> dict | None:
-    """One step: for each of the batch's grids, differentiable marching cubes and
-    dual contouring, loss = mean squared distance of each mesh's vertices to the
-    unit sphere, backward to the grid values (hand-written backward kernels)."""
+    """One step: differentiable marching cubes and dual contouring of the batch's
+    grids (isoext_gb300.diff, batched: one synchronisation per kind), loss = sum
+    over the meshes of the mean squared distance of their vertices to the unit
+    sphere, backward to the grid values (hand-written backward kernels)."""
     import torch
 
     from isoext_gb300 import _ffi, diff
@@ -387,10 +388,12 @@ def run_grad(args, wl, rank, world) -> dict | None:
         nverts.clear()
         for x in xs:
             x.grad = None
-            vm, _ = diff.marching_cubes(x, lo, hi)
-            vd, _ = diff.dual_contouring(x, lo, hi)
-            (loss_of(vm) + loss_of(vd)).backward()
-            nverts.append((len(vm), len(vd)))
+        # every grid's extraction is queued before one synchronisation per kind
+        mcs = diff.marching_cubes_batch(xs, lo, hi)
+        dcs = diff.dual_contouring_batch(xs, lo, hi)
+        loss = sum(loss_of(vm) + loss_of(vd) for (vm, _), (vd, _) in zip(mcs, dcs))
+        loss.backward()
+        nverts.extend((len(vm), len(vd)) for (vm, _), (vd, _) in zip(mcs, dcs))
 
     for _ in range(args.warmup):
         step()

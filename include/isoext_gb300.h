@@ -163,6 +163,15 @@ int iso_dc_dense(const float *values, int nx, int ny, int nz, const float *aabb_
                  const float *aabb_max, float level, float reg, float svd_tol, float *vertices,
                  long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
                  size_t workspace_bytes, long long *counts, int *status, void *stream);
+/* iso_dc_dense, and (each optional) the active cell ids [vertex_capacity] and
+ * their crossing offsets [vertex_capacity + 1] (isoext's Intersection cells
+ * and offsets), and the active cell each vertex came from [vertex_capacity]:
+ * what iso_dc_backward needs. */
+int iso_dc_dense_ex(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                    const float *aabb_max, float level, float reg, float svd_tol, float *vertices,
+                    long long vertex_capacity, int *faces, long long face_capacity, void *workspace,
+                    size_t workspace_bytes, long long *counts, int *status, int *cell_ids,
+                    int *cell_offsets, int *vertex_source, void *stream);
 /* Normals of existing crossings from the grid (src/its.cu:186-268). */
 int iso_dc_normals(const float *values, int nx, int ny, int nz, const float *aabb_min,
                    const float *aabb_max, const float *points, const int *cell_ids,

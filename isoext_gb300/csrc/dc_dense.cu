@@ -648,7 +648,8 @@ WeldDev weld_dev_carve(void* ws, long long capA) {
 size_t weld_dev_workspace(long long capA) { return weld_dev_carve(nullptr, capA).total; }
 
 void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
-                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st) {
+                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
+                     uint32_t* vsrc) {
     const WeldDev w = weld_dev_carve(ws, capA);
     iso::ProfScope ps("dc_weld", st);
     cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
@@ -659,7 +660,7 @@ void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long 
         dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(pts, w.used, capA, w.table, w.hcap - 1, w.rep, eff);
         dc_rep_count<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, eff);
         dc_block_scan<<<1, 1024, 0, st>>>(w.blk, w.nblk, vtot);
-        dc_rep_write<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, pts, w.newidx, vout, nullptr, eff);
+        dc_rep_write<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, pts, w.newidx, vout, vsrc, eff);
     } else {
         cudaMemsetAsync(vtot, 0, 16, st);
     }
@@ -965,10 +966,10 @@ size_t iso_dc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capa
     return carve_dense(nullptr, nx, ny, nz, vertex_capacity, face_capacity / 2).total;
 }
 
-int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
-                 float level, float reg, float svd_tol, float* vertices, long long vertex_capacity, int* faces,
-                 long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
-                 void* stream) {
+int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
+                    float level, float reg, float svd_tol, float* vertices, long long vertex_capacity, int* faces,
+                    long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
+                    int* cell_ids, int* cell_offsets, int* vertex_source, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (!counts || !status || !aabb_min || !aabb_max || vertex_capacity < 0 || face_capacity < 0) return ISO_ERR_ARG;
     if ((long long)nx * ny * nz > 0x7fffffffll) return ISO_ERR_ARG;
@@ -981,6 +982,8 @@ int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
     const DcDenseWs w = carve_dense(workspace, nx, ny, nz, capA, capQ);
     const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     long long* eff = w.tot + 4;
+    uint32_t* cells = cell_ids ? reinterpret_cast<uint32_t*>(cell_ids) : w.cells;
+    uint32_t* offs = cell_offsets ? reinterpret_cast<uint32_t*>(cell_offsets) : w.offs;
     {
         iso::ProfScope ps("mc_signs", st);
         mc_signs_launch(values, nx, ny, nz, level, w.d.S, st);
@@ -996,13 +999,13 @@ int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
     {
         iso::ProfScope ps("dc_intersect", st);
         dc_intersect<<<blocks_for(w.d.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
-            values, w.d.S, g, level, w.d.cwords, w.d.blkC, w.d.actm, w.d.offA, nullptr, nullptr, w.cells, w.offs, 0, 0,
+            values, w.d.S, g, level, w.d.cwords, w.d.blkC, w.d.actm, w.d.offA, nullptr, nullptr, cells, offs, 0, 0,
             eff);
     }
     if (capA > 0) {
         iso::ProfScope ps("dc_solve", st);
         const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-        dc_cell_solve<<<blocks_for(capA, bt), bt, 0, st>>>(values, g, level, w.cells, capA, reg, svd_tol, w.dual,
+        dc_cell_solve<<<blocks_for(capA, bt), bt, 0, st>>>(values, g, level, cells, capA, reg, svd_tol, w.dual,
                                                            eff);
     }
     {
@@ -1010,9 +1013,19 @@ int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_
         dc_quad_emit<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ, w.d.actm,
                                                                            w.d.offA, w.dual, w.tri, eff);
     }
-    weld_dev_launch(w.dual, capA, w.tri, 6 * capQ, eff, w.weld, vertices, faces, w.tot + 8, status, st);
+    weld_dev_launch(w.dual, capA, w.tri, 6 * capQ, eff, w.weld, vertices, faces, w.tot + 8, status, st,
+                    reinterpret_cast<uint32_t*>(vertex_source));
     dc_dense_finish<<<1, 1, 0, st>>>(w.tot + 8, counts);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
+                 float level, float reg, float svd_tol, float* vertices, long long vertex_capacity, int* faces,
+                 long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
+                 void* stream) {
+    return iso_dc_dense_ex(values, nx, ny, nz, aabb_min, aabb_max, level, reg, svd_tol, vertices, vertex_capacity,
+                           faces, face_capacity, workspace, workspace_bytes, counts, status, nullptr, nullptr, nullptr,
+                           stream);
 }
 
 }  // extern "C"

@@ -528,7 +528,8 @@ void iso_block_scan_launch(unsigned long long* blk, long long nblk, long long* t
 // dc_dense.cu: exact-position weld with device-side sizes
 size_t weld_dev_workspace(long long capA);
 void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
-                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st);
+                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
+                     uint32_t* vsrc);
 
 namespace {
 
@@ -731,7 +732,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
                                                          eff);
     }
     weld_dev_launch(w.soup, 3 * face_capacity, nullptr, 3 * face_capacity, eff, w.weld, vertices, faces, w.tot + 8,
-                    status, st);
+                    status, st, nullptr);
     sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }

@@ -34,6 +34,8 @@ from .mc import _first_guess, coarse_float_grid, method_id, workspace_bytes
 _vp, _i, _ll, _f = C.c_void_p, C.c_int, C.c_longlong, C.c_float
 _fa = C.POINTER(C.c_float)
 _ffi.register({
+    "iso_dc_dense_ex": ([_vp, _i, _i, _i, _fa, _fa, _f, _f, _f, _vp, _ll, _vp, _ll, _vp, C.c_size_t, _vp, _vp, _vp, _vp,
+                         _vp, _vp], _i),
     "iso_mc_dense_edges": ([_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp, C.c_size_t, _vp, _vp, _vp,
                             _vp], _i),
     "iso_mc_backward": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _vp, _vp, _vp], _i),
@@ -56,45 +58,57 @@ def _vec3(v):
     return tuple(float(x) for x in v)
 
 
+class _Launch:
+    """The buffers of one queued extraction; `small` receives its sizes."""
+
+    def __init__(self, kind, values, key, **buf):
+        self.kind, self.values, self.key = kind, values, key
+        self.__dict__.update(buf)
+
+
 # ---------------------------------------------------------------------------
 # marching cubes
 
-def _mc_forward(values: torch.Tensor, amin, amax, level: float, method: int):
-    """(vertices, faces, edges): edges[i] = 3 * (low endpoint's point id) + axis of vertex i."""
+def _mc_launch(values: torch.Tensor, amin, amax, level: float, method: int, caps=None) -> _Launch:
+    """Queues iso_mc_dense_edges on the current stream (no synchronisation)."""
     lib = _ffi.lib()
     dev = values.device
     shape = tuple(values.shape)
     key = (shape, amin, amax, float(level), method)
-    if key in _sizes:
-        nv, nf = _sizes[key]
-        cap_v, cap_f = nv + nv // 10 + 1024, nf + nf // 10 + 1024
-    else:
-        cap_v, cap_f = _first_guess(shape)
-    st = _stream(dev)
-    for _ in range(2):
-        vout = torch.empty((cap_v, 3), dtype=torch.float32, device=dev)
-        fout = torch.empty((cap_f, 3), dtype=torch.int32, device=dev)
-        edges = torch.empty(cap_v, dtype=torch.int64, device=dev)
-        ws = torch.empty(workspace_bytes(shape, cap_v, cap_f), dtype=torch.uint8, device=dev)
-        small = torch.zeros(4, dtype=torch.int64, device=dev)
-        _ffi.check(lib.iso_mc_dense_edges(_p(values), *shape, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level),
-                                          int(method), _p(vout), cap_v, _p(fout), cap_f, _p(ws), ws.numel(),
-                                          _p(small), C.c_void_p(small.data_ptr() + 16), _p(edges), st))
-        h = small.cpu()
-        nv, nf, status = int(h[0]), int(h[1]), int(h[2] & 0xFFFFFFFF)
-        if status == _ffi.ISO_ERR_OVERFLOW:
-            cap_v, cap_f = nv + 1024, nf + 1024
-            _sizes[key] = (nv, nf)
-            continue
-        if status:
-            raise RuntimeError(f"isoext_gb300: device error {status} in marching_cubes")
-        old = _sizes.get(key, (0, 0))
-        _sizes[key] = (max(old[0], nv), max(old[1], nf))
-        v, f, e = vout[:nv], fout[:nf], edges[:nv]
-        if nv and nf and coarse_float_grid(shape, amin, amax):
-            v, f, e = _weld_positions(v, f, e)
-        return v.contiguous(), f.contiguous(), e.contiguous()
-    raise RuntimeError("isoext_gb300: marching_cubes output did not fit after resizing")
+    if caps is None:
+        if key in _sizes:
+            nv, nf = _sizes[key]
+            caps = (nv + nv // 10 + 1024, nf + nf // 10 + 1024)
+        else:
+            caps = _first_guess(shape)
+    cap_v, cap_f = caps
+    L = _Launch("mc", values, key, amin=amin, amax=amax, level=level, method=method,
+                vout=torch.empty((cap_v, 3), dtype=torch.float32, device=dev),
+                fout=torch.empty((cap_f, 3), dtype=torch.int32, device=dev),
+                edges=torch.empty(cap_v, dtype=torch.int64, device=dev),
+                ws=torch.empty(workspace_bytes(shape, cap_v, cap_f), dtype=torch.uint8, device=dev),
+                small=torch.zeros(8, dtype=torch.int64, device=dev))
+    _ffi.check(lib.iso_mc_dense_edges(_p(values), *shape, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level),
+                                      int(method), _p(L.vout), cap_v, _p(L.fout), cap_f, _p(L.ws), L.ws.numel(),
+                                      _p(L.small), C.c_void_p(L.small.data_ptr() + 16), _p(L.edges), _stream(dev)))
+    return L
+
+
+def _mc_finish(L: _Launch, h):
+    """(vertices, faces, edges) from the sizes h, or None and the capacities to
+    retry with."""
+    nv, nf, status = int(h[0]), int(h[1]), int(h[2] & 0xFFFFFFFF)
+    if status == _ffi.ISO_ERR_OVERFLOW:
+        _sizes[L.key] = (nv, nf)
+        return None, (nv + 1024, nf + 1024)
+    if status:
+        raise RuntimeError(f"isoext_gb300: device error {status} in marching_cubes")
+    old = _sizes.get(L.key, (0, 0))
+    _sizes[L.key] = (max(old[0], nv), max(old[1], nf))
+    v, f, e = L.vout[:nv], L.fout[:nf], L.edges[:nv]
+    if nv and nf and coarse_float_grid(L.values.shape, L.amin, L.amax):
+        v, f, e = _weld_positions(v, f, e)
+    return (v.contiguous(), f.contiguous(), e.contiguous()), None
 
 
 def _weld_positions(v, f, e):
@@ -113,12 +127,36 @@ def _weld_positions(v, f, e):
     return uniq[used].view(torch.float32), remap[f2].to(torch.int32), e[first[used]]
 
 
+def _collect(launches, relaunch):
+    """One synchronisation for all queued launches; launches whose buffers were
+    too small are queued again with exact capacities (a second one)."""
+    if not launches:
+        return []
+    sizes = torch.stack([L.small for L in launches]).cpu()
+    finish = {"mc": _mc_finish, "dc": _dc_finish}
+    out, again = [None] * len(launches), []
+    for i, (L, h) in enumerate(zip(launches, sizes)):
+        res, caps = finish[L.kind](L, h)
+        if res is None:
+            again.append((i, relaunch(L, caps)))
+        else:
+            out[i] = res
+    if again:
+        sizes = torch.stack([L.small for _, L in again]).cpu()
+        for (i, L), h in zip(again, sizes):
+            res, _ = finish[L.kind](L, h)
+            if res is None:
+                raise RuntimeError(f"isoext_gb300: {L.kind} output did not fit after resizing")
+            out[i] = res
+    return out
+
+
 class _MarchingCubes(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, values, amin, amax, level, method):
-        v, f, e = _mc_forward(values.detach(), amin, amax, level, method)
+    def forward(ctx, values, res, box):
+        v, f, e = res
         ctx.save_for_backward(values, e)
-        ctx.box = (amin, amax, float(level))
+        ctx.box = box
         ctx.mark_non_differentiable(f)
         return v, f
 
@@ -131,7 +169,16 @@ class _MarchingCubes(torch.autograd.Function):
             _ffi.check(_ffi.lib().iso_mc_backward(_p(values), *values.shape, _ffi.fvec3(amin), _ffi.fvec3(amax),
                                                   level, _p(e), e.numel(), _p(gv.contiguous()), _p(grad),
                                                   _stream(values.device)))
-        return grad, None, None, None, None
+        return grad, None, None
+
+
+def _mc_relaunch(L, caps):
+    return _mc_launch(L.values, L.amin, L.amax, L.level, L.method, caps)
+
+
+def _mc_forward(values: torch.Tensor, amin, amax, level: float, method: int):
+    """(vertices, faces, edges): edges[i] = 3 * (low endpoint's point id) + axis of vertex i."""
+    return _collect([_mc_launch(values, amin, amax, level, method)], _mc_relaunch)[0]
 
 
 def marching_cubes(values: torch.Tensor, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0, 1.0, 1.0),
@@ -139,55 +186,87 @@ def marching_cubes(values: torch.Tensor, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(
     """Marching cubes of a dense grid of values [nx, ny, nz] over the box, with
     vertices differentiable with respect to values.  Returns (vertices float32
     [V, 3], faces int32 [F, 3]), the same as isoext_gb300.marching_cubes."""
-    _check_cuda_f32(values, ndim=3)
-    return _MarchingCubes.apply(values, _vec3(aabb_min), _vec3(aabb_max), float(level), method_id(method))
+    return marching_cubes_batch([values], aabb_min, aabb_max, level, method)[0]
+
+
+def marching_cubes_batch(values_list, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0, 1.0, 1.0),
+                         level: float = 0.0, method: str = "nagae"):
+    """marching_cubes of several grids: every extraction is queued before one
+    synchronisation reads all their sizes.  Returns a list of (vertices, faces)."""
+    amin, amax, mid = _vec3(aabb_min), _vec3(aabb_max), method_id(method)
+    for x in values_list:
+        _check_cuda_f32(x, ndim=3)
+    res = _collect([_mc_launch(x.detach(), amin, amax, float(level), mid) for x in values_list], _mc_relaunch)
+    return [_MarchingCubes.apply(x, r, (amin, amax, float(level))) for x, r in zip(values_list, res)]
 
 
 # ---------------------------------------------------------------------------
 # dual contouring
 
-class _Values:
-    """The attributes of a UniformGrid the dense DC steps read, over a values tensor."""
+def _dc_launch(values: torch.Tensor, amin, amax, level: float, reg: float, svd_tol: float, caps=None) -> _Launch:
+    """Queues iso_dc_dense_ex on the current stream (no synchronisation)."""
+    from . import dc
 
-    def __init__(self, values, amin, amax):
-        self._values = values
-        self.shape = list(values.shape)
-        self.aabb_min, self.aabb_max = list(amin), list(amax)
+    lib = _ffi.lib()
+    dev = values.device
+    shape = tuple(values.shape)
+    key = (shape, float(level), tuple(amin), tuple(amax))
+    if caps is None:
+        if key in dc._dc_sizes:
+            a, q = dc._dc_sizes[key]
+            caps = (a + a // 10 + 1024, 2 * q + (2 * q) // 10 + 1024)
+        else:
+            caps = _first_guess(shape)
+    cap_v, cap_f = caps
+    L = _Launch("dc", values, key, amin=amin, amax=amax, level=level, reg=reg, svd_tol=svd_tol,
+                vout=torch.empty((cap_v, 3), dtype=torch.float32, device=dev),
+                fout=torch.empty((cap_f, 3), dtype=torch.int32, device=dev),
+                cells=torch.empty(cap_v, dtype=torch.int32, device=dev),
+                offs=torch.empty(cap_v + 1, dtype=torch.int32, device=dev),
+                src=torch.empty(cap_v, dtype=torch.int32, device=dev),
+                ws=torch.empty(dc.dc_workspace_bytes(shape, cap_v, cap_f), dtype=torch.uint8, device=dev),
+                small=torch.zeros(8, dtype=torch.int64, device=dev))
+    _ffi.check(lib.iso_dc_dense_ex(_p(values), *shape, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level), float(reg),
+                                   float(svd_tol), _p(L.vout), cap_v, _p(L.fout), cap_f, _p(L.ws), L.ws.numel(),
+                                   _p(L.small), C.c_void_p(L.small.data_ptr() + 48), _p(L.cells), _p(L.offs),
+                                   _p(L.src), _stream(dev)))
+    return L
+
+
+def _dc_finish(L: _Launch, h):
+    """(vertices, faces, cells, offsets, source) from the sizes h, or None and
+    the capacities to retry with."""
+    from . import dc
+
+    V, F, A, Q, status = int(h[0]), int(h[1]), int(h[2]), int(h[4]), int(h[6] & 0xFFFFFFFF)
+    dc._dc_sizes[L.key] = (A, Q)
+    if status == _ffi.ISO_ERR_OVERFLOW:
+        return None, (A + 1024, 2 * Q + 1024)
+    if status:
+        raise RuntimeError(f"isoext_gb300: device error {status} in dual_contouring")
+    if V == 0 or F == 0:
+        dev = L.values.device
+        return (torch.zeros((0, 3), dtype=torch.float32, device=dev), torch.zeros((0, 3), dtype=torch.int32, device=dev),
+                None, None, None), None
+    return (L.vout[:V], L.fout[:F], L.cells[:A], L.offs[:A + 1], L.src[:V]), None
+
+
+def _dc_relaunch(L, caps):
+    return _dc_launch(L.values, L.amin, L.amax, L.level, L.reg, L.svd_tol, caps)
 
 
 def _dc_forward(values: torch.Tensor, amin, amax, level: float, reg: float, svd_tol: float):
     """(vertices, faces, cells, offsets, source): cells / offsets are the active
     cells and their crossings' CSR ranges; source[i] = active cell of vertex i."""
-    from . import dc
-
-    lib = _ffi.lib()
-    dev = values.device
-    nx, ny, nz = values.shape
-    st = _stream(dev)
-    empty = (torch.zeros((0, 3), dtype=torch.float32, device=dev), torch.zeros((0, 3), dtype=torch.int32, device=dev))
-    g = _Values(values, amin, amax)
-    ws, (A, K, Q) = dc._classify_quads(g, level)
-    if A == 0 or Q == 0:
-        return (*empty, None, None, None)
-    cells = torch.empty(A, dtype=torch.int32, device=dev)
-    offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
-    dual = torch.empty((A, 3), dtype=torch.float32, device=dev)
-    _ffi.check(lib.iso_dc_intersect_solve(_p(values), nx, ny, nz, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level),
-                                          _p(ws), A, K, _p(cells), _p(offs), float(reg), float(svd_tol), _p(dual),
-                                          st))
-    tri = torch.empty(6 * Q, dtype=torch.int32, device=dev)
-    _ffi.check(lib.iso_dc_quads_emit(nx, ny, nz, _p(ws), _p(dual), _p(tri), st))
-    src = torch.empty(A, dtype=torch.int32, device=dev)
-    v, f = dc.weld_dual(lib, dev, dual, A, tri, st, src=src)
-    return v, f, cells, offs, src[:len(v)]
+    return _collect([_dc_launch(values, amin, amax, level, reg, svd_tol)], _dc_relaunch)[0]
 
 
 class _DualContouring(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, values, amin, amax, level, reg, svd_tol):
-        v, f, cells, offs, src = _dc_forward(values.detach(), amin, amax, level, reg, svd_tol)
+    def forward(ctx, values, res, meta):
+        v, f, cells, offs, src = res
         ctx.save_for_backward(values, cells, offs, src)
-        ctx.meta = (amin, amax, float(level), float(reg), float(svd_tol))
+        ctx.meta = meta
         ctx.mark_non_differentiable(f)
         return v, f
 
@@ -196,7 +275,7 @@ class _DualContouring(torch.autograd.Function):
         values, cells, offs, src = ctx.saved_tensors
         grad = torch.zeros_like(values)
         if gv is None or cells is None or src.numel() == 0:
-            return grad, None, None, None, None, None
+            return grad, None, None
         amin, amax, level, reg, svd_tol = ctx.meta
         A = cells.numel()
         gdual = torch.zeros((A, 3), dtype=torch.float32, device=values.device)
@@ -204,7 +283,7 @@ class _DualContouring(torch.autograd.Function):
         _ffi.check(_ffi.lib().iso_dc_backward(_p(values), *values.shape, _ffi.fvec3(amin), _ffi.fvec3(amax), level,
                                               _p(cells), _p(offs), A, reg, svd_tol, None, _p(gdual), _p(grad), None,
                                               _stream(values.device)))
-        return grad, None, None, None, None, None
+        return grad, None, None
 
 
 def dual_contouring(values: torch.Tensor, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0, 1.0, 1.0),
@@ -214,6 +293,17 @@ def dual_contouring(values: torch.Tensor, aabb_min=(-1.0, -1.0, -1.0), aabb_max=
     and vertices differentiable with respect to values.  Returns (vertices
     float32 [V, 3], faces int32 [F, 3]), the same as
     isoext_gb300.dual_contouring."""
-    _check_cuda_f32(values, ndim=3)
-    return _DualContouring.apply(values, _vec3(aabb_min), _vec3(aabb_max), float(level), float(reg),
-                                 float(svd_tol))
+    return dual_contouring_batch([values], aabb_min, aabb_max, level, reg, svd_tol)[0]
+
+
+def dual_contouring_batch(values_list, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0, 1.0, 1.0),
+                          level: float = 0.0, reg: float = 1e-2, svd_tol: float = 1e-6):
+    """dual_contouring of several grids with one synchronisation (see
+    marching_cubes_batch).  Returns a list of (vertices, faces)."""
+    amin, amax = _vec3(aabb_min), _vec3(aabb_max)
+    for x in values_list:
+        _check_cuda_f32(x, ndim=3)
+    res = _collect([_dc_launch(x.detach(), amin, amax, float(level), float(reg), float(svd_tol)) for x in values_list],
+                   _dc_relaunch)
+    meta = (amin, amax, float(level), float(reg), float(svd_tol))
+    return [_DualContouring.apply(x, r, meta) for x, r in zip(values_list, res)]

@@ -65,3 +65,22 @@ def test_tunables_roundtrip_and_reject_bad_values():
     assert lib.iso_tune_set(b"no.such.key", 1) == 1 and "unknown" in _ffi.last_error()
     tune.apply(old)
     assert tune.current() == old
+
+
+def test_library_has_no_unresolved_symbols_of_its_own():
+    """Every symbol the library calls is defined in it or in the C / C++ runtime
+    (a mismatched declaration between translation units would show up here)."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    from isoext_gb300 import _build
+
+    nm = shutil.which("nm")
+    if not nm:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--undefined-only", str(_build.build())], capture_output=True, text=True).stdout
+    own = [ln.split()[-1] for ln in out.splitlines()
+           if ln.strip() and "@" not in ln and not ln.split()[-1].startswith(("_ITM_", "__gmon_start__"))]
+    assert not own, own

@@ -129,3 +129,24 @@ def test_empty_surface_gives_empty_tensors_and_zero_gradient():
         v.sum().backward()
         assert float(x.grad.abs().max()) == 0.0
         x.grad = None
+
+
+def test_batched_extraction_equals_one_by_one():
+    """The batch entry points queue every grid before one synchronisation; the
+    meshes and gradients are those of one call per grid."""
+    from isoext_gb300 import diff
+
+    grids = [_crop(seed)[0] for seed in (1, 2, 3)]
+    _, lo, hi = _crop(1)
+    xs = [torch.from_numpy(g).cuda().requires_grad_(True) for g in grids]
+    mcs = diff.marching_cubes_batch(xs, lo, hi)
+    dcs = diff.dual_contouring_batch(xs, lo, hi)
+    sum(sphere_loss(v) for v, _ in mcs + dcs).backward()
+    for g, x, (vm, fm), (vd, fd) in zip(grids, xs, mcs, dcs):
+        y = torch.from_numpy(g).cuda().requires_grad_(True)
+        vm1, fm1 = diff.marching_cubes(y, lo, hi)
+        vd1, fd1 = diff.dual_contouring(y, lo, hi)
+        (sphere_loss(vm1) + sphere_loss(vd1)).backward()
+        assert torch.equal(vm, vm1) and torch.equal(fm, fm1) and torch.equal(vd, vd1) and torch.equal(fd, fd1)
+        # atomics make the summation order vary: equal to FP32 rounding
+        assert torch.allclose(x.grad, y.grad, rtol=1e-5, atol=1e-7 * float(y.grad.abs().max()))
