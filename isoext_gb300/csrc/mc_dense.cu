@@ -1081,7 +1081,7 @@ __global__ void __launch_bounds__(SIGN_BLOCK) mc_signs(const float* __restrict__
 #pragma unroll
                 for (int u = 0; u < SIGN_UNROLL; ++u) {
                     const int z = 32 * (w0 + u) + lane;
-                    v[u] = (w0 + u < NWg && z < nz) ? __ldg(rp + z) : level;
+                    v[u] = (w0 + u < NWg && z < nz) ? __ldcs(rp + z) : level;  // read once: evict first
                 }
 #pragma unroll
                 for (int u = 0; u < SIGN_UNROLL; ++u) {
