@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
 // their totals by decoupled look-back.  The last chunk writes the totals and
 // checks the capacities.
 constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_PER = 4;
+constexpr int SCAN_PER = 1;
 
 __global__ void __launch_bounds__(SCAN_THREADS) mc_scan(unsigned long long* blk, uint32_t nseg,
                                                         unsigned long long* ctr, unsigned long long* state,
