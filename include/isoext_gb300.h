@@ -300,6 +300,51 @@ int iso_dc_backward(const float *values, int nx, int ny, int nz, const float *aa
 int iso_sdf_union_grid(const float *prims, int nx, int ny, int nz, const float *aabb_min,
                        const float *aabb_max, float *out, void *stream);
 
+/* ---- native serving loop -------------------------------------------------
+ * No counterpart in isoext.  A server keeps `slots` worker threads on the
+ * current device, each with its own stream, device buffers and CUDA graphs of
+ * iso_sdf_union_grid + iso_mc_dense / iso_dc_dense per (kind, n, method,
+ * level).  Requests are admitted first come, first served when a worker is
+ * free and the running requests' worst-case bytes plus the new one's fit
+ * budget_bytes; results come back in host memory.  Thread-safe. */
+typedef struct IsoServer IsoServer;
+typedef struct {
+    int kind;            /* 0 marching cubes, 1 dual contouring (reg 1e-2, svd_tol 1e-6) */
+    int n;               /* points per axis of the cubic grid over [-1, 1]^3 (2 .. 1290) */
+    int method;          /* marching cubes: 0 nagae, 1 lorensen */
+    float level;
+    int num_prims;       /* 1 .. 32 */
+    const float *prims;  /* host [num_prims][7]: kind (0 sphere, 1 box), centre xyz, radius | half-extents xyz */
+} IsoServeRequest;
+typedef struct {
+    long long ticket;
+    int status;                    /* 0, or an ISO_ERR_* code */
+    int slot;                      /* the worker that ran it */
+    long long num_vertices, num_faces;
+    float *vertices;               /* host [V, 3] (malloc); release with iso_serve_free_result */
+    int *faces;                    /* host [F, 3] */
+    double t_submit, t_start, t_done;  /* steady-clock seconds */
+} IsoServeResult;
+/* warm_sizes: grid sizes whose buffers and graphs (both kinds, nagae, level 0)
+ * every slot builds up front; other keys are built on first use. */
+int iso_serve_create(int slots, long long budget_bytes, const int *warm_sizes, int num_warm_sizes,
+                     IsoServer **server);
+/* Returns the request's ticket (>= 0), or -ISO_ERR_ARG / -ISO_ERR_WORKSPACE
+ * (larger than the budget).  The primitives are copied. */
+long long iso_serve_submit(IsoServer *server, const IsoServeRequest *request);
+/* Blocks until the ticket's request is done (timeout_s < 0: no limit;
+ * ISO_ERR_TIMEOUT when it runs out) and moves its result out. */
+int iso_serve_wait(IsoServer *server, long long ticket, double timeout_s, IsoServeResult *result);
+void iso_serve_free_result(IsoServeResult *result);
+/* stats[0] completed, [1] most requests running at once, [2] most bytes
+ * admitted at once, [3] queued now. */
+int iso_serve_stats(IsoServer *server, long long *stats);
+/* Finishes the queued requests, then frees everything. */
+int iso_serve_destroy(IsoServer *server);
+/* Capacities of the buffers built after the call, as a fraction (0, 1] of the
+ * default bound; meshes that do not fit rerun with exact capacities (tests). */
+int iso_serve_set_capacity_scale(IsoServer *server, double scale);
+
 #ifdef __cplusplus
 }
 #endif

@@ -328,6 +328,116 @@ class Server(Scheduler):
         return v, f
 
 
+class _ServeRequest(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n", C.c_int), ("method", C.c_int), ("level", C.c_float),
+                ("num_prims", C.c_int), ("prims", C.POINTER(C.c_float))]
+
+
+class _ServeResult(C.Structure):
+    _fields_ = [("ticket", C.c_longlong), ("status", C.c_int), ("slot", C.c_int), ("num_vertices", C.c_longlong),
+                ("num_faces", C.c_longlong), ("vertices", C.POINTER(C.c_float)), ("faces", C.POINTER(C.c_int)),
+                ("t_submit", C.c_double), ("t_start", C.c_double), ("t_done", C.c_double)]
+
+
+_ffi.register({
+    "iso_serve_create": ([C.c_int, C.c_longlong, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+    "iso_serve_submit": ([C.c_void_p, C.POINTER(_ServeRequest)], C.c_longlong),
+    "iso_serve_wait": ([C.c_void_p, C.c_longlong, C.c_double, C.POINTER(_ServeResult)], C.c_int),
+    "iso_serve_free_result": ([C.POINTER(_ServeResult)], None),
+    "iso_serve_stats": ([C.c_void_p, C.POINTER(C.c_longlong)], C.c_int),
+    "iso_serve_destroy": ([C.c_void_p], C.c_int),
+    "iso_serve_set_capacity_scale": ([C.c_void_p, C.c_double], C.c_int),
+})
+
+
+class _NativeFuture:
+    def __init__(self, server, ticket: int, rid: int):
+        self._server, self._ticket, self._rid = server, ticket, rid
+        self._result = None
+
+    def result(self, timeout: float | None = None) -> Result:
+        if self._result is None:
+            self._result = self._server._wait(self._ticket, self._rid, timeout)
+        return self._result
+
+
+class NativeServer:
+    """The served loop in C++ (iso_serve_*): worker threads, streams, per-slot
+    buffers and CUDA graphs and the admission all run natively, without the
+    Python interpreter; Python submits requests and collects meshes.  Same
+    requests and results as Server (and solve_plain), bit for bit.
+
+    warm_sizes: grid sizes whose buffers and graphs are built up front (the
+    launch parameters are tuned first on the largest, as Server.warmup does)."""
+
+    def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, warm_sizes=(), tune: bool = True,
+                 device=None):
+        import torch
+
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.tuned = None
+        torch.cuda.set_device(self.device)
+        if tune and warm_sizes:
+            from . import tune as tuner
+
+            n = int(max(warm_sizes))
+            req = random_requests(1, seed=0, sizes=(n,))[0]
+            prims = torch.from_numpy(prims_buffer(req.prims)).to(self.device)
+            self.tuned = _tune_on(n, prims, self.device, 0.0, tuner)
+        sizes = (C.c_int * max(1, len(warm_sizes)))(*[int(n) for n in warm_sizes])
+        handle = C.c_void_p()
+        _ffi.check(_ffi.lib().iso_serve_create(int(slots), int(budget_bytes), sizes, len(warm_sizes), C.byref(handle)))
+        self._h = handle
+        self.budget = int(budget_bytes)
+
+    def submit(self, req: Request) -> _NativeFuture:
+        p = np.ascontiguousarray(np.asarray(req.prims, np.float32).reshape(-1, 7))
+        from .mc import method_id
+
+        q = _ServeRequest(0 if req.kind == "mc" else 1, int(req.n), method_id(req.method), float(req.level), len(p),
+                          p.ctypes.data_as(C.POINTER(C.c_float)))
+        t = _ffi.lib().iso_serve_submit(self._h, C.byref(q))
+        if t < 0:
+            if -t == _ffi.ISO_ERR_WORKSPACE:
+                raise ValueError(f"request needs more than the budget {self.budget}")
+            raise ValueError(f"isoext_gb300: request refused (error {-t})")
+        return _NativeFuture(self, int(t), req.rid)
+
+    def _wait(self, ticket: int, rid: int, timeout: float | None) -> Result:
+        r = _ServeResult()
+        rc = _ffi.lib().iso_serve_wait(self._h, ticket, -1.0 if timeout is None else float(timeout), C.byref(r))
+        if rc == _ffi.ISO_ERR_TIMEOUT:
+            raise TimeoutError(f"request {rid} not done after {timeout} s")
+        _ffi.check(rc)
+        try:
+            if r.status:
+                raise RuntimeError(f"isoext_gb300: device error {r.status} in a served request")
+            V, F = int(r.num_vertices), int(r.num_faces)
+            v = np.ctypeslib.as_array(r.vertices, shape=(V, 3)).copy() if V else np.zeros((0, 3), np.float32)
+            f = np.ctypeslib.as_array(r.faces, shape=(F, 3)).copy() if F else np.zeros((0, 3), np.int32)
+        finally:
+            _ffi.lib().iso_serve_free_result(C.byref(r))
+        return Result(rid, v, f, r.t_submit, r.t_start, r.t_done, int(r.slot))
+
+    def stats(self) -> dict:
+        s = (C.c_longlong * 4)()
+        _ffi.check(_ffi.lib().iso_serve_stats(self._h, s))
+        return {"completed": s[0], "max_running": s[1], "max_admitted_bytes": s[2], "queued": s[3]}
+
+    @property
+    def max_running(self) -> int:
+        return int(self.stats()["max_running"])
+
+    @property
+    def max_reserved(self) -> int:
+        return int(self.stats()["max_admitted_bytes"])
+
+    def close(self) -> None:
+        if self._h:
+            _ffi.lib().iso_serve_destroy(self._h)
+            self._h = None
+
+
 def _tune_on(n: int, prims_dev, device, level: float, tuner) -> dict:
     """Tunes the launch parameters on an n^3 grid of the union in prims_dev."""
     import torch

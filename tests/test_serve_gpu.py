@@ -80,3 +80,47 @@ def test_served_overflow_reruns_with_exact_sizes(monkeypatch):
     srv.close()
     for (r, p), s in zip(big, out):
         assert _same((s.vertices, s.faces), p)
+
+
+def test_native_server_results_equal_plain_results():
+    from isoext_gb300.serve import NativeServer, random_requests, solve_plain
+
+    reqs = random_requests(24, seed=5, sizes=(32, 48, 64))
+    solo = [solve_plain(r) for r in reqs]
+    srv = NativeServer(slots=3, budget_bytes=1 << 30, warm_sizes=(32, 48, 64))
+    futs = [srv.submit(r) for r in reqs]
+    served = [f.result(timeout=300) for f in futs]
+    stats = srv.stats()
+    srv.close()
+    assert stats["completed"] == len(reqs) and stats["max_running"] > 1
+    for r, s, p in zip(reqs, served, solo):
+        assert s.rid == r.rid
+        assert _same((s.vertices, s.faces), p), (r.rid, r.kind, r.n)
+
+
+def test_native_server_reruns_meshes_larger_than_its_buffers():
+    import ctypes
+
+    from isoext_gb300 import _ffi
+    from isoext_gb300.serve import NativeServer, random_requests, solve_plain
+
+    reqs = random_requests(8, seed=9, sizes=(48,))
+    srv = NativeServer(slots=2, budget_bytes=1 << 30, warm_sizes=(), tune=False)
+    assert _ffi.lib().iso_serve_set_capacity_scale(srv._h, ctypes.c_double(1e-4)) == 0
+    out = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    srv.close()
+    for r, s in zip(reqs, out):
+        assert _same((s.vertices, s.faces), solve_plain(r)), (r.rid, r.kind)
+
+
+def test_native_server_refuses_bad_requests():
+    import numpy as np
+
+    from isoext_gb300.serve import NativeServer, Request
+
+    srv = NativeServer(slots=1, budget_bytes=64 << 20, warm_sizes=(), tune=False)
+    with pytest.raises(ValueError, match="budget"):
+        srv.submit(Request("mc", 400, np.zeros((1, 7), np.float32)))
+    with pytest.raises(ValueError):
+        srv.submit(Request("mc", 32, np.zeros((0, 7), np.float32)))
+    srv.close()
