@@ -371,23 +371,30 @@ long long iso_serve_submit(IsoServer* srv, const IsoServeRequest* req) {
         delete job;
         return -ISO_ERR_WORKSPACE;
     }
+    long long ticket;
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         if (srv->closing) {
             delete job;
             return -ISO_ERR_ARG;
         }
-        job->ticket = srv->next_ticket++;
-        srv->queue.push_back(job);
+        ticket = job->ticket = srv->next_ticket++;
+        srv->queue.push_back(job);  // a worker owns (and frees) the job from here
     }
     srv->cv_work.notify_all();
-    return job->ticket;
+    return ticket;
 }
 
 int iso_serve_wait(IsoServer* srv, long long ticket, double timeout_s, IsoServeResult* out) {
-    if (!srv || !out || ticket < 0) return ISO_ERR_ARG;
+    if (!srv || !out || ticket < 0) {
+        iso::set_last_error("iso_serve_wait: null server or result, or a negative ticket");
+        return ISO_ERR_ARG;
+    }
     std::unique_lock<std::mutex> lk(srv->mu);
-    if (ticket >= srv->next_ticket) return ISO_ERR_ARG;
+    if (ticket >= srv->next_ticket) {
+        iso::set_last_error("iso_serve_wait: no such ticket");
+        return ISO_ERR_ARG;
+    }
     const auto ready = [&] { return srv->done.count(ticket) > 0; };
     if (timeout_s < 0) {
         srv->cv_done.wait(lk, ready);
