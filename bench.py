@@ -1087,10 +1087,13 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--slots", type=int, default=None, help="serve workload: worker slots (default 8)")
     ap.add_argument("--quick", action="store_true",
                     help="no load phase before the timed region (for profiler runs; clocks are not sampled under load)")
     args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.slots is not None and wl["kind"] == "serve":
+        wl["slots"] = args.slots
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":
