@@ -39,6 +39,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 WORKLOADS = {
     "mc512": dict(kind="mc", n=512, r=0.8, desc="mc_dense_512_sphere_r0.8"),
     "mc128": dict(kind="mc", n=128, r=0.8, desc="mc_dense_128_sphere_r0.8"),
+    "dc512": dict(kind="dc1", n=512, r=0.8, desc="dc_dense_512_sphere_r0.8"),
     "dc256": dict(kind="dc", n=256, seed=7, desc="dc_dense_256_csg_seed7"),
     "serve": dict(kind="serve", count=512, seed=2026, sizes=(64, 96, 128, 192, 256), mc_share=0.7,
                   slots=8, budget_gb=40, desc="served_mixed_512req_n64-256_mc70"),
@@ -200,6 +201,8 @@ def run_ours(args, wl, rank, world) -> dict | None:
         return run_dc(args, wl, rank, world)
     if wl["kind"] == "serve":
         return run_serve(args, wl, rank)
+    if wl["kind"] == "dc1":
+        return run_dc_one_call(args, wl, rank, world)
     if wl["kind"] == "grad":
         return run_grad(args, wl, rank, world)
     if wl["kind"] == "sparse":
@@ -874,6 +877,134 @@ def run_dc(args, wl, rank, world) -> dict | None:
     return out
 
 
+DC1_KERNELS = ["mc_signs", "dc_classify", "dc_intersect", "dc_solve", "dc_quads", "dc_weld"]
+
+
+def run_dc_one_call(args, wl, rank, world) -> dict | None:
+    """Dense dual contouring of the sphere |p| - r with normals from the grid
+    (isoext.dual_contouring(grid) without an intersection), one call
+    (iso_dc_dense) per step with device buffers."""
+    import torch
+
+    import isoext_gb300 as iso
+    from isoext_gb300 import _ffi
+    from isoext_gb300.dc import dc_dense_into, dc_workspace_bytes
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = wl["n"]
+    vals_np = sphere_values(n, wl["r"])
+    vals = torch.from_numpy(vals_np).to(dev)
+    cells = (n - 1) ** 3
+    lib = _ffi.lib()
+    stream = torch.cuda.current_stream(dev)
+    grid = iso.UniformGrid([n] * 3, device=dev)
+    grid.set_values(vals)
+    v, f = iso.dual_contouring(grid)
+    nv, nf = len(v), len(f)
+    from isoext_gb300 import dc as dcmod
+    A, Q = dcmod._dc_sizes[(tuple(grid.shape), 0.0, tuple(grid.aabb_min), tuple(grid.aabb_max))]
+    capv, capf = A + 1024, 2 * Q + 1024
+    vout = torch.empty((capv, 3), dtype=torch.float32, device=dev)
+    fout = torch.empty((capf, 3), dtype=torch.int32, device=dev)
+    ws = torch.empty(dc_workspace_bytes([n] * 3, capv, capf), dtype=torch.uint8, device=dev)
+    small = torch.zeros(8, dtype=torch.int64, device=dev)
+    lo, hi = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+
+    def step():
+        _ffi.check(dc_dense_into(vals, lo, hi, 0.0, 1e-2, 1e-6, vout, fout, ws, small, stream.cuda_stream))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        t_end = time.perf_counter() + (0.0 if args.quick else 0.6)
+        while time.perf_counter() < t_end:
+            for _ in range(20):
+                step()
+            torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    h = small.cpu()
+    assert int(h[6] & 0xFFFFFFFF) == 0 and (int(h[0]), int(h[1])) == (nv, nf), "dc512 sizes"
+    lib.iso_profile_reset()  # per-kernel times in a separate pass (events between kernels)
+    lib.iso_profile_enable(1)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    lib.iso_profile_enable(0)
+    kt = {k: _ffi.profile_read(k) for k in DC1_KERNELS}
+    kstep = {k: t / args.steps for k, (c, t) in kt.items() if c}
+    launches = sum(c for c, _ in kt.values())
+    # e2e: pinned host values -> grid, dual_contouring, mesh into pinned buffers
+    pinned = torch.from_numpy(vals_np).pin_memory()
+    vh = torch.empty((capv, 3), dtype=torch.float32).pin_memory()
+    fh = torch.empty((capf, 3), dtype=torch.int32).pin_memory()
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        grid.set_values(pinned)
+        vv, ff = iso.dual_contouring(grid)
+        vh[:len(vv)].copy_(vv)
+        fh[:len(ff)].copy_(ff)
+        if i >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e_t)
+    if rank != 0:
+        return None
+    pts, words = n ** 3, n * n * ((n + 31) // 32)
+    kbytes = {"mc_signs": 4 * pts + 4 * words, "dc_classify": 2 * 4 * words, "dc_intersect": 4 * words + 8 * A,
+              "dc_solve": 32 * A + 12 * A, "dc_quads": 4 * words + 24 * Q, "dc_weld": 12 * A + 24 * Q + 12 * nv}
+    top = max(kstep, key=kstep.get)
+    pk = peaks()
+    achieved = kbytes[top] / (kstep[top] * 1e-3) / 1e9
+    algo = 4 * pts + 12 * nv + 12 * nf
+    out = {
+        "metric": METRIC, "value": round(world * cells / (ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": f"synthetic: sphere SDF |p|-{wl['r']} on [-1,1]^3",
+        "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "normals": "from the grid",
+                   "vertices": nv, "faces": nf, "active_cells": A, "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2 (values {4 * pts / 1e6:.0f} MB > 129 MB L2)"},
+        "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 4 * pts, "d2h_bytes_per_step": 12 * (nv + nf)},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
+                     "algorithmic_bytes": kbytes[top], "kernel_ms": round(kstep[top], 4),
+                     "traffic": profiled_traffic(wl["desc"], top),
+                     "pipeline": {"algorithmic_bytes": algo, "achieved": round(algo / (ms * 1e-3) / 1e9, 1),
+                                  "frac": round(algo / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 4)}},
+        "kernel_ms": {k: round(v_, 4) for k, v_ in kstep.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        from oracle import Oracle
+
+        ora = Oracle()
+        m = 128  # a bounded sample: the same sphere on 128^3, one thread
+        sv = sphere_values(m, wl["r"])
+        t0 = time.perf_counter()
+        ora.dc_dense(sv)
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round((m - 1) ** 3 / sec / 1e9, 5), "unit": "Gcells/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"the same sphere on {m}^3 ({(m - 1) ** 3} cells): oracle C port (FP64 QEF), "
+                                         f"1 thread, {sec:.2f} s"}
+    return out
+
+
 def cpu_dc(ora, vals_np, shape) -> float:
     """Seconds for the oracle's C port of the same DC step on one host thread."""
     import torch
@@ -937,7 +1068,7 @@ def run_reference(args, wl, rank) -> dict | None:
         return None
     from oracle import Oracle
 
-    if wl["kind"] in ("sparse", "grad", "serve"):
+    if wl["kind"] in ("sparse", "grad", "serve", "dc1"):
         return run_reference_other(args, wl)
     n = wl["n"]
     if wl["kind"] == "dc":
@@ -995,7 +1126,17 @@ def run_reference_other(args, wl) -> dict:
 
     ora = Oracle()
     threads = os.cpu_count() or 1
-    if wl["kind"] == "sparse":
+    if wl["kind"] == "dc1":
+        m = 256  # a bounded sample of the same sphere, one slab per host thread
+        sv = sphere_values(m, wl["r"])
+        slabs = _slabs(m, threads)
+
+        def one():
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                list(ex.map(lambda ab: ora.dc_dense(np.ascontiguousarray(sv[ab[0]:ab[1] + 1])), slabs))
+        units, unit, metric = (m - 1) ** 3 / 1e9, "Gcells/s", METRIC
+        sample = f"the same sphere on {m}^3 per step as {threads} x-slabs on {threads} threads (oracle C port)"
+    elif wl["kind"] == "sparse":
         import isoext_gb300 as iso
 
         g = iso.SparseGrid([wl["n"]] * 3, device="cpu")
