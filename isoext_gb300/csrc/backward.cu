@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
                                                    float* gnormals) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A) return;
-    double gx[3] = {gdual[3 * a], gdual[3 * a + 1], gdual[3 * a + 2]};
+    float gx[3] = {gdual[3 * a], gdual[3 * a + 1], gdual[3 * a + 2]};
     const uint32_t cid = cell_ids[a];
     const int cz = int(cid % uint32_t(g.nz - 1));
     const uint32_t rr = cid / uint32_t(g.nz - 1);
@@ -183,12 +183,11 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
     for (int q = 0; q < 3; ++q) {
         const float lo = coord(g, q, uint32_t(ci[q])), hi = coord(g, q, uint32_t(ci[q] + 1));
         const float xf = float(Q.x[q]);
-        if (xf < lo || xf > hi) gx[q] = 0.0;  // clipped: the output does not move
+        if (xf < lo || xf > hi) gx[q] = 0.0f;  // clipped: the output does not move
     }
-    if (gx[0] == 0.0 && gx[1] == 0.0 && gx[2] == 0.0) return;
-    double lam[3] = {0.0, 0.0, 0.0};
-    apply_pinv(Q.w, Q.q, Q.keep, gx, lam);
-    const float l[3] = {float(lam[0]), float(lam[1]), float(lam[2])};
+    if (gx[0] == 0.0f && gx[1] == 0.0f && gx[2] == 0.0f) return;
+    float l[3] = {0.0f, 0.0f, 0.0f};
+    apply_pinv_f(Q.w, Q.q, Q.keep, gx, l);  // lambda = pinv(M) g
     const float rk = reg / float(K);
     float gc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < K; ++k) {

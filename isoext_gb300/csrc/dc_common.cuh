@@ -127,16 +127,34 @@ __device__ __forceinline__ void jacobi3f(float a[3][3], float w[3], float q[3][3
 }
 
 // x += pinv(A) r with the eigen-decomposition (w, q) and the kept mask.
-__device__ __forceinline__ void apply_pinv(const float w[3], const float q[3][3], unsigned keep,
-                                           const double r[3], double x[3]) {
+__device__ __forceinline__ void apply_pinv_f(const float w[3], const float q[3][3], unsigned keep, const float r[3],
+                                             float x[3]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (!((keep >> i) & 1u)) continue;
-        const double qr = double(q[0][i]) * r[0] + double(q[1][i]) * r[1] + double(q[2][i]) * r[2];
-        const double c = qr / double(w[i]);
+        const float c = (q[0][i] * r[0] + q[1][i] * r[1] + q[2][i] * r[2]) / w[i];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) x[k] += c * double(q[k][i]);
+        for (int k = 0; k < 3; ++k) x[k] += c * q[k][i];
     }
+}
+
+// b - row . x with FP32 error-free transformations (Dekker's product by fma,
+// Knuth's two-sum), rounded once at the end: the residual to about twice FP32's
+// precision, which is what the refinement step needs (GB300's FP64 rate is a
+// small fraction of its FP32 rate).
+__device__ __forceinline__ float residual_ff(float b, const float* row, const float* x) {
+    float s = b, e = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const float p = __fmul_rn(row[j], x[j]);
+        const float pe = fmaf(row[j], x[j], -p);  // row[j] * x[j] = p + pe exactly
+        const float t = __fsub_rn(s, p);           // two-sum of s and -p
+        const float bb = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(-p, bb));
+        s = t;
+        e = __fadd_rn(e, __fsub_rn(err, pe));
+    }
+    return __fadd_rn(s, e);
 }
 
 // QEF of a cell: normal equations of the crossings' planes plus reg times the
@@ -199,17 +217,16 @@ __device__ __forceinline__ void qef_finish(Qef& Q, uint32_t K, float reg, float 
 #pragma unroll
     for (int i = 0; i < 3; ++i) keep |= (fabsf(Q.w[i]) > thr ? 1u : 0u) << i;
     Q.keep = keep;
-    double* x = Q.x;
-    x[0] = x[1] = x[2] = 0.0;
-    double r[3] = {atb[0], atb[1], atb[2]};
-    apply_pinv(Q.w, Q.q, keep, r, x);
-    // one refinement step with an FP64 residual (the FP32 eigenvectors leave
-    // an error of about cond(A) * eps; the residual recovers it)
+    float xf[3] = {0.0f, 0.0f, 0.0f};
+    apply_pinv_f(Q.w, Q.q, keep, atb, xf);
+    // one refinement step with a residual to twice FP32's precision (the FP32
+    // eigenvectors leave an error of about cond(A) * eps; the residual recovers it)
+    float r[3], dx[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-        r[i] = double(atb[i]) - (double(ata[3 * i]) * x[0] + double(ata[3 * i + 1]) * x[1] +
-                                 double(ata[3 * i + 2]) * x[2]);
-    apply_pinv(Q.w, Q.q, keep, r, x);
+    for (int i = 0; i < 3; ++i) r[i] = residual_ff(atb[i], ata + 3 * i, xf);
+    apply_pinv_f(Q.w, Q.q, keep, r, dx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Q.x[i] = double(xf[i]) + double(dx[i]);
 }
 
 // The QEF of K crossings stored as points [K, 3] and normals [K, 3].
