@@ -162,7 +162,7 @@ __device__ __forceinline__ float residual_ff(float b, const float* row, const fl
 // operation rounded, crossings in order); solved by the pseudo-inverse of the
 // 3x3 system with the threshold svd_tol * largest singular value
 // (src/batched_la.cu:152-178), from an FP32 eigen-decomposition refined once
-// with an FP64 residual.
+// with a double-FP32 residual.
 struct Qef {
     float ata[9], atb[3];  // the system (reg included after qef_finish)
     float px, py, pz;      // sum of the points

@@ -9,8 +9,8 @@
 //   solve      per active cell: QEF normal equations accumulated in the
 //              reference's order (src/dc.cu:14-65), a register-resident 3x3
 //              symmetric Jacobi solve in FP32 with the reference's pseudo-inverse
-//              threshold (src/batched_la.cu:152-178) refined once with an FP64
-//              residual, clipped to the cell (src/dc.cu:82-99).
+//              threshold (src/batched_la.cu:152-178) refined once with a
+//              double-FP32 residual, clipped to the cell (src/dc.cu:82-99).
 //   quads      crossed grid edges in the reference's quad order (by low
 //              endpoint, then z, y, x edge; src/grid/uniform.cu:60-83), their 4
 //              cells, orientation and diagonal split (src/dc.cu:101-157).
@@ -411,6 +411,41 @@ __device__ __forceinline__ float dist3(const float* a, const float* b) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
 }
 
+// Lane whose inclusive prefix first exceeds j (prefixes nondecreasing, j < total).
+__device__ __forceinline__ int owner_lane(uint32_t incl, uint32_t j) {
+    int lo = 0;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const uint32_t pv = __shfl_sync(~0u, incl, lo + s - 1);
+        if (pv <= j) lo += s;
+    }
+    return lo;
+}
+
+// The k-th quad of a point word in the reference's order: by bit (low endpoint
+// z) ascending, then the bit's z, y, x edges.
+__device__ __forceinline__ void kth_quad(uint32_t mz, uint32_t my, uint32_t mx, uint32_t k, int& b, int& ax) {
+    int lo = 0;  // largest lo with (quads of bits < lo) <= k
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const uint32_t m = (1u << (lo + s)) - 1u;  // lo + s <= 31
+        if (uint32_t(__popc(mz & m) + __popc(my & m) + __popc(mx & m)) <= k) lo += s;
+    }
+    b = lo;
+    const uint32_t below = (1u << lo) - 1u;
+    uint32_t r = k - uint32_t(__popc(mz & below) + __popc(my & below) + __popc(mx & below));
+    ax = 0;
+    if ((mz >> b) & 1u) {
+        if (r == 0) { ax = 2; return; }
+        --r;
+    }
+    if ((my >> b) & 1u) {
+        if (r == 0) { ax = 1; return; }
+    }
+}
+
+// The quads of a block of point words, handed out over the lanes of each warp
+// (a word has 0 .. 96 of them): every lane emits one quad per round.
 __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restrict__ S, Grid3 g,
                                                          long long nwords,
                                                          const unsigned long long* __restrict__ blk,
@@ -422,9 +457,10 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
     __shared__ uint32_t sm[66];
     const long long i = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
     const int NWg = (g.nz + 31) / 32;
+    const int lane = threadIdx.x & 31;
     // dn: the triangle indices the output holds (6 Q, or 0 over capacity)
     const unsigned long long qmax = dn ? (unsigned long long)(dn[2] / 6) : ~0ull;
-    uint32_t mz = 0, my = 0, mx = 0;
+    uint32_t mz = 0, my = 0, mx = 0, sw = 0;
     int x = 0, y = 0, w = 0;
     if (i < nwords) {
         w = int(i % NWg);
@@ -432,55 +468,67 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
         y = int(r % g.ny);
         x = int(r / g.ny);
         quad_masks(S, g, x, y, w, mz, my, mx);
+        sw = srow(S, g, x, y)[w];
     }
+    const uint32_t nq = __popc(mz) + __popc(my) + __popc(mx);
     uint32_t eq, e1, tq, t1;
-    block_scan2(__popc(mz) + __popc(my) + __popc(mx), 0u, eq, e1, tq, t1, sm);
-    if (i >= nwords) return;
-    unsigned long long q = blk[2 * blockIdx.x] + eq;
-    if (q + __popc(mz) + __popc(my) + __popc(mx) > qmax) return;
-    const uint32_t s = srow(S, g, x, y)[w];
-    uint32_t all = mz | my | mx;
-    while (all) {
-        const int b = __ffs(all) - 1;
-        all &= all - 1;
-        const int z = 32 * w + b;
+    block_scan2(nq, 0u, eq, e1, tq, t1, sm);
+    const unsigned long long qb = blk[2 * blockIdx.x];
+    uint32_t incl = nq;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(~0u, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(~0u, incl, 31);
+    for (uint32_t rr = 0; rr < total; rr += 32) {
+        const uint32_t j = rr + lane;
+        const int o = owner_lane(incl, min(j, total - 1));
+        const uint32_t oexcl = __shfl_sync(~0u, incl - nq, o), oeq = __shfl_sync(~0u, eq, o);
+        const uint32_t omz = __shfl_sync(~0u, mz, o), omy = __shfl_sync(~0u, my, o), omx = __shfl_sync(~0u, mx, o);
+        const uint32_t os = __shfl_sync(~0u, sw, o);
+        const int ox = __shfl_sync(~0u, x, o), oy = __shfl_sync(~0u, y, o), ow = __shfl_sync(~0u, w, o);
+        if (j >= total) continue;
+        const uint32_t k = j - oexcl;
+        const unsigned long long q = qb + oeq + k;
+        if (q >= qmax) continue;
+        int b, ax;
+        kth_quad(omz, omy, omx, k, b, ax);
+        const int z = 32 * ow + b;
         // is_out = v(p0) <= v(p1): for a crossed edge this holds exactly when
         // the low endpoint p0 is below the level
-        const bool out = (s >> b) & 1u;
+        const bool out = (os >> b) & 1u;
+        // edge_neighbors_table (src/shared_luts.cu:78-81): the 4 cells are p - o_i
+        int c[4][3];
+        if (ax == 0) {
+            const int off[4][3] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}};
+            for (int t = 0; t < 4; ++t) { c[t][0] = ox - off[t][0]; c[t][1] = oy - off[t][1]; c[t][2] = z - off[t][2]; }
+        } else if (ax == 1) {
+            const int off[4][3] = {{0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 0, 0}};
+            for (int t = 0; t < 4; ++t) { c[t][0] = ox - off[t][0]; c[t][1] = oy - off[t][1]; c[t][2] = z - off[t][2]; }
+        } else {
+            const int off[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+            for (int t = 0; t < 4; ++t) { c[t][0] = ox - off[t][0]; c[t][1] = oy - off[t][1]; c[t][2] = z - off[t][2]; }
+        }
+        int32_t qi[4];
 #pragma unroll
-        for (int ax = 2; ax >= 0; --ax) {  // quad order for one point: z, y, x edge
-            const uint32_t m = ax == 2 ? mz : (ax == 1 ? my : mx);
-            if (!((m >> b) & 1u)) continue;
-            // edge_neighbors_table (src/shared_luts.cu:78-81): the 4 cells are p - o_i
-            int c[4][3];
-            if (ax == 0) {
-                const int o[4][3] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}};
-                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
-            } else if (ax == 1) {
-                const int o[4][3] = {{0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 0, 0}};
-                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
-            } else {
-                const int o[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
-                for (int k = 0; k < 4; ++k) { c[k][0] = x - o[k][0]; c[k][1] = y - o[k][1]; c[k][2] = z - o[k][2]; }
-            }
-            int32_t qi[4];
-            for (int k = 0; k < 4; ++k) qi[k] = int32_t(active_index(actm, offA, g, c[k][0], c[k][1], c[k][2]));
-            if (!out) {
-                const int32_t t0 = qi[0], t1 = qi[1];
-                qi[0] = qi[3]; qi[1] = qi[2]; qi[2] = t1; qi[3] = t0;
-            }
-            float v[4][3];
-            for (int k = 0; k < 4; ++k)
-                for (int a = 0; a < 3; ++a) v[k][a] = dual[3 * (long long)qi[k] + a];
-            int32_t* o6 = tri + 6 * q;
-            if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
-                o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0];
-                o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
-            } else {
-                o6[0] = qi[2]; o6[1] = qi[0]; o6[2] = qi[1];
-                o6[3] = qi[0]; o6[4] = qi[2]; o6[5] = qi[3];
-            }
-            ++q;
+        for (int t = 0; t < 4; ++t) qi[t] = int32_t(active_index(actm, offA, g, c[t][0], c[t][1], c[t][2]));
+        if (!out) {
+            const int32_t t0 = qi[0], t1q = qi[1];
+            qi[0] = qi[3]; qi[1] = qi[2]; qi[2] = t1q; qi[3] = t0;
+        }
+        float v[4][3];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) v[t][a] = dual[3 * (long long)qi[t] + a];
+        int32_t* o6 = tri + 6 * q;
+        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+            o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0];
+            o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
+        } else {
+            o6[0] = qi[2]; o6[1] = qi[0]; o6[2] = qi[1];
+            o6[3] = qi[0]; o6[4] = qi[2]; o6[5] = qi[3];
         }
     }
 }
