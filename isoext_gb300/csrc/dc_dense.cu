@@ -68,6 +68,16 @@ __device__ __forceinline__ uint32_t case_of(const uint32_t* cw8, int b) {
     return cs;
 }
 
+// Crossings of the active cells of a cell word: the edge table's crossed
+// edges are exactly the edges whose corners differ in sign, and corner j's sign
+// word is cw8[j], so this is a sum of 12 popcounts.
+__device__ __forceinline__ uint32_t word_crossings(const uint32_t* cw8, uint32_t act) {
+    uint32_t nk = 0;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) nk += __popc((cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)]) & act);
+    return nk;
+}
+
 // Block-wide exclusive scan of two values per thread (DC_BLOCK threads).
 __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea, uint32_t& eb,
                                             uint32_t& ta, uint32_t& tb, uint32_t* sm /*66*/) {
@@ -113,13 +123,9 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_cell_count(const uint32_t* __rest
         const long long r = i / NWc;
         const int cy = int(r % (g.ny - 1)), cx = int(r / (g.ny - 1));
         uint32_t cw8[8];
-        uint32_t act = cell_act(S, g, cx, cy, w, cw8);
+        const uint32_t act = cell_act(S, g, cx, cy, w, cw8);
         na = __popc(act);
-        while (act) {
-            const int b = __ffs(act) - 1;
-            act &= act - 1;
-            nk += __popc(uint32_t(ISO_EDGE_STATUS[case_of(cw8, b)]));
-        }
+        nk = word_crossings(cw8, act);
     }
     uint32_t ea, ek, ta, tk;
     block_scan2(na, nk, ea, ek, ta, tk, sm);
@@ -196,12 +202,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_intersect(const float* __restrict
         cx = int(r / (g.ny - 1));
         act = cell_act(S, g, cx, cy, w, cw8);
         na = __popc(act);
-        uint32_t m = act;
-        while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1;
-            nk += __popc(uint32_t(ISO_EDGE_STATUS[case_of(cw8, b)]));
-        }
+        nk = word_crossings(cw8, act);
     }
     uint32_t ea, ek, ta, tk;
     block_scan2(na, nk, ea, ek, ta, tk, sm);
