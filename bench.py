@@ -877,7 +877,7 @@ def run_dc(args, wl, rank, world) -> dict | None:
     return out
 
 
-DC1_KERNELS = ["mc_signs", "dc_classify", "dc_intersect", "dc_solve", "dc_quads", "dc_weld"]
+DC1_KERNELS = ["mc_signs", "dc_classify", "dc_solve", "dc_weld", "dc_quads"]
 
 
 def run_dc_one_call(args, wl, rank, world) -> dict | None:
@@ -963,8 +963,10 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
     if rank != 0:
         return None
     pts, words = n ** 3, n * n * ((n + 31) // 32)
-    kbytes = {"mc_signs": 4 * pts + 4 * words, "dc_classify": 2 * 4 * words, "dc_intersect": 4 * words + 8 * A,
-              "dc_solve": 32 * A + 12 * A, "dc_quads": 4 * words + 24 * Q, "dc_weld": 12 * A + 24 * Q + 12 * nv}
+    # per kernel: the bitmap / values it must read and what it must write
+    kbytes = {"mc_signs": 4 * pts + 4 * words, "dc_classify": 4 * words + 8 * words + 8 * A,
+              "dc_solve": 4 * A + 32 * A + 12 * A + A, "dc_weld": A + 12 * A + 4 * A + 4 * A + 12 * nv,
+              "dc_quads": 8 * A + 12 * A + 4 * A + 24 * Q}
     top = max(kstep, key=kstep.get)
     pk = peaks()
     achieved = kbytes[top] / (kstep[top] * 1e-3) / 1e9

@@ -23,6 +23,7 @@
 #define ISO_LUT_DECL static __constant__ const
 #include "luts.h"
 #include "dc_common.cuh"
+#include "lookback.cuh"
 #include "profile.cuh"
 
 namespace {
@@ -247,8 +248,8 @@ __global__ void __launch_bounds__(256) dc_points(const float* __restrict__ vals,
     const uint32_t est = ISO_EDGE_STATUS[cs];
     unsigned long long k = cell_off[a];
 #pragma unroll 1
-    for (int e = 0; e < 12; ++e) {
-        if (!((est >> e) & 1u)) continue;
+    for (uint32_t em = est; em; em &= em - 1) {  // this lane's crossed edges, ascending
+        const int e = __ffs(em) - 1;
         float p[3];
         edge_cross(cc, level, e, p);
         points[3 * k + 0] = p[0];
@@ -288,13 +289,34 @@ __global__ void dc_normals(const float* __restrict__ vals, Grid3 g, const float*
     }
 }
 
+// Whether faces use the dual vertex of active cell (cx, cy, cz) with crossed
+// edges est: some crossed edge has all four of its cells inside the grid (then
+// its quad is emitted).  Cells at least one cell away from the grid's faces
+// have only such edges.
+__device__ __forceinline__ bool cell_used(const Grid3& g, int cx, int cy, int cz, uint32_t est) {
+    if (cx >= 1 && cx <= g.nx - 3 && cy >= 1 && cy <= g.ny - 3 && cz >= 1 && cz <= g.nz - 3) return est != 0;
+    for (uint32_t em = est; em; em &= em - 1) {
+        const int e = __ffs(em) - 1;
+        const int ca = ISO_EDGE_CORNERS[2 * e], ax = ca ^ ISO_EDGE_CORNERS[2 * e + 1];  // 4 x, 2 y, 1 z
+        const int x = cx + (ca >> 2), y = cy + ((ca >> 1) & 1), z = cz + (ca & 1);
+        const bool okx = ax == 4 || (x >= 1 && x <= g.nx - 2);
+        const bool oky = ax == 2 || (y >= 1 && y <= g.ny - 2);
+        const bool okz = ax == 1 || (z >= 1 && z <= g.nz - 2);
+        if (okx && oky && okz) return true;
+    }
+    return false;
+}
+
 // Crossings, grid normals and the QEF solve of each active cell in one pass,
 // when nobody asked for the intersection: the same arithmetic as dc_points
-// followed by dc_solve, without writing points and normals.
+// followed by dc_solve, without writing points and normals.  used (optional):
+// per cell, whether faces use its dual vertex.
 __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
                                                      float svd_tol, float* __restrict__ dual,
-                                                     const long long* __restrict__ dn) {
+                                                     const long long* __restrict__ dn,
+                                                     uint8_t* __restrict__ used) {
+    iso::grid_wait();
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) A = dn[0];
     if (a >= A) return;
@@ -308,12 +330,13 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
     const uint32_t est = ISO_EDGE_STATUS[cs];
+    if (used) used[a] = cell_used(g, cx, cy, cz, est) ? 1 : 0;
     Qef Q;
     qef_init(Q);
     uint32_t K = 0;
 #pragma unroll 1
-    for (int e = 0; e < 12; ++e) {
-        if (!((est >> e) & 1u)) continue;
+    for (uint32_t em = est; em; em &= em - 1) {  // this lane's crossed edges, ascending
+        const int e = __ffs(em) - 1;
         float p[3], n[3];
         edge_cross(cc, level, e, p);
         cell_normal(cc, p, n);
@@ -636,26 +659,292 @@ __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uin
     if (i < n) fout[i] = int32_t(newidx[rep[tri ? tri[i] : int32_t(i)]]);
 }
 
-// One-call dual contouring: the sizes found on the device, checked against the
-// capacities.  eff = (A, K, 6 Q) the later kernels use, all 0 when something
-// does not fit (the status says so; counts hold the sizes for a retry).
-__global__ void dc_dense_sizes(const long long* __restrict__ tak, const long long* __restrict__ tq,
-                               long long capA, long long capQ, long long* eff, long long* counts, int* status) {
-    const long long A = tak[0], K = tak[1], Q = tq[0];
-    const bool ok = A <= capA && Q <= capQ && A < 0x7fffffffll && 6 * Q < 0x7fffffffll && K < 0x7fffffffll;
-    if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
-    eff[0] = ok ? A : 0;
-    eff[1] = ok ? K : 0;
-    eff[2] = ok ? 6 * Q : 0;
-    eff[3] = capA;  // V <= A <= capA
-    counts[0] = 0;
-    counts[1] = ok ? 2 * Q : 0;
-    counts[2] = A;
-    counts[3] = K;
-    counts[4] = Q;
+
+// ---------------------------------------------------------------------------
+// One-call dual contouring: after the sign pass, four kernels chained by
+// programmatic dependent launch, with the sizes kept on the device.
+//
+//   dc_cells       per cell word: active cells, crossings, and the quads each
+//                  active cell owns.  A quad's owner is the cell whose lowest
+//                  corner is the low endpoint of the quad's edge, so the
+//                  reference's quad order (low endpoint, then z, y, x edge) is
+//                  the owners' order.  One pass, offsets by decoupled
+//                  look-back; the last tile checks the sizes.
+//   dc_cell_solve  the QEF solve and whether faces use the cell.
+//   dc_weld_local  the exact-position weld.  A dual vertex is clipped to its
+//                  cell's closed box, and the boxes of different cells meet only
+//                  on shared faces, so a vertex strictly inside its box has a
+//                  position of its own, and one on a face can only equal the
+//                  vertices of the cells around that face, edge or corner.
+//                  Representatives (smallest index of a position) are numbered
+//                  in cell order by a look-back.
+//   dc_cell_quads  each active cell's quads with the final vertex numbers.
+
+// Crossed edges of one cell (bit b of a cell word): the 12 corner-sign XORs.
+__device__ __forceinline__ uint32_t cell_crossings(const uint32_t* ex, int b) {
+    uint32_t n = 0;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) n += (ex[e] >> b) & 1u;
+    return n;
 }
 
-__global__ void dc_dense_finish(const long long* __restrict__ vtot, long long* counts) { counts[0] = vtot[0]; }
+__global__ void __launch_bounds__(DC_BLOCK) dc_cells(const uint32_t* __restrict__ S, Grid3 g, long long nwords,
+                                                     unsigned long long* ticket, unsigned long long* stAQ,
+                                                     unsigned long long* stK, uint32_t* __restrict__ actm,
+                                                     uint32_t* __restrict__ offA, uint32_t* __restrict__ cell_ids,
+                                                     uint32_t* __restrict__ qoff, uint32_t* __restrict__ cell_off,
+                                                     long long capA, long long capQ, long long* eff,
+                                                     long long* counts, int* status) {
+    __shared__ uint32_t sm[66];
+    __shared__ uint32_t tile_s;
+    __shared__ unsigned long long pre_s[3];
+    iso::grid_wait();
+    if (threadIdx.x == 0) tile_s = uint32_t(atomicAdd(ticket, 1ull));
+    __syncthreads();
+    const uint32_t tile = tile_s;
+    const long long i = (long long)tile * DC_BLOCK + threadIdx.x;
+    const int NWc = (g.nz - 1 + 31) / 32;
+    uint32_t act = 0, qz = 0, qy = 0, qx = 0, na = 0, nk = 0, nq = 0;
+    uint32_t cw8[8];
+    int cx = 0, cy = 0, w = 0;
+    if (i < nwords) {
+        w = int(i % NWc);
+        const long long r = i / NWc;
+        cy = int(r % (g.ny - 1));
+        cx = int(r / (g.ny - 1));
+        act = cell_act(S, g, cx, cy, w, cw8);
+        if (act) {
+            na = __popc(act);
+            nk = word_crossings(cw8, act);
+            // owned edges: corner 0 to corner 1 (z), 2 (y), 4 (x); complete when
+            // the edge's other two coordinates are >= 1 (the upper bounds hold
+            // for every cell)
+            const uint32_t zin = iso::range_mask(w, 1, g.nz - 2);
+            if (cx >= 1 && cy >= 1) qz = (cw8[0] ^ cw8[1]) & act;
+            if (cx >= 1) qy = (cw8[0] ^ cw8[2]) & act & zin;
+            if (cy >= 1) qx = (cw8[0] ^ cw8[4]) & act & zin;
+            nq = __popc(qz) + __popc(qy) + __popc(qx);
+        }
+    }
+    uint32_t ea, eq, ta, tq, ek, e_, tk, t_;
+    block_scan2(na, nq, ea, eq, ta, tq, sm);
+    block_scan2(nk, 0u, ek, e_, tk, t_, sm);
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        unsigned long long pa, pq;
+        lb_tile(stAQ, tile, ta, tq, pa, pq, status);
+        if (threadIdx.x == 0) { pre_s[0] = pa; pre_s[1] = pq; }
+    } else if (warp == 1) {
+        unsigned long long pk, p_;
+        lb_tile(stK, tile, tk, 0, pk, p_, status);
+        if (threadIdx.x == 32) pre_s[2] = pk;
+    }
+    __syncthreads();
+    const unsigned long long A0 = pre_s[0], Q0 = pre_s[1], K0 = pre_s[2];
+    if (threadIdx.x == 0 && tile == uint32_t((nwords + DC_BLOCK - 1) / DC_BLOCK) - 1) {
+        const long long A = (long long)(A0 + ta), K = (long long)(K0 + tk), Q = (long long)(Q0 + tq);
+        const bool ok = A <= capA && Q <= capQ && A < (long long)LB_MASK31 && K < (long long)LB_MASK31 &&
+                        6 * Q < 0x7fffffffll;
+        if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+        eff[0] = ok ? A : 0;
+        eff[1] = ok ? K : 0;
+        eff[2] = ok ? 6 * Q : 0;
+        eff[3] = capA;
+        counts[0] = 0;
+        counts[1] = ok ? 2 * Q : 0;
+        counts[2] = A;
+        counts[3] = K;
+        counts[4] = Q;
+        if (cell_off && ok) cell_off[A] = uint32_t(K);
+    }
+    if (i >= nwords) return;
+    actm[i] = act;
+    offA[i] = uint32_t(A0 + ea);
+    if (!act) return;
+    uint32_t ex[12];
+#pragma unroll
+    for (int e = 0; e < 12; ++e) ex[e] = cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)];
+    unsigned long long a = A0 + ea, q = Q0 + eq, k = K0 + ek;
+    const long long row = ((long long)cx * (g.ny - 1) + cy) * (g.nz - 1);
+    while (act && a < (unsigned long long)capA) {
+        const int b = __ffs(act) - 1;
+        act &= act - 1;
+        cell_ids[a] = uint32_t(row + 32 * w + b);
+        qoff[a] = uint32_t(q);
+        if (cell_off) cell_off[a] = uint32_t(k);
+        q += ((qz >> b) & 1u) + ((qy >> b) & 1u) + ((qx >> b) & 1u);
+        k += cell_crossings(ex, b);
+        ++a;
+    }
+}
+
+// Cells along one axis whose closed interval [coord(i), coord(i + 1)] holds v,
+// for v in cell c's interval: [i0, i1] around c (wider than c +- 1 only when
+// grid coordinates repeat, on grids finer than FP32 resolves).
+__device__ __forceinline__ void cells_holding(const Grid3& g, int axis, int c, float v, int& i0, int& i1) {
+    const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    i0 = c;
+    i1 = c;
+    while (i0 > 0 && coord(g, axis, uint32_t(i0)) == v) --i0;
+    while (i1 < n - 2 && coord(g, axis, uint32_t(i1 + 1)) == v) ++i1;
+}
+
+__global__ void __launch_bounds__(DC_BLOCK) dc_weld_local(Grid3 g, const uint32_t* __restrict__ cell_ids,
+                                                          const uint8_t* __restrict__ used,
+                                                          const float* __restrict__ dual,
+                                                          const uint32_t* __restrict__ actm,
+                                                          const uint32_t* __restrict__ offA,
+                                                          const long long* __restrict__ eff,
+                                                          unsigned long long* ticket, unsigned long long* state,
+                                                          uint32_t* __restrict__ vmap, float* __restrict__ vout,
+                                                          uint32_t* __restrict__ vsrc, long long* counts,
+                                                          int* status) {
+    __shared__ uint32_t sm[66];
+    __shared__ uint32_t tile_s;
+    __shared__ unsigned long long pre_s;
+    iso::grid_wait();
+    if (threadIdx.x == 0) tile_s = uint32_t(atomicAdd(ticket, 1ull));
+    __syncthreads();
+    const uint32_t tile = tile_s;
+    const long long a = (long long)tile * DC_BLOCK + threadIdx.x;
+    const long long A = eff[0];
+    uint32_t is = 0, m = 0xffffffffu;
+    float p[3] = {0.0f, 0.0f, 0.0f};
+    if (a < A && used[a]) {
+        p[0] = dual[3 * a];
+        p[1] = dual[3 * a + 1];
+        p[2] = dual[3 * a + 2];
+        const uint32_t cid = cell_ids[a];
+        const int cz = int(cid % uint32_t(g.nz - 1));
+        const uint32_t rr = cid / uint32_t(g.nz - 1);
+        const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+        int x0, x1, y0, y1, z0, z1;
+        cells_holding(g, 0, cx, p[0], x0, x1);
+        cells_holding(g, 1, cy, p[1], y0, y1);
+        cells_holding(g, 2, cz, p[2], z0, z1);
+        uint32_t rep = uint32_t(a);
+        if (x0 != x1 || y0 != y1 || z0 != z1) {
+            const int NWc = (g.nz - 1 + 31) / 32;
+            const uint32_t k0 = pos_bits(p[0]), k1 = pos_bits(p[1]), k2 = pos_bits(p[2]);
+            for (int x = x0; x <= x1; ++x)
+                for (int y = y0; y <= y1; ++y)
+                    for (int z = z0; z <= z1; ++z) {
+                        if (x == cx && y == cy && z == cz) continue;
+                        const long long wi = ((long long)x * (g.ny - 1) + y) * NWc + (z >> 5);
+                        const uint32_t mw = actm[wi], bit = uint32_t(z & 31);
+                        if (!((mw >> bit) & 1u)) continue;
+                        const uint32_t ib = offA[wi] + __popc(mw & ((1u << bit) - 1u));
+                        if (ib < rep && used[ib] && pos_bits(dual[3ll * ib]) == k0 &&
+                            pos_bits(dual[3ll * ib + 1]) == k1 && pos_bits(dual[3ll * ib + 2]) == k2)
+                            rep = ib;
+                    }
+        }
+        is = rep == uint32_t(a) ? 1u : 0u;
+        if (!is) m = 0x80000000u | rep;
+    }
+    uint32_t e, e_, t, t_;
+    block_scan2(is, 0u, e, e_, t, t_, sm);
+    if (threadIdx.x < 32) {
+        unsigned long long pv, p_;
+        lb_tile(state, tile, t, 0, pv, p_, status);
+        if (threadIdx.x == 0) {
+            pre_s = pv;
+            if (tile == gridDim.x - 1) counts[0] = (long long)(pv + t);
+        }
+    }
+    __syncthreads();
+    if (is) {
+        const unsigned long long o = pre_s + e;  // < V <= A: inside the vertex capacity
+        m = uint32_t(o);
+        vout[3 * o] = p[0];
+        vout[3 * o + 1] = p[1];
+        vout[3 * o + 2] = p[2];
+        if (vsrc) vsrc[o] = uint32_t(a);
+    }
+    if (a < A) vmap[a] = m;
+}
+
+__device__ __forceinline__ uint32_t sign_at(const uint32_t* S, const Grid3& g, int x, int y, int z) {
+    return (srow(S, g, x, y)[z >> 5] >> (z & 31)) & 1u;
+}
+
+// Final vertex number of active cell i: its own, or its representative's.
+__device__ __forceinline__ int32_t vertex_of(const uint32_t* vmap, uint32_t i) {
+    uint32_t m = vmap[i];
+    if (m != 0xffffffffu && (m & 0x80000000u)) m = vmap[m & 0x7fffffffu];
+    return int32_t(m);
+}
+
+// The quads active cell a owns, in the reference's order and orientation
+// (src/dc.cu:101-157): the 4 cells around the edge are p - o_i with the offsets
+// of edge_neighbors_table (src/shared_luts.cu:78-81), the owner being o_0 = 0.
+__global__ void __launch_bounds__(256) dc_cell_quads(const uint32_t* __restrict__ S, Grid3 g,
+                                                     const uint32_t* __restrict__ cell_ids,
+                                                     const uint32_t* __restrict__ qoff,
+                                                     const uint32_t* __restrict__ actm,
+                                                     const uint32_t* __restrict__ offA,
+                                                     const float* __restrict__ dual,
+                                                     const uint32_t* __restrict__ vmap,
+                                                     const long long* __restrict__ eff, int32_t* __restrict__ faces) {
+    iso::grid_wait();
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= eff[0]) return;
+    const uint32_t cid = cell_ids[a];
+    const int cz = int(cid % uint32_t(g.nz - 1));
+    const uint32_t rr = cid / uint32_t(g.nz - 1);
+    const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+    const uint32_t s0 = sign_at(S, g, cx, cy, cz);
+    // owned edges, in the order z, y, x
+    const bool ez = cx >= 1 && cy >= 1 && sign_at(S, g, cx, cy, cz + 1) != s0;
+    const bool ey = cx >= 1 && cz >= 1 && sign_at(S, g, cx, cy + 1, cz) != s0;
+    const bool ex = cy >= 1 && cz >= 1 && sign_at(S, g, cx + 1, cy, cz) != s0;
+    if (!(ez || ey || ex)) return;
+    unsigned long long q = qoff[a];
+    const float own[3] = {dual[3 * a], dual[3 * a + 1], dual[3 * a + 2]};
+#pragma unroll
+    for (int ax = 2; ax >= 0; --ax) {
+        if (!(ax == 2 ? ez : (ax == 1 ? ey : ex))) continue;
+        // offsets o_1..o_3 of the other three cells
+        int o[3][3];
+        if (ax == 0) {
+            const int t[3][3] = {{0, 1, 0}, {0, 1, 1}, {0, 0, 1}};
+            for (int u = 0; u < 3; ++u) for (int d = 0; d < 3; ++d) o[u][d] = t[u][d];
+        } else if (ax == 1) {
+            const int t[3][3] = {{0, 0, 1}, {1, 0, 1}, {1, 0, 0}};
+            for (int u = 0; u < 3; ++u) for (int d = 0; d < 3; ++d) o[u][d] = t[u][d];
+        } else {
+            const int t[3][3] = {{1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+            for (int u = 0; u < 3; ++u) for (int d = 0; d < 3; ++d) o[u][d] = t[u][d];
+        }
+        uint32_t qi[4];
+        qi[0] = uint32_t(a);
+#pragma unroll
+        for (int u = 0; u < 3; ++u)
+            qi[u + 1] = active_index(actm, offA, g, cx - o[u][0], cy - o[u][1], cz - o[u][2]);
+        // is_out = v(p0) <= v(p1): for a crossed edge, p0 below the level
+        if (!s0) {
+            const uint32_t t0 = qi[0], t1 = qi[1];
+            qi[0] = qi[3]; qi[1] = qi[2]; qi[2] = t1; qi[3] = t0;
+        }
+        float v[4][3];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) v[t][d] = qi[t] == uint32_t(a) ? own[d] : dual[3ll * qi[t] + d];
+        int32_t f[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) f[t] = vertex_of(vmap, qi[t]);
+        int32_t* o6 = faces + 6 * q;
+        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+            o6[0] = f[1]; o6[1] = f[3]; o6[2] = f[0];
+            o6[3] = f[3]; o6[4] = f[1]; o6[5] = f[2];
+        } else {
+            o6[0] = f[2]; o6[1] = f[0]; o6[2] = f[1];
+            o6[3] = f[0]; o6[4] = f[2]; o6[5] = f[3];
+        }
+        ++q;
+    }
+}
 
 }  // namespace
 
@@ -833,7 +1122,7 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
     iso::ProfScope ps("dc_solve", st);
     const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
     dc_cell_solve<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
-                                                      reg, svd_tol, dual, nullptr);
+                                                      reg, svd_tol, dual, nullptr, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -977,31 +1266,45 @@ int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long 
 namespace {
 struct DcDenseWs {
     DcWs d;
-    long long* tot;  // [0..1] A, K  [2..3] Q, 0  [4..7] eff  [8..9] V, 0
-    uint32_t *cells, *offs;
+    unsigned long long* zero;  // cleared by the sign pass: misc, then the look-back states
+    long long nzero;
+    long long* misc;           // [0..3] unused  [4..7] eff  [8] [9] tickets
+    unsigned long long *stAQ, *stK, *stV;
+    long long ntC, ntV;        // tiles of dc_cells and dc_weld_local
+    uint32_t *cells, *qoff, *vmap;
+    uint8_t* used;
     float* dual;
-    int32_t* tri;
-    void* weld;  // weld_dev_workspace(capA) bytes
     size_t total;
 };
 
-DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA, long long capQ) {
+DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
     DcDenseWs w{};
     const size_t base = iso_dc_workspace_size(nx, ny, nz);
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     if (ws) w.d = carve(b, nx, ny, nz);
+    const long long NWc = (nz - 1 + 31) / 32;
+    const long long cwords = (long long)(nx - 1) * (ny - 1) * NWc;
+    w.ntC = (cwords + DC_BLOCK - 1) / DC_BLOCK;
+    w.ntV = (capA + DC_BLOCK - 1) / DC_BLOCK;
     size_t o = (base + 255) & ~size_t(255);
     auto take = [&](size_t bytes) {
         uint8_t* p = ws ? b + o : nullptr;
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.tot = reinterpret_cast<long long*>(take(16 * 8));
+    w.nzero = 16 + 2 * w.ntC + w.ntV;
+    w.zero = reinterpret_cast<unsigned long long*>(take(size_t(w.nzero) * 8));
+    if (ws) {
+        w.misc = reinterpret_cast<long long*>(w.zero);
+        w.stAQ = w.zero + 16;
+        w.stK = w.stAQ + w.ntC;
+        w.stV = w.stK + w.ntC;
+    }
     w.cells = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.offs = reinterpret_cast<uint32_t*>(take(size_t(capA + 1) * 4));
+    w.qoff = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.vmap = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
+    w.used = take(size_t(capA));
     w.dual = reinterpret_cast<float*>(take(size_t(capA) * 12));
-    w.tri = reinterpret_cast<int32_t*>(take(size_t(capQ) * 24));
-    w.weld = take(weld_dev_workspace(capA));
     w.total = o + 256;
     return w;
 }
@@ -1012,7 +1315,7 @@ extern "C" {
 size_t iso_dc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity, long long face_capacity) {
     if (nx < 2 || ny < 2 || nz < 2) return 256;
     if (vertex_capacity < 0 || face_capacity < 0) return 0;
-    return carve_dense(nullptr, nx, ny, nz, vertex_capacity, face_capacity / 2).total;
+    return carve_dense(nullptr, nx, ny, nz, vertex_capacity).total;
 }
 
 int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
@@ -1028,43 +1331,45 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
     const long long capA = vertex_capacity, capQ = face_capacity / 2;
     if (workspace_bytes < iso_dc_dense_workspace_size(nx, ny, nz, vertex_capacity, face_capacity))
         return ISO_ERR_WORKSPACE;
-    const DcDenseWs w = carve_dense(workspace, nx, ny, nz, capA, capQ);
+    const DcDenseWs w = carve_dense(workspace, nx, ny, nz, capA);
     const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
-    long long* eff = w.tot + 4;
+    long long* eff = w.misc + 4;
     uint32_t* cells = cell_ids ? reinterpret_cast<uint32_t*>(cell_ids) : w.cells;
-    uint32_t* offs = cell_offsets ? reinterpret_cast<uint32_t*>(cell_offsets) : w.offs;
     {
         iso::ProfScope ps("mc_signs", st);
-        mc_signs_launch(values, nx, ny, nz, level, w.d.S, st);
+        mc_signs_launch(values, nx, ny, nz, level, w.d.S, st, w.zero, w.nzero);
     }
     {
         iso::ProfScope ps("dc_classify", st);
-        dc_cell_count<<<blocks_for(w.d.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.cwords, w.d.blkC);
-        dc_block_scan<<<1, 1024, 0, st>>>(w.d.blkC, w.d.nblkC, w.tot);
-        dc_quad_count<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ);
-        dc_block_scan<<<1, 1024, 0, st>>>(w.d.blkQ, w.d.nblkQ, w.tot + 2);
-        dc_dense_sizes<<<1, 1, 0, st>>>(w.tot, w.tot + 2, capA, capQ, eff, counts, status);
-    }
-    {
-        iso::ProfScope ps("dc_intersect", st);
-        dc_intersect<<<blocks_for(w.d.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
-            values, w.d.S, g, level, w.d.cwords, w.d.blkC, w.d.actm, w.d.offA, nullptr, nullptr, cells, offs, 0, 0,
-            eff);
+        iso::launch_pdl(dc_cells, unsigned(w.ntC), DC_BLOCK, st, w.d.S, g, w.d.cwords,
+                        reinterpret_cast<unsigned long long*>(w.misc + 8), w.stAQ, w.stK, w.d.actm, w.d.offA, cells,
+                        w.qoff, reinterpret_cast<uint32_t*>(cell_offsets), capA, capQ, eff, counts, status);
     }
     if (capA > 0) {
-        iso::ProfScope ps("dc_solve", st);
-        const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-        dc_cell_solve<<<blocks_for(capA, bt), bt, 0, st>>>(values, g, level, cells, capA, reg, svd_tol, w.dual,
-                                                           eff);
+        {
+            iso::ProfScope ps("dc_solve", st);
+            const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+            iso::launch_pdl(dc_cell_solve, blocks_for(capA, bt), unsigned(bt), st, values, g, level,
+                            static_cast<const uint32_t*>(cells), capA, reg, svd_tol, w.dual,
+                            static_cast<const long long*>(eff), w.used);
+        }
+        {
+            iso::ProfScope ps("dc_weld", st);
+            iso::launch_pdl(dc_weld_local, unsigned(w.ntV), DC_BLOCK, st, g, static_cast<const uint32_t*>(cells),
+                            static_cast<const uint8_t*>(w.used), static_cast<const float*>(w.dual),
+                            static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.d.offA),
+                            static_cast<const long long*>(eff), reinterpret_cast<unsigned long long*>(w.misc + 9),
+                            w.stV, w.vmap, vertices, reinterpret_cast<uint32_t*>(vertex_source), counts, status);
+        }
+        {
+            iso::ProfScope ps("dc_quads", st);
+            iso::launch_pdl(dc_cell_quads, blocks_for(capA, 256), 256u, st, static_cast<const uint32_t*>(w.d.S), g,
+                            static_cast<const uint32_t*>(cells), static_cast<const uint32_t*>(w.qoff),
+                            static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.d.offA),
+                            static_cast<const float*>(w.dual), static_cast<const uint32_t*>(w.vmap),
+                            static_cast<const long long*>(eff), faces);
+        }
     }
-    {
-        iso::ProfScope ps("dc_quads", st);
-        dc_quad_emit<<<blocks_for(w.d.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.d.S, g, w.d.pwords, w.d.blkQ, w.d.actm,
-                                                                           w.d.offA, w.dual, w.tri, eff);
-    }
-    weld_dev_launch(w.dual, capA, w.tri, 6 * capQ, eff, w.weld, vertices, faces, w.tot + 8, status, st,
-                    reinterpret_cast<uint32_t*>(vertex_source));
-    dc_dense_finish<<<1, 1, 0, st>>>(w.tot + 8, counts);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 

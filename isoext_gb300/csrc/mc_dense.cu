@@ -43,6 +43,7 @@
 #include "common.cuh"
 #define ISO_LUT_DECL static __constant__ const
 #include "luts.h"
+#include "lookback.cuh"
 #include "mc_dense.cuh"
 #include "profile.cuh"
 
@@ -289,56 +290,6 @@ __device__ __forceinline__ void advance(const McGrid& g, int& x, int& y, int& w)
     if (++w == g.NW) {
         w = 0;
         if (++y == g.ny) { y = 0; ++x; }
-    }
-}
-
-// Look-back state of a segment: flag << 62 | V << 31 | F (V, F < 2^31).
-constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62;
-constexpr unsigned long long LB_MASK31 = 0x7fffffffull;
-
-__device__ __forceinline__ unsigned long long lb_pack(unsigned long long flag, unsigned long long v,
-                                                      unsigned long long f) {
-    return flag | (min(v, LB_MASK31) << 31) | min(f, LB_MASK31);
-}
-
-// Exclusive (V, F) prefix of segment seg; run by warp 0 after publishing the
-// segment's aggregate.  Waits are bounded: on a timeout the status is set and
-// the prefix returned is wrong (the host sees the status).
-__device__ void look_back(volatile unsigned long long* state, uint32_t seg, unsigned long long& ev,
-                          unsigned long long& ef, int* status, uint32_t limit = ISO_SPIN_LIMIT) {
-    const int lane = threadIdx.x & 31;
-    ev = 0;
-    ef = 0;
-    long long j = (long long)seg - 1 - lane;
-    while (true) {
-        unsigned long long st = LB_INC;  // before segment 0: inclusive zero
-        if (j >= 0) {
-            uint32_t spins = 0;
-            do {
-                st = state[j];
-                if ((st >> 62) != 0) break;
-                if (++spins > limit) {
-                    atomicCAS(status, 0, int(ISO_ERR_TIMEOUT));
-                    st = LB_INC;
-                    break;
-                }
-                __nanosleep(20);
-            } while (true);
-        }
-        const uint32_t inc = __ballot_sync(~0u, (st >> 62) == 2);
-        // lanes up to and including the nearest inclusive state contribute
-        const int stop = inc ? __ffs(inc) - 1 : 31;
-        unsigned long long v = lane <= stop ? (st >> 31) & LB_MASK31 : 0ull;
-        unsigned long long f = lane <= stop ? st & LB_MASK31 : 0ull;
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) {
-            v += __shfl_xor_sync(~0u, v, d);
-            f += __shfl_xor_sync(~0u, f, d);
-        }
-        ev += v;
-        ef += f;
-        if (inc) break;
-        j -= 32;
     }
 }
 

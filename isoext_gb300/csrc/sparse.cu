@@ -304,8 +304,8 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_its_emit(SpGrid g, const int* __r
     act_sparse[a] = int(c);
     act_uniform[a] = ids[c];
     offsets[a] = int(k);
-    for (int e = 0; e < 12; ++e) {
-        if (!((est >> e) & 1u)) continue;
+    for (uint32_t em = est; em; em &= em - 1) {  // this lane's crossed edges, ascending
+        const int e = __ffs(em) - 1;
         float p[3];
         edge_point(cc, e, g.level, p);
         points[3 * k] = p[0]; points[3 * k + 1] = p[1]; points[3 * k + 2] = p[2];

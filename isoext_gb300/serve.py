@@ -80,9 +80,8 @@ def prims_buffer(prims: np.ndarray) -> np.ndarray:
 
 # Kernels of this library one request launches: marching cubes = grid evaluation
 # + mc_signs, mc_count, mc_scan, mc_emit; dual contouring = grid evaluation +
-# mc_signs, cell count + scan, quad count + scan, sizes, intersect, solve, quad
-# emit, weld (mark, insert, lookup, count, scan, write, finish, remap).
-KERNELS_PER_REQUEST = {"mc": 5, "dc": 18}
+# mc_signs, cells, solve, weld, quads.
+KERNELS_PER_REQUEST = {"mc": 5, "dc": 6}
 
 
 # ---------------------------------------------------------------------------

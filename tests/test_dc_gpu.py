@@ -213,3 +213,37 @@ def test_dc_one_call_retries_when_buffers_are_small():
     v1, f1 = iso.dual_contouring(g)
     assert torch.equal(v0, v1) and torch.equal(f0, f1)
     assert dc._dc_sizes[key][0] >= len(v0)
+
+
+def _cuboid_sdf(shape, half=0.5, lo=(-1, -1, -1), hi=(1, 1, 1)):
+    p = torch.from_numpy(grid_points(shape, lo, hi)).double()
+    c = torch.tensor([(lo[k] + hi[k]) / 2 for k in range(3)], dtype=torch.float64)
+    q = (p - c).abs() - half * torch.tensor([(hi[k] - lo[k]) / 2 for k in range(3)], dtype=torch.float64)
+    return (torch.clamp(q, min=0).norm(dim=-1) + torch.clamp(q.max(dim=-1).values, max=0)).float().numpy()
+
+
+@pytest.mark.parametrize("case", ["cuboid", "zeros", "repeated_coords"])
+def test_dc_one_call_weld_equals_hash_weld(case):
+    """The one-call path welds a dual vertex that lies on a face of its cell by
+    comparing it with the cells around that face; the call sequence hashes every
+    position.  Both must give the same bits: on a cuboid whose vertices clip to
+    cell faces, on noise with exact zeros (crossings on grid points), and on a
+    grid finer than FP32 resolves at its coordinates (coordinates repeat, so
+    more than the neighbouring cells share a face position)."""
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    if case == "cuboid":
+        vals = _cuboid_sdf((33, 29, 31))
+    elif case == "zeros":
+        vals = noise((26, 22, 30), seed=9, zero_frac=0.3)
+    else:
+        lo, hi = (1000.0, -1.0, 1000.0), (1000.001, 1.0, 1000.002)
+        vals = _cuboid_sdf((24, 20, 28), 0.6, lo, hi)
+    g = make_grid(vals, lo, hi)
+    v0, f0 = iso.dual_contouring(g)
+    its = iso.get_intersection(g, compute_normals=True)
+    v1, f1 = iso.dual_contouring(g, intersection=its)
+    assert v0 is not None and len(f0) > 0
+    assert torch.equal(v0, v1) and torch.equal(f0, f1)
+    if case == "repeated_coords":  # the grid does repeat coordinates, and the weld merged across them
+        pts = g.get_points().reshape(-1, 3)
+        assert len(torch.unique(pts[:, 0])) < g.shape[0]
