@@ -40,6 +40,7 @@ WORKLOADS = {
     "mc512": dict(kind="mc", n=512, r=0.8, desc="mc_dense_512_sphere_r0.8"),
     "mc128": dict(kind="mc", n=128, r=0.8, desc="mc_dense_128_sphere_r0.8"),
     "dc512": dict(kind="dc1", n=512, r=0.8, desc="dc_dense_512_sphere_r0.8"),
+    "dc384": dict(kind="dc1", n=384, r=0.8, desc="dc_dense_384_sphere_r0.8"),
     "dc256": dict(kind="dc", n=256, seed=7, desc="dc_dense_256_csg_seed7"),
     "serve": dict(kind="serve", count=512, seed=2026, sizes=(64, 96, 128, 192, 256), mc_share=0.7,
                   slots=8, budget_gb=40, desc="served_mixed_512req_n64-256_mc70"),

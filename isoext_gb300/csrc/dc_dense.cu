@@ -79,7 +79,9 @@ __device__ __forceinline__ uint32_t word_crossings(const uint32_t* cw8, uint32_t
     return nk;
 }
 
-// Block-wide exclusive scan of two values per thread (DC_BLOCK threads).
+// Block-wide exclusive scan of two values per thread (NT threads, a multiple
+// of 32).
+template <int NT = DC_BLOCK>
 __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea, uint32_t& eb,
                                             uint32_t& ta, uint32_t& tb, uint32_t* sm /*66*/) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -92,7 +94,8 @@ __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea
     if (lane == 31) { sm[warp] = ia; sm[32 + warp] = ib; }
     __syncthreads();
     if (warp == 0) {
-        uint32_t x = sm[lane], y = sm[32 + lane];
+        constexpr int NWARP = NT / 32;
+        uint32_t x = lane < NWARP ? sm[lane] : 0u, y = lane < NWARP ? sm[32 + lane] : 0u;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t u = __shfl_up_sync(~0u, x, d), v = __shfl_up_sync(~0u, y, d);
@@ -688,61 +691,190 @@ __device__ __forceinline__ uint32_t cell_crossings(const uint32_t* ex, int b) {
     return n;
 }
 
-__global__ void __launch_bounds__(DC_BLOCK) dc_cells(const uint32_t* __restrict__ S, Grid3 g, long long nwords,
-                                                     unsigned long long* ticket, unsigned long long* stAQ,
-                                                     unsigned long long* stK, uint32_t* __restrict__ actm,
-                                                     uint32_t* __restrict__ offA, uint32_t* __restrict__ cell_ids,
-                                                     uint32_t* __restrict__ qoff, uint32_t* __restrict__ cell_off,
-                                                     long long capA, long long capQ, long long* eff,
-                                                     long long* counts, int* status) {
-    __shared__ uint32_t sm[66];
-    __shared__ uint32_t tile_s;
+constexpr int CELLS_THREADS = 512;  // dc_cells: threads per CTA
+constexpr int CELLS_WPT = 4;        // point words per thread and round (one 16-byte load per row)
+constexpr int CELLS_ROUNDS = 2;
+constexpr int CELLS_TILE = CELLS_THREADS * CELLS_WPT * CELLS_ROUNDS;  // point words per CTA
+
+// Owned quad edges of a cell word's active cells: corner 0 to corner 1 (z),
+// 2 (y), 4 (x); complete when the edge's other two coordinates are >= 1 (the
+// upper bounds hold for every cell).
+__device__ __forceinline__ void owned_quads(const Grid3& g, const uint32_t* cw8, uint32_t act, int cx, int cy, int w,
+                                            uint32_t& qz, uint32_t& qy, uint32_t& qx) {
+    const uint32_t zin = iso::range_mask(w, 1, g.nz - 2);
+    qz = (cx >= 1 && cy >= 1) ? (cw8[0] ^ cw8[1]) & act : 0u;
+    qy = cx >= 1 ? (cw8[0] ^ cw8[2]) & act & zin : 0u;
+    qx = cy >= 1 ? (cw8[0] ^ cw8[4]) & act & zin : 0u;
+}
+
+// The sign words pw .. pw+3 of the rows (x, y), (x, y+1), (x+1, y), (x+1, y+1)
+// of point word pw (flat offsets 0, syw, sxw, sxw + syw), and each row's word
+// pw+4 (the next lane's first word, or a load).  All lanes call it.
+struct QuadRows {
+    uint32_t r[4][CELLS_WPT];  // row k = 2 dx + dy
+    uint32_t n4[4];
+};
+
+__device__ __forceinline__ void load_quad_rows(const uint32_t* __restrict__ S, uint32_t pw, uint32_t sxw,
+                                               uint32_t syw, uint32_t PW, bool vec, int lane, QuadRows& q) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t o = pw + (k >> 1) * sxw + (k & 1) * syw;
+        if (vec && o + CELLS_WPT <= PW) {
+            const uint4 v4 = __ldg(reinterpret_cast<const uint4*>(S + o));
+            q.r[k][0] = v4.x; q.r[k][1] = v4.y; q.r[k][2] = v4.z; q.r[k][3] = v4.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < CELLS_WPT; ++j) q.r[k][j] = o + j < PW ? __ldg(S + o + j) : 0u;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        q.n4[k] = __shfl_down_sync(~0u, q.r[k][0], 1);
+        if (lane == 31) {
+            const uint32_t o = pw + CELLS_WPT + (k >> 1) * sxw + (k & 1) * syw;
+            q.n4[k] = o < PW ? __ldg(S + o) : 0u;
+        }
+    }
+}
+
+// No cell of the lane's words can be active: all 20 words equal, all 0 or ~0.
+__device__ __forceinline__ bool quad_rows_quiet(const QuadRows& q) {
+    const uint32_t u = q.r[0][0];
+    uint32_t d = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        d |= q.n4[k] ^ u;
+#pragma unroll
+        for (int j = 0; j < CELLS_WPT; ++j) d |= q.r[k][j] ^ u;
+    }
+    return (u == 0u || u == ~0u) && d == 0u;
+}
+
+// Corner words (cw8[2k]: dz 0, cw8[2k+1]: dz 1) and active cells of word j of
+// the lane, point word (x, y, w).
+__device__ __forceinline__ uint32_t quad_word_act(const Grid3& g, int nwg, int nwc, const QuadRows& q, int j, int x,
+                                                  int y, int w, uint32_t* cw8) {
+    const bool nxt = w + 1 < nwg;
+    uint32_t and8 = ~0u, or8 = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t a = q.r[k][j];
+        const uint32_t nb = nxt ? (j + 1 < CELLS_WPT ? q.r[k][(j + 1) % CELLS_WPT] : q.n4[k]) : 0u;
+        const uint32_t b = __funnelshift_r(a, nb, 1);  // bit z <- z + 1
+        cw8[2 * k] = a;
+        cw8[2 * k + 1] = b;
+        and8 &= a & b;
+        or8 |= a | b;
+    }
+    if (x >= g.nx - 1 || y >= g.ny - 1 || w >= nwc) return 0u;
+    return (or8 & ~and8) & iso::range_mask(w, 0, g.nz - 2);
+}
+
+// Next point word in (x, y, w) order.
+__device__ __forceinline__ void next_point_word(const Grid3& g, int nwg, int& x, int& y, int& w) {
+    if (++w == nwg) {
+        w = 0;
+        if (++y == g.ny) { y = 0; ++x; }
+    }
+}
+
+// Active cells, crossings and owned quads of CELLS_TILE consecutive point words
+// per CTA, in the flat bitmap order (x, y, w), which orders cells as their ids
+// do.  A lane takes 4 consecutive words per round: one 16-byte load per row,
+// and a warp whose 128 words are all inside or outside skips the rest.  Pass 1
+// counts, the tile's offsets come by look-back, pass 2 recounts busy rounds
+// and writes.  actm / offA are indexed by point word.
+__global__ void __launch_bounds__(CELLS_THREADS, 2) dc_cells(const uint32_t* __restrict__ S, Grid3 g,
+                                                          unsigned long long* ticket, unsigned long long* stAQ,
+                                                          unsigned long long* stK, uint32_t* __restrict__ actm,
+                                                          uint32_t* __restrict__ offA,
+                                                          uint32_t* __restrict__ cell_ids,
+                                                          uint32_t* __restrict__ qoff,
+                                                          uint32_t* __restrict__ cell_off, long long capA,
+                                                          long long capQ, long long* eff, long long* counts,
+                                                          int* status) {
+    constexpr int NWARP = CELLS_THREADS / 32;
+    __shared__ uint32_t wsum[3][NWARP];  // per warp: active cells, owned quads, crossings
+    __shared__ uint32_t tile_s, ttot[3];
     __shared__ unsigned long long pre_s[3];
     iso::grid_wait();
     if (threadIdx.x == 0) tile_s = uint32_t(atomicAdd(ticket, 1ull));
     __syncthreads();
     const uint32_t tile = tile_s;
-    const long long i = (long long)tile * DC_BLOCK + threadIdx.x;
-    const int NWc = (g.nz - 1 + 31) / 32;
-    uint32_t act = 0, qz = 0, qy = 0, qx = 0, na = 0, nk = 0, nq = 0;
-    uint32_t cw8[8];
-    int cx = 0, cy = 0, w = 0;
-    if (i < nwords) {
-        w = int(i % NWc);
-        const long long r = i / NWc;
-        cy = int(r % (g.ny - 1));
-        cx = int(r / (g.ny - 1));
-        act = cell_act(S, g, cx, cy, w, cw8);
-        if (act) {
-            na = __popc(act);
-            nk = word_crossings(cw8, act);
-            // owned edges: corner 0 to corner 1 (z), 2 (y), 4 (x); complete when
-            // the edge's other two coordinates are >= 1 (the upper bounds hold
-            // for every cell)
-            const uint32_t zin = iso::range_mask(w, 1, g.nz - 2);
-            if (cx >= 1 && cy >= 1) qz = (cw8[0] ^ cw8[1]) & act;
-            if (cx >= 1) qy = (cw8[0] ^ cw8[2]) & act & zin;
-            if (cy >= 1) qx = (cw8[0] ^ cw8[4]) & act & zin;
-            nq = __popc(qz) + __popc(qy) + __popc(qx);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int NWg = (g.nz + 31) / 32, NWc = (g.nz - 1 + 31) / 32;
+    const uint32_t syw = uint32_t(NWg), sxw = uint32_t(g.ny) * syw;
+    const uint32_t PW = uint32_t(g.nx) * sxw;  // point words (< 2^32)
+    const bool vec = (NWg & 3) == 0;           // rows start on 16-byte boundaries
+    const uint32_t ntile = (PW + CELLS_TILE - 1) / CELLS_TILE;
+    // round j of this lane: words pw(j) .. pw(j) + 3; a warp's rounds are
+    // consecutive, so its words are too
+    auto pw_of = [&](int j) {
+        return tile * uint32_t(CELLS_TILE) + uint32_t(warp * (32 * CELLS_WPT * CELLS_ROUNDS)) +
+               uint32_t(j * 32 * CELLS_WPT) + uint32_t(lane * CELLS_WPT);
+    };
+    uint32_t sa = 0, sq = 0, sk = 0, busy = 0;
+    for (int j = 0; j < CELLS_ROUNDS; ++j) {
+        const uint32_t pw = pw_of(j);
+        QuadRows q;
+        load_quad_rows(S, pw, sxw, syw, PW, vec, lane, q);
+        if (__all_sync(~0u, quad_rows_quiet(q) || pw >= PW)) continue;
+        busy |= 1u << j;
+        if (pw >= PW) continue;
+        const uint32_t row = pw / syw;
+        int w = int(pw - row * syw), x = int(row / uint32_t(g.ny)), y = int(row - uint32_t(x) * uint32_t(g.ny));
+#pragma unroll
+        for (int k = 0; k < CELLS_WPT; ++k) {
+            uint32_t cw8[8];
+            const uint32_t act = pw + k < PW ? quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8) : 0u;
+            if (act) {
+                uint32_t qz, qy, qx;
+                owned_quads(g, cw8, act, x, y, w, qz, qy, qx);
+                sa += __popc(act);
+                sq += __popc(qz) + __popc(qy) + __popc(qx);
+                sk += word_crossings(cw8, act);
+            }
+            next_point_word(g, NWg, x, y, w);
         }
     }
-    uint32_t ea, eq, ta, tq, ek, e_, tk, t_;
-    block_scan2(na, nq, ea, eq, ta, tq, sm);
-    block_scan2(nk, 0u, ek, e_, tk, t_, sm);
-    const int warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        unsigned long long pa, pq;
-        lb_tile(stAQ, tile, ta, tq, pa, pq, status);
-        if (threadIdx.x == 0) { pre_s[0] = pa; pre_s[1] = pq; }
-    } else if (warp == 1) {
-        unsigned long long pk, p_;
-        lb_tile(stK, tile, tk, 0, pk, p_, status);
-        if (threadIdx.x == 32) pre_s[2] = pk;
+    const uint32_t wbusy = __reduce_or_sync(~0u, busy);
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+        sa += __shfl_xor_sync(~0u, sa, d);
+        sq += __shfl_xor_sync(~0u, sq, d);
+        sk += __shfl_xor_sync(~0u, sk, d);
+    }
+    if (lane == 0) { wsum[0][warp] = sa; wsum[1][warp] = sq; wsum[2][warp] = sk; }
+    __syncthreads();
+    if (warp == 0) {  // exclusive prefix over the warps, tile totals
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            const uint32_t x = lane < NWARP ? wsum[v][lane] : 0u;
+            uint32_t incl = x;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(~0u, incl, d);
+                if (lane >= d) incl += t;
+            }
+            if (lane < NWARP) wsum[v][lane] = incl - x;
+            if (lane == 31) ttot[v] = incl;
+        }
     }
     __syncthreads();
-    const unsigned long long A0 = pre_s[0], Q0 = pre_s[1], K0 = pre_s[2];
-    if (threadIdx.x == 0 && tile == uint32_t((nwords + DC_BLOCK - 1) / DC_BLOCK) - 1) {
-        const long long A = (long long)(A0 + ta), K = (long long)(K0 + tk), Q = (long long)(Q0 + tq);
+    if (warp == 0) {
+        unsigned long long pa, pq;
+        lb_tile(stAQ, tile, ttot[0], ttot[1], pa, pq, status);
+        if (lane == 0) { pre_s[0] = pa; pre_s[1] = pq; }
+    } else if (warp == 1) {
+        unsigned long long pk, p_;
+        lb_tile(stK, tile, ttot[2], 0, pk, p_, status);
+        if (lane == 0) pre_s[2] = pk;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && tile == ntile - 1) {
+        const long long A = (long long)(pre_s[0] + ttot[0]), K = (long long)(pre_s[2] + ttot[2]);
+        const long long Q = (long long)(pre_s[1] + ttot[1]);
         const bool ok = A <= capA && Q <= capQ && A < (long long)LB_MASK31 && K < (long long)LB_MASK31 &&
                         6 * Q < 0x7fffffffll;
         if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
@@ -757,25 +889,96 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_cells(const uint32_t* __restrict_
         counts[4] = Q;
         if (cell_off && ok) cell_off[A] = uint32_t(K);
     }
-    if (i >= nwords) return;
-    actm[i] = act;
-    offA[i] = uint32_t(A0 + ea);
-    if (!act) return;
-    uint32_t ex[12];
+    // pass 2: the warp's running offsets; busy rounds are recounted and scanned
+    unsigned long long ra = pre_s[0] + wsum[0][warp], rq = pre_s[1] + wsum[1][warp], rk = pre_s[2] + wsum[2][warp];
+    for (int j = 0; j < CELLS_ROUNDS; ++j) {
+        const uint32_t pw = pw_of(j);
+        if (!((wbusy >> j) & 1u)) {  // no active cell in the round
+            if (pw + CELLS_WPT <= PW) {
+                *reinterpret_cast<uint4*>(actm + pw) = make_uint4(0u, 0u, 0u, 0u);
+                const uint32_t o = uint32_t(ra);
+                *reinterpret_cast<uint4*>(offA + pw) = make_uint4(o, o, o, o);
+            } else {
+                for (uint32_t k = pw; k < PW; ++k) { actm[k] = 0u; offA[k] = uint32_t(ra); }
+            }
+            continue;
+        }
+        QuadRows q;
+        load_quad_rows(S, pw, sxw, syw, PW, vec, lane, q);
+        uint32_t act[CELLS_WPT];
+        int x = 0, y = 0, w = 0;
+        if (pw < PW) {
+            const uint32_t row = pw / syw;
+            w = int(pw - row * syw);
+            x = int(row / uint32_t(g.ny));
+            y = int(row - uint32_t(x) * uint32_t(g.ny));
+        }
+        const int x0 = x, y0 = y, w0 = w;
+        uint32_t la = 0, lq = 0, lk = 0;
 #pragma unroll
-    for (int e = 0; e < 12; ++e) ex[e] = cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)];
-    unsigned long long a = A0 + ea, q = Q0 + eq, k = K0 + ek;
-    const long long row = ((long long)cx * (g.ny - 1) + cy) * (g.nz - 1);
-    while (act && a < (unsigned long long)capA) {
-        const int b = __ffs(act) - 1;
-        act &= act - 1;
-        cell_ids[a] = uint32_t(row + 32 * w + b);
-        qoff[a] = uint32_t(q);
-        if (cell_off) cell_off[a] = uint32_t(k);
-        q += ((qz >> b) & 1u) + ((qy >> b) & 1u) + ((qx >> b) & 1u);
-        k += cell_crossings(ex, b);
-        ++a;
+        for (int k = 0; k < CELLS_WPT; ++k) {
+            uint32_t cw8[8];
+            act[k] = pw + k < PW ? quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8) : 0u;
+            if (act[k]) {
+                uint32_t qz, qy, qx;
+                owned_quads(g, cw8, act[k], x, y, w, qz, qy, qx);
+                la += __popc(act[k]);
+                lq += __popc(qz) + __popc(qy) + __popc(qx);
+                lk += word_crossings(cw8, act[k]);
+            }
+            next_point_word(g, NWg, x, y, w);
+        }
+        uint32_t ia = la, iq = lq, ik = lk;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t ta = __shfl_up_sync(~0u, ia, d), tq = __shfl_up_sync(~0u, iq, d),
+                           tk = __shfl_up_sync(~0u, ik, d);
+            if (lane >= d) { ia += ta; iq += tq; ik += tk; }
+        }
+        unsigned long long a = ra + ia - la, qq = rq + iq - lq, kk = rk + ik - lk;
+        ra += __shfl_sync(~0u, ia, 31);
+        rq += __shfl_sync(~0u, iq, 31);
+        rk += __shfl_sync(~0u, ik, 31);
+        x = x0; y = y0; w = w0;
+#pragma unroll
+        for (int k = 0; k < CELLS_WPT; ++k) {
+            if (pw + k < PW) {
+                actm[pw + k] = act[k];
+                offA[pw + k] = uint32_t(a);
+            }
+            if (act[k]) {
+                uint32_t cw8[8], ex[12], qz, qy, qx;
+                quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8);
+                owned_quads(g, cw8, act[k], x, y, w, qz, qy, qx);
+#pragma unroll
+                for (int e = 0; e < 12; ++e) ex[e] = cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)];
+                const uint32_t row = (uint32_t(x) * uint32_t(g.ny - 1) + uint32_t(y)) * uint32_t(g.nz - 1) + 32u * w;
+                uint32_t m = act[k];
+                while (m) {
+                    const int b = __ffs(m) - 1;
+                    m &= m - 1;
+                    if (a < (unsigned long long)capA) {
+                        cell_ids[a] = row + b;
+                        qoff[a] = uint32_t(qq);
+                        if (cell_off) cell_off[a] = uint32_t(kk);
+                    }
+                    qq += ((qz >> b) & 1u) + ((qy >> b) & 1u) + ((qx >> b) & 1u);
+                    kk += cell_crossings(ex, b);
+                    ++a;
+                }
+            }
+            next_point_word(g, NWg, x, y, w);
+        }
     }
+}
+
+// Active index of cell (cx, cy, cz) from the point-word masks and prefixes of
+// dc_cells.
+__device__ __forceinline__ uint32_t active_index_pw(const uint32_t* actm, const uint32_t* offA, const Grid3& g,
+                                                    int cx, int cy, int cz) {
+    const int NWg = (g.nz + 31) / 32;
+    const long long wi = ((long long)cx * g.ny + cy) * NWg + (cz >> 5);
+    return offA[wi] + __popc(actm[wi] & ((1u << (cz & 31)) - 1u));
 }
 
 // Cells along one axis whose closed interval [coord(i), coord(i + 1)] holds v,
@@ -824,13 +1027,13 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_weld_local(Grid3 g, const uint32_
         cells_holding(g, 2, cz, p[2], z0, z1);
         uint32_t rep = uint32_t(a);
         if (x0 != x1 || y0 != y1 || z0 != z1) {
-            const int NWc = (g.nz - 1 + 31) / 32;
+            const int NWg = (g.nz + 31) / 32;
             const uint32_t k0 = pos_bits(p[0]), k1 = pos_bits(p[1]), k2 = pos_bits(p[2]);
             for (int x = x0; x <= x1; ++x)
                 for (int y = y0; y <= y1; ++y)
                     for (int z = z0; z <= z1; ++z) {
                         if (x == cx && y == cy && z == cz) continue;
-                        const long long wi = ((long long)x * (g.ny - 1) + y) * NWc + (z >> 5);
+                        const long long wi = ((long long)x * g.ny + y) * NWg + (z >> 5);  // point word
                         const uint32_t mw = actm[wi], bit = uint32_t(z & 31);
                         if (!((mw >> bit) & 1u)) continue;
                         const uint32_t ib = offA[wi] + __popc(mw & ((1u << bit) - 1u));
@@ -920,7 +1123,7 @@ __global__ void __launch_bounds__(256) dc_cell_quads(const uint32_t* __restrict_
         qi[0] = uint32_t(a);
 #pragma unroll
         for (int u = 0; u < 3; ++u)
-            qi[u + 1] = active_index(actm, offA, g, cx - o[u][0], cy - o[u][1], cz - o[u][2]);
+            qi[u + 1] = active_index_pw(actm, offA, g, cx - o[u][0], cy - o[u][1], cz - o[u][2]);
         // is_out = v(p0) <= v(p1): for a crossed edge, p0 below the level
         if (!s0) {
             const uint32_t t0 = qi[0], t1 = qi[1];
@@ -1028,8 +1231,8 @@ size_t iso_dc_workspace_size(int nx, int ny, int nz) {
     size_t o = 0;
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     o = al(o + size_t(pwords) * 4);       // signs
-    o = al(o + size_t(cwords) * 4);       // active masks
-    o = al(o + size_t(cwords) * 4);       // active prefix
+    o = al(o + size_t(std::max(cwords, pwords)) * 4);  // active masks (by cell word, or by point word)
+    o = al(o + size_t(std::max(cwords, pwords)) * 4);  // active prefixes
     o = al(o + size_t(nblk) * 16);        // cell block sums
     o = al(o + size_t(nblk) * 16);        // quad block sums
     return o + 1024;
@@ -1055,8 +1258,9 @@ DcWs carve(void* ws, int nx, int ny, int nz) {
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     size_t o = 0;
     w.S = reinterpret_cast<uint32_t*>(b + o);    o = al(o + size_t(w.pwords) * 4);
-    w.actm = reinterpret_cast<uint32_t*>(b + o); o = al(o + size_t(w.cwords) * 4);
-    w.offA = reinterpret_cast<uint32_t*>(b + o); o = al(o + size_t(w.cwords) * 4);
+    const size_t nmask = size_t(std::max(w.cwords, w.pwords));
+    w.actm = reinterpret_cast<uint32_t*>(b + o); o = al(o + nmask * 4);
+    w.offA = reinterpret_cast<uint32_t*>(b + o); o = al(o + nmask * 4);
     w.blkC = reinterpret_cast<unsigned long long*>(b + o); o = al(o + size_t(nblk) * 16);
     w.blkQ = reinterpret_cast<unsigned long long*>(b + o);
     return w;
@@ -1282,9 +1486,8 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
     const size_t base = iso_dc_workspace_size(nx, ny, nz);
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     if (ws) w.d = carve(b, nx, ny, nz);
-    const long long NWc = (nz - 1 + 31) / 32;
-    const long long cwords = (long long)(nx - 1) * (ny - 1) * NWc;
-    w.ntC = (cwords + DC_BLOCK - 1) / DC_BLOCK;
+    const long long pwords = (long long)nx * ny * ((nz + 31) / 32);
+    w.ntC = (pwords + CELLS_TILE - 1) / CELLS_TILE;
     w.ntV = (capA + DC_BLOCK - 1) / DC_BLOCK;
     size_t o = (base + 255) & ~size_t(255);
     auto take = [&](size_t bytes) {
@@ -1341,7 +1544,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
     }
     {
         iso::ProfScope ps("dc_classify", st);
-        iso::launch_pdl(dc_cells, unsigned(w.ntC), DC_BLOCK, st, w.d.S, g, w.d.cwords,
+        iso::launch_pdl(dc_cells, unsigned(w.ntC), unsigned(CELLS_THREADS), st, static_cast<const uint32_t*>(w.d.S), g,
                         reinterpret_cast<unsigned long long*>(w.misc + 8), w.stAQ, w.stK, w.d.actm, w.d.offA, cells,
                         w.qoff, reinterpret_cast<uint32_t*>(cell_offsets), capA, capQ, eff, counts, status);
     }
