@@ -664,15 +664,16 @@ __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uin
 
 
 // ---------------------------------------------------------------------------
-// One-call dual contouring: after the sign pass, four kernels chained by
+// One-call dual contouring: after the sign pass, six kernels chained by
 // programmatic dependent launch, with the sizes kept on the device.
 //
-//   dc_cells       per cell word: active cells, crossings, and the quads each
+//   dc_cells_count / _scan / _write
+//                  per point word: active cells, crossings, and the quads each
 //                  active cell owns.  A quad's owner is the cell whose lowest
 //                  corner is the low endpoint of the quad's edge, so the
 //                  reference's quad order (low endpoint, then z, y, x edge) is
-//                  the owners' order.  One pass, offsets by decoupled
-//                  look-back; the last tile checks the sizes.
+//                  the owners' order.  Counts per warp, one CTA scans them and
+//                  checks the sizes, then the words are written with offsets.
 //   dc_cell_solve  the QEF solve and whether faces use the cell.
 //   dc_weld_local  the exact-position weld.  A dual vertex is clipped to its
 //                  cell's closed box, and the boxes of different cells meet only
@@ -691,7 +692,7 @@ __device__ __forceinline__ uint32_t cell_crossings(const uint32_t* ex, int b) {
     return n;
 }
 
-constexpr int CELLS_THREADS = 512;  // dc_cells: threads per CTA
+constexpr int CELLS_THREADS = 256;  // dc_cells: threads per CTA
 constexpr int CELLS_WPT = 4;        // point words per thread and round (one 16-byte load per row)
 constexpr int CELLS_ROUNDS = 2;
 constexpr int CELLS_TILE = CELLS_THREADS * CELLS_WPT * CELLS_ROUNDS;  // point words per CTA
@@ -779,104 +780,172 @@ __device__ __forceinline__ void next_point_word(const Grid3& g, int nwg, int& x,
     }
 }
 
-// Active cells, crossings and owned quads of CELLS_TILE consecutive point words
-// per CTA, in the flat bitmap order (x, y, w), which orders cells as their ids
-// do.  A lane takes 4 consecutive words per round: one 16-byte load per row,
-// and a warp whose 128 words are all inside or outside skips the rest.  Pass 1
-// counts, the tile's offsets come by look-back, pass 2 recounts busy rounds
-// and writes.  actm / offA are indexed by point word.
-__global__ void __launch_bounds__(CELLS_THREADS, 2) dc_cells(const uint32_t* __restrict__ S, Grid3 g,
-                                                          unsigned long long* ticket, unsigned long long* stAQ,
-                                                          unsigned long long* stK, uint32_t* __restrict__ actm,
-                                                          uint32_t* __restrict__ offA,
-                                                          uint32_t* __restrict__ cell_ids,
-                                                          uint32_t* __restrict__ qoff,
-                                                          uint32_t* __restrict__ cell_off, long long capA,
-                                                          long long capQ, long long* eff, long long* counts,
-                                                          int* status) {
-    constexpr int NWARP = CELLS_THREADS / 32;
-    __shared__ uint32_t wsum[3][NWARP];  // per warp: active cells, owned quads, crossings
-    __shared__ uint32_t tile_s, ttot[3];
-    __shared__ unsigned long long pre_s[3];
+// Geometry of the flat point-word bitmap, shared by the dc_cells kernels.
+struct PwGrid {
+    int NWg, NWc;
+    uint32_t syw, sxw, PW;  // row stride, plane stride, point words (< 2^32)
+    bool vec;               // rows start on 16-byte boundaries
+};
+
+__device__ __forceinline__ PwGrid pw_grid(const Grid3& g) {
+    PwGrid p;
+    p.NWg = (g.nz + 31) / 32;
+    p.NWc = (g.nz - 1 + 31) / 32;
+    p.syw = uint32_t(p.NWg);
+    p.sxw = uint32_t(g.ny) * p.syw;
+    p.PW = uint32_t(g.nx) * p.sxw;
+    p.vec = (p.NWg & 3) == 0;
+    return p;
+}
+
+// Round j of a lane of warp gw (over the grid): point words pw .. pw + 3.  A
+// warp's rounds are consecutive, so its words are too.
+__device__ __forceinline__ uint32_t cells_pw(uint32_t gw, int lane, int j) {
+    return gw * uint32_t(32 * CELLS_WPT * CELLS_ROUNDS) + uint32_t(j * 32 * CELLS_WPT) + uint32_t(lane * CELLS_WPT);
+}
+
+__device__ __forceinline__ void pw_xyw(const Grid3& g, const PwGrid& p, uint32_t pw, int& x, int& y, int& w) {
+    const uint32_t row = pw / p.syw;
+    w = int(pw - row * p.syw);
+    x = int(row / uint32_t(g.ny));
+    y = int(row - uint32_t(x) * uint32_t(g.ny));
+}
+
+// Per warp of 256 point words (flat bitmap order (x, y, w), which orders cells
+// as their ids do): the active masks (written here), and the counts of active
+// cells, owned quads and crossings.  A lane takes 4 consecutive words per
+// round: one 16-byte load per row, and a warp whose 128 words are all inside
+// or outside skips the rest.  wsum[warp] = the warp's exclusive prefix within
+// its CTA and its busy rounds; csum[CTA] = the CTA's sums.
+constexpr int CELLS_WARPS = CELLS_THREADS / 32;
+
+__device__ __forceinline__ void store_masks(uint32_t* __restrict__ m, uint32_t pw, uint32_t PW, const uint32_t* v) {
+    if (pw + CELLS_WPT <= PW) {
+        *reinterpret_cast<uint4*>(m + pw) = make_uint4(v[0], v[1], v[2], v[3]);
+    } else {
+        for (int k = 0; k < CELLS_WPT; ++k)
+            if (pw + k < PW) m[pw + k] = v[k];
+    }
+}
+
+__global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_count(const uint32_t* __restrict__ S, Grid3 g,
+                                                                   uint32_t* __restrict__ actm,
+                                                                   uint32_t* __restrict__ wsum,
+                                                                   uint32_t* __restrict__ csum) {
+    __shared__ uint32_t ws[3][CELLS_WARPS];
     iso::grid_wait();
-    if (threadIdx.x == 0) tile_s = uint32_t(atomicAdd(ticket, 1ull));
-    __syncthreads();
-    const uint32_t tile = tile_s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int NWg = (g.nz + 31) / 32, NWc = (g.nz - 1 + 31) / 32;
-    const uint32_t syw = uint32_t(NWg), sxw = uint32_t(g.ny) * syw;
-    const uint32_t PW = uint32_t(g.nx) * sxw;  // point words (< 2^32)
-    const bool vec = (NWg & 3) == 0;           // rows start on 16-byte boundaries
-    const uint32_t ntile = (PW + CELLS_TILE - 1) / CELLS_TILE;
-    // round j of this lane: words pw(j) .. pw(j) + 3; a warp's rounds are
-    // consecutive, so its words are too
-    auto pw_of = [&](int j) {
-        return tile * uint32_t(CELLS_TILE) + uint32_t(warp * (32 * CELLS_WPT * CELLS_ROUNDS)) +
-               uint32_t(j * 32 * CELLS_WPT) + uint32_t(lane * CELLS_WPT);
-    };
+    const uint32_t gw = blockIdx.x * CELLS_WARPS + warp;
+    const PwGrid p = pw_grid(g);
     uint32_t sa = 0, sq = 0, sk = 0, busy = 0;
     for (int j = 0; j < CELLS_ROUNDS; ++j) {
-        const uint32_t pw = pw_of(j);
+        const uint32_t pw = cells_pw(gw, lane, j);
         QuadRows q;
-        load_quad_rows(S, pw, sxw, syw, PW, vec, lane, q);
-        if (__all_sync(~0u, quad_rows_quiet(q) || pw >= PW)) continue;
-        busy |= 1u << j;
-        if (pw >= PW) continue;
-        const uint32_t row = pw / syw;
-        int w = int(pw - row * syw), x = int(row / uint32_t(g.ny)), y = int(row - uint32_t(x) * uint32_t(g.ny));
+        load_quad_rows(S, pw, p.sxw, p.syw, p.PW, p.vec, lane, q);
+        uint32_t act[CELLS_WPT] = {0u, 0u, 0u, 0u};
+        if (!__all_sync(~0u, quad_rows_quiet(q) || pw >= p.PW)) {
+            busy |= 1u << j;
+            int x = 0, y = 0, w = 0;
+            if (pw < p.PW) pw_xyw(g, p, pw, x, y, w);
 #pragma unroll
-        for (int k = 0; k < CELLS_WPT; ++k) {
-            uint32_t cw8[8];
-            const uint32_t act = pw + k < PW ? quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8) : 0u;
-            if (act) {
-                uint32_t qz, qy, qx;
-                owned_quads(g, cw8, act, x, y, w, qz, qy, qx);
-                sa += __popc(act);
-                sq += __popc(qz) + __popc(qy) + __popc(qx);
-                sk += word_crossings(cw8, act);
+            for (int k = 0; k < CELLS_WPT; ++k) {
+                uint32_t cw8[8];
+                act[k] = pw + k < p.PW ? quad_word_act(g, p.NWg, p.NWc, q, k, x, y, w, cw8) : 0u;
+                if (act[k]) {
+                    uint32_t qz, qy, qx;
+                    owned_quads(g, cw8, act[k], x, y, w, qz, qy, qx);
+                    sa += __popc(act[k]);
+                    sq += __popc(qz) + __popc(qy) + __popc(qx);
+                    sk += word_crossings(cw8, act[k]);
+                }
+                next_point_word(g, p.NWg, x, y, w);
             }
-            next_point_word(g, NWg, x, y, w);
         }
+        if (pw < p.PW) store_masks(actm, pw, p.PW, act);
     }
-    const uint32_t wbusy = __reduce_or_sync(~0u, busy);
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
         sa += __shfl_xor_sync(~0u, sa, d);
         sq += __shfl_xor_sync(~0u, sq, d);
         sk += __shfl_xor_sync(~0u, sk, d);
     }
-    if (lane == 0) { wsum[0][warp] = sa; wsum[1][warp] = sq; wsum[2][warp] = sk; }
+    if (lane == 0) { ws[0][warp] = sa; ws[1][warp] = sq; ws[2][warp] = sk; }
     __syncthreads();
-    if (warp == 0) {  // exclusive prefix over the warps, tile totals
+    if (warp == 0) {
+        uint32_t e[3], t[3];
 #pragma unroll
         for (int v = 0; v < 3; ++v) {
-            const uint32_t x = lane < NWARP ? wsum[v][lane] : 0u;
+            const uint32_t x = lane < CELLS_WARPS ? ws[v][lane] : 0u;
             uint32_t incl = x;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(~0u, incl, d);
-                if (lane >= d) incl += t;
+                const uint32_t u = __shfl_up_sync(~0u, incl, d);
+                if (lane >= d) incl += u;
             }
-            if (lane < NWARP) wsum[v][lane] = incl - x;
-            if (lane == 31) ttot[v] = incl;
+            e[v] = incl - x;
+            t[v] = __shfl_sync(~0u, incl, 31);
         }
+        if (lane < CELLS_WARPS) *reinterpret_cast<uint4*>(wsum + 4u * (blockIdx.x * CELLS_WARPS + lane)) =
+            make_uint4(e[0], e[1], e[2], 0u);
+        if (lane == 0) *reinterpret_cast<uint4*>(csum + 4u * blockIdx.x) = make_uint4(t[0], t[1], t[2], 0u);
     }
+    __syncthreads();  // the record's busy word after warp 0's store of the prefixes
+    if (lane == 0) wsum[4u * gw + 3] = busy;
+}
+
+// One CTA: exclusive scan of the CTAs' (active, quads, crossings) sums in
+// place, the totals checked against the capacities.
+__global__ void __launch_bounds__(1024) dc_cells_scan(uint32_t* __restrict__ csum, long long ncta, long long capA,
+                                                      long long capQ, long long* eff, long long* counts,
+                                                      uint32_t* __restrict__ cell_off, int* status) {
+    __shared__ unsigned long long part[3][32], carry[3];
+    iso::grid_wait();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < 3) carry[tid] = 0;
     __syncthreads();
-    if (warp == 0) {
-        unsigned long long pa, pq;
-        lb_tile(stAQ, tile, ttot[0], ttot[1], pa, pq, status);
-        if (lane == 0) { pre_s[0] = pa; pre_s[1] = pq; }
-    } else if (warp == 1) {
-        unsigned long long pk, p_;
-        lb_tile(stK, tile, ttot[2], 0, pk, p_, status);
-        if (lane == 0) pre_s[2] = pk;
+    for (long long base = 0; base < ncta; base += 1024) {
+        const long long i = base + tid;
+        const uint4 v = i < ncta ? *reinterpret_cast<const uint4*>(csum + 4 * i) : make_uint4(0u, 0u, 0u, 0u);
+        const unsigned long long c[3] = {v.x, v.y, v.z};
+        unsigned long long in[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                const unsigned long long u = __shfl_up_sync(~0u, in[t], d);
+                if (lane >= d) in[t] += u;
+            }
+        if (lane == 31)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) part[t][warp] = in[t];
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                unsigned long long x = part[t][lane];
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const unsigned long long u = __shfl_up_sync(~0u, x, d);
+                    if (lane >= d) x += u;
+                }
+                part[t][lane] = x;
+            }
+        }
+        __syncthreads();
+        if (i < ncta) {
+            unsigned long long e[3];
+#pragma unroll
+            for (int t = 0; t < 3; ++t) e[t] = carry[t] + (warp ? part[t][warp - 1] : 0ull) + in[t] - c[t];
+            // offsets past 2^32 only matter when the sizes overflow (then nothing is used)
+            *reinterpret_cast<uint4*>(csum + 4 * i) = make_uint4(uint32_t(e[0]), uint32_t(e[1]), uint32_t(e[2]), 0u);
+        }
+        __syncthreads();
+        if (tid < 3) carry[tid] += part[tid][31];
+        __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && tile == ntile - 1) {
-        const long long A = (long long)(pre_s[0] + ttot[0]), K = (long long)(pre_s[2] + ttot[2]);
-        const long long Q = (long long)(pre_s[1] + ttot[1]);
-        const bool ok = A <= capA && Q <= capQ && A < (long long)LB_MASK31 && K < (long long)LB_MASK31 &&
-                        6 * Q < 0x7fffffffll;
+    if (tid == 0) {
+        const long long A = (long long)carry[0], Q = (long long)carry[1], K = (long long)carry[2];
+        const bool ok = A <= capA && Q <= capQ && A < 0x7fffffffll && K < 0x7fffffffll && 6 * Q < 0x7fffffffll;
         if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
         eff[0] = ok ? A : 0;
         eff[1] = ok ? K : 0;
@@ -889,44 +958,60 @@ __global__ void __launch_bounds__(CELLS_THREADS, 2) dc_cells(const uint32_t* __r
         counts[4] = Q;
         if (cell_off && ok) cell_off[A] = uint32_t(K);
     }
-    // pass 2: the warp's running offsets; busy rounds are recounted and scanned
-    unsigned long long ra = pre_s[0] + wsum[0][warp], rq = pre_s[1] + wsum[1][warp], rk = pre_s[2] + wsum[2][warp];
+}
+
+// The busy rounds of dc_cells_count again, with each warp's offsets: active
+// prefixes per point word (rounds without an active cell have none to look
+// up), and per active cell its id, its first owned quad and (when asked) its
+// first crossing.
+__global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_write(const uint32_t* __restrict__ S, Grid3 g,
+                                                                   const uint32_t* __restrict__ actm,
+                                                                   const uint32_t* __restrict__ wsum,
+                                                                   const uint32_t* __restrict__ csum,
+                                                                   uint32_t* __restrict__ offA,
+                                                                   uint32_t* __restrict__ cell_ids,
+                                                                   uint32_t* __restrict__ qoff,
+                                                                   uint32_t* __restrict__ cell_off, long long capA) {
+    iso::grid_wait();
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = blockIdx.x * CELLS_WARPS + (threadIdx.x >> 5);
+    const PwGrid p = pw_grid(g);
+    const uint4 wo = *reinterpret_cast<const uint4*>(wsum + 4u * gw);
+    const uint4 co = *reinterpret_cast<const uint4*>(csum + 4u * blockIdx.x);
+    const uint32_t wbusy = wo.w;
+    if (!wbusy) return;
+    unsigned long long ra = (unsigned long long)co.x + wo.x, rq = (unsigned long long)co.y + wo.y,
+                       rk = (unsigned long long)co.z + wo.z;
+    const unsigned long long cap = (unsigned long long)capA;  // over capacity the caller reruns
+    const bool want_k = cell_off != nullptr;
     for (int j = 0; j < CELLS_ROUNDS; ++j) {
-        const uint32_t pw = pw_of(j);
-        if (!((wbusy >> j) & 1u)) {  // no active cell in the round
-            if (pw + CELLS_WPT <= PW) {
-                *reinterpret_cast<uint4*>(actm + pw) = make_uint4(0u, 0u, 0u, 0u);
-                const uint32_t o = uint32_t(ra);
-                *reinterpret_cast<uint4*>(offA + pw) = make_uint4(o, o, o, o);
-            } else {
-                for (uint32_t k = pw; k < PW; ++k) { actm[k] = 0u; offA[k] = uint32_t(ra); }
-            }
-            continue;
+        if (!((wbusy >> j) & 1u)) continue;  // no active cell: nothing to number
+        const uint32_t pw = cells_pw(gw, lane, j);
+        uint32_t act[CELLS_WPT] = {0u, 0u, 0u, 0u};
+        if (pw + CELLS_WPT <= p.PW) {
+            const uint4 a4 = *reinterpret_cast<const uint4*>(actm + pw);
+            act[0] = a4.x; act[1] = a4.y; act[2] = a4.z; act[3] = a4.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < CELLS_WPT; ++k) act[k] = pw + k < p.PW ? actm[pw + k] : 0u;
         }
         QuadRows q;
-        load_quad_rows(S, pw, sxw, syw, PW, vec, lane, q);
-        uint32_t act[CELLS_WPT];
+        load_quad_rows(S, pw, p.sxw, p.syw, p.PW, p.vec, lane, q);
         int x = 0, y = 0, w = 0;
-        if (pw < PW) {
-            const uint32_t row = pw / syw;
-            w = int(pw - row * syw);
-            x = int(row / uint32_t(g.ny));
-            y = int(row - uint32_t(x) * uint32_t(g.ny));
-        }
+        if (pw < p.PW) pw_xyw(g, p, pw, x, y, w);
         const int x0 = x, y0 = y, w0 = w;
         uint32_t la = 0, lq = 0, lk = 0;
 #pragma unroll
         for (int k = 0; k < CELLS_WPT; ++k) {
-            uint32_t cw8[8];
-            act[k] = pw + k < PW ? quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8) : 0u;
             if (act[k]) {
-                uint32_t qz, qy, qx;
+                uint32_t cw8[8], qz, qy, qx;
+                quad_word_act(g, p.NWg, p.NWc, q, k, x, y, w, cw8);
                 owned_quads(g, cw8, act[k], x, y, w, qz, qy, qx);
                 la += __popc(act[k]);
                 lq += __popc(qz) + __popc(qy) + __popc(qx);
-                lk += word_crossings(cw8, act[k]);
+                if (want_k) lk += word_crossings(cw8, act[k]);
             }
-            next_point_word(g, NWg, x, y, w);
+            next_point_word(g, p.NWg, x, y, w);
         }
         uint32_t ia = la, iq = lq, ik = lk;
 #pragma unroll
@@ -939,36 +1024,38 @@ __global__ void __launch_bounds__(CELLS_THREADS, 2) dc_cells(const uint32_t* __r
         ra += __shfl_sync(~0u, ia, 31);
         rq += __shfl_sync(~0u, iq, 31);
         rk += __shfl_sync(~0u, ik, 31);
+        uint32_t offs[CELLS_WPT];
         x = x0; y = y0; w = w0;
 #pragma unroll
         for (int k = 0; k < CELLS_WPT; ++k) {
-            if (pw + k < PW) {
-                actm[pw + k] = act[k];
-                offA[pw + k] = uint32_t(a);
-            }
+            offs[k] = uint32_t(a);
             if (act[k]) {
-                uint32_t cw8[8], ex[12], qz, qy, qx;
-                quad_word_act(g, NWg, NWc, q, k, x, y, w, cw8);
+                uint32_t cw8[8], qz, qy, qx;
+                quad_word_act(g, p.NWg, p.NWc, q, k, x, y, w, cw8);
                 owned_quads(g, cw8, act[k], x, y, w, qz, qy, qx);
+                uint32_t ex[12];
+                if (want_k) {
 #pragma unroll
-                for (int e = 0; e < 12; ++e) ex[e] = cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)];
+                    for (int e = 0; e < 12; ++e) ex[e] = cw8[iso_edge_corner(2 * e)] ^ cw8[iso_edge_corner(2 * e + 1)];
+                }
                 const uint32_t row = (uint32_t(x) * uint32_t(g.ny - 1) + uint32_t(y)) * uint32_t(g.nz - 1) + 32u * w;
                 uint32_t m = act[k];
                 while (m) {
                     const int b = __ffs(m) - 1;
                     m &= m - 1;
-                    if (a < (unsigned long long)capA) {
+                    if (a < cap) {
                         cell_ids[a] = row + b;
                         qoff[a] = uint32_t(qq);
-                        if (cell_off) cell_off[a] = uint32_t(kk);
+                        if (want_k) cell_off[a] = uint32_t(kk);
                     }
                     qq += ((qz >> b) & 1u) + ((qy >> b) & 1u) + ((qx >> b) & 1u);
-                    kk += cell_crossings(ex, b);
+                    if (want_k) kk += cell_crossings(ex, b);
                     ++a;
                 }
             }
-            next_point_word(g, NWg, x, y, w);
+            next_point_word(g, p.NWg, x, y, w);
         }
+        if (pw < p.PW) store_masks(offA, pw, p.PW, offs);
     }
 }
 
@@ -1470,11 +1557,12 @@ int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long 
 namespace {
 struct DcDenseWs {
     DcWs d;
-    unsigned long long* zero;  // cleared by the sign pass: misc, then the look-back states
+    unsigned long long* zero;  // cleared by the sign pass: misc, then the weld's look-back states
     long long nzero;
-    long long* misc;           // [0..3] unused  [4..7] eff  [8] [9] tickets
-    unsigned long long *stAQ, *stK, *stV;
-    long long ntC, ntV;        // tiles of dc_cells and dc_weld_local
+    long long* misc;           // [0..3] unused  [4..7] eff  [9] the weld's ticket
+    unsigned long long* stV;
+    uint32_t *wsum, *csum;     // dc_cells: 4 words per warp, per CTA
+    long long ntC, ntV;        // CTAs of the dc_cells kernels and of dc_weld_local
     uint32_t *cells, *qoff, *vmap;
     uint8_t* used;
     float* dual;
@@ -1495,14 +1583,14 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.nzero = 16 + 2 * w.ntC + w.ntV;
+    w.nzero = 16 + w.ntV;
     w.zero = reinterpret_cast<unsigned long long*>(take(size_t(w.nzero) * 8));
     if (ws) {
         w.misc = reinterpret_cast<long long*>(w.zero);
-        w.stAQ = w.zero + 16;
-        w.stK = w.stAQ + w.ntC;
-        w.stV = w.stK + w.ntC;
+        w.stV = w.zero + 16;
     }
+    w.wsum = reinterpret_cast<uint32_t*>(take(size_t(w.ntC) * CELLS_WARPS * 16));
+    w.csum = reinterpret_cast<uint32_t*>(take(size_t(w.ntC) * 16));
     w.cells = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.qoff = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.vmap = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
@@ -1544,9 +1632,15 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
     }
     {
         iso::ProfScope ps("dc_classify", st);
-        iso::launch_pdl(dc_cells, unsigned(w.ntC), unsigned(CELLS_THREADS), st, static_cast<const uint32_t*>(w.d.S), g,
-                        reinterpret_cast<unsigned long long*>(w.misc + 8), w.stAQ, w.stK, w.d.actm, w.d.offA, cells,
-                        w.qoff, reinterpret_cast<uint32_t*>(cell_offsets), capA, capQ, eff, counts, status);
+        const uint32_t* S = w.d.S;
+        iso::launch_pdl(dc_cells_count, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g, w.d.actm, w.wsum,
+                        w.csum);
+        iso::launch_pdl(dc_cells_scan, 1u, 1024u, st, w.csum, w.ntC, capA, capQ, eff, counts,
+                        reinterpret_cast<uint32_t*>(cell_offsets), status);
+        iso::launch_pdl(dc_cells_write, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g,
+                        static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.wsum),
+                        static_cast<const uint32_t*>(w.csum), w.d.offA, cells, w.qoff,
+                        reinterpret_cast<uint32_t*>(cell_offsets), capA);
     }
     if (capA > 0) {
         {
