@@ -239,24 +239,52 @@ __device__ __forceinline__ void qef_solve(const float* points, const float* norm
     qef_finish(Q, K, reg, svd_tol);
 }
 
-// Crossing of edge e of a cell: t and the point (the reference's lerp).  The
-// edge's corners are selected, not indexed, so the cell stays in registers when
-// e is not a constant.
-__device__ __forceinline__ float edge_cross(const CellCorners& cc, float level, int e, float* p) {
-    const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-    float va = cc.v[0], vb = cc.v[0], pa[3] = {cc.p[0][0], cc.p[0][1], cc.p[0][2]}, pb[3] = {pa[0], pa[1], pa[2]};
+// The corners of edge e (ISO_EDGE_CORNERS) from two packed immediates, 3 bits
+// per corner: lanes with different edges do not serialise on a constant-memory
+// load.
+constexpr unsigned long long pack_corners(int end) {
+    unsigned long long p = 0;
+    for (int e = 0; e < 12; ++e) p |= (unsigned long long)iso_edge_corner(2 * e + end) << (3 * e);
+    return p;
+}
+constexpr unsigned long long EDGE_CA = pack_corners(0), EDGE_CB = pack_corners(1);
+__device__ __forceinline__ int edge_ca(int e) { return int((EDGE_CA >> (3 * e)) & 7ull); }
+__device__ __forceinline__ int edge_cb(int e) { return int((EDGE_CB >> (3 * e)) & 7ull); }
+
+// Crossed edges of a cell with case bits cs (ISO_EDGE_STATUS[cs]): the edges
+// whose corners differ in sign.
+__device__ __forceinline__ uint32_t edge_status(uint32_t cs) {
+    uint32_t est = 0;
 #pragma unroll
-    for (int j = 1; j < 8; ++j) {
-        if (j == ca) {
-            va = cc.v[j];
-            pa[0] = cc.p[j][0]; pa[1] = cc.p[j][1]; pa[2] = cc.p[j][2];
-        }
-        if (j == cb) {
-            vb = cc.v[j];
-            pb[0] = cc.p[j][0]; pb[1] = cc.p[j][1]; pb[2] = cc.p[j][2];
-        }
-    }
-    const float t = iso::cross_t(level, va, vb);
+    for (int e = 0; e < 12; ++e)
+        est |= (((cs >> iso_edge_corner(2 * e)) ^ (cs >> iso_edge_corner(2 * e + 1))) & 1u) << e;
+    return est;
+}
+
+// Value at corner j of a cell, selected (not indexed), so the cell stays in
+// registers when j is not a constant.
+__device__ __forceinline__ float corner_value(const CellCorners& cc, int j) {
+    const float a = (j & 1) ? cc.v[1] : cc.v[0], b = (j & 1) ? cc.v[3] : cc.v[2];
+    const float c = (j & 1) ? cc.v[5] : cc.v[4], d = (j & 1) ? cc.v[7] : cc.v[6];
+    const float lo = (j & 2) ? b : a, hi = (j & 2) ? d : c;
+    return (j & 4) ? hi : lo;
+}
+
+// Position of corner j = 4 dx + 2 dy + dz: each coordinate is the low or the
+// high one of the cell (corner 0 or corner 7).
+__device__ __forceinline__ void corner_pos(const CellCorners& cc, int j, float* q) {
+    q[0] = (j & 4) ? cc.p[7][0] : cc.p[0][0];
+    q[1] = (j & 2) ? cc.p[7][1] : cc.p[0][1];
+    q[2] = (j & 1) ? cc.p[7][2] : cc.p[0][2];
+}
+
+// Crossing of edge e of a cell: t and the point (the reference's lerp).
+__device__ __forceinline__ float edge_cross(const CellCorners& cc, float level, int e, float* p) {
+    const int ca = edge_ca(e), cb = edge_cb(e);
+    float pa[3], pb[3];
+    corner_pos(cc, ca, pa);
+    corner_pos(cc, cb, pb);
+    const float t = iso::cross_t(level, corner_value(cc, ca), corner_value(cc, cb));
 #pragma unroll
     for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, pa[q], pb[q]);
     return t;

@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) dc_points(const float* __restrict__ vals,
     uint32_t cs = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
-    const uint32_t est = ISO_EDGE_STATUS[cs];
+    const uint32_t est = edge_status(cs);
     unsigned long long k = cell_off[a];
 #pragma unroll 1
     for (uint32_t em = est; em; em &= em - 1) {  // this lane's crossed edges, ascending
@@ -300,7 +300,7 @@ __device__ __forceinline__ bool cell_used(const Grid3& g, int cx, int cy, int cz
     if (cx >= 1 && cx <= g.nx - 3 && cy >= 1 && cy <= g.ny - 3 && cz >= 1 && cz <= g.nz - 3) return est != 0;
     for (uint32_t em = est; em; em &= em - 1) {
         const int e = __ffs(em) - 1;
-        const int ca = ISO_EDGE_CORNERS[2 * e], ax = ca ^ ISO_EDGE_CORNERS[2 * e + 1];  // 4 x, 2 y, 1 z
+        const int ca = edge_ca(e), ax = ca ^ edge_cb(e);  // 4 x, 2 y, 1 z
         const int x = cx + (ca >> 2), y = cy + ((ca >> 1) & 1), z = cz + (ca & 1);
         const bool okx = ax == 4 || (x >= 1 && x <= g.nx - 2);
         const bool oky = ax == 2 || (y >= 1 && y <= g.ny - 2);
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     uint32_t cs = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
-    const uint32_t est = ISO_EDGE_STATUS[cs];
+    const uint32_t est = edge_status(cs);
     if (used) used[a] = cell_used(g, cx, cy, cz, est) ? 1 : 0;
     Qef Q;
     qef_init(Q);
