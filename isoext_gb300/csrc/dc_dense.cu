@@ -23,7 +23,6 @@
 #define ISO_LUT_DECL static __constant__ const
 #include "luts.h"
 #include "dc_common.cuh"
-#include "lookback.cuh"
 #include "profile.cuh"
 
 namespace {
@@ -143,6 +142,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_cell_count(const uint32_t* __rest
 __global__ void __launch_bounds__(1024) dc_block_scan(unsigned long long* blk, long long nblk,
                                                       long long* totals) {
     __shared__ unsigned long long wa[32], wb[32], carry[2];
+    iso::grid_wait();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) { carry[0] = 0; carry[1] = 0; }
     __syncthreads();
@@ -313,7 +313,8 @@ __device__ __forceinline__ bool cell_used(const Grid3& g, int cx, int cy, int cz
 // Crossings, grid normals and the QEF solve of each active cell in one pass,
 // when nobody asked for the intersection: the same arithmetic as dc_points
 // followed by dc_solve, without writing points and normals.  used (optional):
-// per cell, whether faces use its dual vertex.
+// per cell, 0 when no face uses its dual vertex, else 1, or 3 when the vertex
+// lies on a face of the cell's box.
 __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
                                                      float svd_tol, float* __restrict__ dual,
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
     const uint32_t est = edge_status(cs);
-    if (used) used[a] = cell_used(g, cx, cy, cz, est) ? 1 : 0;
+    const bool is_used = used && cell_used(g, cx, cy, cz, est);
     Qef Q;
     qef_init(Q);
     uint32_t K = 0;
@@ -348,11 +349,15 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     }
     qef_finish(Q, K, reg, svd_tol);
     const int ci[3] = {cx, cy, cz};
+    bool face = false;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const float lo = coord(g, q, uint32_t(ci[q])), hi = coord(g, q, uint32_t(ci[q] + 1));
-        dual[3 * a + q] = fminf(fmaxf(float(Q.x[q]), lo), hi);
+        const float x = fminf(fmaxf(float(Q.x[q]), lo), hi);
+        face |= x == lo || x == hi;
+        dual[3 * a + q] = x;
     }
+    if (used) used[a] = is_used ? (face ? 3 : 1) : 0;  // bit 1: on a face of its cell's box
 }
 
 // ---------------------------------------------------------------------------
@@ -664,7 +669,7 @@ __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uin
 
 
 // ---------------------------------------------------------------------------
-// One-call dual contouring: after the sign pass, six kernels chained by
+// One-call dual contouring: after the sign pass, eight kernels chained by
 // programmatic dependent launch, with the sizes kept on the device.
 //
 //   dc_cells_count / _scan / _write
@@ -675,13 +680,14 @@ __global__ void dc_remap(const int32_t* __restrict__ tri, long long n, const uin
 //                  the owners' order.  Counts per warp, one CTA scans them and
 //                  checks the sizes, then the words are written with offsets.
 //   dc_cell_solve  the QEF solve and whether faces use the cell.
-//   dc_weld_local  the exact-position weld.  A dual vertex is clipped to its
+//   dc_weld_flags / dc_block_scan / dc_weld_number
+//                  the exact-position weld.  A dual vertex is clipped to its
 //                  cell's closed box, and the boxes of different cells meet only
 //                  on shared faces, so a vertex strictly inside its box has a
 //                  position of its own, and one on a face can only equal the
 //                  vertices of the cells around that face, edge or corner.
 //                  Representatives (smallest index of a position) are numbered
-//                  in cell order by a look-back.
+//                  in cell order.
 //   dc_cell_quads  each active cell's quads with the final vertex numbers.
 
 // Crossed edges of one cell (bit b of a cell word): the 12 corner-sign XORs.
@@ -1079,79 +1085,97 @@ __device__ __forceinline__ void cells_holding(const Grid3& g, int axis, int c, f
     while (i1 < n - 2 && coord(g, axis, uint32_t(i1 + 1)) == v) ++i1;
 }
 
-__global__ void __launch_bounds__(DC_BLOCK) dc_weld_local(Grid3 g, const uint32_t* __restrict__ cell_ids,
+// Representative of used cell a whose vertex p lies on a face of its box: the
+// smallest index among the used cells around that face with the same position.
+__device__ __noinline__ uint32_t face_rep(const Grid3& g, uint32_t a, uint32_t cid, float px, float py, float pz,
+                                          const uint8_t* __restrict__ used, const float* __restrict__ dual,
+                                          const uint32_t* __restrict__ actm, const uint32_t* __restrict__ offA) {
+    const float p[3] = {px, py, pz};
+    const int cz = int(cid % uint32_t(g.nz - 1));
+    const uint32_t rr = cid / uint32_t(g.nz - 1);
+    const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+    int x0, x1, y0, y1, z0, z1;
+    cells_holding(g, 0, cx, p[0], x0, x1);
+    cells_holding(g, 1, cy, p[1], y0, y1);
+    cells_holding(g, 2, cz, p[2], z0, z1);
+    const int NWg = (g.nz + 31) / 32;
+    const uint32_t k0 = pos_bits(p[0]), k1 = pos_bits(p[1]), k2 = pos_bits(p[2]);
+    uint32_t rep = a;
+    for (int x = x0; x <= x1; ++x)
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) {
+                if (x == cx && y == cy && z == cz) continue;
+                const long long wi = ((long long)x * g.ny + y) * NWg + (z >> 5);  // point word
+                const uint32_t mw = actm[wi], bit = uint32_t(z & 31);
+                if (!((mw >> bit) & 1u)) continue;
+                const uint32_t ib = offA[wi] + __popc(mw & ((1u << bit) - 1u));
+                if (ib < rep && used[ib] && pos_bits(dual[3ll * ib]) == k0 && pos_bits(dual[3ll * ib + 1]) == k1 &&
+                    pos_bits(dual[3ll * ib + 2]) == k2)
+                    rep = ib;
+            }
+    return rep;
+}
+
+// Weld, step 1 (one thread per active cell): vmap[a] = 0xffffffff when no face
+// uses the cell, 0 when its vertex is a representative (numbered in step 3),
+// else 0x80000000 | its representative; representatives per block of DC_BLOCK
+// cells into blk.
+__global__ void __launch_bounds__(DC_BLOCK) dc_weld_flags(Grid3 g, const uint32_t* __restrict__ cell_ids,
                                                           const uint8_t* __restrict__ used,
                                                           const float* __restrict__ dual,
                                                           const uint32_t* __restrict__ actm,
                                                           const uint32_t* __restrict__ offA,
                                                           const long long* __restrict__ eff,
-                                                          unsigned long long* ticket, unsigned long long* state,
-                                                          uint32_t* __restrict__ vmap, float* __restrict__ vout,
-                                                          uint32_t* __restrict__ vsrc, long long* counts,
-                                                          int* status) {
+                                                          uint32_t* __restrict__ vmap,
+                                                          unsigned long long* __restrict__ blk) {
     __shared__ uint32_t sm[66];
-    __shared__ uint32_t tile_s;
-    __shared__ unsigned long long pre_s;
     iso::grid_wait();
-    if (threadIdx.x == 0) tile_s = uint32_t(atomicAdd(ticket, 1ull));
-    __syncthreads();
-    const uint32_t tile = tile_s;
-    const long long a = (long long)tile * DC_BLOCK + threadIdx.x;
+    const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
     const long long A = eff[0];
-    uint32_t is = 0, m = 0xffffffffu;
-    float p[3] = {0.0f, 0.0f, 0.0f};
-    if (a < A && used[a]) {
-        p[0] = dual[3 * a];
-        p[1] = dual[3 * a + 1];
-        p[2] = dual[3 * a + 2];
-        const uint32_t cid = cell_ids[a];
-        const int cz = int(cid % uint32_t(g.nz - 1));
-        const uint32_t rr = cid / uint32_t(g.nz - 1);
-        const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
-        int x0, x1, y0, y1, z0, z1;
-        cells_holding(g, 0, cx, p[0], x0, x1);
-        cells_holding(g, 1, cy, p[1], y0, y1);
-        cells_holding(g, 2, cz, p[2], z0, z1);
-        uint32_t rep = uint32_t(a);
-        if (x0 != x1 || y0 != y1 || z0 != z1) {
-            const int NWg = (g.nz + 31) / 32;
-            const uint32_t k0 = pos_bits(p[0]), k1 = pos_bits(p[1]), k2 = pos_bits(p[2]);
-            for (int x = x0; x <= x1; ++x)
-                for (int y = y0; y <= y1; ++y)
-                    for (int z = z0; z <= z1; ++z) {
-                        if (x == cx && y == cy && z == cz) continue;
-                        const long long wi = ((long long)x * g.ny + y) * NWg + (z >> 5);  // point word
-                        const uint32_t mw = actm[wi], bit = uint32_t(z & 31);
-                        if (!((mw >> bit) & 1u)) continue;
-                        const uint32_t ib = offA[wi] + __popc(mw & ((1u << bit) - 1u));
-                        if (ib < rep && used[ib] && pos_bits(dual[3ll * ib]) == k0 &&
-                            pos_bits(dual[3ll * ib + 1]) == k1 && pos_bits(dual[3ll * ib + 2]) == k2)
-                            rep = ib;
-                    }
+    uint32_t is = 0;
+    if (a < A) {
+        const uint32_t u = used[a];
+        uint32_t m = 0xffffffffu;
+        if (u) {
+            uint32_t rep = uint32_t(a);
+            if (u & 2u) rep = face_rep(g, rep, cell_ids[a], dual[3 * a], dual[3 * a + 1], dual[3 * a + 2], used, dual,
+                                       actm, offA);
+            is = rep == uint32_t(a) ? 1u : 0u;
+            m = is ? 0u : (0x80000000u | rep);
         }
-        is = rep == uint32_t(a) ? 1u : 0u;
-        if (!is) m = 0x80000000u | rep;
+        vmap[a] = m;
     }
-    uint32_t e, e_, t, t_;
-    block_scan2(is, 0u, e, e_, t, t_, sm);
-    if (threadIdx.x < 32) {
-        unsigned long long pv, p_;
-        lb_tile(state, tile, t, 0, pv, p_, status);
-        if (threadIdx.x == 0) {
-            pre_s = pv;
-            if (tile == gridDim.x - 1) counts[0] = (long long)(pv + t);
-        }
+    uint32_t e0, e1, t0, t1;
+    block_scan2(is, 0u, e0, e1, t0, t1, sm);
+    if (threadIdx.x == 0) {
+        blk[2 * blockIdx.x] = t0;
+        blk[2 * blockIdx.x + 1] = 0;
     }
-    __syncthreads();
-    if (is) {
-        const unsigned long long o = pre_s + e;  // < V <= A: inside the vertex capacity
-        m = uint32_t(o);
-        vout[3 * o] = p[0];
-        vout[3 * o + 1] = p[1];
-        vout[3 * o + 2] = p[2];
-        if (vsrc) vsrc[o] = uint32_t(a);
-    }
-    if (a < A) vmap[a] = m;
+}
+
+// Weld, step 3: representatives numbered in cell order (block offsets from the
+// scan of step 2), their positions (and source cells) written.
+__global__ void __launch_bounds__(DC_BLOCK) dc_weld_number(const float* __restrict__ dual,
+                                                           const long long* __restrict__ eff,
+                                                           const unsigned long long* __restrict__ blk,
+                                                           const long long* __restrict__ vtot,
+                                                           uint32_t* __restrict__ vmap, float* __restrict__ vout,
+                                                           uint32_t* __restrict__ vsrc, long long* counts) {
+    __shared__ uint32_t sm[66];
+    iso::grid_wait();
+    const long long a = (long long)blockIdx.x * DC_BLOCK + threadIdx.x;
+    const long long A = eff[0];
+    const uint32_t is = (a < A && vmap[a] == 0u) ? 1u : 0u;
+    uint32_t e0, e1, t0, t1;
+    block_scan2(is, 0u, e0, e1, t0, t1, sm);
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[0] = vtot[0];
+    if (!is) return;
+    const unsigned long long o = blk[2 * blockIdx.x] + e0;  // < V <= A: inside the vertex capacity
+    vmap[a] = uint32_t(o);
+    vout[3 * o] = dual[3 * a];
+    vout[3 * o + 1] = dual[3 * a + 1];
+    vout[3 * o + 2] = dual[3 * a + 2];
+    if (vsrc) vsrc[o] = uint32_t(a);
 }
 
 __device__ __forceinline__ uint32_t sign_at(const uint32_t* S, const Grid3& g, int x, int y, int z) {
@@ -1557,12 +1581,12 @@ int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long 
 namespace {
 struct DcDenseWs {
     DcWs d;
-    unsigned long long* zero;  // cleared by the sign pass: misc, then the weld's look-back states
+    unsigned long long* zero;  // cleared by the sign pass
     long long nzero;
-    long long* misc;           // [0..3] unused  [4..7] eff  [9] the weld's ticket
-    unsigned long long* stV;
+    long long* misc;           // [0..1] V  [4..7] eff
+    unsigned long long* wblk;  // weld: representatives per block of DC_BLOCK cells
     uint32_t *wsum, *csum;     // dc_cells: 4 words per warp, per CTA
-    long long ntC, ntV;        // CTAs of the dc_cells kernels and of dc_weld_local
+    long long ntC, ntV;        // CTAs of the dc_cells kernels and of the weld
     uint32_t *cells, *qoff, *vmap;
     uint8_t* used;
     float* dual;
@@ -1583,12 +1607,10 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.nzero = 16 + w.ntV;
+    w.nzero = 16;
     w.zero = reinterpret_cast<unsigned long long*>(take(size_t(w.nzero) * 8));
-    if (ws) {
-        w.misc = reinterpret_cast<long long*>(w.zero);
-        w.stV = w.zero + 16;
-    }
+    w.misc = reinterpret_cast<long long*>(w.zero);
+    w.wblk = reinterpret_cast<unsigned long long*>(take(size_t(w.ntV + 1) * 16));
     w.wsum = reinterpret_cast<uint32_t*>(take(size_t(w.ntC) * CELLS_WARPS * 16));
     w.csum = reinterpret_cast<uint32_t*>(take(size_t(w.ntC) * 16));
     w.cells = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
@@ -1652,11 +1674,16 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         }
         {
             iso::ProfScope ps("dc_weld", st);
-            iso::launch_pdl(dc_weld_local, unsigned(w.ntV), DC_BLOCK, st, g, static_cast<const uint32_t*>(cells),
-                            static_cast<const uint8_t*>(w.used), static_cast<const float*>(w.dual),
-                            static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.d.offA),
-                            static_cast<const long long*>(eff), reinterpret_cast<unsigned long long*>(w.misc + 9),
-                            w.stV, w.vmap, vertices, reinterpret_cast<uint32_t*>(vertex_source), counts, status);
+            iso::launch_pdl(dc_weld_flags, unsigned(w.ntV), unsigned(DC_BLOCK), st, g,
+                            static_cast<const uint32_t*>(cells), static_cast<const uint8_t*>(w.used),
+                            static_cast<const float*>(w.dual), static_cast<const uint32_t*>(w.d.actm),
+                            static_cast<const uint32_t*>(w.d.offA), static_cast<const long long*>(eff), w.vmap,
+                            w.wblk);
+            iso::launch_pdl(dc_block_scan, 1u, 1024u, st, w.wblk, w.ntV, w.misc);
+            iso::launch_pdl(dc_weld_number, unsigned(w.ntV), unsigned(DC_BLOCK), st,
+                            static_cast<const float*>(w.dual), static_cast<const long long*>(eff),
+                            static_cast<const unsigned long long*>(w.wblk), static_cast<const long long*>(w.misc),
+                            w.vmap, vertices, reinterpret_cast<uint32_t*>(vertex_source), counts);
         }
         {
             iso::ProfScope ps("dc_quads", st);

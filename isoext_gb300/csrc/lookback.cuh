@@ -24,7 +24,7 @@ __device__ __forceinline__ unsigned long long lb_pack(unsigned long long flag, u
 
 // Exclusive (a, b) prefix of tile seg; run by one full warp after the tile's
 // aggregate is published.
-__device__ void look_back(volatile unsigned long long* state, uint32_t seg, unsigned long long& ev,
+__device__ __forceinline__ void look_back(volatile unsigned long long* state, uint32_t seg, unsigned long long& ev,
                           unsigned long long& ef, int* status, uint32_t limit = ISO_SPIN_LIMIT) {
     const int lane = threadIdx.x & 31;
     ev = 0;

@@ -80,8 +80,9 @@ def prims_buffer(prims: np.ndarray) -> np.ndarray:
 
 # Kernels of this library one request launches: marching cubes = grid evaluation
 # + mc_signs, mc_count, mc_scan, mc_emit; dual contouring = grid evaluation +
-# mc_signs, cell count, scan and write, solve, weld, quads.
-KERNELS_PER_REQUEST = {"mc": 5, "dc": 8}
+# mc_signs, cell count, scan and write, solve, weld flags, scan and numbering,
+# quads.
+KERNELS_PER_REQUEST = {"mc": 5, "dc": 10}
 
 
 # ---------------------------------------------------------------------------
