@@ -968,8 +968,9 @@ __global__ void __launch_bounds__(1024) dc_cells_scan(uint32_t* __restrict__ csu
 
 // The busy rounds of dc_cells_count again, with each warp's offsets: active
 // prefixes per point word (rounds without an active cell have none to look
-// up), and per active cell its id, its first owned quad and (when asked) its
-// first crossing.
+// up), and per active cell its id, its first owned quad, its owned quad edges
+// (bits 0-2: z, y, x) with the sign of its lowest corner (bit 3), and (when
+// asked) its first crossing.
 __global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_write(const uint32_t* __restrict__ S, Grid3 g,
                                                                    const uint32_t* __restrict__ actm,
                                                                    const uint32_t* __restrict__ wsum,
@@ -977,6 +978,7 @@ __global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_write(const uint32_
                                                                    uint32_t* __restrict__ offA,
                                                                    uint32_t* __restrict__ cell_ids,
                                                                    uint32_t* __restrict__ qoff,
+                                                                   uint8_t* __restrict__ qbits,
                                                                    uint32_t* __restrict__ cell_off, long long capA) {
     iso::grid_wait();
     const int lane = threadIdx.x & 31;
@@ -1049,12 +1051,14 @@ __global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_write(const uint32_
                 while (m) {
                     const int b = __ffs(m) - 1;
                     m &= m - 1;
+                    const uint32_t oz = (qz >> b) & 1u, oy = (qy >> b) & 1u, ox = (qx >> b) & 1u;
                     if (a < cap) {
                         cell_ids[a] = row + b;
                         qoff[a] = uint32_t(qq);
+                        qbits[a] = uint8_t(oz | (oy << 1) | (ox << 2) | (((cw8[0] >> b) & 1u) << 3));
                         if (want_k) cell_off[a] = uint32_t(kk);
                     }
-                    qq += ((qz >> b) & 1u) + ((qy >> b) & 1u) + ((qx >> b) & 1u);
+                    qq += oz + oy + ox;
                     if (want_k) kk += cell_crossings(ex, b);
                     ++a;
                 }
@@ -1178,10 +1182,6 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_weld_number(const float* __restri
     if (vsrc) vsrc[o] = uint32_t(a);
 }
 
-__device__ __forceinline__ uint32_t sign_at(const uint32_t* S, const Grid3& g, int x, int y, int z) {
-    return (srow(S, g, x, y)[z >> 5] >> (z & 31)) & 1u;
-}
-
 // Final vertex number of active cell i: its own, or its representative's.
 __device__ __forceinline__ int32_t vertex_of(const uint32_t* vmap, uint32_t i) {
     uint32_t m = vmap[i];
@@ -1192,7 +1192,7 @@ __device__ __forceinline__ int32_t vertex_of(const uint32_t* vmap, uint32_t i) {
 // The quads active cell a owns, in the reference's order and orientation
 // (src/dc.cu:101-157): the 4 cells around the edge are p - o_i with the offsets
 // of edge_neighbors_table (src/shared_luts.cu:78-81), the owner being o_0 = 0.
-__global__ void __launch_bounds__(256) dc_cell_quads(const uint32_t* __restrict__ S, Grid3 g,
+__global__ void __launch_bounds__(256) dc_cell_quads(const uint8_t* __restrict__ qbits, Grid3 g,
                                                      const uint32_t* __restrict__ cell_ids,
                                                      const uint32_t* __restrict__ qoff,
                                                      const uint32_t* __restrict__ actm,
@@ -1207,12 +1207,11 @@ __global__ void __launch_bounds__(256) dc_cell_quads(const uint32_t* __restrict_
     const int cz = int(cid % uint32_t(g.nz - 1));
     const uint32_t rr = cid / uint32_t(g.nz - 1);
     const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
-    const uint32_t s0 = sign_at(S, g, cx, cy, cz);
-    // owned edges, in the order z, y, x
-    const bool ez = cx >= 1 && cy >= 1 && sign_at(S, g, cx, cy, cz + 1) != s0;
-    const bool ey = cx >= 1 && cz >= 1 && sign_at(S, g, cx, cy + 1, cz) != s0;
-    const bool ex = cy >= 1 && cz >= 1 && sign_at(S, g, cx + 1, cy, cz) != s0;
-    if (!(ez || ey || ex)) return;
+    // owned edges (z, y, x) and the sign of the low corner, from dc_cells_write
+    const uint32_t qb = qbits[a];
+    const bool ez = qb & 1u, ey = qb & 2u, ex = qb & 4u;
+    const uint32_t s0 = (qb >> 3) & 1u;
+    if (!(qb & 7u)) return;
     unsigned long long q = qoff[a];
     const float own[3] = {dual[3 * a], dual[3 * a + 1], dual[3 * a + 2]};
 #pragma unroll
@@ -1588,7 +1587,7 @@ struct DcDenseWs {
     uint32_t *wsum, *csum;     // dc_cells: 4 words per warp, per CTA
     long long ntC, ntV;        // CTAs of the dc_cells kernels and of the weld
     uint32_t *cells, *qoff, *vmap;
-    uint8_t* used;
+    uint8_t *used, *qbits;
     float* dual;
     size_t total;
 };
@@ -1617,6 +1616,7 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
     w.qoff = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.vmap = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.used = take(size_t(capA));
+    w.qbits = take(size_t(capA));
     w.dual = reinterpret_cast<float*>(take(size_t(capA) * 12));
     w.total = o + 256;
     return w;
@@ -1661,7 +1661,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
                         reinterpret_cast<uint32_t*>(cell_offsets), status);
         iso::launch_pdl(dc_cells_write, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g,
                         static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.wsum),
-                        static_cast<const uint32_t*>(w.csum), w.d.offA, cells, w.qoff,
+                        static_cast<const uint32_t*>(w.csum), w.d.offA, cells, w.qoff, w.qbits,
                         reinterpret_cast<uint32_t*>(cell_offsets), capA);
     }
     if (capA > 0) {
@@ -1687,7 +1687,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         }
         {
             iso::ProfScope ps("dc_quads", st);
-            iso::launch_pdl(dc_cell_quads, blocks_for(capA, 256), 256u, st, static_cast<const uint32_t*>(w.d.S), g,
+            iso::launch_pdl(dc_cell_quads, blocks_for(capA, 256), 256u, st, static_cast<const uint8_t*>(w.qbits), g,
                             static_cast<const uint32_t*>(cells), static_cast<const uint32_t*>(w.qoff),
                             static_cast<const uint32_t*>(w.d.actm), static_cast<const uint32_t*>(w.d.offA),
                             static_cast<const float*>(w.dual), static_cast<const uint32_t*>(w.vmap),

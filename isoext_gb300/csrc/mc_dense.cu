@@ -234,10 +234,6 @@ __device__ __forceinline__ uint32_t cell_case(const Words& d, int b) {
     return cs;
 }
 
-__device__ __forceinline__ const signed char* tri_row(int method, uint32_t cs) {
-    return method == 0 ? ISO_TRI_NAGAE + cs * 15 : ISO_TRI_LORENSEN + cs * 12;
-}
-
 // Block-wide exclusive scan of two counts; totals in ta, tb.
 template <int BLOCK>
 __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea, uint32_t& eb, uint32_t& ta,
