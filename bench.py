@@ -901,6 +901,9 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
     stream = torch.cuda.current_stream(dev)
     grid = iso.UniformGrid([n] * 3, device=dev)
     grid.set_values(vals)
+    # launch parameters for this GPU and grid (isoext_gb300.tune), before timing
+    from isoext_gb300 import tune
+    tuned = tune.autotune(grid, kinds=("dc",), repeats=10)
     v, f = iso.dual_contouring(grid)
     nv, nf = len(v), len(f)
     from isoext_gb300 import dc as dcmod
@@ -979,6 +982,8 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
         "data": f"synthetic: sphere SDF |p|-{wl['r']} on [-1,1]^3",
         "config": {"workload": wl["desc"], "grid": [n, n, n], "cells": cells, "normals": "from the grid",
                    "vertices": nv, "faces": nf, "active_cells": A, "parallelism": f"replicas x{world}",
+                   "tuned": {k: v_ for k, v_ in tuned["best"].items() if k.startswith("dc.")},
+                   "tuning_ms": tuned["ms"],
                    "l2": f"inputs larger than L2 (values {4 * pts / 1e6:.0f} MB > 129 MB L2)"},
         "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 4 * pts, "d2h_bytes_per_step": 12 * (nv + nf)},

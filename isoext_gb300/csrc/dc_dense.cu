@@ -360,6 +360,17 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     if (used) used[a] = is_used ? (face ? 3 : 1) : 0;  // bit 1: on a face of its cell's box
 }
 
+// Lane whose inclusive prefix first exceeds j (prefixes nondecreasing, j < total).
+__device__ __forceinline__ int owner_lane(uint32_t incl, uint32_t j) {
+    int lo = 0;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const uint32_t pv = __shfl_sync(~0u, incl, lo + s - 1);
+        if (pv <= j) lo += s;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------------------
 // solve
 
@@ -441,17 +452,6 @@ __device__ __forceinline__ uint32_t active_index(const uint32_t* actm, const uin
 __device__ __forceinline__ float dist3(const float* a, const float* b) {
     const float dx = __fsub_rn(a[0], b[0]), dy = __fsub_rn(a[1], b[1]), dz = __fsub_rn(a[2], b[2]);
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-}
-
-// Lane whose inclusive prefix first exceeds j (prefixes nondecreasing, j < total).
-__device__ __forceinline__ int owner_lane(uint32_t incl, uint32_t j) {
-    int lo = 0;
-#pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) {
-        const uint32_t pv = __shfl_sync(~0u, incl, lo + s - 1);
-        if (pv <= j) lo += s;
-    }
-    return lo;
 }
 
 // The k-th quad of a point word in the reference's order: by bit (low endpoint

@@ -247,3 +247,25 @@ def test_dc_one_call_weld_equals_hash_weld(case):
     if case == "repeated_coords":  # the grid does repeat coordinates, and the weld merged across them
         pts = g.get_points().reshape(-1, 3)
         assert len(torch.unique(pts[:, 0])) < g.shape[0]
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 3, 3), (2, 5, 33), (5, 3, 32), (37, 41, 128), (33, 29, 97)])
+def test_dc_one_call_shapes(oracle, shape):
+    """The one-call path numbers cells over the flat point-word bitmap, four words
+    per lane with 16-byte loads when rows hold a multiple of 4 words (nz in
+    97..128 here) and scalar loads otherwise; rows of one word (nz <= 33) and the
+    smallest grids exercise the edges of that walk.  The mesh must equal the call
+    sequence's bit for bit and the oracle's within the tolerance."""
+    rng = np.random.default_rng(sum(shape))
+    vals = sphere(shape, 0.45, center=(0.05, -0.02, 0.01)) if min(shape) > 3 else \
+        rng.uniform(-1, 1, size=shape).astype(np.float32)
+    g = make_grid(vals)
+    v0, f0 = iso.dual_contouring(g)
+    its = iso.get_intersection(g, compute_normals=True)
+    v1, f1 = iso.dual_contouring(g, intersection=its)
+    if v0 is None:
+        assert v1 is None
+        return
+    assert torch.equal(v0, v1) and torch.equal(f0, f1)
+    vo, fo, _ = oracle.dc_dense(vals)
+    assert_dc_match(v0.cpu().numpy(), f0.cpu().numpy(), vo, fo, cell_h(shape), f"shape {shape}")
