@@ -69,7 +69,8 @@ __device__ __forceinline__ void tri_weights(const float t[3], float w[8], float 
 
 // Gradient of the grid normal at crossing point p (cell_normal) given dL/dn:
 // adds to the cell's corner values (gc) and to the point (gp).
-__device__ void normal_backward(const CellCorners& cc, const float* p, const float* gn, float* gp, float* gc) {
+__device__ __forceinline__ void normal_backward(const CellCorners& cc, const float* p, const float* gn, float* gp,
+                                                float* gc) {
     const float eps = 0.02f;
     float cmin[3], csz[3], t[3], tin[3];
 #pragma unroll
@@ -133,6 +134,10 @@ __device__ void normal_backward(const CellCorners& cc, const float* p, const flo
     for (int b = 0; b < 3; ++b) gp[b] += gt[b] * tin[b] / csz[b];
 }
 
+// One thread per active cell.  The crossings, their normals and the QEF are
+// recomputed in the forward's order (the same bits), then the crossings are
+// walked again for the gradients; the cell's corners stay in registers (edge
+// corners are selected, not indexed).
 __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ vals, Grid3 g, float level,
                                                    const uint32_t* __restrict__ cell_ids,
                                                    const uint32_t* __restrict__ cell_off, long long A,
@@ -149,35 +154,29 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
     const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
     CellCorners cc;
     load_cell(vals, g, cx, cy, cz, cc);
-    // the crossings in the forward's order (edges of the case, ascending)
     uint32_t cs = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
-    const uint32_t est = ISO_EDGE_STATUS[cs];
-    float pk[12][3], nk[12][3], tk[12];
-    int ek[12];
-    int K = 0;
-    for (int e = 0; e < 12; ++e) {
-        if (!((est >> e) & 1u)) continue;
-        const int ca = ISO_EDGE_CORNERS[2 * e], cb = ISO_EDGE_CORNERS[2 * e + 1];
-        const float t = iso::cross_t(level, cc.v[ca], cc.v[cb]);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) pk[K][q] = iso::lerp1(t, cc.p[ca][q], cc.p[cb][q]);
-        tk[K] = t;
-        ek[K] = e;
-        ++K;
-    }
+    const uint32_t est = edge_status(cs);
     const uint32_t k0 = cell_off[a];
-    for (int k = 0; k < K; ++k) {
+    // the forward again: the QEF of the crossings in edge order
+    Qef Q;
+    qef_init(Q);
+    uint32_t K = 0;
+#pragma unroll 1
+    for (uint32_t em = est; em; em &= em - 1, ++K) {
+        const int e = __ffs(em) - 1;
+        float p[3], n[3];
+        edge_cross(cc, level, e, p);
         if (user_normals) {
 #pragma unroll
-            for (int q = 0; q < 3; ++q) nk[k][q] = user_normals[3ll * (k0 + k) + q];
+            for (int q = 0; q < 3; ++q) n[q] = user_normals[3ll * (k0 + K) + q];
         } else {
-            cell_normal(cc, pk[k], nk[k]);
+            cell_normal(cc, p, n);
         }
+        qef_add(Q, p[0], p[1], p[2], n[0], n[1], n[2]);
     }
-    Qef Q;
-    qef_solve(&pk[0][0], &nk[0][0], uint32_t(K), reg, svd_tol, Q);
+    qef_finish(Q, K, reg, svd_tol);
     const int ci[3] = {cx, cy, cz};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -190,16 +189,27 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
     apply_pinv_f(Q.w, Q.q, Q.keep, gx, l);  // lambda = pinv(M) g
     const float rk = reg / float(K);
     float gc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < K; ++k) {
+    uint32_t k = 0;
+#pragma unroll 1
+    for (uint32_t em = est; em; em &= em - 1, ++k) {
+        const int e = __ffs(em) - 1;
+        float p[3], n[3];
+        const float t = edge_cross(cc, level, e, p);
+        if (user_normals) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) n[q] = user_normals[3ll * (k0 + k) + q];
+        } else {
+            cell_normal(cc, p, n);
+        }
         float u[3], gn[3], gp[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) u[q] = float(double(pk[k][q]) - Q.x[q]);
-        const float ln = l[0] * nk[k][0] + l[1] * nk[k][1] + l[2] * nk[k][2];
-        const float nu = nk[k][0] * u[0] + nk[k][1] * u[1] + nk[k][2] * u[2];
+        for (int q = 0; q < 3; ++q) u[q] = float(double(p[q]) - Q.x[q]);
+        const float ln = l[0] * n[0] + l[1] * n[1] + l[2] * n[2];
+        const float nu = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             gn[q] = l[q] * nu + u[q] * ln;
-            gp[q] = nk[k][q] * ln + rk * l[q];
+            gp[q] = n[q] * ln + rk * l[q];
         }
         if (user_normals) {
             if (gnormals) {
@@ -207,16 +217,21 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
                 for (int q = 0; q < 3; ++q) gnormals[3ll * (k0 + k) + q] = gn[q];
             }
         } else {
-            normal_backward(cc, pk[k], gn, gp, gc);
+            normal_backward(cc, p, gn, gp, gc);
         }
-        const int ca = ISO_EDGE_CORNERS[2 * ek[k]], cb = ISO_EDGE_CORNERS[2 * ek[k] + 1];
-        const float d = cc.v[cb] - cc.v[ca];
+        // through the crossing's t to the edge's two corner values
+        const int ca = edge_ca(e), cb = edge_cb(e);
+        const float d = corner_value(cc, cb) - corner_value(cc, ca);
         if (d == 0.0f) continue;
+        float pa[3], pb[3];
+        corner_pos(cc, ca, pa);
+        corner_pos(cc, cb, pb);
         float gt = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) gt += gp[q] * (cc.p[cb][q] - cc.p[ca][q]);
-        gc[ca] -= gt * (1.0f - tk[k]) / d;
-        gc[cb] -= gt * tk[k] / d;
+        for (int q = 0; q < 3; ++q) gt += gp[q] * (pb[q] - pa[q]);
+        const float ga = -(gt * (1.0f - t) / d), gb = -(gt * t / d);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) gc[j] += (j == ca ? ga : 0.0f) + (j == cb ? gb : 0.0f);
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
