@@ -273,7 +273,7 @@ def run_ours(args, wl, rank, world) -> dict | None:
     assert int(host[2] & 0xffffffff) == 0, f"device status {int(host[2])}"
     assert (int(host[0]), int(host[1])) == (nv, nf)
     kt = {k: _ffi.profile_read(k) for k in kernels}
-    launches = sum(c for c, _ in kt.values())
+    launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     # per extraction: the sum of the kernel's launches in one call
     kavg = {k: t / args.steps for k, (c, t) in kt.items()}
     top = max(kavg, key=kavg.get)
@@ -422,7 +422,7 @@ def run_grad(args, wl, rank, world) -> dict | None:
     lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in GRAD_KERNELS}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
-    launches = sum(c for c, _ in kt.values())
+    launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     # e2e: grids from pinned host memory, gradients back to the host
     hosts = [x.detach().cpu().pin_memory() for x in xs]
     outs = [torch.empty_like(h).pin_memory() for h in hosts]
@@ -565,7 +565,7 @@ def run_sparse(args, wl, rank, world) -> dict | None:
     lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in ("sparse_mc", "dc_weld")}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
-    launches = sum(c for c, _ in kt.values())
+    launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     # e2e: ids and values from pinned host memory, the mesh back
     ids_h = grid.get_cell_indices().cpu().pin_memory()
     vals_h = grid.get_values().cpu().pin_memory()
@@ -823,7 +823,7 @@ def run_dc(args, wl, rank, world) -> dict | None:
     lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in DC_KERNELS}
     kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
-    launches = sum(c for c, _ in kt.values())
+    launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     ms = max_over_ranks(ms, world, dev)
 
     # e2e: host values -> device -> grid -> the step -> mesh to host
@@ -948,7 +948,7 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
     lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in DC1_KERNELS}
     kstep = {k: t / args.steps for k, (c, t) in kt.items() if c}
-    launches = sum(c for c, _ in kt.values())
+    launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     # e2e: pinned host values -> grid, dual_contouring, mesh into pinned buffers
     pinned = torch.from_numpy(vals_np).pin_memory()
     vh = torch.empty((capv, 3), dtype=torch.float32).pin_memory()

@@ -70,13 +70,16 @@ int iso_test_wait_timeout(unsigned spin_limit, unsigned long long *state, int *s
                           unsigned long long *out, void *stream);
 
 /* Kernel timing for benchmarks (no counterpart in the reference).  While
- * enabled, each kernel the library launches is bracketed by CUDA events on its
- * stream.  iso_profile_read synchronises on the recorded events and returns the
- * number of launches and their total device time in ms for one kernel name
- * ("mc_signs", "mc_count", "mc_scan", "mc_emit", "mc_fixup", ...; NULL = all). */
+ * enabled, each kernel (or short group of kernels) the library launches is
+ * bracketed by CUDA events on its stream.  iso_profile_read synchronises on the
+ * recorded events and returns the number of timed groups and their total
+ * device time in ms for one name ("mc_signs", "mc_count", "mc_scan", "mc_emit",
+ * "dc_classify", ...; NULL = all); iso_profile_kernels returns how many kernels
+ * those groups launched. */
 int iso_profile_enable(int on);
 void iso_profile_reset(void);
 int iso_profile_read(const char *kernel, long long *launches, double *total_ms);
+int iso_profile_kernels(const char *kernel, long long *kernels);
 
 /* Workspace bytes iso_mc_dense needs for a grid and output capacities. */
 size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,

@@ -39,6 +39,7 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_profile_enable.argtypes = [_i]
     lib.iso_profile_reset.restype = None
     lib.iso_profile_read.argtypes = [C.c_char_p, C.POINTER(_ll), C.POINTER(C.c_double)]
+    lib.iso_profile_kernels.argtypes = [C.c_char_p, C.POINTER(_ll)]
     lib.iso_mc_dense_workspace_size.argtypes = [_i, _i, _i, _ll, _ll]
     lib.iso_mc_dense_workspace_size.restype = C.c_size_t
     lib.iso_mc_dense.argtypes = [_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp,
@@ -98,7 +99,14 @@ def fvec3(xs) -> C.Array:
 
 
 def profile_read(kernel: str | None) -> tuple[int, float]:
-    """(launches, total ms) recorded for a kernel since the last reset."""
+    """(timed groups, total ms) recorded under a name since the last reset."""
     n, t = _ll(), C.c_double()
     check(lib().iso_profile_read(kernel.encode() if kernel else None, C.byref(n), C.byref(t)))
     return n.value, t.value
+
+
+def profile_kernels(kernel: str | None) -> int:
+    """Kernels launched under a name (None: all) since the last reset."""
+    n = _ll()
+    check(lib().iso_profile_kernels(kernel.encode() if kernel else None, C.byref(n)))
+    return n.value

@@ -1302,7 +1302,7 @@ void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long 
                      void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
                      uint32_t* vsrc) {
     const WeldDev w = weld_dev_carve(ws, capA);
-    iso::ProfScope ps("dc_weld", st);
+    iso::ProfScope ps("dc_weld", st, (capT > 0 ? 2 : 0) + (capA > 0 ? 5 : 0));
     cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
     cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
     if (capT > 0) dc_mark_used<<<blocks_for(capT, 256), 256, 0, st>>>(tri, capT, w.used, eff);
@@ -1391,7 +1391,7 @@ int iso_dc_classify(const float* values, int nx, int ny, int nz, float level, vo
         iso::ProfScope ps("mc_signs", st);
         mc_signs_launch(values, nx, ny, nz, level, w.S, st);
     }
-    iso::ProfScope ps("dc_classify", st);
+    iso::ProfScope ps("dc_classify", st, 2);
     dc_cell_count<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.cwords, w.blkC);
     dc_block_scan<<<1, 1024, 0, st>>>(w.blkC, w.nblkC, counts);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -1404,7 +1404,7 @@ int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* a
     if (nx < 2 || ny < 2 || nz < 2) return 0;
     DcWs w = carve(ws, nx, ny, nz);
     Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
-    iso::ProfScope ps("dc_intersect", st);
+    iso::ProfScope ps("dc_intersect", st, A > 0 && points ? 2 : 1);
     dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
         values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, points, normals,
         reinterpret_cast<uint32_t*>(cell_ids), reinterpret_cast<uint32_t*>(cell_offsets), A, K, nullptr);
@@ -1487,7 +1487,7 @@ int iso_dc_quads_count(int nx, int ny, int nz, void* ws, long long* counts, void
     DcWs w = carve(ws, nx, ny, nz);
     const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
     Grid3 g = make_grid(nx, ny, nz, amin, amax);
-    iso::ProfScope ps("dc_quads", st);
+    iso::ProfScope ps("dc_quads", st, 2);
     dc_quad_count<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ);
     dc_block_scan<<<1, 1024, 0, st>>>(w.blkQ, w.nblkQ, counts);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -1527,7 +1527,7 @@ int iso_dc_weld_count(const float* dual, long long A, const int* tri, long long 
     unsigned long long* blk = reinterpret_cast<unsigned long long*>(
         (reinterpret_cast<uintptr_t>(table + cap) + 15) & ~uintptr_t(15));
     const long long nblk = (A + DC_BLOCK - 1) / DC_BLOCK;
-    iso::ProfScope ps("dc_weld", st);
+    iso::ProfScope ps("dc_weld", st, (ntri > 0 ? 1 : 0) + (A > 0 ? 4 : 0));
     cudaMemsetAsync(used, 0, size_t(A) * 4, st);
     cudaMemsetAsync(table, 0xff, size_t(cap) * 4, st);
     if (ntri > 0) dc_mark_used<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, used, nullptr);
@@ -1557,7 +1557,7 @@ int iso_dc_weld_write_src(const float* dual, long long A, const int* tri, long l
     unsigned long long* blk = reinterpret_cast<unsigned long long*>(
         (reinterpret_cast<uintptr_t>(table + cap) + 15) & ~uintptr_t(15));
     const long long nblk = (A + DC_BLOCK - 1) / DC_BLOCK;
-    iso::ProfScope ps("dc_weld", st);
+    iso::ProfScope ps("dc_weld", st, (A > 0 ? 1 : 0) + (ntri > 0 ? 1 : 0));
     if (A > 0)
         dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk, dual, newidx, vout,
                                                            reinterpret_cast<uint32_t*>(vertex_source), nullptr);
@@ -1653,7 +1653,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         mc_signs_launch(values, nx, ny, nz, level, w.d.S, st, w.zero, w.nzero);
     }
     {
-        iso::ProfScope ps("dc_classify", st);
+        iso::ProfScope ps("dc_classify", st, 3);
         const uint32_t* S = w.d.S;
         iso::launch_pdl(dc_cells_count, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g, w.d.actm, w.wsum,
                         w.csum);
@@ -1673,7 +1673,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
                             static_cast<const long long*>(eff), w.used);
         }
         {
-            iso::ProfScope ps("dc_weld", st);
+            iso::ProfScope ps("dc_weld", st, 3);
             iso::launch_pdl(dc_weld_flags, unsigned(w.ntV), unsigned(DC_BLOCK), st, g,
                             static_cast<const uint32_t*>(cells), static_cast<const uint8_t*>(w.used),
                             static_cast<const float*>(w.dual), static_cast<const uint32_t*>(w.d.actm),

@@ -13,6 +13,7 @@ namespace {
 struct Rec {
     const char* name;
     cudaEvent_t a, b;
+    int kernels;
 };
 std::mutex g_mu;
 bool g_on = false;
@@ -32,7 +33,8 @@ cudaEvent_t get_event() {
 }  // namespace
 
 namespace iso {
-ProfScope::ProfScope(const char* name, cudaStream_t st) : name_(name), st_(st), a_(nullptr) {
+ProfScope::ProfScope(const char* name, cudaStream_t st, int kernels)
+    : name_(name), st_(st), a_(nullptr), kernels_(kernels) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_on) return;
     a_ = get_event();
@@ -43,7 +45,7 @@ ProfScope::~ProfScope() {
     std::lock_guard<std::mutex> lk(g_mu);
     cudaEvent_t b = get_event();
     cudaEventRecord(b, st_);
-    g_recs.push_back({name_, a_, b});
+    g_recs.push_back({name_, a_, b, kernels_});
 }
 }  // namespace iso
 
@@ -78,6 +80,16 @@ int iso_profile_read(const char* kernel, long long* launches, double* total_ms) 
     }
     if (launches) *launches = n;
     if (total_ms) *total_ms = t;
+    return ISO_OK;
+}
+
+int iso_profile_kernels(const char* kernel, long long* kernels) {
+    if (!kernels) return ISO_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_mu);
+    long long n = 0;
+    for (auto& r : g_recs)
+        if (!kernel || std::strcmp(kernel, r.name) == 0) n += r.kernels;
+    *kernels = n;
     return ISO_OK;
 }
 

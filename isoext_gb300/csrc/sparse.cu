@@ -593,7 +593,7 @@ int iso_sparse_mc_count(const int* ids, const float* vals, long long n, int nx, 
     if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
     if (method != 0 && method != 1) return ISO_ERR_ARG;
     SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
-    iso::ProfScope ps("sparse_mc", st);
+    iso::ProfScope ps("sparse_mc", st, 2);
     sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -616,7 +616,7 @@ int iso_sparse_its_count(const float* vals, long long n, float level, void* blk,
     if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
     SpGrid g{};
     g.level = level;
-    iso::ProfScope ps("sparse_its", st);
+    iso::ProfScope ps("sparse_its", st, 2);
     sp_its_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, vals, n, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -656,7 +656,7 @@ int iso_sparse_quads_count(const int* ids, const float* vals, long long n, int n
     if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
     const float z3[3] = {0, 0, 0}, o3[3] = {1, 1, 1};
     SpGrid g = mk(nx, ny, nz, z3, o3, level, 0);
-    iso::ProfScope ps("sparse_quads", st);
+    iso::ProfScope ps("sparse_quads", st, 2);
     sp_quad_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, reinterpret_cast<const uint32_t*>(rank),
                                                         (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
@@ -680,6 +680,7 @@ int iso_sparse_points(const int* ids, long long m, int nx, int ny, int nz, const
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (m <= 0) return 0;
     SpGrid g = mk(nx, ny, nz, amin, amax, 0.0f, 0);
+    iso::ProfScope ps("sparse_populate", st);
     sp_points<<<nb(m * 8, 256), 256, 0, st>>>(g, ids, m, out);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
@@ -688,6 +689,7 @@ int iso_sparse_filter_count(const float* vals, long long m, float level, void* b
                             void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (m <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    iso::ProfScope ps("sparse_populate", st, 2);
     sp_filter_count<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(vals, m, level, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(m, SP_BLOCK), counts, st);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
@@ -697,6 +699,7 @@ int iso_sparse_filter_write(const int* ids, const float* vals, long long m, floa
                             int* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (m <= 0) return 0;
+    iso::ProfScope ps("sparse_populate", st);
     sp_filter_write<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(ids, vals, m, level, (const unsigned long long*)blk, out);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
@@ -724,7 +727,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     const SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     long long* eff = w.tot + 4;
     {
-        iso::ProfScope ps("sparse_mc", st);
+        iso::ProfScope ps("sparse_mc", st, 4);
         sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk);
         iso_block_scan_launch((unsigned long long*)w.blk, nb(n, SP_BLOCK), w.tot, st);
         sp_mc_sizes<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
@@ -733,7 +736,10 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     }
     weld_dev_launch(w.soup, 3 * face_capacity, nullptr, 3 * face_capacity, eff, w.weld, vertices, faces, w.tot + 8,
                     status, st, nullptr);
-    sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
+    {
+        iso::ProfScope ps("sparse_mc", st);
+        sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
