@@ -949,21 +949,29 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
     kt = {k: _ffi.profile_read(k) for k in DC1_KERNELS}
     kstep = {k: t / args.steps for k, (c, t) in kt.items() if c}
     launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
-    # e2e: pinned host values -> grid, dual_contouring, mesh into pinned buffers
+    # e2e: pinned host values -> a grid, dual_contouring, mesh into pinned buffers
     pinned = torch.from_numpy(vals_np).pin_memory()
+    egrid = iso.UniformGrid([n] * 3, device=dev)
     vh = torch.empty((capv, 3), dtype=torch.float32).pin_memory()
     fh = torch.empty((capf, 3), dtype=torch.int32).pin_memory()
-    e2e_t = []
+    e2e_t, h2d_t, d2h_t = [], [], []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        grid.set_values(pinned)
-        vv, ff = iso.dual_contouring(grid)
+        egrid.set_values(pinned)
+        t1 = time.perf_counter()
+        vv, ff = iso.dual_contouring(egrid)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
         vh[:len(vv)].copy_(vv)
         fh[:len(ff)].copy_(ff)
+        t3 = time.perf_counter()
         if i >= args.warmup:
-            e2e_t.append(time.perf_counter() - t0)
+            e2e_t.append(t3 - t0)
+            h2d_t.append(t1 - t0)
+            d2h_t.append(t3 - t2)
     e2e_ms = 1e3 * statistics.mean(e2e_t)
+    e2e_split = {"h2d_ms": round(1e3 * statistics.mean(h2d_t), 3), "d2h_ms": round(1e3 * statistics.mean(d2h_t), 3)}
     if rank != 0:
         return None
     pts, words = n ** 3, n * n * ((n + 31) // 32)
@@ -986,7 +994,8 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
                    "tuning_ms": tuned["ms"],
                    "l2": f"inputs larger than L2 (values {4 * pts / 1e6:.0f} MB > 129 MB L2)"},
         "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gcells/s",
-                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 4 * pts, "d2h_bytes_per_step": 12 * (nv + nf)},
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 4 * pts, "d2h_bytes_per_step": 12 * (nv + nf),
+                **e2e_split},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
                      "algorithmic_bytes": kbytes[top], "kernel_ms": round(kstep[top], 4),
