@@ -156,9 +156,9 @@ int iso_dc_intersect_solve(const float *values, int nx, int ny, int nz, const fl
  * faces [F, 3] as the step-by-step entry points give them (bit for bit).
  *   vertex_capacity bounds the active cells A (one dual vertex each, V <= A);
  *   face_capacity the faces F = 2 Q (two per quad).
- *   counts: device int64[5] <- (V, F, A, K, Q).  When A or F exceed the
- *   capacities the status is 6 (ISO_ERR_OVERFLOW), nothing is written to the
- *   outputs, and counts[2..4] give the sizes for a retry.
+ *   counts: device int64[5] <- (V, F, A, K, Q), K the crossings.  When A or F
+ *   exceed the capacities the status is 6 (ISO_ERR_OVERFLOW), no vertex or face
+ *   is written, and counts[2..4] give the sizes for a retry.
  *   workspace: iso_dc_dense_workspace_size bytes.  Capturable in a CUDA graph. */
 size_t iso_dc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
                                    long long face_capacity);
