@@ -1124,12 +1124,12 @@ void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uin
 // close to an endpoint only if t * h <= 2^-22 * max|coord| (h the spacing);
 // tau = 2^-20 * (1 + max|coord| / h) keeps a factor of 4 on that, and the same
 // holds for 1 - t.
-float snap_tau(const McParams& p) {
-    const int n[3] = {p.nx, p.ny, p.nz};
+float snap_tau_box(int nx, int ny, int nz, const float* amin_, const float* asize) {
+    const int n[3] = {nx, ny, nz};
     double r = 0;
     for (int k = 0; k < 3; ++k) {
-        const double amin = p.amin[k], amax = double(p.amin[k]) + double(p.asize[k]);
-        const double size = p.asize[k];
+        const double amin = amin_[k], amax = double(amin_[k]) + double(asize[k]);
+        const double size = asize[k];
         const double m = std::max(std::fabs(amin), std::fabs(amax));
         if (size == 0.0 || !std::isfinite(size)) return 1.0f;
         r = std::max(r, m * double(std::max(n[k] - 1, 1)) / std::fabs(size));
@@ -1137,6 +1137,8 @@ float snap_tau(const McParams& p) {
     const double tau = std::ldexp(1.0, -20) * (1.0 + r);
     return tau >= 0.5 ? 1.0f : float(tau);
 }
+
+float snap_tau(const McParams& p) { return snap_tau_box(p.nx, p.ny, p.nz, p.amin, p.asize); }
 
 size_t mc_workspace_bytes(int nx, int ny, int nz, long long capV, long long capF) {
     return carve(nx, ny, nz, capV, capF, nullptr).total;

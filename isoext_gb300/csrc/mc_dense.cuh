@@ -46,3 +46,8 @@ int mc_launch(const McParams& p, void* workspace, size_t ws_bytes, cudaStream_t 
 // counters), or nullptr / 0.
 void mc_signs_launch(const float* vals, int nx, int ny, int nz, float level, uint32_t* out,
                      cudaStream_t st, unsigned long long* zero = nullptr, long long nzero = 0);
+
+// Bound on an edge parameter t within which a vertex can land on an endpoint's
+// position (and so meet another edge's vertex): tau = 2^-20 (1 + max|coord| / h),
+// 1 when the grid is too fine for FP32.  asize = aabb_max - aabb_min.
+float snap_tau_box(int nx, int ny, int nz, const float* amin, const float* asize);

@@ -20,6 +20,7 @@
 #include "common.cuh"
 #define ISO_LUT_DECL static __constant__ const
 #include "luts.h"
+#include "mc_dense.cuh"
 #include "profile.cuh"
 
 namespace {
@@ -31,6 +32,7 @@ struct SpGrid {
     float amin[3], asize[3];
     float level;
     int method;
+    float tau;  // edge parameters within tau of 0 or 1 may put two vertices on one position
 };
 
 __device__ __forceinline__ void cell_xyz(const SpGrid& g, uint32_t id, int& x, int& y, int& z) {
@@ -161,6 +163,22 @@ __device__ __forceinline__ void block_scan1(uint32_t a, uint32_t& ea, uint32_t& 
     __syncthreads();
 }
 
+// Faces of a crossed cell when no two of its vertices can share a position: all
+// its crossed edges have t within [tau, 1 - tau], so no vertex comes within
+// rounding of a corner (two edges' vertices can only meet there) and none of
+// the case's triangles is degenerate.  Otherwise ~0u (count by positions).
+__device__ __forceinline__ uint32_t mc_cell_fast(const SpGrid& g, const Cell8& cc, uint32_t cs) {
+    bool near = false;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+        const int a = iso_edge_corner(2 * e), b = iso_edge_corner(2 * e + 1);
+        if ((((cs >> a) ^ (cs >> b)) & 1u) == 0u) continue;  // not crossed
+        const float t = iso::cross_t(g.level, cc.v[a], cc.v[b]);
+        near |= !(t >= g.tau && t <= 1.0f - g.tau);
+    }
+    return near ? ~0u : uint32_t(ISO_NTRI[g.method * 256 + cs]);
+}
+
 __global__ void __launch_bounds__(SP_BLOCK) sp_mc_count(SpGrid g, const int* __restrict__ ids,
                                                         const float* __restrict__ vals, long long n,
                                                         unsigned long long* blk) {
@@ -169,10 +187,19 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_count(SpGrid g, const int* __r
     uint32_t nf = 0;
     if (c < n) {
         Cell8 cc;
-        const uint32_t cs = load_active(g, ids, vals, c, cc);
+        load_vals(vals, c, cc);
+        uint32_t cs = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cs |= (iso::below(cc.v[k], g.level) ? 1u : 0u) << k;
         if (cs != 0 && cs != 255) {
-            float ev[12][3];
-            nf = mc_cell(g, cc, ev);
+            nf = mc_cell_fast(g, cc, cs);
+            if (nf == ~0u) {  // a vertex near a corner: compare positions, as the emit pass does
+                int x, y, z;
+                cell_xyz(g, uint32_t(ids[c]), x, y, z);
+                set_coords(g, x, y, z, cc);
+                float ev[12][3];
+                nf = mc_cell(g, cc, ev);
+            }
         }
     }
     uint32_t e, t;
@@ -191,9 +218,22 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __re
     Cell8 cc;
     float ev[12][3];
     uint32_t cs = 0;
+    bool fast = false;
     if (c < n) {
         cs = load_active(g, ids, vals, c, cc);
-        if (cs != 0 && cs != 255) nf = mc_cell(g, cc, ev);
+        if (cs != 0 && cs != 255) {
+            // the count pass's decision: far from corners every triangle of the case
+            nf = mc_cell_fast(g, cc, cs);
+            fast = nf != ~0u;
+            if (fast) {
+                const uint32_t est = ISO_EDGE_STATUS[cs];
+#pragma unroll
+                for (int q = 0; q < 12; ++q)
+                    if ((est >> q) & 1u) edge_point(cc, q, g.level, ev[q]);
+            } else {
+                nf = mc_cell(g, cc, ev);
+            }
+        }
     }
     uint32_t e, t;
     block_scan1(nf, e, t, sm);
@@ -205,7 +245,7 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __re
         const float* a = ev[tr[k]];
         const float* b = ev[tr[k + 1]];
         const float* cpos = ev[tr[k + 2]];
-        if (eq3(a, b) || eq3(a, cpos) || eq3(b, cpos)) continue;
+        if (!fast && (eq3(a, b) || eq3(a, cpos) || eq3(b, cpos))) continue;
         float* o = soup + 9 * f;
         o[0] = a[0]; o[1] = a[1]; o[2] = a[2];
         o[3] = b[0]; o[4] = b[1]; o[5] = b[2];
@@ -517,6 +557,7 @@ SpGrid mk(int nx, int ny, int nz, const float* amin, const float* amax, float le
     for (int k = 0; k < 3; ++k) { g.amin[k] = amin[k]; g.asize[k] = amax[k] - amin[k]; }
     g.level = level;
     g.method = method;
+    g.tau = snap_tau_box(nx, ny, nz, g.amin, g.asize);
     return g;
 }
 unsigned nb(long long n, int b) { return unsigned(std::max<long long>(1, (n + b - 1) / b)); }
