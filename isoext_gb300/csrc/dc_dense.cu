@@ -584,16 +584,24 @@ __global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint3
     if (i < n) used[tri ? tri[i] : int32_t(i)] = 1u;  // tri == nullptr: triangle i is point i
 }
 
-// Insert used vertices; a slot keeps the smallest index with its position.
+// Probes before an insert gives up (the table is at most half full when the
+// caller's capacity holds the distinct positions; past it the status says
+// overflow and the counts give a size that fits).  Once the status says
+// overflow, later threads skip their probes: the call's output is discarded.
+constexpr uint32_t HASH_PROBES = 512;
+
+// Insert used vertices (used == nullptr: all); a slot keeps the smallest index
+// with its position.
 __global__ void dc_hash_insert(const float* __restrict__ dual, const uint32_t* __restrict__ used,
                                long long A, uint32_t* table, uint32_t mask, int* status,
                                const long long* __restrict__ dn) {
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) A = dn[0];
-    if (a >= A || !used[a]) return;
+    if (a >= A || (used && !used[a])) return;
+    if (status && *(volatile int*)status == int(ISO_ERR_OVERFLOW)) return;
     const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
     uint32_t h = pos_hash(k0, k1, k2) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+    for (uint32_t probe = 0; probe <= mask && probe < HASH_PROBES; ++probe, h = (h + 1) & mask) {
         const uint32_t cur = atomicCAS(&table[h], 0xffffffffu, uint32_t(a));
         if (cur == 0xffffffffu) return;
         const uint32_t j = cur;
@@ -603,7 +611,7 @@ __global__ void dc_hash_insert(const float* __restrict__ dual, const uint32_t* _
             return;
         }
     }
-    atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+    if (status) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
 }
 
 // rep[a] = smallest index with the same position (for used vertices).
@@ -613,10 +621,10 @@ __global__ void dc_hash_lookup(const float* __restrict__ dual, const uint32_t* _
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) A = dn[0];
     if (a >= A) return;
-    if (!used[a]) { rep[a] = 0xffffffffu; return; }
+    if (used && !used[a]) { rep[a] = 0xffffffffu; return; }
     const uint32_t k0 = pos_bits(dual[3 * a]), k1 = pos_bits(dual[3 * a + 1]), k2 = pos_bits(dual[3 * a + 2]);
     uint32_t h = pos_hash(k0, k1, k2) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+    for (uint32_t probe = 0; probe <= mask && probe < HASH_PROBES; ++probe, h = (h + 1) & mask) {
         const uint32_t j = table[h];
         if (j == 0xffffffffu) break;
         if (pos_bits(dual[3ll * j]) == k0 && pos_bits(dual[3ll * j + 1]) == k1 &&
@@ -1268,17 +1276,18 @@ __global__ void __launch_bounds__(256) dc_cell_quads(const uint8_t* __restrict__
 // capacities capA / capT.
 
 struct WeldDev {
-    uint32_t *used, *rep, *newidx, *table;
+    uint32_t *rep, *newidx, *table;
     unsigned long long* blk;
     uint32_t hcap;
     long long nblk;
     size_t total;
 };
 
-WeldDev weld_dev_carve(void* ws, long long capA) {
+WeldDev weld_dev_carve(void* ws, long long capA, long long capU) {
     WeldDev w{};
+    const long long u = capU > 0 && capU < capA ? capU : capA;  // distinct positions the table must hold
     w.hcap = 1024;
-    while ((long long)w.hcap < 2 * capA + 1024) w.hcap <<= 1;
+    while ((long long)w.hcap < 2 * u + 1024) w.hcap <<= 1;
     w.nblk = (capA + DC_BLOCK - 1) / DC_BLOCK;
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     size_t o = 0;
@@ -1287,7 +1296,6 @@ WeldDev weld_dev_carve(void* ws, long long capA) {
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.used = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.rep = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
     w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
@@ -1296,19 +1304,17 @@ WeldDev weld_dev_carve(void* ws, long long capA) {
     return w;
 }
 
-size_t weld_dev_workspace(long long capA) { return weld_dev_carve(nullptr, capA).total; }
+size_t weld_dev_workspace(long long capA, long long capU) { return weld_dev_carve(nullptr, capA, capU).total; }
 
-void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
-                     void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
-                     uint32_t* vsrc) {
-    const WeldDev w = weld_dev_carve(ws, capA);
-    iso::ProfScope ps("dc_weld", st, (capT > 0 ? 2 : 0) + (capA > 0 ? 5 : 0));
-    cudaMemsetAsync(w.used, 0, size_t(capA) * 4, st);
+void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
+                     const long long* eff, void* ws, float* vout, int32_t* fout, long long* vtot, int* status,
+                     cudaStream_t st, uint32_t* vsrc) {
+    const WeldDev w = weld_dev_carve(ws, capA, capU);
+    iso::ProfScope ps("dc_weld", st, (capT > 0 ? 1 : 0) + (capA > 0 ? 5 : 0));
     cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
-    if (capT > 0) dc_mark_used<<<blocks_for(capT, 256), 256, 0, st>>>(tri, capT, w.used, eff);
-    if (capA > 0) {
-        dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(pts, w.used, capA, w.table, w.hcap - 1, status, eff);
-        dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(pts, w.used, capA, w.table, w.hcap - 1, w.rep, eff);
+    if (capA > 0) {  // every point is used: a point list or a triangle soup
+        dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(pts, nullptr, capA, w.table, w.hcap - 1, status, eff);
+        dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(pts, nullptr, capA, w.table, w.hcap - 1, w.rep, eff);
         dc_rep_count<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, eff);
         dc_block_scan<<<1, 1024, 0, st>>>(w.blk, w.nblk, vtot);
         dc_rep_write<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, pts, w.newidx, vout, vsrc, eff);

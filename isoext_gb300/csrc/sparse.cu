@@ -567,8 +567,9 @@ unsigned nb(long long n, int b) { return unsigned(std::max<long long>(1, (n + b 
 // dc_block_scan lives in dc_dense.cu
 void iso_block_scan_launch(unsigned long long* blk, long long nblk, long long* totals, cudaStream_t st);
 // dc_dense.cu: exact-position weld with device-side sizes
-size_t weld_dev_workspace(long long capA);
-void weld_dev_launch(const float* pts, long long capA, const int32_t* tri, long long capT, const long long* eff,
+size_t weld_dev_workspace(long long capA, long long capU);
+void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
+                     const long long* eff,
                      void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
                      uint32_t* vsrc);
 
@@ -603,7 +604,7 @@ struct SpMcWs {
     size_t total;
 };
 
-SpMcWs sp_mc_carve(void* ws, long long n, long long capF) {
+SpMcWs sp_mc_carve(void* ws, long long n, long long capV, long long capF) {
     SpMcWs w{};
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     size_t o = 0;
@@ -615,7 +616,7 @@ SpMcWs sp_mc_carve(void* ws, long long n, long long capF) {
     w.blk = take(size_t((n + SP_BLOCK - 1) / SP_BLOCK + 1) * 16);
     w.tot = reinterpret_cast<long long*>(take(16 * 8));
     w.soup = reinterpret_cast<float*>(take(size_t(3 * capF) * 12));
-    w.weld = take(weld_dev_workspace(3 * capF));
+    w.weld = take(weld_dev_workspace(3 * capF, capV));
     w.total = o + 256;
     return w;
 }
@@ -751,7 +752,7 @@ int iso_sparse_filter_write(const int* ids, const float* vals, long long m, floa
 // when F > face_capacity or V > vertex_capacity, and a retry sizes from counts.
 size_t iso_sparse_mc_workspace_size(long long n, long long vertex_capacity, long long face_capacity) {
     if (n < 0 || vertex_capacity < 0 || face_capacity < 0) return 0;
-    return sp_mc_carve(nullptr, n, face_capacity).total;
+    return sp_mc_carve(nullptr, n, vertex_capacity, face_capacity).total;
 }
 
 int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny, int nz, const float* amin,
@@ -764,7 +765,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     if (n == 0) return cudaMemsetAsync(counts, 0, 24, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
     if (!ids || !vals || (vertex_capacity && !vertices) || (face_capacity && !faces)) return ISO_ERR_ARG;
     if (workspace_bytes < iso_sparse_mc_workspace_size(n, vertex_capacity, face_capacity)) return ISO_ERR_WORKSPACE;
-    const SpMcWs w = sp_mc_carve(workspace, n, face_capacity);
+    const SpMcWs w = sp_mc_carve(workspace, n, vertex_capacity, face_capacity);
     const SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     long long* eff = w.tot + 4;
     {
@@ -775,8 +776,10 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
         sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.soup,
                                                          eff);
     }
-    weld_dev_launch(w.soup, 3 * face_capacity, nullptr, 3 * face_capacity, eff, w.weld, vertices, faces, w.tot + 8,
-                    status, st, nullptr);
+    // the weld's table holds vertex_capacity distinct positions; more report an
+    // overflow with a vertex count that fits on the rerun
+    weld_dev_launch(w.soup, 3 * face_capacity, std::max<long long>(vertex_capacity, 1), nullptr, 3 * face_capacity,
+                    eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr);
     {
         iso::ProfScope ps("sparse_mc", st);
         sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
