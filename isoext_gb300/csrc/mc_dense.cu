@@ -267,9 +267,9 @@ __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea
 }
 
 // ---------------------------------------------------------------------------
-// 2. count: persistent CTAs take segments of SEG point words in ticket order;
-// each segment's (V, F) prefix comes from a decoupled look-back over the
-// segments before it, so no separate scan pass is needed.
+// 2. count: one CTA per segment of SEG point words: per-word vertex entries,
+// per-cell entries, and the segment's (V, F) sums, which mc_scan turns into
+// offsets.
 
 // Segment holding point word pw.
 __device__ __forceinline__ uint32_t seg_of(uint32_t pw) { return pw / SEG; }
