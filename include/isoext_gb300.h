@@ -290,6 +290,14 @@ int iso_dc_backward(const float *values, int nx, int ny, int nz, const float *aa
                     const float *aabb_max, float level, const int *cell_ids, const int *cell_offsets,
                     long long A, float reg, float svd_tol, const float *normals, const float *grad_dual,
                     float *grad_values, float *grad_normals, void *stream);
+/* iso_dc_backward from the gradient of the welded vertices: vertex i came from
+ * active cell vertex_source[i] (iso_dc_dense_ex), grad_vertices [V, 3];
+ * grad_dual_ws is a device scratch of A * 3 floats.  grad_values is zeroed
+ * first, then written (not accumulated). */
+int iso_dc_backward_src(const float *values, int nx, int ny, int nz, const float *aabb_min,
+                        const float *aabb_max, float level, const int *cell_ids, const int *cell_offsets,
+                        long long A, float reg, float svd_tol, const int *vertex_source, long long V,
+                        const float *grad_vertices, float *grad_dual_ws, float *grad_values, void *stream);
 
 /* ------------------------------------------------------------------------- */
 /* Grid values of a union of spheres and boxes, for the served request stream

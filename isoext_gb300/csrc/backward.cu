@@ -241,6 +241,18 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
     }
 }
 
+// grad_dual[src[i]] = grad_vertices[i]: each dual vertex is the source of at
+// most one welded vertex.
+__global__ void dc_scatter_src(const int* __restrict__ src, long long V, const float* __restrict__ gv,
+                               float* __restrict__ gdual) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const long long a = src[i];
+    gdual[3 * a] = gv[3 * i];
+    gdual[3 * a + 1] = gv[3 * i + 1];
+    gdual[3 * a + 2] = gv[3 * i + 2];
+}
+
 }  // namespace
 
 extern "C" {
@@ -272,6 +284,24 @@ int iso_dc_backward(const float* values, int nx, int ny, int nz, const float* aa
                                                     reinterpret_cast<const uint32_t*>(cell_offsets), A, reg,
                                                     svd_tol, normals, grad_dual, grad_values, grad_normals);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+}
+
+int iso_dc_backward_src(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
+                        float level, const int* cell_ids, const int* cell_offsets, long long A, float reg,
+                        float svd_tol, const int* vertex_source, long long V, const float* grad_vertices,
+                        float* grad_dual_ws, float* grad_values, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (A < 0 || V < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max || !grad_values) return ISO_ERR_ARG;
+    if (cudaMemsetAsync(grad_values, 0, size_t(nx) * ny * nz * sizeof(float), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (A == 0 || V == 0) return 0;
+    if (!values || !cell_ids || !cell_offsets || !vertex_source || !grad_vertices || !grad_dual_ws) return ISO_ERR_ARG;
+    if (cudaMemsetAsync(grad_dual_ws, 0, size_t(A) * 3 * sizeof(float), st) != cudaSuccess) return ISO_ERR_CUDA;
+    {
+        iso::ProfScope ps("dc_backward", st);
+        dc_scatter_src<<<blocks_for(V, 256), 256, 0, st>>>(vertex_source, V, grad_vertices, grad_dual_ws);
+    }
+    return iso_dc_backward(values, nx, ny, nz, aabb_min, aabb_max, level, cell_ids, cell_offsets, A, reg, svd_tol,
+                           nullptr, grad_dual_ws, grad_values, nullptr, stream);
 }
 
 }  // extern "C"

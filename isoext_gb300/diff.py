@@ -40,6 +40,8 @@ _ffi.register({
                             _vp], _i),
     "iso_mc_backward": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _ll, _vp, _vp, _vp], _i),
     "iso_dc_backward": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _vp, _ll, _f, _f, _vp, _vp, _vp, _vp, _vp], _i),
+    "iso_dc_backward_src": ([_vp, _i, _i, _i, _fa, _fa, _f, _vp, _vp, _ll, _f, _f, _vp, _ll, _vp, _vp, _vp, _vp],
+                            _i),
 })
 
 # Output sizes seen per (shape, box, level, method), for sizing the next call.
@@ -69,8 +71,9 @@ class _Launch:
 # ---------------------------------------------------------------------------
 # marching cubes
 
-def _mc_launch(values: torch.Tensor, amin, amax, level: float, method: int, caps=None) -> _Launch:
-    """Queues iso_mc_dense_edges on the current stream (no synchronisation)."""
+def _mc_launch(values: torch.Tensor, amin, amax, level: float, method: int, caps=None, small=None) -> _Launch:
+    """Queues iso_mc_dense_edges on the current stream (no synchronisation).
+    small: a zeroed int64[8] device tensor for the sizes (one is made if None)."""
     lib = _ffi.lib()
     dev = values.device
     shape = tuple(values.shape)
@@ -87,7 +90,7 @@ def _mc_launch(values: torch.Tensor, amin, amax, level: float, method: int, caps
                 fout=torch.empty((cap_f, 3), dtype=torch.int32, device=dev),
                 edges=torch.empty(cap_v, dtype=torch.int64, device=dev),
                 ws=torch.empty(workspace_bytes(shape, cap_v, cap_f), dtype=torch.uint8, device=dev),
-                small=torch.zeros(8, dtype=torch.int64, device=dev))
+                small=small if small is not None else torch.zeros(8, dtype=torch.int64, device=dev))
     _ffi.check(lib.iso_mc_dense_edges(_p(values), *shape, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level),
                                       int(method), _p(L.vout), cap_v, _p(L.fout), cap_f, _p(L.ws), L.ws.numel(),
                                       _p(L.small), C.c_void_p(L.small.data_ptr() + 16), _p(L.edges), _stream(dev)))
@@ -125,6 +128,15 @@ def _weld_positions(v, f, e):
     used[f2.reshape(-1)] = True
     remap = torch.cumsum(used.to(torch.int64), 0) - 1
     return uniq[used].view(torch.float32), remap[f2].to(torch.int32), e[first[used]]
+
+
+def _smalls(values_list):
+    """A zeroed int64 [8] size record per extraction: rows of one tensor when the
+    grids share a device."""
+    devs = {x.device for x in values_list}
+    if len(devs) == 1:
+        return list(torch.zeros((len(values_list), 8), dtype=torch.int64, device=devs.pop()).unbind(0))
+    return [torch.zeros(8, dtype=torch.int64, device=x.device) for x in values_list]
 
 
 def _collect(launches, relaunch):
@@ -196,15 +208,19 @@ def marching_cubes_batch(values_list, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.0
     amin, amax, mid = _vec3(aabb_min), _vec3(aabb_max), method_id(method)
     for x in values_list:
         _check_cuda_f32(x, ndim=3)
-    res = _collect([_mc_launch(x.detach(), amin, amax, float(level), mid) for x in values_list], _mc_relaunch)
+    smalls = _smalls(values_list)  # the sizes of all the batch's extractions, zeroed at once
+    res = _collect([_mc_launch(x.detach(), amin, amax, float(level), mid, small=smalls[i])
+                    for i, x in enumerate(values_list)], _mc_relaunch)
     return [_MarchingCubes.apply(x, r, (amin, amax, float(level))) for x, r in zip(values_list, res)]
 
 
 # ---------------------------------------------------------------------------
 # dual contouring
 
-def _dc_launch(values: torch.Tensor, amin, amax, level: float, reg: float, svd_tol: float, caps=None) -> _Launch:
-    """Queues iso_dc_dense_ex on the current stream (no synchronisation)."""
+def _dc_launch(values: torch.Tensor, amin, amax, level: float, reg: float, svd_tol: float, caps=None,
+               small=None) -> _Launch:
+    """Queues iso_dc_dense_ex on the current stream (no synchronisation).
+    small: a zeroed int64[8] device tensor for the sizes (one is made if None)."""
     from . import dc
 
     lib = _ffi.lib()
@@ -225,7 +241,7 @@ def _dc_launch(values: torch.Tensor, amin, amax, level: float, reg: float, svd_t
                 offs=torch.empty(cap_v + 1, dtype=torch.int32, device=dev),
                 src=torch.empty(cap_v, dtype=torch.int32, device=dev),
                 ws=torch.empty(dc.dc_workspace_bytes(shape, cap_v, cap_f), dtype=torch.uint8, device=dev),
-                small=torch.zeros(8, dtype=torch.int64, device=dev))
+                small=small if small is not None else torch.zeros(8, dtype=torch.int64, device=dev))
     _ffi.check(lib.iso_dc_dense_ex(_p(values), *shape, _ffi.fvec3(amin), _ffi.fvec3(amax), float(level), float(reg),
                                    float(svd_tol), _p(L.vout), cap_v, _p(L.fout), cap_f, _p(L.ws), L.ws.numel(),
                                    _p(L.small), C.c_void_p(L.small.data_ptr() + 48), _p(L.cells), _p(L.offs),
@@ -273,16 +289,18 @@ class _DualContouring(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gv, gf):
         values, cells, offs, src = ctx.saved_tensors
-        grad = torch.zeros_like(values)
         if gv is None or cells is None or src.numel() == 0:
-            return grad, None, None
+            return torch.zeros_like(values), None, None
         amin, amax, level, reg, svd_tol = ctx.meta
         A = cells.numel()
-        gdual = torch.zeros((A, 3), dtype=torch.float32, device=values.device)
-        gdual[src.long()] = gv.to(torch.float32)  # each dual vertex is the source of at most one vertex
-        _ffi.check(_ffi.lib().iso_dc_backward(_p(values), *values.shape, _ffi.fvec3(amin), _ffi.fvec3(amax), level,
-                                              _p(cells), _p(offs), A, reg, svd_tol, None, _p(gdual), _p(grad), None,
-                                              _stream(values.device)))
+        grad = torch.empty_like(values)  # zeroed by the call
+        gdual = torch.empty((A, 3), dtype=torch.float32, device=values.device)
+        gvc = gv.to(torch.float32).contiguous()
+        # each dual vertex is the source of at most one vertex: the call scatters
+        # grad_vertices to their source cells, then differentiates the solve
+        _ffi.check(_ffi.lib().iso_dc_backward_src(_p(values), *values.shape, _ffi.fvec3(amin), _ffi.fvec3(amax),
+                                                  level, _p(cells), _p(offs), A, reg, svd_tol, _p(src), src.numel(),
+                                                  _p(gvc), _p(gdual), _p(grad), _stream(values.device)))
         return grad, None, None
 
 
@@ -303,7 +321,9 @@ def dual_contouring_batch(values_list, aabb_min=(-1.0, -1.0, -1.0), aabb_max=(1.
     amin, amax = _vec3(aabb_min), _vec3(aabb_max)
     for x in values_list:
         _check_cuda_f32(x, ndim=3)
-    res = _collect([_dc_launch(x.detach(), amin, amax, float(level), float(reg), float(svd_tol)) for x in values_list],
+    smalls = _smalls(values_list)  # the sizes of all the batch's extractions, zeroed at once
+    res = _collect([_dc_launch(x.detach(), amin, amax, float(level), float(reg), float(svd_tol), small=smalls[i])
+                    for i, x in enumerate(values_list)],
                    _dc_relaunch)
     meta = (amin, amax, float(level), float(reg), float(svd_tol))
     return [_DualContouring.apply(x, r, meta) for x, r in zip(values_list, res)]
