@@ -47,6 +47,25 @@ const char *iso_last_error(void);
 /* ABI version of this library (2). */
 int iso_abi_version(void);
 
+/* Which reading of isoext's FP32 expressions the kernels compute, process-wide
+ * (read at each launch).  No counterpart in the reference, which has one per
+ * build:
+ *   1 (default) -- its CUDA build: nvcc's default FMA contraction of its source
+ *                  (grid positions, lerp, the normal stencil, norms), so
+ *                  vertices, intersection points and normals equal that
+ *                  build's, bit for bit.
+ *   0           -- its host build: every operation rounded on its own.
+ * Returns ISO_ERR_ARG for other values. */
+int iso_set_arith(int mode);
+int iso_get_arith(void);
+
+/* Coordinates of the n points of one grid axis, amin + (i / (float)(n - 1)) *
+ * (amax - amin), in the current reading: out is DEVICE float [n].  Replaces
+ * the position arithmetic behind UniformGrid.get_points (src/isoext_ext.cu:
+ * 149-156 -> src/grid/uniform.cu get_points -> include/utils.cuh:62-80,
+ * get_vtx_pos_op); the grid of points is their outer product. */
+int iso_axis_coords(float *out, int n, float amin, float amax, void *stream);
+
 /* Threads per CTA of iso_mc_dense's emit kernel (128 or 256; default 256).
  * Process-wide; the autotuner sets it.  No counterpart in the reference (it
  * has no tunables). */
@@ -113,11 +132,14 @@ int iso_mc_dense(const float *values, int nx, int ny, int nz, const float *aabb_
  *   - A grid plus capacities whose iso_mc_dense_workspace_size exceeds the
  *     limit -> ISO_ERR_WORKSPACE with a message; nothing is queued. 256^3 with
  *     capacities near its mesh size fits.
- *   - The first call on a device does set-up: it looks up the array's address
- *     with that device current. Make it before any stream capture.
- *   - All calls on one device share the array. Calls not ordered on the device
- *     (different streams or threads without events) race. Each call clears,
- *     on its stream, what must start at zero. */
+ *   - Each call looks up the array's address in the CUDA context current on
+ *     the calling thread (a context made after cudaDeviceReset, or the
+ *     caller's own driver context, has its own copy). The first call in a
+ *     context can load the module that holds the array: make it before any
+ *     stream capture.
+ *   - All calls in one context share the array. Calls not ordered on the
+ *     device (different streams or threads without events) race. Each call
+ *     clears, on its stream, what must start at zero. */
 #define ISO_MC_NOALLOC_SCRATCH_BYTES (32u << 20)
 int iso_mc_dense_noalloc(const float *values, int nx, int ny, int nz, const float *aabb_min,
                          const float *aabb_max, float level, int method, float *vertices,

@@ -10,10 +10,14 @@
     sparse.set_values(sdf(sparse.get_points()))   # [N, 8]
     v, f = isoext.dual_contouring(sparse)
 
+``set_arithmetic("nvcc" | "host")`` picks which of isoext's two builds the
+FP32 results equal bit for bit: its CUDA build (default) or its host build.
+
 The extraction functions run hand-written sm_103a kernels through the C ABI of
 ``_lib/libisoext_gb300.so`` (include/isoext_gb300.h); there is no CPU fallback.
 """
 
+from ._ffi import get_arithmetic, set_arithmetic
 from .dc import Intersection, dual_contouring, get_intersection
 from .grids import FLT_MAX, Grid, UniformGrid
 from .mc import marching_cubes
@@ -28,8 +32,10 @@ __all__ = [
     "UniformGrid",
     "dual_contouring",
     "gaussian_smooth",
+    "get_arithmetic",
     "get_intersection",
     "make_grid",
     "marching_cubes",
+    "set_arithmetic",
     "write_obj",
 ]

@@ -44,6 +44,9 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_mc_dense_workspace_size.restype = C.c_size_t
     lib.iso_mc_dense.argtypes = [_vp, _i, _i, _i, _fa, _fa, _f, _i, _vp, _ll, _vp, _ll, _vp,
                                  C.c_size_t, _vp, _vp, _vp]
+    lib.iso_set_arith.argtypes = [_i]
+    lib.iso_get_arith.restype = _i
+    lib.iso_axis_coords.argtypes = [_vp, _i, _f, _f, _vp]
     _apply(lib, _EXTRA)
 
 
@@ -92,6 +95,28 @@ def check(rc: int) -> None:
     if rc == ISO_ERR_ARG:
         raise RuntimeError(msg)
     raise RuntimeError(f"isoext_gb300 error {rc}: {msg}")
+
+
+ARITH = {"host": 0, "nvcc": 1}
+
+
+def set_arithmetic(mode: str) -> None:
+    """Which reading of isoext's FP32 expressions the kernels compute (process-wide).
+
+    ``"nvcc"`` (default): the arithmetic of isoext's CUDA build, whose compiler
+    fuses multiply-adds in its grid positions, lerps, normal stencil and norms;
+    vertices, intersection points and normals equal that build's bit for bit.
+    ``"host"``: every operation rounded on its own, as isoext's host build (and
+    the reference's source read literally) computes.  No counterpart in isoext,
+    which has one arithmetic per build."""
+    if mode not in ARITH:
+        raise ValueError(f"arithmetic must be one of {sorted(ARITH)}, not {mode!r}")
+    check(lib().iso_set_arith(ARITH[mode]))
+
+
+def get_arithmetic() -> str:
+    m = lib().iso_get_arith()
+    return next(k for k, v in ARITH.items() if v == m)
 
 
 def fvec3(xs) -> C.Array:

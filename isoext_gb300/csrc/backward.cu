@@ -89,8 +89,9 @@ __device__ __forceinline__ void normal_backward(const CellCorners& cc, const flo
         tm[a] = fmaxf(__fsub_rn(t[a], eps), 0.01f);
         sp[a] = __fadd_rn(t[a], eps) < 0.99f ? 1.0f : 0.0f;
         sm[a] = __fsub_rn(t[a], eps) > 0.01f ? 1.0f : 0.0f;
-        fp[a] = trilin(cc.v, tp[0], tp[1], tp[2]);
-        fm[a] = trilin(cc.v, tm[0], tm[1], tm[2]);
+        // the adjoint needs the stencil's values only to first order
+        fp[a] = iso::trilin_t<false, false>(cc.v, tp[0], tp[1], tp[2]);
+        fm[a] = iso::trilin_t<false, false>(cc.v, tm[0], tm[1], tm[2]);
         den[a] = __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]);
         d[a] = __fdiv_rn(__fsub_rn(fp[a], fm[a]), den[a]);
     }
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(128) dc_backward(const float* __restrict__ val
     const uint32_t k0 = cell_off[a];
     // the forward again: the QEF of the crossings in edge order
     Qef Q;
-    qef_init(Q);
+    qef_init(Q, g.fma);
     uint32_t K = 0;
 #pragma unroll 1
     for (uint32_t em = est; em; em &= em - 1, ++K) {

@@ -34,13 +34,42 @@ void set_last_error(const char* msg) { g_err = msg; }
 // the per-active-cell DC kernels.
 std::atomic<int> g_tune[TUNE_KEYS] = {{32}, {128}};
 int tune_get(int key) { return key >= 0 && key < TUNE_KEYS ? g_tune[key].load(std::memory_order_relaxed) : 0; }
+
+// Arithmetic reading of the reference's expressions (common.cuh): 1 = its CUDA
+// build's fused multiply-adds (the default), 0 = its host build.
+std::atomic<int> g_arith{1};
+bool arith_fma() { return g_arith.load(std::memory_order_relaxed) != 0; }
 }  // namespace iso
+
+namespace {
+// Coordinates of the n points of one grid axis (include/utils.cuh:62-80).
+__global__ void axis_coords_kernel(float* out, int n, float amin, float size, bool fma) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = iso::grid_coord(uint32_t(i), uint32_t(n), amin, size, fma);
+}
+}  // namespace
 
 extern "C" {
 
 const char* iso_last_error(void) { return g_err.c_str(); }
 
 int iso_abi_version(void) { return 2; }
+
+int iso_set_arith(int mode) {
+    if (mode != 0 && mode != 1) return fail(ISO_ERR_ARG, "iso_set_arith: mode must be 0 (host build) or 1 (CUDA build)");
+    iso::g_arith.store(mode, std::memory_order_relaxed);
+    return ISO_OK;
+}
+
+int iso_get_arith(void) { return iso::g_arith.load(std::memory_order_relaxed); }
+
+int iso_axis_coords(float* out, int n, float amin, float amax, void* stream) {
+    if (n < 0 || (n > 0 && !out)) return fail(ISO_ERR_ARG, "iso_axis_coords: bad arguments");
+    if (n == 0) return ISO_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    axis_coords_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(out, n, amin, amax - amin, iso::arith_fma());
+    return cudaGetLastError() == cudaSuccess ? ISO_OK : fail(ISO_ERR_CUDA, "iso_axis_coords: launch failed");
+}
 
 int iso_mc_set_config(int threads) {
     if (mc_set_block(threads)) return fail(ISO_ERR_ARG, "iso_mc_set_config: threads must be 128 or 256");

@@ -22,27 +22,106 @@ enum IsoStatus : int {
 namespace iso {
 
 // ---------------------------------------------------------------------------
-// Exact FP32 arithmetic.  Every operation is rounded on its own (no FMA
-// contraction): this is the reference's source read literally, and what its
-// host build computes.
+// The reference's FP32 expressions, in two readings selected by `fma`:
+//   true  -- what nvcc's default FMA contraction (-fmad=true) makes of isoext's
+//            source, i.e. the arithmetic of its CUDA build, which is what isoext
+//            users run.  The fused forms below were measured on sm_103a with
+//            nvcc 13.0: a restatement of the source compiled with default flags
+//            gives these bits on every input tried (tests/nvcc_expr.cu).
+//   false -- every operation rounded on its own: the source read literally,
+//            which is what its host build (x86, no FMA) computes.
+// Every other operation is explicitly rounded, so neither reading depends on
+// how this library itself is compiled.
 
 // Grid point coordinate: amin + (i / (float)(n - 1)) * size
-// (include/utils.cuh:62-80, get_vtx_pos_op).
-__device__ __forceinline__ float grid_coord(uint32_t i, uint32_t n, float amin, float size) {
-    float f = __fdiv_rn(__uint2float_rn(i), __uint2float_rn(n - 1u));
-    return __fadd_rn(amin, __fmul_rn(f, size));
+// (include/utils.cuh:62-80, get_vtx_pos_op); nvcc fuses the multiply-add.
+__device__ __forceinline__ float grid_coord(uint32_t i, uint32_t n, float amin, float size, bool fma) {
+    const float f = __fdiv_rn(__uint2float_rn(i), __uint2float_rn(n - 1u));
+    return fma ? __fmaf_rn(f, size, amin) : __fadd_rn(amin, __fmul_rn(f, size));
 }
 
 // Edge crossing parameter t = (level - va) / (vb - va), 0 when vb == va
-// (src/mc/nagae.cu:52-53).
+// (src/mc/nagae.cu:52-53).  Nothing to fuse.
 __device__ __forceinline__ float cross_t(float level, float va, float vb) {
-    float d = __fsub_rn(vb, va);
+    const float d = __fsub_rn(vb, va);
     return d != 0.0f ? __fdiv_rn(__fsub_rn(level, va), d) : 0.0f;
 }
 
+// x * ox + y * oy, the shape of lerp and of each trilinear step.  nvcc fuses
+// the first product (fma(x, ox, y * oy)); `swap` is the other fusion,
+// fma(y, oy, x * ox), which it picks for some steps of the normal stencil.
+__device__ __forceinline__ float blend2(float x, float ox, float y, float oy, bool fma, bool swap = false) {
+    if (!fma) return __fadd_rn(__fmul_rn(x, ox), __fmul_rn(y, oy));
+    return swap ? __fmaf_rn(y, oy, __fmul_rn(x, ox)) : __fmaf_rn(x, ox, __fmul_rn(y, oy));
+}
+
 // lerp(t, a, b) = (1 - t) * a + t * b per component (include/math.cuh:77-81).
-__device__ __forceinline__ float lerp1(float t, float a, float b) {
-    return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, t), a), __fmul_rn(t, b));
+__device__ __forceinline__ float lerp1(float t, float a, float b, bool fma) {
+    return blend2(__fsub_rn(1.0f, t), a, t, b, fma);
+}
+
+// |d| = sqrt(d.x*d.x + d.y*d.y + d.z*d.z) (include/math.cuh, norm and dot);
+// nvcc: sqrt(fma(z, z, fma(x, x, y * y))).
+__device__ __forceinline__ float norm3f(float x, float y, float z, bool fma) {
+    if (!fma) return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+    return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(x, x, __fmul_rn(y, y))));
+}
+
+// Trilinear interpolation of corner values cv (corner j = 4x + 2y + z) at t
+// (src/its.cu:170-184): along z, then y, then x.  kSwapLowZ: the nvcc fusion
+// of the two x = 0 steps along z is the swapped one (see stencil_normal).
+template <bool F, bool kSwapLowZ>
+__device__ __forceinline__ float trilin_t(const float* cv, float tx, float ty, float tz) {
+    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
+    const float c00 = blend2(cv[0], oz, cv[1], tz, F, kSwapLowZ);
+    const float c01 = blend2(cv[2], oz, cv[3], tz, F, kSwapLowZ);
+    const float c10 = blend2(cv[4], oz, cv[5], tz, F);
+    const float c11 = blend2(cv[6], oz, cv[7], tz, F);
+    const float c0 = blend2(c00, oy, c01, ty, F);
+    const float c1 = blend2(c10, oy, c11, ty, F);
+    return blend2(c0, ox, c1, tx, F);
+}
+
+template <bool F>
+__device__ __forceinline__ void stencil_normal_t(const float* v, const float* lo, const float* hi, const float* p,
+                                                 float* n) {
+    float csz[3], t[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        csz[a] = __fsub_rn(hi[a], lo[a]);
+        t[a] = __fdiv_rn(__fsub_rn(p[a], lo[a]), csz[a]);
+        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
+    }
+    const float eps = 0.02f;
+    const float xp = fminf(__fadd_rn(t[0], eps), 0.99f), xm = fmaxf(__fsub_rn(t[0], eps), 0.01f);
+    const float yp = fminf(__fadd_rn(t[1], eps), 0.99f), ym = fmaxf(__fsub_rn(t[1], eps), 0.01f);
+    const float zp = fminf(__fadd_rn(t[2], eps), 0.99f), zm = fmaxf(__fsub_rn(t[2], eps), 0.01f);
+    // the four samples at the crossing's own z share their steps along z; for
+    // those nvcc swaps the fusion of the x = 0 steps
+    const float dx = __fdiv_rn(__fsub_rn(trilin_t<F, true>(v, xp, t[1], t[2]), trilin_t<F, true>(v, xm, t[1], t[2])),
+                               __fmul_rn(__fsub_rn(xp, xm), csz[0]));
+    const float dy = __fdiv_rn(__fsub_rn(trilin_t<F, true>(v, t[0], yp, t[2]), trilin_t<F, true>(v, t[0], ym, t[2])),
+                               __fmul_rn(__fsub_rn(yp, ym), csz[1]));
+    const float dz = __fdiv_rn(__fsub_rn(trilin_t<F, false>(v, t[0], t[1], zp), trilin_t<F, false>(v, t[0], t[1], zm)),
+                               __fmul_rn(__fsub_rn(zp, zm), csz[2]));
+    const float len = norm3f(dx, dy, dz, F);
+    if (len > 1e-8f) {
+        n[0] = __fdiv_rn(dx, len);
+        n[1] = __fdiv_rn(dy, len);
+        n[2] = __fdiv_rn(dz, len);
+    } else {
+        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
+    }
+}
+
+// Normal at crossing point p of the cell with corner values v and corners lo
+// (corner 0) and hi (corner 7): central differences of the trilinear
+// interpolant at +-0.02 cell units, clamped to [0.01, 0.99], normalised
+// (src/its.cu:186-268).
+__device__ __forceinline__ void stencil_normal(const float* v, const float* lo, const float* hi, const float* p,
+                                               float* n, bool fma) {
+    if (fma) stencil_normal_t<true>(v, lo, hi, p, n);
+    else stencil_normal_t<false>(v, lo, hi, p, n);
 }
 
 // Case bit of a corner: (v - level < 0) (include/utils.cuh:96-99).
@@ -89,5 +168,9 @@ cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, unsigned block,
 
 enum TuneKey { TUNE_MC_SIGN_CTAS = 0, TUNE_DC_CELL_THREADS = 1, TUNE_KEYS = 2 };
 int tune_get(int key);
+
+// Arithmetic reading for the next launches (iso_set_arith; process-wide):
+// true = the reference's CUDA build (fused), false = its host build.
+bool arith_fma();
 
 }  // namespace iso

@@ -15,20 +15,23 @@ namespace {
 struct Grid3 {
     int nx, ny, nz;
     float amin[3], asize[3];
+    bool fma;  // arithmetic reading (iso::arith_fma at the call)
 };
 
 __device__ __forceinline__ float coord(const Grid3& g, int axis, uint32_t i) {
     const uint32_t n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-    return iso::grid_coord(i, n, g.amin[axis], g.asize[axis]);
+    return iso::grid_coord(i, n, g.amin[axis], g.asize[axis], g.fma);
 }
 
 struct CellCorners {
     float v[8];
     float p[8][3];
+    bool fma;  // the grid's arithmetic reading
 };
 
 __device__ __forceinline__ void load_cell(const float* vals, const Grid3& g, int cx, int cy, int cz,
                                           CellCorners& cc) {
+    cc.fma = g.fma;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int x = cx + (k >> 2), y = cy + ((k >> 1) & 1), z = cz + (k & 1);
@@ -39,48 +42,9 @@ __device__ __forceinline__ void load_cell(const float* vals, const Grid3& g, int
     }
 }
 
-// Trilinear interpolation at t in [0,1]^3 (src/its.cu:170-184).
-__device__ __forceinline__ float trilin(const float* cv, float tx, float ty, float tz) {
-    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
-    const float c00 = __fadd_rn(__fmul_rn(cv[0], oz), __fmul_rn(cv[1], tz));
-    const float c01 = __fadd_rn(__fmul_rn(cv[2], oz), __fmul_rn(cv[3], tz));
-    const float c10 = __fadd_rn(__fmul_rn(cv[4], oz), __fmul_rn(cv[5], tz));
-    const float c11 = __fadd_rn(__fmul_rn(cv[6], oz), __fmul_rn(cv[7], tz));
-    const float c0 = __fadd_rn(__fmul_rn(c00, oy), __fmul_rn(c01, ty));
-    const float c1 = __fadd_rn(__fmul_rn(c10, oy), __fmul_rn(c11, ty));
-    return __fadd_rn(__fmul_rn(c0, ox), __fmul_rn(c1, tx));
-}
-
 // Normal at crossing point p of a cell (src/its.cu:186-268).
 __device__ __forceinline__ void cell_normal(const CellCorners& cc, const float* p, float* n) {
-    float cmin[3], csz[3], t[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        cmin[a] = cc.p[0][a];
-        csz[a] = __fsub_rn(cc.p[7][a], cc.p[0][a]);
-        t[a] = __fdiv_rn(__fsub_rn(p[a], cmin[a]), csz[a]);
-        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
-    }
-    const float eps = 0.02f;
-    float d[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float tp[3] = {t[0], t[1], t[2]}, tm[3] = {t[0], t[1], t[2]};
-        tp[a] = fminf(__fadd_rn(t[a], eps), 0.99f);
-        tm[a] = fmaxf(__fsub_rn(t[a], eps), 0.01f);
-        const float fp = trilin(cc.v, tp[0], tp[1], tp[2]);
-        const float fm = trilin(cc.v, tm[0], tm[1], tm[2]);
-        d[a] = __fdiv_rn(__fsub_rn(fp, fm), __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]));
-    }
-    const float len =
-        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
-    if (len > 1e-8f) {
-        n[0] = __fdiv_rn(d[0], len);
-        n[1] = __fdiv_rn(d[1], len);
-        n[2] = __fdiv_rn(d[2], len);
-    } else {
-        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
-    }
+    iso::stencil_normal(cc.v, cc.p[0], cc.p[7], p, n, cc.fma);
 }
 
 // Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
@@ -158,29 +122,38 @@ __device__ __forceinline__ float residual_ff(float b, const float* row, const fl
 }
 
 // QEF of a cell: normal equations of the crossings' planes plus reg times the
-// distance to their mean point, accumulated as src/dc.cu:26-62 does (each
-// operation rounded, crossings in order); solved by the pseudo-inverse of the
-// 3x3 system with the threshold svd_tol * largest singular value
-// (src/batched_la.cu:152-178), from an FP32 eigen-decomposition refined once
-// with a double-FP32 residual.
+// distance to their mean point, accumulated as src/dc.cu:26-62 does (crossings
+// in order, in the grid's arithmetic reading: the CUDA build fuses the dot
+// product as the norm, and each `+= a * b` into fma(a, b, acc)); solved by the
+// pseudo-inverse of the 3x3 system with the threshold svd_tol * largest
+// singular value (src/batched_la.cu:152-178), from an FP32 eigen-decomposition
+// refined once with a double-FP32 residual.
 struct Qef {
     float ata[9], atb[3];  // the system (reg included after qef_finish)
     float px, py, pz;      // sum of the points
     float w[3], q[3][3];   // its eigenvalues and eigenvectors (columns)
     unsigned keep;         // eigenvalues above the threshold
     double x[3];           // the solution before clipping
+    bool fma;              // arithmetic reading of the accumulation
 };
 
-__device__ __forceinline__ void qef_init(Qef& Q) {
+__device__ __forceinline__ void qef_init(Qef& Q, bool fma) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) Q.ata[i] = 0.0f;
     Q.atb[0] = Q.atb[1] = Q.atb[2] = 0.0f;
     Q.px = Q.py = Q.pz = 0.0f;
+    Q.fma = fma;
+}
+
+// acc += a * b
+__device__ __forceinline__ float acc_mul(float acc, float a, float b, bool fma) {
+    return fma ? __fmaf_rn(a, b, acc) : __fadd_rn(acc, __fmul_rn(a, b));
 }
 
 // One crossing: point (qx, qy, qz), normal (nx, ny, nz).
 __device__ __forceinline__ void qef_add(Qef& Q, float qx, float qy, float qz, float nx, float ny, float nz) {
-    const float d = __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
+    const float d = Q.fma ? __fmaf_rn(nz, qz, __fmaf_rn(nx, qx, __fmul_rn(ny, qy)))
+                          : __fadd_rn(__fadd_rn(__fmul_rn(nx, qx), __fmul_rn(ny, qy)), __fmul_rn(nz, qz));
     Q.px = __fadd_rn(Q.px, qx);
     Q.py = __fadd_rn(Q.py, qy);
     Q.pz = __fadd_rn(Q.pz, qz);
@@ -188,10 +161,10 @@ __device__ __forceinline__ void qef_add(Qef& Q, float qx, float qy, float qz, fl
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) Q.ata[3 * i + j] = __fadd_rn(Q.ata[3 * i + j], __fmul_rn(n3[i], n3[j]));
-    Q.atb[0] = __fadd_rn(Q.atb[0], __fmul_rn(nx, d));
-    Q.atb[1] = __fadd_rn(Q.atb[1], __fmul_rn(ny, d));
-    Q.atb[2] = __fadd_rn(Q.atb[2], __fmul_rn(nz, d));
+        for (int j = 0; j < 3; ++j) Q.ata[3 * i + j] = acc_mul(Q.ata[3 * i + j], n3[i], n3[j], Q.fma);
+    Q.atb[0] = acc_mul(Q.atb[0], nx, d, Q.fma);
+    Q.atb[1] = acc_mul(Q.atb[1], ny, d, Q.fma);
+    Q.atb[2] = acc_mul(Q.atb[2], nz, d, Q.fma);
 }
 
 // The regularisation, the eigen-decomposition and the solution of K crossings.
@@ -201,9 +174,9 @@ __device__ __forceinline__ void qef_finish(Qef& Q, uint32_t K, float reg, float 
     const float cnt = __uint2float_rn(K);
     const float px = __fdiv_rn(Q.px, cnt), py = __fdiv_rn(Q.py, cnt), pz = __fdiv_rn(Q.pz, cnt);
     ata[0] = __fadd_rn(ata[0], reg); ata[4] = __fadd_rn(ata[4], reg); ata[8] = __fadd_rn(ata[8], reg);
-    atb[0] = __fadd_rn(atb[0], __fmul_rn(reg, px));
-    atb[1] = __fadd_rn(atb[1], __fmul_rn(reg, py));
-    atb[2] = __fadd_rn(atb[2], __fmul_rn(reg, pz));
+    atb[0] = acc_mul(atb[0], reg, px, Q.fma);
+    atb[1] = acc_mul(atb[1], reg, py, Q.fma);
+    atb[2] = acc_mul(atb[2], reg, pz, Q.fma);
     // pseudo-inverse solve: singular values of the symmetric system are |w|
     float m[3][3];
 #pragma unroll
@@ -231,8 +204,8 @@ __device__ __forceinline__ void qef_finish(Qef& Q, uint32_t K, float reg, float 
 
 // The QEF of K crossings stored as points [K, 3] and normals [K, 3].
 __device__ __forceinline__ void qef_solve(const float* points, const float* normals, uint32_t K, float reg,
-                                          float svd_tol, Qef& Q) {
-    qef_init(Q);
+                                          float svd_tol, bool fma, Qef& Q) {
+    qef_init(Q, fma);
     for (uint32_t k = 0; k < K; ++k)
         qef_add(Q, points[3 * k], points[3 * k + 1], points[3 * k + 2], normals[3 * k], normals[3 * k + 1],
                 normals[3 * k + 2]);
@@ -286,13 +259,14 @@ __device__ __forceinline__ float edge_cross(const CellCorners& cc, float level, 
     corner_pos(cc, cb, pb);
     const float t = iso::cross_t(level, corner_value(cc, ca), corner_value(cc, cb));
 #pragma unroll
-    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, pa[q], pb[q]);
+    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, pa[q], pb[q], cc.fma);
     return t;
 }
 
 Grid3 make_grid(int nx, int ny, int nz, const float* amin, const float* amax) {
     Grid3 g;
     g.nx = nx; g.ny = ny; g.nz = nz;
+    g.fma = iso::arith_fma();
     for (int k = 0; k < 3; ++k) {
         g.amin[k] = amin[k];
         g.asize[k] = amax[k] - amin[k];

@@ -314,7 +314,9 @@ __device__ __forceinline__ bool cell_used(const Grid3& g, int cx, int cy, int cz
 // when nobody asked for the intersection: the same arithmetic as dc_points
 // followed by dc_solve, without writing points and normals.  used (optional):
 // per cell, 0 when no face uses its dual vertex, else 1, or 3 when the vertex
-// lies on a face of the cell's box.
+// lies on a face of the cell's box.  F: the arithmetic reading (g.fma), a
+// template argument so that each reading compiles without the other's code.
+template <bool F>
 __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
                                                      float svd_tol, float* __restrict__ dual,
@@ -328,6 +330,7 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     const int cz = int(cid % uint32_t(g.nz - 1));
     const uint32_t rr = cid / uint32_t(g.nz - 1);
     const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
+    g.fma = F;
     CellCorners cc;
     load_cell(vals, g, cx, cy, cz, cc);
     uint32_t cs = 0;
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     const uint32_t est = edge_status(cs);
     const bool is_used = used && cell_used(g, cx, cy, cz, est);
     Qef Q;
-    qef_init(Q);
+    qef_init(Q, g.fma);
     uint32_t K = 0;
 #pragma unroll 1
     for (uint32_t em = est; em; em &= em - 1) {  // this lane's crossed edges, ascending
@@ -381,7 +384,7 @@ __global__ void dc_solve(const float* __restrict__ points, const float* __restri
     if (a >= A) return;
     const uint32_t k0 = cell_off[a], k1 = cell_off[a + 1];
     Qef Q;
-    qef_solve(points + 3ll * k0, normals + 3ll * k0, k1 - k0, reg, svd_tol, Q);
+    qef_solve(points + 3ll * k0, normals + 3ll * k0, k1 - k0, reg, svd_tol, g.fma, Q);
     const double* x = Q.x;
     // clip to the cell box (corner 0 .. corner 7)
     const uint32_t cid = cell_ids[a];
@@ -449,9 +452,10 @@ __device__ __forceinline__ uint32_t active_index(const uint32_t* actm, const uin
     return offA[wi] + __popc(actm[wi] & ((1u << (cz & 31)) - 1u));
 }
 
-__device__ __forceinline__ float dist3(const float* a, const float* b) {
+// |a - b| (norm(v0 - v2) of src/dc.cu:139), in the grid's arithmetic reading.
+__device__ __forceinline__ float dist3(const float* a, const float* b, bool fma) {
     const float dx = __fsub_rn(a[0], b[0]), dy = __fsub_rn(a[1], b[1]), dz = __fsub_rn(a[2], b[2]);
-    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    return iso::norm3f(dx, dy, dz, fma);
 }
 
 // The k-th quad of a point word in the reference's order: by bit (low endpoint
@@ -555,7 +559,7 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
 #pragma unroll
             for (int a = 0; a < 3; ++a) v[t][a] = dual[3 * (long long)qi[t] + a];
         int32_t* o6 = tri + 6 * q;
-        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+        if (dist3(v[0], v[2], g.fma) > dist3(v[1], v[3], g.fma)) {
             o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0];
             o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
         } else {
@@ -1256,7 +1260,7 @@ __global__ void __launch_bounds__(256) dc_cell_quads(const uint8_t* __restrict__
 #pragma unroll
         for (int t = 0; t < 4; ++t) f[t] = vertex_of(vmap, qi[t]);
         int32_t* o6 = faces + 6 * q;
-        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+        if (dist3(v[0], v[2], g.fma) > dist3(v[1], v[3], g.fma)) {
             o6[0] = f[1]; o6[1] = f[3]; o6[2] = f[0];
             o6[3] = f[3]; o6[4] = f[1]; o6[5] = f[2];
         } else {
@@ -1441,7 +1445,7 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
     }
     iso::ProfScope ps("dc_solve", st);
     const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-    dc_cell_solve<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
+    (g.fma ? dc_cell_solve<true> : dc_cell_solve<false>)<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
                                                       reg, svd_tol, dual, nullptr, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
@@ -1674,7 +1678,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         {
             iso::ProfScope ps("dc_solve", st);
             const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-            iso::launch_pdl(dc_cell_solve, blocks_for(capA, bt), unsigned(bt), st, values, g, level,
+            iso::launch_pdl(g.fma ? dc_cell_solve<true> : dc_cell_solve<false>, blocks_for(capA, bt), unsigned(bt), st, values, g, level,
                             static_cast<const uint32_t*>(cells), capA, reg, svd_tol, w.dual,
                             static_cast<const long long*>(eff), w.used);
         }

@@ -27,7 +27,9 @@
 // triangles of active cells in ascending cell id, drops triangles with two equal
 // vertex positions (src/mc/nagae.cu:71), and welds vertices by exact position
 // (src/utils.cu:32-59).  Positions here use the reference's operation order
-// with every FP32 operation rounded on its own, so they are bit-identical.  Two
+// and its rounding, in either reading of its arithmetic (the fused one of its
+// CUDA build or the unfused one of its host build, common.cuh), so they are
+// bit-identical.  Two
 // distinct crossed edges give equal positions only when both vertices land on
 // the same grid point (on grids whose spacing is far above float resolution;
 // the host layer handles the rest), and those are the snapped vertices the
@@ -84,6 +86,7 @@ struct McGrid {
     // Vertices whose edge parameter t is within tau of 0 or 1 are the only ones
     // that can share a position with a vertex of another edge (mc_snap_tau).
     float tau;
+    bool fma;  // arithmetic reading (iso::arith_fma at the call)
 };
 
 // Workspace carved from one buffer (offsets 256-aligned).
@@ -347,9 +350,9 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     const uint32_t gid = blockIdx.x * CNT_THREADS + threadIdx.x;
     const uint32_t ncoord = uint32_t(g.nx + g.ny + g.nz);
     if (gid < ncoord) {
-        if (gid < uint32_t(g.nx)) gc[gid] = iso::grid_coord(gid, g.nx, amin0, size0);
-        else if (gid < uint32_t(g.nx + g.ny)) gc[gid] = iso::grid_coord(gid - g.nx, g.ny, amin1, size1);
-        else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2);
+        if (gid < uint32_t(g.nx)) gc[gid] = iso::grid_coord(gid, g.nx, amin0, size0, g.fma);
+        else if (gid < uint32_t(g.nx + g.ny)) gc[gid] = iso::grid_coord(gid - g.nx, g.ny, amin1, size1, g.fma);
+        else gc[gid] = iso::grid_coord(gid - g.nx - g.ny, g.nz, amin2, size2, g.fma);
     }
     const uint32_t seg = blockIdx.x;
     if (seg >= nseg) return;  // CTAs past the segments only write coordinates
@@ -750,7 +753,8 @@ __device__ void emit_vertices(const McGrid& g, const EmitArgs& a, unsigned bi, u
         const float xb = ax == 0 ? gx(g, x + 1) : xa;
         const float yb = ax == 1 ? gy(g, y + 1) : ya;
         const float zb = ax == 2 ? gz(g, z + 1) : za;
-        const float px = iso::lerp1(t, xa, xb), py = iso::lerp1(t, ya, yb), pz = iso::lerp1(t, za, zb);
+        const float px = iso::lerp1(t, xa, xb, g.fma), py = iso::lerp1(t, ya, yb, g.fma),
+                    pz = iso::lerp1(t, za, zb, g.fma);
         float* vo = vout + 3ll * vi;
         vo[0] = px;
         vo[1] = py;
@@ -1158,6 +1162,7 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.level = p.level;
     g.method = p.method;
     g.tau = snap_tau(p);
+    g.fma = iso::arith_fma();
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
     {

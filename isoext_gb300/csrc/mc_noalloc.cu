@@ -12,71 +12,52 @@
 //   - The scratch holds kScratchBytes (32 MiB) per device. A grid and output
 //     capacities that need more are rejected with ISO_ERR_WORKSPACE before
 //     anything is queued.
-//   - The first call on a device does set-up. With that device current, it
-//     looks up the scratch's device address (cudaGetSymbolAddress). That can
-//     load the module holding the array. Make this first call before any stream
-//     capture. Later calls reuse the address.
-//   - All calls on a device share one scratch. Calls that overlap on the
+//   - Every call looks up the scratch's device address (cudaGetSymbolAddress)
+//     in the CUDA context current on the calling thread, so a context made
+//     after a cudaDeviceReset, or a caller's own driver context, gets its own
+//     copy of the array. The first lookup in a context can load the module
+//     holding the array: make that first call before any stream capture.
+//   - All calls in one context share one scratch. Calls that overlap on the
 //     device, on different streams or from different host threads without
 //     ordering between them, race on it. Order them on one stream, or with
 //     events.
-//   - Each call clears, on its stream, the parts that must start at zero
-//     (per-block tile sums and staging counters; mc_launch does this). Every
-//     other byte a call reads, the same call wrote first.
+//   - Each call clears, on its stream, the parts that must start at zero: the
+//     sign pass (mc_signs) zeroes the counters, the scan's look-back states and
+//     the merge hash before the later kernels read them. Every other byte a call
+//     reads, the same call wrote first.
 #include <cstddef>
 #include <cstdio>
-#include <mutex>
 
 #include <cuda_runtime.h>
 
-#include "common.cuh"
+#include "isoext_gb300.h"
 
 namespace iso {
 void set_last_error(const char* msg);  // capi.cu
 }
 
-extern "C" size_t iso_mc_dense_workspace_size(int nx, int ny, int nz, long long vertex_capacity,
-                                              long long face_capacity);
-extern "C" int iso_mc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min,
-                            const float* aabb_max, float level, int method, float* vertices,
-                            long long vertex_capacity, int* faces, long long face_capacity, void* workspace,
-                            size_t workspace_bytes, long long* counts, int* status, void* stream);
-
 namespace {
 
-// Must equal ISO_MC_NOALLOC_SCRATCH_BYTES in include/isoext_gb300.h.
 constexpr size_t kScratchBytes = size_t(32) << 20;
+static_assert(kScratchBytes == ISO_MC_NOALLOC_SCRATCH_BYTES, "the header states the scratch size");
 
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
+// The scratch's address in the context current on this thread.  Looked up on
+// every call rather than cached per device: a cached address would outlive a
+// cudaDeviceReset, and would be another context's memory for a caller that
+// makes its own driver context current.
 int scratch_address(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) {
-        iso::set_last_error("iso_mc_dense_noalloc: cudaGetDevice failed");
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "iso_mc_dense_noalloc: cudaGetSymbolAddress failed: %s",
+                      cudaGetErrorString(e));
+        iso::set_last_error(msg);
         return ISO_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        iso::set_last_error("iso_mc_dense_noalloc: device ordinal above 63");
-        return ISO_ERR_ARG;
-    }
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            char msg[160];
-            std::snprintf(msg, sizeof msg, "iso_mc_dense_noalloc: cudaGetSymbolAddress failed: %s",
-                          cudaGetErrorString(e));
-            iso::set_last_error(msg);
-            return ISO_ERR_CUDA;
-        }
-        g_addr[dev] = p;
-    }
-    *out = g_addr[dev];
+    *out = p;
     return ISO_OK;
 }
 

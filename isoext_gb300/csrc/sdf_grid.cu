@@ -20,7 +20,7 @@ constexpr int MAX_PRIMS = 32;
 // 1 box), centre x y z, radius | half-extents x y z.
 __global__ void __launch_bounds__(256) sdf_union_grid(const float* __restrict__ prims, int nx, int ny, int nz,
                                                       float ax, float ay, float az, float sx, float sy, float sz,
-                                                      float* __restrict__ out) {
+                                                      bool fma, float* __restrict__ out) {
     __shared__ float pr[MAX_PRIMS][7];
     __shared__ int np;
     if (threadIdx.x == 0) np = min(max(int(prims[0]), 0), MAX_PRIMS);
@@ -33,9 +33,9 @@ __global__ void __launch_bounds__(256) sdf_union_grid(const float* __restrict__ 
         const int z = int(i % nz);
         const long long r = i / nz;
         const int y = int(r % ny), x = int(r / ny);
-        const float px = iso::grid_coord(uint32_t(x), uint32_t(nx), ax, sx);
-        const float py = iso::grid_coord(uint32_t(y), uint32_t(ny), ay, sy);
-        const float pz = iso::grid_coord(uint32_t(z), uint32_t(nz), az, sz);
+        const float px = iso::grid_coord(uint32_t(x), uint32_t(nx), ax, sx, fma);
+        const float py = iso::grid_coord(uint32_t(y), uint32_t(ny), ay, sy, fma);
+        const float pz = iso::grid_coord(uint32_t(z), uint32_t(nz), az, sz, fma);
         float d = 3.402823466e38f;
         for (int k = 0; k < np; ++k) {
             const float dx = __fsub_rn(px, pr[k][1]), dy = __fsub_rn(py, pr[k][2]), dz = __fsub_rn(pz, pr[k][3]);
@@ -79,7 +79,7 @@ int iso_sdf_union_grid(const float* prims, int nx, int ny, int nz, const float* 
     iso::ProfScope ps("sdf_union_grid", st);
     sdf_union_grid<<<unsigned(grid), 256, 0, st>>>(prims, nx, ny, nz, aabb_min[0], aabb_min[1], aabb_min[2],
                                                    aabb_max[0] - aabb_min[0], aabb_max[1] - aabb_min[1],
-                                                   aabb_max[2] - aabb_min[2], out);
+                                                   aabb_max[2] - aabb_min[2], iso::arith_fma(), out);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 

@@ -33,6 +33,7 @@ struct SpGrid {
     float level;
     int method;
     float tau;  // edge parameters within tau of 0 or 1 may put two vertices on one position
+    bool fma;   // arithmetic reading (iso::arith_fma at the call)
 };
 
 __device__ __forceinline__ void cell_xyz(const SpGrid& g, uint32_t id, int& x, int& y, int& z) {
@@ -45,6 +46,7 @@ __device__ __forceinline__ void cell_xyz(const SpGrid& g, uint32_t id, int& x, i
 struct Cell8 {
     float v[8];
     float p[8][3];
+    bool fma;  // the grid's arithmetic reading (set with the positions)
 };
 
 // The 8 values of cell c (two 16-byte loads).
@@ -57,12 +59,13 @@ __device__ __forceinline__ void load_vals(const float* vals, long long c, Cell8&
 
 // Corner positions of cell (x, y, z) (include/utils.cuh:62-80).
 __device__ __forceinline__ void set_coords(const SpGrid& g, int x, int y, int z, Cell8& cc) {
-    const float cx0 = iso::grid_coord(x, g.nx, g.amin[0], g.asize[0]);
-    const float cx1 = iso::grid_coord(x + 1, g.nx, g.amin[0], g.asize[0]);
-    const float cy0 = iso::grid_coord(y, g.ny, g.amin[1], g.asize[1]);
-    const float cy1 = iso::grid_coord(y + 1, g.ny, g.amin[1], g.asize[1]);
-    const float cz0 = iso::grid_coord(z, g.nz, g.amin[2], g.asize[2]);
-    const float cz1 = iso::grid_coord(z + 1, g.nz, g.amin[2], g.asize[2]);
+    const float cx0 = iso::grid_coord(x, g.nx, g.amin[0], g.asize[0], g.fma);
+    const float cx1 = iso::grid_coord(x + 1, g.nx, g.amin[0], g.asize[0], g.fma);
+    const float cy0 = iso::grid_coord(y, g.ny, g.amin[1], g.asize[1], g.fma);
+    const float cy1 = iso::grid_coord(y + 1, g.ny, g.amin[1], g.asize[1], g.fma);
+    const float cz0 = iso::grid_coord(z, g.nz, g.amin[2], g.asize[2], g.fma);
+    const float cz1 = iso::grid_coord(z + 1, g.nz, g.amin[2], g.asize[2], g.fma);
+    cc.fma = g.fma;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         cc.p[k][0] = (k >> 2) ? cx1 : cx0;
@@ -105,7 +108,7 @@ __device__ __forceinline__ void edge_point(const Cell8& cc, int e, float level, 
     const int a = ISO_EDGE_CORNERS[2 * e], b = ISO_EDGE_CORNERS[2 * e + 1];
     const float t = iso::cross_t(level, cc.v[a], cc.v[b]);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[a][q], cc.p[b][q]);
+    for (int q = 0; q < 3; ++q) p[q] = iso::lerp1(t, cc.p[a][q], cc.p[b][q], cc.fma);
 }
 
 __device__ __forceinline__ bool eq3(const float* a, const float* b) {
@@ -256,41 +259,9 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __re
 
 // --- intersections -----------------------------------------------------------
 
-__device__ __forceinline__ float trilin(const float* cv, float tx, float ty, float tz) {
-    const float oz = __fsub_rn(1.0f, tz), oy = __fsub_rn(1.0f, ty), ox = __fsub_rn(1.0f, tx);
-    const float c00 = __fadd_rn(__fmul_rn(cv[0], oz), __fmul_rn(cv[1], tz));
-    const float c01 = __fadd_rn(__fmul_rn(cv[2], oz), __fmul_rn(cv[3], tz));
-    const float c10 = __fadd_rn(__fmul_rn(cv[4], oz), __fmul_rn(cv[5], tz));
-    const float c11 = __fadd_rn(__fmul_rn(cv[6], oz), __fmul_rn(cv[7], tz));
-    const float c0 = __fadd_rn(__fmul_rn(c00, oy), __fmul_rn(c01, ty));
-    const float c1 = __fadd_rn(__fmul_rn(c10, oy), __fmul_rn(c11, ty));
-    return __fadd_rn(__fmul_rn(c0, ox), __fmul_rn(c1, tx));
-}
-
+// Normal at crossing point p (src/its.cu:186-268).
 __device__ __forceinline__ void cell_normal(const Cell8& cc, const float* p, float* n) {
-    float csz[3], t[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        csz[a] = __fsub_rn(cc.p[7][a], cc.p[0][a]);
-        t[a] = __fdiv_rn(__fsub_rn(p[a], cc.p[0][a]), csz[a]);
-        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
-    }
-    float d[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float tp[3] = {t[0], t[1], t[2]}, tm[3] = {t[0], t[1], t[2]};
-        tp[a] = fminf(__fadd_rn(t[a], 0.02f), 0.99f);
-        tm[a] = fmaxf(__fsub_rn(t[a], 0.02f), 0.01f);
-        d[a] = __fdiv_rn(__fsub_rn(trilin(cc.v, tp[0], tp[1], tp[2]), trilin(cc.v, tm[0], tm[1], tm[2])),
-                         __fmul_rn(__fsub_rn(tp[a], tm[a]), csz[a]));
-    }
-    const float len =
-        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
-    if (len > 1e-8f) {
-        n[0] = __fdiv_rn(d[0], len); n[1] = __fdiv_rn(d[1], len); n[2] = __fdiv_rn(d[2], len);
-    } else {
-        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
-    }
+    iso::stencil_normal(cc.v, cc.p[0], cc.p[7], p, n, cc.fma);
 }
 
 __global__ void __launch_bounds__(SP_BLOCK) sp_its_count(SpGrid g, const float* __restrict__ vals,
@@ -452,9 +423,10 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_quad_count(SpGrid g, const int* _
     if (threadIdx.x == 0) { blk[2 * blockIdx.x] = t; blk[2 * blockIdx.x + 1] = 0; }
 }
 
-__device__ __forceinline__ float dist3(const float* a, const float* b) {
+// |a - b| (norm(v0 - v2) of src/dc.cu:139), in the grid's arithmetic reading.
+__device__ __forceinline__ float dist3(const float* a, const float* b, bool fma) {
     const float dx = __fsub_rn(a[0], b[0]), dy = __fsub_rn(a[1], b[1]), dz = __fsub_rn(a[2], b[2]);
-    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    return iso::norm3f(dx, dy, dz, fma);
 }
 
 __global__ void __launch_bounds__(SP_BLOCK) sp_quad_emit(SpGrid g, const int* __restrict__ ids,
@@ -492,7 +464,7 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_quad_emit(SpGrid g, const int* __
         for (int i = 0; i < 4; ++i)
             for (int k = 0; k < 3; ++k) v[i][k] = dual[3 * (long long)qi[i] + k];
         int* o6 = tri + 6 * qo;
-        if (dist3(v[0], v[2]) > dist3(v[1], v[3])) {
+        if (dist3(v[0], v[2], g.fma) > dist3(v[1], v[3], g.fma)) {
             o6[0] = qi[1]; o6[1] = qi[3]; o6[2] = qi[0]; o6[3] = qi[3]; o6[4] = qi[1]; o6[5] = qi[2];
         } else {
             o6[0] = qi[2]; o6[1] = qi[0]; o6[2] = qi[1]; o6[3] = qi[0]; o6[4] = qi[2]; o6[5] = qi[3];
@@ -511,9 +483,9 @@ __global__ void sp_points(SpGrid g, const int* __restrict__ ids, long long m, fl
     const int k = int(i & 7);
     int x, y, z;
     cell_xyz(g, uint32_t(ids[c]), x, y, z);
-    out[3 * i] = iso::grid_coord(x + (k >> 2), g.nx, g.amin[0], g.asize[0]);
-    out[3 * i + 1] = iso::grid_coord(y + ((k >> 1) & 1), g.ny, g.amin[1], g.asize[1]);
-    out[3 * i + 2] = iso::grid_coord(z + (k & 1), g.nz, g.amin[2], g.asize[2]);
+    out[3 * i] = iso::grid_coord(x + (k >> 2), g.nx, g.amin[0], g.asize[0], g.fma);
+    out[3 * i + 1] = iso::grid_coord(y + ((k >> 1) & 1), g.ny, g.amin[1], g.asize[1], g.fma);
+    out[3 * i + 2] = iso::grid_coord(z + (k & 1), g.nz, g.amin[2], g.asize[2], g.fma);
 }
 
 // Keep the ids whose 8 values straddle the level (src/grid/sparse.cu:150-179),
@@ -558,6 +530,7 @@ SpGrid mk(int nx, int ny, int nz, const float* amin, const float* amax, float le
     g.level = level;
     g.method = method;
     g.tau = snap_tau_box(nx, ny, nz, g.amin, g.asize);
+    g.fma = iso::arith_fma();
     return g;
 }
 unsigned nb(long long n, int b) { return unsigned(std::max<long long>(1, (n + b - 1) / b)); }

@@ -41,12 +41,18 @@ def _check_cuda_f32(t, ndim: int | None = None, last: int | None = None, what: s
         raise TypeError(f"{what} must have shape (-1, {last})")
 
 
-def grid_positions(index: torch.Tensor, n: int, amin: float, size: float) -> torch.Tensor:
-    """Coordinate of grid index i along one axis: amin + (i / (float)(n - 1)) * size,
-    each operation rounded in FP32 (include/utils.cuh:62-80)."""
-    f = index.to(torch.float32) / torch.tensor(float(n - 1), dtype=torch.float32, device=index.device)
-    return f * torch.tensor(size, dtype=torch.float32, device=index.device) + \
-        torch.tensor(amin, dtype=torch.float32, device=index.device)
+def grid_positions(index: torch.Tensor, n: int, amin: float, amax: float) -> torch.Tensor:
+    """Coordinate of grid index i along one axis of n points over [amin, amax]:
+    amin + (i / (float)(n - 1)) * (amax - amin) in FP32, as isoext computes it
+    (include/utils.cuh:62-80), in the library's current arithmetic reading
+    (``set_arithmetic``).  ``index`` is an integer CUDA tensor."""
+    from . import _ffi
+
+    table = torch.empty(max(int(n), 0), dtype=torch.float32, device=index.device)
+    with torch.cuda.device(index.device):
+        _ffi.check(_ffi.lib().iso_axis_coords(table.data_ptr(), int(n), float(amin), float(amax),
+                                              torch.cuda.current_stream(index.device).cuda_stream))
+    return table[index.long()]
 
 
 class Grid:
@@ -99,7 +105,7 @@ class UniformGrid(Grid):
         axes = []
         for k in range(3):
             idx = torch.arange(self.shape[k], device=dev, dtype=torch.int64)
-            axes.append(grid_positions(idx, self.shape[k], self.aabb_min[k], self._size[k]))
+            axes.append(grid_positions(idx, self.shape[k], self.aabb_min[k], self.aabb_max[k]))
         gx, gy, gz = torch.meshgrid(axes[0], axes[1], axes[2], indexing="ij")
         return torch.stack([gx, gy, gz], dim=-1).contiguous()
 

@@ -177,7 +177,7 @@ class SparseGrid(SparseGridBase):
         from .grids import grid_positions
 
         size = [float(np.float32(b) - np.float32(a)) for a, b in zip(self.aabb_min, self.aabb_max)]
-        axes = [grid_positions(torch.arange(shape[k], device=dev), shape[k], self.aabb_min[k], size[k])
+        axes = [grid_positions(torch.arange(shape[k], device=dev), shape[k], self.aabb_min[k], self.aabb_max[k])
                 for k in range(3)]
         h = [abs(size[k]) / (shape[k] - 1) for k in range(3)]
         band = 2.0 * max(h) if band is None else float(band)

@@ -25,7 +25,9 @@ HERE = pathlib.Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 ORACLE_SO = BUILD / "libiso_oracle.so"
 REF_SO = HERE / "_ref" / "libisoext_ref.so"
-REF_SRC = pathlib.Path(os.environ.get("ISOEXT_REFERENCE", "/root/reference"))
+# The isoext checkout to build the reference from: an argument of
+# build_reference(), else the ISOEXT_REFERENCE environment variable.
+REF_ENV = "ISOEXT_REFERENCE"
 
 _f = C.POINTER(C.c_float)
 _i32 = C.POINTER(C.c_int32)
@@ -50,13 +52,17 @@ def build_oracle(force: bool = False) -> pathlib.Path:
     return ORACLE_SO
 
 
-def build_reference(force: bool = False) -> pathlib.Path | None:
-    """Compile the reference's own sources for the host, if they are present."""
+def build_reference(src: str | os.PathLike | None = None, force: bool = False) -> pathlib.Path | None:
+    """Compile the reference's own sources for the host.
+
+    ``src`` is the isoext checkout (else ``$ISOEXT_REFERENCE``).  Returns None
+    when neither names a checkout and no earlier build exists."""
     if REF_SO.exists() and not force:
         return REF_SO
-    if not (REF_SRC / "src").is_dir():
+    src = src or os.environ.get(REF_ENV)
+    if not src or not (pathlib.Path(src) / "src").is_dir():
         return None
-    subprocess.check_call(["bash", str(HERE / "build_ref.sh"), str(REF_SRC)],
+    subprocess.check_call(["bash", str(HERE / "build_ref.sh"), str(src)],
                           stdout=subprocess.DEVNULL)
     return REF_SO
 
@@ -81,11 +87,22 @@ class _ItsT(C.Structure):
                 ("edges", _u32), ("is_out", _u8), ("cells", _u32), ("offsets", _u32)]
 
 
-class Oracle:
-    """CPU restatement (iso_oracle.c).  All arrays are numpy, C-contiguous."""
+ARITH = {"host": 0, "nvcc": 1}
 
-    def __init__(self):
+
+class Oracle:
+    """CPU restatement (iso_oracle.c).  All arrays are numpy, C-contiguous.
+
+    ``arith`` is the reading of the reference's FP32 expressions: ``"nvcc"``
+    (its CUDA build, the default) or ``"host"`` (its host build)."""
+
+    def __init__(self, arith: str = "nvcc"):
+        if arith not in ARITH:
+            raise ValueError(f"arith must be one of {sorted(ARITH)}")
+        self.arith = arith
         lib = C.CDLL(str(build_oracle()))
+        lib.ora_set_arith.argtypes = [C.c_int]
+        lib.ora_axis_coords.argtypes = [C.c_int, C.c_float, C.c_float, _f]
         lib.ora_mc_dense.argtypes = [_f, C.c_int, C.c_int, C.c_int, _f, _f, C.c_float, C.c_int,
                                      C.POINTER(_f), C.POINTER(_i64), C.POINTER(_i32),
                                      C.POINTER(_i64), C.POINTER(_u32)]
@@ -100,9 +117,42 @@ class Oracle:
                                C.POINTER(_ItsT), C.c_float, C.c_float, C.POINTER(_f),
                                C.POINTER(_i64), C.POINTER(_i32), C.POINTER(_i64),
                                C.POINTER(_d)]
+        lib.ora_qef.argtypes = [_f, _f, _u32, _i64, C.c_float, _f, _f]
         lib.ora_its_free.argtypes = [C.POINTER(_ItsT)]
         lib.ora_free.argtypes = [C.c_void_p]
-        self.lib = lib
+        self._lib = lib
+
+    @property
+    def lib(self):
+        """The C library, set to this oracle's arithmetic reading (the setting is
+        the library's own, so it is made before every call)."""
+        self._lib.ora_set_arith(ARITH[self.arith])
+        return self._lib
+
+    def axis_coords(self, n: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+        """The FP32 coordinates of the n points of one axis over [lo, hi]."""
+        out = np.empty(max(n, 0), np.float32)
+        if n > 0:
+            self.lib.ora_axis_coords(n, lo, hi, _fp(out))
+        return out
+
+    def qef(self, points, normals, offsets, reg=1e-2):
+        """(ATA [A, 9], ATb [A, 3]) of each cell's crossings (src/dc.cu:14-65)."""
+        points = np.ascontiguousarray(points, np.float32)
+        normals = np.ascontiguousarray(normals, np.float32)
+        offsets = np.ascontiguousarray(offsets, np.uint32)
+        A = len(offsets) - 1
+        ata = np.zeros((max(A, 0), 9), np.float32)
+        atb = np.zeros((max(A, 0), 3), np.float32)
+        if A > 0:
+            self.lib.ora_qef(_fp(points), _fp(normals), offsets.ctypes.data_as(_u32), A, reg, _fp(ata), _fp(atb))
+        return ata, atb
+
+    def grid_points(self, shape, lo=(-1, -1, -1), hi=(1, 1, 1)) -> np.ndarray:
+        """Point positions [nx, ny, nz, 3] as the reference's get_points gives them."""
+        ax = [self.axis_coords(shape[k], lo[k], hi[k]) for k in range(3)]
+        X, Y, Z = np.meshgrid(*ax, indexing="ij")
+        return np.stack([X, Y, Z], axis=-1)
 
     def _free(self, p):
         self.lib.ora_free(C.cast(p, C.c_void_p))

@@ -3,11 +3,11 @@
 # CPU (Thrust OpenMP backend) into oracle/_ref/libisoext_ref.so.
 #
 # The sources are compiled where they lie under the isoext checkout given as $1
-# (default /root/reference); nothing is copied.  src/isoext_ext.cu (nanobind) and
+# (required); nothing is copied.  src/isoext_ext.cu (nanobind) and
 # src/batched_la.cu (cuSOLVER/cuBLAS, GPU only) are left out; ref_la_host.cpp
 # stands in for the latter.  TEST INFRASTRUCTURE ONLY.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:?usage: build_ref.sh <isoext checkout>}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 1; }

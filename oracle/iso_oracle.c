@@ -5,14 +5,24 @@
  * against; it is compiled and called only by tests/, __graft_entry__.smoke()
  * and bench.py's cpu_baseline leg.  The product never links or calls it.
  *
- * It restates the reference's algorithm step by step in FP32 with every
- * operation rounded separately (built with -ffp-contract=off), which is the
- * arithmetic of the reference's own source read literally (and of its host
- * build), and welds vertices the way the reference does: by exact position,
- * sorted lexicographically.  Its outputs are therefore the reference's output
- * tensors, bit for bit.  It is pinned against the reference's own code compiled
- * for the host (oracle/_ref, see build_ref.sh) and against the counts published
- * in the reference's notebooks (tests/golden).
+ * It restates the reference's algorithm step by step in FP32, and welds
+ * vertices the way the reference does: by exact position, sorted
+ * lexicographically.  Its outputs are therefore the reference's output
+ * tensors, bit for bit, in either of two readings of the reference's FP32
+ * expressions (ora_set_arith):
+ *   1 (default) -- its CUDA build: nvcc's default FMA contraction fuses the
+ *                  multiply-adds of the grid position, the lerp, the steps of
+ *                  the trilinear interpolant and the dot product (which
+ *                  product it fuses is spelt out at each use below; it was
+ *                  measured on a restatement of the source compiled by nvcc
+ *                  with default flags, tests/nvcc_expr.cu);
+ *   0           -- its host build (and its source read literally): every
+ *                  operation rounded on its own.
+ * The file is built with -ffp-contract=off, so only the explicit fmaf calls
+ * fuse.  Reading 0 is pinned against the reference's own code compiled for the
+ * host (oracle/_ref, see build_ref.sh) and against the counts published in the
+ * reference's notebooks (tests/golden); reading 1 against the nvcc-compiled
+ * restatement on the GPU.
  *
  * Reference anchors (paths inside the isoext project):
  *   grid point position         include/utils.cuh:62-80   (get_vtx_pos_op)
@@ -48,22 +58,55 @@ typedef struct { float x, y, z; } f3;
 static f3 mk(float x, float y, float z) { f3 r = {x, y, z}; return r; }
 static f3 add3(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
 static f3 sub3(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
-static f3 smul(float s, f3 a) { return mk(s * a.x, s * a.y, s * a.z); }
-static f3 mul3(f3 a, f3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
 static f3 div3(f3 a, f3 b) { return mk(a.x / b.x, a.y / b.y, a.z / b.z); }
 static f3 divs(f3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
 static int eq3(f3 a, f3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
-static float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* the arithmetic reading: 1 = the reference's CUDA build, 0 = its host build */
+static int g_fma = 1;
+void ora_set_arith(int fma) { g_fma = fma != 0; }
+int ora_get_arith(void) { return g_fma; }
+
+/* x * ox + y * oy; the CUDA build fuses the first product, or with swap the
+ * second */
+static float blend(float x, float ox, float y, float oy, int swap) {
+    if (!g_fma) return x * ox + y * oy;
+    return swap ? fmaf(y, oy, x * ox) : fmaf(x, ox, y * oy);
+}
+
+/* acc + a * b; fused in the CUDA build */
+static float acc_mul(float acc, float a, float b) { return g_fma ? fmaf(a, b, acc) : acc + a * b; }
+
+/* dot(a, b) = a.x * b.x + a.y * b.y + a.z * b.z, include/math.cuh;
+ * CUDA build: fma(a.z, b.z, fma(a.x, b.x, a.y * b.y)) */
+static float dot3(f3 a, f3 b) {
+    if (!g_fma) return a.x * b.x + a.y * b.y + a.z * b.z;
+    return fmaf(a.z, b.z, fmaf(a.x, b.x, a.y * b.y));
+}
 static float norm3(f3 a) { return sqrtf(dot3(a, a)); }
 
 /* lerp(t, a, b) = (1 - t) * a + t * b, include/math.cuh:77-81 */
-static f3 lerp3(float t, f3 a, f3 b) { return add3(smul(1.0f - t, a), smul(t, b)); }
+static f3 lerp3(float t, f3 a, f3 b) {
+    float u = 1.0f - t;
+    return mk(blend(u, a.x, t, b.x, 0), blend(u, a.y, t, b.y, 0), blend(u, a.z, t, b.z, 0));
+}
+
+/* one coordinate amin + pos * size; the CUDA build fuses it */
+static float pos_coord(float pos, float amin, float size) {
+    return g_fma ? fmaf(pos, size, amin) : amin + pos * size;
+}
 
 /* Grid point position, include/utils.cuh:62-80. */
 static f3 grid_pos(uint32_t ix, uint32_t iy, uint32_t iz, const uint32_t n[3], f3 amin, f3 asize) {
     f3 p = mk((float)ix / (float)(n[0] - 1), (float)iy / (float)(n[1] - 1),
               (float)iz / (float)(n[2] - 1));
-    return add3(amin, mul3(p, asize));
+    return mk(pos_coord(p.x, amin.x, asize.x), pos_coord(p.y, amin.y, asize.y),
+              pos_coord(p.z, amin.z, asize.z));
+}
+
+/* The n coordinates of one axis over [amin, amax]. */
+void ora_axis_coords(int n, float amin, float amax, float *out) {
+    float size = amax - amin;
+    for (int i = 0; i < n; i++) out[i] = pos_coord((float)i / (float)(n - 1), amin, size);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -295,15 +338,18 @@ typedef struct {
     uint32_t *offsets; /* [A+1] CSR */
 } ora_its_t;
 
-/* trilinear interpolation, src/its.cu:170-184 */
-static float trilin(f3 t, const float *cv) {
-    float c00 = cv[0] * (1 - t.z) + cv[1] * t.z;
-    float c01 = cv[2] * (1 - t.z) + cv[3] * t.z;
-    float c10 = cv[4] * (1 - t.z) + cv[5] * t.z;
-    float c11 = cv[6] * (1 - t.z) + cv[7] * t.z;
-    float c0 = c00 * (1 - t.y) + c01 * t.y;
-    float c1 = c10 * (1 - t.y) + c11 * t.y;
-    return c0 * (1 - t.x) + c1 * t.x;
+/* trilinear interpolation, src/its.cu:170-184.  swap_low_z: in the CUDA build
+ * the two x = 0 steps along z fuse their second product; nvcc does that for the
+ * four stencil samples at the crossing's own z, which share those steps. */
+static float trilin(f3 t, const float *cv, int swap_low_z) {
+    float oz = 1 - t.z, oy = 1 - t.y, ox = 1 - t.x;
+    float c00 = blend(cv[0], oz, cv[1], t.z, swap_low_z);
+    float c01 = blend(cv[2], oz, cv[3], t.z, swap_low_z);
+    float c10 = blend(cv[4], oz, cv[5], t.z, 0);
+    float c11 = blend(cv[6], oz, cv[7], t.z, 0);
+    float c0 = blend(c00, oy, c01, t.y, 0);
+    float c1 = blend(c10, oy, c11, t.y, 0);
+    return blend(c0, ox, c1, t.x, 0);
 }
 
 /* normal at one crossing from the cell's corners, src/its.cu:186-268 */
@@ -318,9 +364,9 @@ static f3 cell_normal(const cell_t *c, f3 p) {
     f3 tpx = mk(fminf(t.x + eps, 0.99f), t.y, t.z), tmx = mk(fmaxf(t.x - eps, 0.01f), t.y, t.z);
     f3 tpy = mk(t.x, fminf(t.y + eps, 0.99f), t.z), tmy = mk(t.x, fmaxf(t.y - eps, 0.01f), t.z);
     f3 tpz = mk(t.x, t.y, fminf(t.z + eps, 0.99f)), tmz = mk(t.x, t.y, fmaxf(t.z - eps, 0.01f));
-    float dx = (trilin(tpx, c->val) - trilin(tmx, c->val)) / ((tpx.x - tmx.x) * csz.x);
-    float dy = (trilin(tpy, c->val) - trilin(tmy, c->val)) / ((tpy.y - tmy.y) * csz.y);
-    float dz = (trilin(tpz, c->val) - trilin(tmz, c->val)) / ((tpz.z - tmz.z) * csz.z);
+    float dx = (trilin(tpx, c->val, 1) - trilin(tmx, c->val, 1)) / ((tpx.x - tmx.x) * csz.x);
+    float dy = (trilin(tpy, c->val, 1) - trilin(tmy, c->val, 1)) / ((tpy.y - tmy.y) * csz.y);
+    float dz = (trilin(tpz, c->val, 0) - trilin(tmz, c->val, 0)) / ((tpz.z - tmz.z) * csz.z);
     f3 g = mk(dx, dy, dz);
     float len = norm3(g);
     return len > 1e-8f ? divs(g, len) : mk(0.0f, 0.0f, 1.0f);
@@ -495,6 +541,43 @@ static int qcmp(const void *a_, const void *b_) {
     return a->ord < b->ord ? -1 : (a->ord > b->ord ? 1 : 0);
 }
 
+/* The QEF of one cell's crossings [b0, b1) (src/dc.cu:26-62): ata and atb
+ * (zeroed by the caller) in the current arithmetic reading. */
+static void qef_cell(const float *points, const float *normals, uint32_t b0, uint32_t b1, float reg,
+                     float *ata, float *atb) {
+    f3 pavg = mk(0, 0, 0);
+    for (uint32_t i = b0; i < b1; i++) {
+        f3 nn = mk(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]);
+        f3 p = mk(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+        float d = dot3(nn, p);
+        pavg = add3(pavg, p);
+        /* acc += a * b; the CUDA build fuses each into fma(a, b, acc) */
+        ata[0] = acc_mul(ata[0], nn.x, nn.x); ata[1] = acc_mul(ata[1], nn.x, nn.y);
+        ata[2] = acc_mul(ata[2], nn.x, nn.z); ata[3] = acc_mul(ata[3], nn.y, nn.x);
+        ata[4] = acc_mul(ata[4], nn.y, nn.y); ata[5] = acc_mul(ata[5], nn.y, nn.z);
+        ata[6] = acc_mul(ata[6], nn.z, nn.x); ata[7] = acc_mul(ata[7], nn.z, nn.y);
+        ata[8] = acc_mul(ata[8], nn.z, nn.z);
+        atb[0] = acc_mul(atb[0], nn.x, d); /* += (n * dot(n, p)).x */
+        atb[1] = acc_mul(atb[1], nn.y, d);
+        atb[2] = acc_mul(atb[2], nn.z, d);
+    }
+    pavg = divs(pavg, (float)(b1 - b0));
+    ata[0] += reg; ata[4] += reg; ata[8] += reg;
+    atb[0] = acc_mul(atb[0], reg, pavg.x);
+    atb[1] = acc_mul(atb[1], reg, pavg.y);
+    atb[2] = acc_mul(atb[2], reg, pavg.z);
+}
+
+/* The QEFs of A cells with CSR offsets: ata [A, 9], atb [A, 3]. */
+void ora_qef(const float *points, const float *normals, const uint32_t *offsets, int64_t A, float reg,
+             float *ata, float *atb) {
+    for (int64_t a = 0; a < A; a++) {
+        memset(ata + 9 * a, 0, 9 * sizeof(float));
+        memset(atb + 3 * a, 0, 3 * sizeof(float));
+        qef_cell(points, normals, offsets[a], offsets[a + 1], reg, ata + 9 * a, atb + 3 * a);
+    }
+}
+
 /* Dual contouring (src/dc.cu:162-218) over a dense grid (sparse == 0) or a
  * sparse grid (sparse == 1: cell_ids/values describe the sparse cells and the
  * intersection's edges and cells are sparse-local).  dual_out (optional)
@@ -534,22 +617,7 @@ int ora_dc(const float *vals, const int32_t *cell_ids, int64_t nsparse, int spar
     if (!dual || !d64) { free(qe); free(dual); free(d64); return -1; }
     for (int64_t a = 0; a < A; a++) {
         float ata[9] = {0}, atb[3] = {0};
-        f3 pavg = mk(0, 0, 0);
-        uint32_t b0 = its->offsets[a], b1 = its->offsets[a + 1];
-        for (uint32_t i = b0; i < b1; i++) {
-            f3 nn = mk(its->normals[3 * i], its->normals[3 * i + 1], its->normals[3 * i + 2]);
-            f3 p = mk(its->points[3 * i], its->points[3 * i + 1], its->points[3 * i + 2]);
-            float d = dot3(nn, p);
-            f3 nnp = mk(nn.x * d, nn.y * d, nn.z * d); /* n * dot(n, p) */
-            pavg = add3(pavg, p);
-            ata[0] += nn.x * nn.x; ata[1] += nn.x * nn.y; ata[2] += nn.x * nn.z;
-            ata[3] += nn.y * nn.x; ata[4] += nn.y * nn.y; ata[5] += nn.y * nn.z;
-            ata[6] += nn.z * nn.x; ata[7] += nn.z * nn.y; ata[8] += nn.z * nn.z;
-            atb[0] += nnp.x; atb[1] += nnp.y; atb[2] += nnp.z;
-        }
-        pavg = divs(pavg, (float)(b1 - b0));
-        ata[0] += reg; ata[4] += reg; ata[8] += reg;
-        atb[0] += reg * pavg.x; atb[1] += reg * pavg.y; atb[2] += reg * pavg.z;
+        qef_cell(its->points, its->normals, its->offsets[a], its->offsets[a + 1], reg, ata, atb);
         double x[3];
         lsq_sym(ata, atb, svd_tol, x);
         d64[3 * a] = x[0]; d64[3 * a + 1] = x[1]; d64[3 * a + 2] = x[2];

@@ -5,6 +5,7 @@ oracle/_ref/libisoext_ref.so) on small seeded inputs and stores inputs and
 outputs.  Run here, where the isoext checkout exists:
 
     python tests/golden/make_golden.py
+    python tests/golden/make_golden.py luts <isoext checkout>   # luts_ref.npz
 
 The GPU machine has no isoext sources; tests there read these files.
 """
@@ -55,7 +56,32 @@ def sparse_case(shape=(16, 16, 16), r=0.55):
     return ids[order], vals[keep][order].astype(np.float32)
 
 
+def _c_table(path: str, name: str) -> list[int]:
+    """The integers of a C array initialiser ``name = { ... }`` in a source file."""
+    import re
+
+    s = open(path).read()
+    i = s.index(name)
+    body = re.sub(r"//.*", "", s[s.index("{", i) + 1: s.index("}", i)])
+    return [int(x, 0) for x in re.findall(r"-?0b[01]+|-?\d+", body)]
+
+
+def write_luts(checkout: str) -> None:
+    """Store the reference's MC tables (read from its sources) as luts_ref.npz."""
+    j = os.path.join
+    rec = {
+        "nagae_tri": _c_table(j(checkout, "include/mc/nagae.cuh"), "tri_table[]"),
+        "lorensen_tri": _c_table(j(checkout, "include/mc/lorensen.cuh"), "tri_table[]"),
+        "edge_status": _c_table(j(checkout, "src/shared_luts.cu"), "edge_status_table[edge_table_size]"),
+    }
+    np.savez_compressed(j(HERE, "luts_ref.npz"), **{k: np.asarray(v, np.int32) for k, v in rec.items()})
+    print("luts_ref", {k: len(v) for k, v in rec.items()})
+
+
 def main() -> None:
+    if len(sys.argv) == 3 and sys.argv[1] == "luts":
+        write_luts(sys.argv[2])
+        return
     ref = Reference()
     for name, c in dense_cases().items():
         rec = {"values": c["values"], "level": np.float32(c["level"])}

@@ -6,6 +6,10 @@ oracle solves in FP64, this path in FP32 refined with an FP64 residual, and
 positions must agree within 1e-4 * h (h = smallest cell size).  Faces must
 match quad by quad; a quad may use the other diagonal only where its two
 diagonals are equally long within that tolerance.
+
+Tests with the ``oracle`` fixture run in both readings of isoext's FP32
+arithmetic (its CUDA build's, the default, and its host build's); the golden
+fixtures come from the host build and are compared in that reading.
 """
 
 import os
@@ -70,7 +74,7 @@ def check_dc(oracle, values, level=0.0, lo=(-1, -1, -1), hi=(1, 1, 1), what=""):
 
 
 @pytest.mark.parametrize("name", ["sphere20", "torus24", "aniso"])
-def test_intersection_matches_reference_fixture(name):
+def test_intersection_matches_reference_fixture(name, host_arith):
     gd = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     g = make_grid(gd["values"])
     its = iso.get_intersection(g, level=float(gd["level"]), compute_normals=True)
@@ -97,14 +101,14 @@ def test_intersection_matches_oracle(oracle, shape, r):
 
 
 @pytest.mark.parametrize("name", ["sphere20", "torus24", "aniso"])
-def test_dc_matches_reference_fixture(name):
+def test_dc_matches_reference_fixture(name, host_arith):
     gd = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     g = make_grid(gd["values"])
     v, f = iso.dual_contouring(g, level=float(gd["level"]))
     assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), gd["dc_v"], gd["dc_f"], cell_h(gd["values"].shape), name)
 
 
-def test_dc_cuboid_fixture():
+def test_dc_cuboid_fixture(host_arith):
     gd = np.load(os.path.join(GOLDEN, "cuboid24.npz"))
     g = make_grid(gd["values"])
     v, f = iso.dual_contouring(g)

@@ -72,7 +72,7 @@ def test_sparse_surface_cells_give_the_dense_mesh_at_1024():
     vs, fs = iso.marching_cubes(sg)
     from isoext_gb300.grids import grid_positions
 
-    ax = grid_positions(torch.arange(n, device="cuda"), n, -1.0, 2.0)  # the lattice's FP32 coordinates
+    ax = grid_positions(torch.arange(n, device="cuda"), n, -1.0, 1.0)  # the lattice's FP32 coordinates
     x, y, z = ax.view(-1, 1, 1), ax.view(1, -1, 1), ax.view(1, 1, -1)
     dg = iso.UniformGrid([n] * 3)
     dg.set_values((torch.sqrt((x * x + y * y) + z * z) - 0.7).contiguous())  # sdf's arithmetic, broadcast

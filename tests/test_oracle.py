@@ -13,47 +13,48 @@ from helpers import assert_same_mesh, grid_points, sphere
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 DENSE = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if not os.path.basename(p).startswith(("sparse", "cuboid", "sdf_")))
+               if not os.path.basename(p).startswith(("sparse", "cuboid", "sdf_", "luts")))
 
 
 @pytest.mark.parametrize("path", DENSE, ids=lambda p: os.path.basename(p)[:-4])
 @pytest.mark.parametrize("method", ["nagae", "lorensen"])
-def test_oracle_mc_matches_reference_fixture(oracle, path, method):
+def test_oracle_mc_matches_reference_fixture(host_oracle, path, method):
     g = np.load(path)
-    v, f, _ = oracle.mc_dense(g["values"], level=float(g["level"]), method=method)
+    v, f, _ = host_oracle.mc_dense(g["values"], level=float(g["level"]), method=method)
     # The oracle also welds like the reference, so even the vertex order matches.
     assert np.array_equal(v, g[f"mc_{method}_v"])
     assert np.array_equal(f, g[f"mc_{method}_f"])
 
 
 @pytest.mark.parametrize("name", ["sphere20", "torus24", "aniso"])
-def test_oracle_intersection_and_dc_match_reference_fixture(oracle, name):
+def test_oracle_intersection_and_dc_match_reference_fixture(host_oracle, name):
     g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
-    its = oracle.intersection_dense(g["values"], level=float(g["level"]), normals=True)
+    its = host_oracle.intersection_dense(g["values"], level=float(g["level"]), normals=True)
     for k in ["points", "normals", "edges", "is_out", "cell_indices", "cell_offsets"]:
         assert np.array_equal(its[k], g[f"its_{k}"]), k
-    v, f, _ = oracle.dc_dense(g["values"], level=float(g["level"]))
+    v, f, _ = host_oracle.dc_dense(g["values"], level=float(g["level"]))
     assert np.array_equal(v, g["dc_v"]) and np.array_equal(f, g["dc_f"])
 
 
-def test_oracle_dc_cuboid_fixture(oracle):
+def test_oracle_dc_cuboid_fixture(host_oracle):
     g = np.load(os.path.join(GOLDEN, "cuboid24.npz"))
-    v, f, _ = oracle.dc_dense(g["values"])
+    v, f, _ = host_oracle.dc_dense(g["values"])
     assert np.array_equal(v, g["dc_v"]) and np.array_equal(f, g["dc_f"])
 
 
 @pytest.mark.parametrize("method", ["nagae", "lorensen"])
-def test_oracle_sparse_fixture(oracle, method):
+def test_oracle_sparse_fixture(host_oracle, method):
     g = np.load(os.path.join(GOLDEN, "sparse16.npz"))
     shape = tuple(int(x) for x in g["shape"])
-    v, f, _ = oracle.mc_sparse(g["cell_ids"], g["values"], shape, method=method)
+    v, f, _ = host_oracle.mc_sparse(g["cell_ids"], g["values"], shape, method=method)
     assert np.array_equal(v, g[f"mc_{method}_v"]) and np.array_equal(f, g[f"mc_{method}_f"])
-    its = oracle.intersection_sparse(g["cell_ids"], g["values"], shape)
-    v, f, _ = oracle.dc(its, shape, values=g["values"], cell_ids=g["cell_ids"])
+    its = host_oracle.intersection_sparse(g["cell_ids"], g["values"], shape)
+    v, f, _ = host_oracle.dc(its, shape, values=g["values"], cell_ids=g["cell_ids"])
     assert np.array_equal(v, g["dc_v"]) and np.array_equal(f, g["dc_f"])
 
 
-# --- known answers from the reference's notebooks -------------------------
+# --- known answers from the reference's notebooks (run on its CUDA build), in
+# both readings of its arithmetic -------------------------------------------
 
 def _torch_points(n):
     return torch.from_numpy(grid_points((n, n, n)))
@@ -108,7 +109,7 @@ def test_known_answer_config1_sphere128(oracle):
     assert (len(v), len(f)) == (48576, 97148)
 
 
-def test_oracle_matches_reference_build_random(oracle, reference):
+def test_oracle_matches_reference_build_random(host_oracle, reference):
     # random fields with exact zeros, both tables, compared with the reference's
     # own code compiled for the host (skipped where that build is unavailable)
     from helpers import noise
@@ -116,7 +117,7 @@ def test_oracle_matches_reference_build_random(oracle, reference):
     for seed in range(3):
         vals = noise((10, 11, 9), seed=seed, zero_frac=0.25)
         for m in ["nagae", "lorensen"]:
-            v, f, _ = oracle.mc_dense(vals, method=m)
+            v, f, _ = host_oracle.mc_dense(vals, method=m)
             rv, rf = reference.mc_dense(vals, method=m)
             assert np.array_equal(v, rv) and np.array_equal(f, rf)
             assert_same_mesh(v, f, rv, rf)

@@ -3,7 +3,8 @@
 MC: bit-exact positions, faces equal after relabelling (isoext welds by
 position; here vertices come in first-occurrence order).  Intersections:
 bit-exact.  DC: positions within 1e-4 * h of the FP64 oracle, quads as in
-test_dc_gpu.
+test_dc_gpu.  Tests with the ``oracle`` fixture run in both readings of
+isoext's FP32 arithmetic; the golden fixtures (host build) in the host one.
 """
 
 import os
@@ -53,7 +54,7 @@ def make_sparse(shape, ids, vals, lo=(-1, -1, -1), hi=(1, 1, 1)):
 # --- fixtures from the reference's host build -----------------------------------
 
 @pytest.mark.parametrize("method", ["nagae", "lorensen"])
-def test_sparse_mc_matches_reference_fixture(method):
+def test_sparse_mc_matches_reference_fixture(method, host_arith):
     gd = np.load(os.path.join(GOLDEN, "sparse16.npz"))
     shape = tuple(int(x) for x in gd["shape"])
     g = make_sparse(shape, gd["cell_ids"], gd["values"])
@@ -61,7 +62,7 @@ def test_sparse_mc_matches_reference_fixture(method):
     assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), gd[f"mc_{method}_v"], gd[f"mc_{method}_f"], method)
 
 
-def test_sparse_dc_matches_reference_fixture():
+def test_sparse_dc_matches_reference_fixture(host_arith):
     gd = np.load(os.path.join(GOLDEN, "sparse16.npz"))
     shape = tuple(int(x) for x in gd["shape"])
     g = make_sparse(shape, gd["cell_ids"], gd["values"])

@@ -110,9 +110,33 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     need = lib.iso_mc_dense_workspace_size(64, 64, 64, cap_v, cap_f)
     assert need > limit
     o = Out(cap_v, cap_f)
+    o.small.fill_(-1)  # a sentinel that any queued kernel or clear would overwrite
+    torch.cuda.synchronize()
     rc = _noalloc(lib, vals, o)
     assert rc == _ffi.ISO_ERR_WORKSPACE
     msg = _ffi.last_error()
     assert "scratch" in msg and str(limit) in msg and str(need) in msg, msg
     torch.cuda.synchronize()
-    assert int(o.small[0]) == 0 and int(o.small[1]) == 0  # nothing was queued
+    assert (o.small == -1).all(), "a rejected call queued work"  # nothing was queued
+
+
+def test_noalloc_accepts_sizes_just_under_its_scratch():
+    """Capacities whose workspace is the largest that fits the header's limit run
+    and equal the workspace entry point (the library's own limit is the header's)."""
+    lib = _lib()
+    limit = _header_limit()
+    vals = torch.from_numpy(sphere((64, 64, 64), 0.5)).cuda()
+    lo, hi = 1, 1 << 22  # largest vertex capacity (faces twice as many) that fits
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        if lib.iso_mc_dense_workspace_size(64, 64, 64, mid, 2 * mid) <= limit:
+            lo = mid
+        else:
+            hi = mid - 1
+    cap_v, cap_f = lo, 2 * lo
+    assert lib.iso_mc_dense_workspace_size(64, 64, 64, cap_v, cap_f) <= limit
+    assert lib.iso_mc_dense_workspace_size(64, 64, 64, cap_v + 1, cap_f + 2) > limit
+    o = Out(cap_v, cap_f)
+    assert _noalloc(lib, vals, o) == 0, _ffi.last_error()
+    torch.cuda.synchronize()
+    _same(o.mesh(), _with_workspace(vals, cap_v, cap_f), "capacities at the scratch limit")
