@@ -135,25 +135,10 @@ class ClockSampler:
 
 
 def csg_sdf(seed: int):
-    """Seeded CSG: (box with half-extents U[0.3,0.6]) minus (sphere r U[0.2,0.4]),
-    unioned with (torus R U[0.3,0.5], r U[0.05,0.15]); centres U[-0.3,0.3]^3."""
-    import torch
+    """Seeded CSG of the DC workload (tests/helpers.py csg_shape)."""
+    from helpers import csg_shape
 
-    from isoext_gb300 import sdf
-
-    g = torch.Generator().manual_seed(seed)
-
-    def u(lo, hi, k=1):
-        return (lo + (hi - lo) * torch.rand(k, generator=g)).tolist()
-
-    half = u(0.3, 0.6, 3)
-    rs = u(0.2, 0.4)[0]
-    big, small = u(0.3, 0.5)[0], u(0.05, 0.15)[0]
-    c_box, c_sph, c_tor = u(-0.3, 0.3, 3), u(-0.3, 0.3, 3), u(-0.3, 0.3, 3)
-    box = sdf.TranslationOp(sdf.CuboidSDF([2 * h for h in half]), c_box)
-    hole = sdf.NegationOp(sdf.TranslationOp(sdf.SphereSDF(rs), c_sph))
-    ring = sdf.TranslationOp(sdf.TorusSDF(big, small), c_tor)
-    return sdf.UnionOp([sdf.IntersectionOp([box, hole]), ring])
+    return csg_shape(seed)
 
 
 def sphere_values(n: int, r: float) -> np.ndarray:
@@ -506,14 +491,10 @@ def cpu_baseline_grad(wl) -> dict:
 
 
 def smoothmin_spheres(wl):
-    """Smooth-min (k) union of seeded spheres: centres U[-0.7, 0.7]^3, radii U[0.05, 0.25]."""
-    from isoext_gb300 import sdf as S
+    """Smooth-min union of the sparse workload's seeded spheres (tests/helpers.py)."""
+    from helpers import smoothmin_spheres as field
 
-    rng = np.random.default_rng(wl["seed"])
-    c = rng.uniform(-0.7, 0.7, size=(wl["spheres"], 3))
-    r = rng.uniform(0.05, 0.25, size=wl["spheres"])
-    return S.SmoothUnionOp([S.TranslationOp(S.SphereSDF(float(ri)), [float(x) for x in ci]) for ci, ri in zip(c, r)],
-                           wl["k"])
+    return field(wl["seed"], wl["spheres"], wl["k"])
 
 
 def run_sparse(args, wl, rank, world) -> dict | None:

@@ -77,3 +77,38 @@ def fourier_sphere(points: np.ndarray, seed: int, k: int = 32) -> np.ndarray:
     for i in range(k):
         out += a[i] * np.sin(p @ w[i] + phi[i])
     return out.astype(np.float32)
+
+
+def csg_shape(seed: int):
+    """The dual-contouring benchmark's seeded CSG (an isoext_gb300.sdf callable on
+    torch points): (box with half-extents U[0.3,0.6]) minus (sphere, r U[0.2,0.4]),
+    unioned with (torus R U[0.3,0.5], r U[0.05,0.15]); centres U[-0.3,0.3]^3."""
+    import torch
+
+    from isoext_gb300 import sdf
+
+    g = torch.Generator().manual_seed(seed)
+
+    def u(lo, hi, k=1):
+        return (lo + (hi - lo) * torch.rand(k, generator=g)).tolist()
+
+    half = u(0.3, 0.6, 3)
+    rs = u(0.2, 0.4)[0]
+    big, small = u(0.3, 0.5)[0], u(0.05, 0.15)[0]
+    c_box, c_sph, c_tor = u(-0.3, 0.3, 3), u(-0.3, 0.3, 3), u(-0.3, 0.3, 3)
+    box = sdf.TranslationOp(sdf.CuboidSDF([2 * h for h in half]), c_box)
+    hole = sdf.NegationOp(sdf.TranslationOp(sdf.SphereSDF(rs), c_sph))
+    ring = sdf.TranslationOp(sdf.TorusSDF(big, small), c_tor)
+    return sdf.UnionOp([sdf.IntersectionOp([box, hole]), ring])
+
+
+def smoothmin_spheres(seed: int, spheres: int = 64, k: float = 0.05):
+    """The sparse benchmark's field: smooth-min (k) union of seeded spheres,
+    centres U[-0.7, 0.7]^3, radii U[0.05, 0.25] (an isoext_gb300.sdf callable)."""
+    from isoext_gb300 import sdf as S
+
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-0.7, 0.7, size=(spheres, 3))
+    r = rng.uniform(0.05, 0.25, size=spheres)
+    return S.SmoothUnionOp([S.TranslationOp(S.SphereSDF(float(ri)), [float(x) for x in ci]) for ci, ri in zip(c, r)],
+                           k)
