@@ -1,7 +1,7 @@
 """Benchmark: dense 512^3 FP32 marching cubes (sphere |p| - 0.8) in Gcells/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload mc512|mc128|dc256]
+                    [--workload mc512|mc128|dc512|dc256|serve|grad|sparse1024] [--mc-only]
 
 One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
   value  device-timed throughput with the grid resident in HBM (C ABI call with
@@ -14,6 +14,10 @@ One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
          over the step time.
   cpu_baseline  the oracle's C restatement of the reference's algorithm on all
          host cores (x slabs on threads; rank 0 only).
+  dc512, serve  (default run on one GPU) the metric's other halves in the same
+         line: dual contouring of the same grid (value, roofline, e2e, its own
+         CPU baseline) and a short served mixed stream against the plain path
+         (req/s, p50 / p99).
 --impl reference runs the reference's algorithm on the CPU (the oracle port:
 the isoext sources are not available on the GPU host) and prints the same line.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -324,6 +328,14 @@ def run_ours(args, wl, rank, world) -> dict | None:
     }
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(vals_np, cells)
+    if wl["desc"] == WORKLOADS["mc512"]["desc"] and not args.mc_only and world == 1:
+        # the metric's other halves, measured in the same run: dense DC of the
+        # same grid, and the served stream against the plain path (one GPU; the
+        # replicas run of N > 1 times MC alone)
+        dc = run_dc_one_call(args, WORKLOADS["dc512"], rank, world)
+        out["dc512"] = {k: dc[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "roofline",
+                                           "kernel_ms", "gpu_launches", "clocks", "cpu_baseline") if k in dc}
+        out["serve"] = serve_summary(args, dev)
     return out
 
 
@@ -751,6 +763,43 @@ def run_serve(args, wl, rank) -> dict | None:
     }
 
 
+def serve_summary(args, dev, count: int = 128) -> dict:
+    """A short run of the served mixed stream (config of the serve workload, first
+    `count` requests): the C++ serving loop against the plain one-call-per-grid
+    path, saturated (req/s) and at 0.8 x the plain capacity (p50 / p99)."""
+    from isoext_gb300 import serve
+
+    wl = WORKLOADS["serve"]
+    sizes = tuple(wl["sizes"])
+    reqs = serve.random_requests(count, wl["seed"], sizes, wl["mc_share"])
+    warm = serve.random_requests(16, wl["seed"] + 1, sizes, wl["mc_share"])
+    gaps = np.random.default_rng(wl["seed"] + 2).exponential(1.0, size=len(reqs))
+    nsrv = serve.NativeServer(slots=wl["slots"], budget_bytes=int(wl["budget_gb"] * (1 << 30)),
+                              warm_sizes=sizes, tune=False, device=dev)
+    try:
+        for r in warm:
+            serve.solve_plain(r, dev)
+        for f in [nsrv.submit(r) for r in warm]:
+            f.result()
+        sat = np.cumsum(gaps) * 50e-6
+        plain_sat = _plain_pass(reqs, sat, lambda r: serve.solve_plain(r, dev))
+        native_sat = _serve_pass(nsrv, reqs, sat)
+        load = np.cumsum(gaps) / (0.8 * plain_sat[0])
+        plain_load = _plain_pass(reqs, load, lambda r: serve.solve_plain(r, dev))
+        native_load = _serve_pass(nsrv, reqs, load)
+    finally:
+        nsrv.close()
+    same = sum(a == b for a, b in zip(plain_sat[2], native_sat[2]))
+    return {"workload": f"{wl['desc']} (first {count} requests)", "served_req_s": round(native_sat[0], 1),
+            "plain_req_s": round(plain_sat[0], 1), "speedup": round(native_sat[0] / plain_sat[0], 2),
+            "saturated": {"served_p50_ms": _pct(native_sat[1], 50), "served_p99_ms": _pct(native_sat[1], 99),
+                          "plain_p50_ms": _pct(plain_sat[1], 50), "plain_p99_ms": _pct(plain_sat[1], 99)},
+            "at_load": {"rate_req_s": round(0.8 * plain_sat[0], 1),
+                        "served_p50_ms": _pct(native_load[1], 50), "served_p99_ms": _pct(native_load[1], 99),
+                        "plain_p50_ms": _pct(plain_load[1], 50), "plain_p99_ms": _pct(plain_load[1], 99)},
+            "identical_results": f"{same}/{len(reqs)}", "loop": "C++ (iso_serve_*)"}
+
+
 def run_dc(args, wl, rank, world) -> dict | None:
     """One step: get_intersection -> analytic normals (autograd of the SDF, FP32)
     -> set_normals -> dual_contouring, the flow of isoext's DC notebook."""
@@ -990,17 +1039,29 @@ def run_dc_one_call(args, wl, rank, world) -> dict | None:
     if not args.no_cpu:
         from oracle import Oracle
 
-        ora = Oracle()
-        m = 128  # a bounded sample: the same sphere on 128^3, one thread
-        sv = sphere_values(m, wl["r"])
-        t0 = time.perf_counter()
-        ora.dc_dense(sv)
-        sec = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": round((m - 1) ** 3 / sec / 1e9, 5), "unit": "Gcells/s", "cores": 1,
+        threads = os.cpu_count() or 1
+        sec = cpu_dc_slabs(Oracle(), vals_np, threads)
+        out["cpu_baseline"] = {"value": round(cells / sec / 1e9, 5), "unit": "Gcells/s", "cores": threads,
                                "kind": "port",
-                               "sample": f"the same sphere on {m}^3 ({(m - 1) ** 3} cells): oracle C port (FP64 QEF), "
-                                         f"1 thread, {sec:.2f} s"}
+                               "sample": f"one dual contouring of the same grid ({cells} cells): oracle C port "
+                                         f"(FP64 QEF) over {threads} x-slabs on {threads} threads, {sec:.2f} s"}
     return out
+
+
+def cpu_dc_slabs(ora, vals_np, threads: int) -> float:
+    """Seconds for one dual contouring of the grid by the oracle's C port, split
+    into x slabs (one point plane shared by neighbours, so each slab's cells are
+    the grid's cells once) run on `threads` host threads (ctypes releases the
+    GIL).  Quads whose four cells straddle two slabs are not formed: a timing of
+    the same per-cell work, not a mesh."""
+    import concurrent.futures as cf
+
+    n = vals_np.shape[0]
+    slabs = _slabs(n, threads)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda ab: ora.dc_dense(np.ascontiguousarray(vals_np[ab[0]:ab[1] + 1])), slabs))
+    return time.perf_counter() - t0
 
 
 def cpu_dc(ora, vals_np, shape) -> float:
@@ -1226,6 +1287,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mc512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--mc-only", action="store_true",
+                    help="mc512: leave out the DC 512^3 and served-stream blocks of the default line")
     ap.add_argument("--slots", type=int, default=None, help="serve workload: worker slots (default 8)")
     ap.add_argument("--quick", action="store_true",
                     help="no load phase before the timed region (for profiler runs; clocks are not sampled under load)")
