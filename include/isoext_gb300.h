@@ -335,11 +335,15 @@ int iso_sdf_union_grid(const float *prims, int nx, int ny, int nz, const float *
 
 /* ---- native serving loop -------------------------------------------------
  * No counterpart in isoext.  A server keeps `slots` worker threads on the
- * current device, each with its own stream, device buffers and CUDA graphs of
- * iso_sdf_union_grid + iso_mc_dense / iso_dc_dense per (kind, n, method,
- * level).  Requests are admitted first come, first served when a worker is
- * free and the running requests' worst-case bytes plus the new one's fit
- * budget_bytes; results come back in host memory.  Thread-safe. */
+ * current device, each with its own stream and a cache of entries: device
+ * buffers and a CUDA graph of iso_sdf_union_grid + iso_mc_dense / iso_dc_dense
+ * per (kind, n, method, level).  Requests are taken first come, first served
+ * by free workers.  Every device byte the server holds counts against
+ * budget_bytes: a new entry evicts least-recently-used idle entries to fit, or
+ * waits for running requests.  A new entry is sized from a count pass on its
+ * request (the extraction at capacity 1 reports the exact sizes); a larger
+ * mesh later grows its entry from the sizes it reported.  Results come back in
+ * host memory.  Thread-safe. */
 typedef struct IsoServer IsoServer;
 typedef struct {
     int kind;            /* 0 marching cubes, 1 dual contouring (reg 1e-2, svd_tol 1e-6) */
@@ -358,8 +362,9 @@ typedef struct {
     int *faces;                    /* host [F, 3] */
     double t_submit, t_start, t_done;  /* steady-clock seconds */
 } IsoServeResult;
-/* warm_sizes: grid sizes whose buffers and graphs (both kinds, nagae, level 0)
- * every slot builds up front; other keys are built on first use. */
+/* warm_sizes: grid sizes whose entries (both kinds, nagae, level 0) every
+ * slot builds up front, with capacities of the closed-surface bound
+ * (24 (n - 1)^2 + 4096 faces); other keys are built on first use. */
 int iso_serve_create(int slots, long long budget_bytes, const int *warm_sizes, int num_warm_sizes,
                      IsoServer **server);
 /* Returns the request's ticket (>= 0), or -ISO_ERR_ARG / -ISO_ERR_WORKSPACE
@@ -369,13 +374,17 @@ long long iso_serve_submit(IsoServer *server, const IsoServeRequest *request);
  * ISO_ERR_TIMEOUT when it runs out) and moves its result out. */
 int iso_serve_wait(IsoServer *server, long long ticket, double timeout_s, IsoServeResult *result);
 void iso_serve_free_result(IsoServeResult *result);
-/* stats[0] completed, [1] most requests running at once, [2] most bytes
- * admitted at once, [3] queued now. */
+/* stats[0] completed, [1] most requests running at once, [2] most device
+ * bytes the server held at once (never above budget_bytes), [3] queued now. */
 int iso_serve_stats(IsoServer *server, long long *stats);
+/* The first `count` (<= 10) of: the four above, [4] device bytes held now,
+ * [5] entries evicted, [6] entries cached, [7] count passes run, [8] entries
+ * grown for a larger mesh, [9] the budget. */
+int iso_serve_stats_ex(IsoServer *server, long long *stats, int count);
 /* Finishes the queued requests, then frees everything. */
 int iso_serve_destroy(IsoServer *server);
-/* Capacities of the buffers built after the call, as a fraction (0, 1] of the
- * default bound; meshes that do not fit rerun with exact capacities (tests). */
+/* Capacities of the entries built after the call, as a fraction (0, 1] of the
+ * counted sizes; meshes that do not fit grow their entry and run again (tests). */
 int iso_serve_set_capacity_scale(IsoServer *server, double scale);
 
 #ifdef __cplusplus

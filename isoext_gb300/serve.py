@@ -345,6 +345,7 @@ _ffi.register({
     "iso_serve_wait": ([C.c_void_p, C.c_longlong, C.c_double, C.POINTER(_ServeResult)], C.c_int),
     "iso_serve_free_result": ([C.POINTER(_ServeResult)], None),
     "iso_serve_stats": ([C.c_void_p, C.POINTER(C.c_longlong)], C.c_int),
+    "iso_serve_stats_ex": ([C.c_void_p, C.POINTER(C.c_longlong), C.c_int], C.c_int),
     "iso_serve_destroy": ([C.c_void_p], C.c_int),
     "iso_serve_set_capacity_scale": ([C.c_void_p, C.c_double], C.c_int),
 })
@@ -366,6 +367,10 @@ class NativeServer:
     buffers and CUDA graphs and the admission all run natively, without the
     Python interpreter; Python submits requests and collects meshes.  Same
     requests and results as Server (and solve_plain), bit for bit.
+
+    Device memory stays within budget_bytes, cached buffers included: entries
+    are sized from a count pass on their first request, evicted least recently
+    used when a new one needs room, and grown when a later mesh is larger.
 
     warm_sizes: grid sizes whose buffers and graphs are built up front (the
     launch parameters are tuned first on the largest, as Server.warmup does)."""
@@ -420,9 +425,13 @@ class NativeServer:
         return Result(rid, v, f, r.t_submit, r.t_start, r.t_done, int(r.slot))
 
     def stats(self) -> dict:
-        s = (C.c_longlong * 4)()
-        _ffi.check(_ffi.lib().iso_serve_stats(self._h, s))
-        return {"completed": s[0], "max_running": s[1], "max_admitted_bytes": s[2], "queued": s[3]}
+        """Counters of the loop.  Device bytes: every byte the server holds
+        (slot buffers and cached entries) counts against the budget."""
+        s = (C.c_longlong * 10)()
+        _ffi.check(_ffi.lib().iso_serve_stats_ex(self._h, s, 10))
+        return {"completed": s[0], "max_running": s[1], "max_held_bytes": s[2], "max_admitted_bytes": s[2],
+                "queued": s[3], "held_bytes": s[4], "evictions": s[5], "entries": s[6], "count_passes": s[7],
+                "grown": s[8], "budget": s[9]}
 
     @property
     def max_running(self) -> int:

@@ -108,9 +108,33 @@ def test_native_server_reruns_meshes_larger_than_its_buffers():
     srv = NativeServer(slots=2, budget_bytes=1 << 30, warm_sizes=(), tune=False)
     assert _ffi.lib().iso_serve_set_capacity_scale(srv._h, ctypes.c_double(1e-4)) == 0
     out = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    stats = srv.stats()
     srv.close()
+    assert stats["grown"] > 0  # entries built too small grew from the sizes their run counted
     for r, s in zip(reqs, out):
         assert _same((s.vertices, s.faces), solve_plain(r)), (r.rid, r.kind)
+
+
+def test_native_server_memory_stays_within_budget():
+    """50 requests of distinct (size, level) keys, each needing an entry of its
+    own, under a budget that holds a few: entries are sized by a count pass,
+    the least recently used idle ones are evicted, the bytes held never exceed
+    the budget, and every result equals the plain path's."""
+    from isoext_gb300.serve import NativeServer, random_requests, solve_plain
+
+    reqs = random_requests(50, seed=21, sizes=(24, 32, 40, 48, 56, 64, 72, 80))
+    for i, r in enumerate(reqs):
+        r.level = float(np.float32(-0.05 + 0.002 * i))
+    budget = 48 << 20
+    srv = NativeServer(slots=3, budget_bytes=budget, warm_sizes=(), tune=False)
+    out = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    stats = srv.stats()
+    srv.close()
+    assert stats["completed"] == len(reqs)
+    assert stats["max_held_bytes"] <= budget, stats
+    assert stats["evictions"] > 0 and stats["count_passes"] == len(reqs), stats
+    for r, s in zip(reqs, out):
+        assert _same((s.vertices, s.faces), solve_plain(r)), (r.rid, r.kind, r.n, r.level)
 
 
 def test_native_server_refuses_bad_requests():
