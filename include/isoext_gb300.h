@@ -77,6 +77,8 @@ int iso_mc_get_config(int *threads);
  *   "mc.emit_threads"     128 | 256   threads per CTA of the MC emit kernel
  *   "mc.sign_ctas_per_sm" 1 .. 64     CTAs per SM of the sign pass (MC and DC)
  *   "dc.cell_threads"     64 | 128 | 256  threads per CTA of the per-cell DC kernels
+ *   "mc.count_threads"    128 | 256   threads per CTA of the MC count kernel (its
+ *                                     scan segment is 4 words per thread)
  * Results do not depend on them. */
 int iso_tune_set(const char *key, int value);
 int iso_tune_get(const char *key, int *value);

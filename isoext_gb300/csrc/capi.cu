@@ -31,8 +31,8 @@ namespace iso {
 void set_last_error(const char* msg) { g_err = msg; }
 
 // Tunables: sign-pass CTAs per SM (MC and DC sign bitmaps), threads per block of
-// the per-active-cell DC kernels.
-std::atomic<int> g_tune[TUNE_KEYS] = {{32}, {128}};
+// the per-active-cell DC kernels, threads per block of the MC count kernel.
+std::atomic<int> g_tune[TUNE_KEYS] = {{32}, {128}, {256}};
 int tune_get(int key) { return key >= 0 && key < TUNE_KEYS ? g_tune[key].load(std::memory_order_relaxed) : 0; }
 
 // Arithmetic reading of the reference's expressions (common.cuh): 1 = its CUDA
@@ -97,6 +97,11 @@ int iso_tune_set(const char* key, int value) {
         iso::g_tune[iso::TUNE_DC_CELL_THREADS] = value;
         return ISO_OK;
     }
+    if (!strcmp(key, "mc.count_threads")) {
+        if (value != 128 && value != 256) return fail(ISO_ERR_ARG, "mc.count_threads must be 128 or 256");
+        iso::g_tune[iso::TUNE_MC_COUNT_THREADS] = value;
+        return ISO_OK;
+    }
     return fail(ISO_ERR_ARG, "iso_tune_set: unknown key");
 }
 
@@ -105,6 +110,7 @@ int iso_tune_get(const char* key, int* value) {
     if (!strcmp(key, "mc.emit_threads")) *value = mc_get_block();
     else if (!strcmp(key, "mc.sign_ctas_per_sm")) *value = iso::tune_get(iso::TUNE_MC_SIGN_CTAS);
     else if (!strcmp(key, "dc.cell_threads")) *value = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
+    else if (!strcmp(key, "mc.count_threads")) *value = iso::tune_get(iso::TUNE_MC_COUNT_THREADS);
     else return fail(ISO_ERR_ARG, "iso_tune_get: unknown key");
     return ISO_OK;
 }

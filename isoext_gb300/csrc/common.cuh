@@ -166,7 +166,7 @@ cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, unsigned block,
 // ---------------------------------------------------------------------------
 // Launch parameters the autotuner may change (process-wide; iso_tune_set).
 
-enum TuneKey { TUNE_MC_SIGN_CTAS = 0, TUNE_DC_CELL_THREADS = 1, TUNE_KEYS = 2 };
+enum TuneKey { TUNE_MC_SIGN_CTAS = 0, TUNE_DC_CELL_THREADS = 1, TUNE_MC_COUNT_THREADS = 2, TUNE_KEYS = 3 };
 int tune_get(int key);
 
 // Arithmetic reading for the next launches (iso_set_arith; process-wide):

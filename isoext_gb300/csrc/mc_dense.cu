@@ -87,6 +87,7 @@ struct McGrid {
     // that can share a position with a vertex of another edge (mc_snap_tau).
     float tau;
     bool fma;  // arithmetic reading (iso::arith_fma at the call)
+    int lgseg; // log2 of the point words per segment (the count kernel's CTA size times WPT)
 };
 
 // Workspace carved from one buffer (offsets 256-aligned).
@@ -109,16 +110,15 @@ struct McWs {
     uint32_t* newidx;           // compacted vertex index [capV]
     int32_t* ftmp;              // compacted faces [capF, 3]
     float* vtmp;                // compacted vertices [capV, 3]
-    long long nBlk;             // segments of SEG point words
+    long long nBlk;             // segments at most (SEG_MIN point words each)
     uint32_t HC;
     size_t total;
 };
 
 constexpr uint32_t SMALL_HC = 1u << 15;  // merge-detection hash of emit (entries: vertex + 1, 0 = empty)
 constexpr int NCTR = 16;
-constexpr int CNT_THREADS = 256;             // count kernel CTA size
 constexpr int WPT = 4;                       // point words per count thread
-constexpr uint32_t SEG = CNT_THREADS * WPT;  // words per segment (one scan entry)
+constexpr uint32_t SEG_MIN = 128 * WPT;      // words per segment (one scan entry) with 128-thread count CTAs
 
 inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -135,7 +135,7 @@ McWs carve(int nx, int ny, int nz, long long capV, long long capF, uint8_t* base
     McWs w{};
     const long long NW = (nz + 31) / 32;
     const long long PW = (long long)nx * ny * NW;
-    w.nBlk = (PW + SEG - 1) / SEG;
+    w.nBlk = (PW + SEG_MIN - 1) / SEG_MIN;  // segments at most (the smallest count CTA)
     w.HC = hash_cap(capV);
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -270,12 +270,13 @@ __device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea
 }
 
 // ---------------------------------------------------------------------------
-// 2. count: one CTA per segment of SEG point words: per-word vertex entries,
+// 2. count: one CTA per segment of CNT_THREADS * WPT point words (the CTA size
+// is a launch parameter, "mc.count_threads"): per-word vertex entries,
 // per-cell entries, and the segment's (V, F) sums, which mc_scan turns into
 // offsets.
 
 // Segment holding point word pw.
-__device__ __forceinline__ uint32_t seg_of(uint32_t pw) { return pw / SEG; }
+__device__ __forceinline__ uint32_t seg_of(const McGrid& g, uint32_t pw) { return pw >> g.lgseg; }
 
 // (x, y, w) of point word pw.
 __device__ __forceinline__ void word_xyw(const McGrid& g, uint32_t pw, int& x, int& y, int& w) {
@@ -328,6 +329,7 @@ __device__ __forceinline__ int owner_of(uint32_t incl, uint32_t j) {
     return lo;
 }
 
+template <int CNT_THREADS>
 __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const float amin0, const float amin1,
                                                         const float amin2, const float size0, const float size1,
                                                         const float size2, const uint32_t* __restrict__ S,
@@ -338,6 +340,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                                                         uint32_t* __restrict__ foff, unsigned long long* ctr,
                                                         float* __restrict__ gc, const uint32_t nseg,
                                                         const long long capV, const long long capF) {
+    constexpr uint32_t SEG = CNT_THREADS * WPT;  // words of the segment
     __shared__ uint32_t sm[64];
     __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
     __shared__ uint32_t wcell[CNT_THREADS / 32];
@@ -741,7 +744,7 @@ __device__ void emit_vertices(const McGrid& g, const EmitArgs& a, unsigned bi, u
         const unsigned long long e = vlist[i];
         const uint32_t pw = uint32_t(e);
         const int ax = int((e >> 32) & 3u), b = int((e >> 34) & 31u);
-        const uint32_t vi = uint32_t(blk[2 * seg_of(pw)]) + uint32_t((e >> 39) & 0xfffffu);
+        const uint32_t vi = uint32_t(blk[2 * seg_of(g, pw)]) + uint32_t((e >> 39) & 0xfffffu);
         int x, y, w;
         word_xyw(g, pw, x, y, w);
         const int z = 32 * w + b;
@@ -811,7 +814,7 @@ __device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsi
         const uint32_t cs = uint32_t((e >> 37) & 255u);
         int x, y, w;
         word_xyw(g, pw, x, y, w);
-        const unsigned long long fo = blk[2 * seg_of(pw) + 1] + foff[pw] + ((e >> 45) & 255u);
+        const unsigned long long fo = blk[2 * seg_of(g, pw) + 1] + foff[pw] + ((e >> 45) & 255u);
         Words d;
         load_words(g, S, pw, x, y, w, d);
         const uint32_t zm = zmask(g, w);
@@ -831,7 +834,7 @@ __device__ void emit_faces(const McGrid& g, const EmitArgs& a, unsigned bi, unsi
             else m = ez_of(d.s[adx][ady][0], d.s[adx][ady][1], zm);
             const uint32_t q = pw + uint32_t(adx) * sxw + uint32_t(ady) * uint32_t(g.NW) + uint32_t(ww);
             const uint32_t inf = info[q];
-            uint32_t off = uint32_t(blk[2 * seg_of(q)]) + (inf & 0xfffffu);
+            uint32_t off = uint32_t(blk[2 * seg_of(g, q)]) + (inf & 0xfffffu);
             if (ax >= 1) off += (inf >> 20) & 63u;
             if (ax == 2) off += (inf >> 26) & 63u;
             vid[k][tid] = off + __popc(m & ((1u << bit) - 1u));
@@ -1081,15 +1084,17 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
     {
         iso::ProfScope ps("mc_count", st);
         const long long ncoord = (long long)p.nx + p.ny + p.nz;
-        const long long grid = std::max<long long>(w.nBlk, (ncoord + CNT_THREADS - 1) / CNT_THREADS);
-        iso::launch_pdl(mc_count, unsigned(grid), CNT_THREADS, st, g, p.amin[0], p.amin[1], p.amin[2], p.asize[0],
-                   p.asize[1], p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist, w.foff, w.ctr, w.gc,
-                   uint32_t(w.nBlk), p.capV, p.capF);
+        const int ct = 1 << (g.lgseg - 2);  // the count CTA's threads (WPT = 4 words each)
+        const long long nseg = (g.PW + (1ll << g.lgseg) - 1) >> g.lgseg;
+        const long long grid = std::max<long long>(nseg, (ncoord + ct - 1) / ct);
+        iso::launch_pdl(ct == 128 ? mc_count<128> : mc_count<256>, unsigned(grid), unsigned(ct), st, g, p.amin[0],
+                        p.amin[1], p.amin[2], p.asize[0], p.asize[1], p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist,
+                        w.foff, w.ctr, w.gc, uint32_t(nseg), p.capV, p.capF);
         if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
     }
     {
         iso::ProfScope ps("mc_scan", st);
-        const uint32_t nseg = uint32_t(w.nBlk);
+        const uint32_t nseg = uint32_t((g.PW + (1ll << g.lgseg) - 1) >> g.lgseg);
         const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
         iso::launch_pdl(mc_scan, nchunk, SCAN_THREADS, st, w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV,
                    p.capF);
@@ -1163,6 +1168,7 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.method = p.method;
     g.tau = snap_tau(p);
     g.fma = iso::arith_fma();
+    g.lgseg = iso::tune_get(iso::TUNE_MC_COUNT_THREADS) == 128 ? 9 : 10;
     g.gc = w.gc;
     if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
     {

@@ -144,14 +144,15 @@ class SparseGrid(SparseGridBase):
                 for s in range(0, total, chunk)]
 
     def populate(self, sdf, level: float = 0.0, mode: str = "brick", band: float | None = None,
-                 brick: int = 8, max_points: int = 1 << 23) -> None:
+                 brick: int | None = None, max_points: int = 1 << 23) -> None:
         """Builds the grid's cells and values from an SDF on the device, replacing
         both.  No counterpart in isoext: it stands in for the documented loop
         get_potential_cell_indices -> get_points_by_cell_indices -> sdf ->
         filter_cell_indices -> add_cells -> set_values (src/grid/sparse.cu:71-179),
         which visits every lattice cell.
 
-        The lattice is tiled by bricks of brick^3 cells.  A brick is a candidate
+        The lattice is tiled by bricks of brick^3 cells (brick defaults to the
+        autotuner's choice, tune.populate_brick(), 8 until tuned).  A brick is a candidate
         when |sdf(centre) - level| <= band + its half-diagonal; sdf must therefore
         be 1-Lipschitz (a distance or a lower bound of one).  band defaults to 2 h
         (h the longest cell edge).  The SDF is evaluated once per lattice point of
@@ -165,6 +166,10 @@ class SparseGrid(SparseGridBase):
         sdf: callable on float32 CUDA points [..., 3] returning [...] distances."""
         if mode not in ("brick", "surface"):
             raise ValueError('mode must be "brick" or "surface"')
+        if brick is None:
+            from .tune import populate_brick
+
+            brick = populate_brick()
         if brick < 1:
             raise ValueError("brick must be positive")
         dev = self.device

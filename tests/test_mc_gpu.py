@@ -229,6 +229,26 @@ def test_launch_parameters_do_not_change_results():
         tune.apply(old)
 
 
+def test_autotune_cache_applies_stored_results(tmp_path):
+    from isoext_gb300 import tune
+
+    vals = sphere((64, 64, 64), 0.6)
+    g = iso.UniformGrid(list(vals.shape))
+    g.set_values(torch.from_numpy(vals).cuda())
+    old = tune.current()
+    path = str(tmp_path / "tune.json")
+    try:
+        first = tune.autotune(g, kinds=("mc",), repeats=2, cache=path)
+        assert not first["cached"]
+        tune.apply({k: tune.KNOBS[k][0] for k in tune.KNOBS})  # anything else
+        second = tune.autotune(g, kinds=("mc",), repeats=2, cache=path)
+        assert second["cached"]
+        assert {k: v for k, v in second["best"].items() if k.startswith("mc.")} == \
+            {k: v for k, v in first["best"].items() if k.startswith("mc.")}
+    finally:
+        tune.apply(old)
+
+
 def test_bounded_wait_times_out_with_a_status():
     """A look-back wait on states nobody publishes gives up after its limit and
     reports ISO_ERR_TIMEOUT; the context stays usable."""

@@ -298,6 +298,38 @@ def test_populate_brick_mode_keeps_whole_bricks_around_the_surface():
     assert torch.equal(g.get_values(), f(g.get_points()).contiguous())
 
 
+def test_populate_brick_size_does_not_change_the_mesh():
+    """The brick edge (an autotuner knob) decides only which empty cells near the
+    surface are kept: MC and DC meshes are the same for every brick size."""
+    from isoext_gb300 import tune
+
+    shape = (72, 64, 80)
+    f = _spheres(10, seed=12)
+    meshes = {}
+    for b in tune.BRICKS:
+        g = iso.SparseGrid(shape)
+        g.populate(f, mode="brick", brick=b)
+        meshes[b] = (iso.marching_cubes(g), iso.dual_contouring(g), g.get_num_cells())
+    (mc0, dc0, n0) = meshes[tune.BRICKS[0]]
+    assert len({n for _, _, n in meshes.values()}) > 1  # the kept cells differ
+    for b, (mc, dc, _) in meshes.items():
+        assert torch.equal(mc[0], mc0[0]) and torch.equal(mc[1], mc0[1]), b
+        assert torch.equal(dc[0], dc0[0]) and torch.equal(dc[1], dc0[1]), b
+
+
+def test_autotune_populate_picks_a_brick(tmp_path):
+    from isoext_gb300 import tune
+
+    old = tune.populate_brick()
+    try:
+        rep = tune.autotune_populate((96, 96, 96), _spheres(8, seed=3), repeats=1, cache=str(tmp_path / "t.json"))
+        assert rep["best"]["sparse.brick"] in tune.BRICKS and tune.populate_brick() == rep["best"]["sparse.brick"]
+        again = tune.autotune_populate((96, 96, 96), _spheres(8, seed=3), cache=str(tmp_path / "t.json"))
+        assert again["cached"] and again["best"] == rep["best"]
+    finally:
+        tune.set_populate_brick(old)
+
+
 def test_sparse_mc_retries_when_buffers_are_small():
     vals = sphere((40, 40, 40), 0.6)
     ids, cv = sparse_from_dense(vals, extra=200, seed=1)
