@@ -335,6 +335,19 @@ int iso_dc_backward_src(const float *values, int nx, int ny, int nz, const float
 int iso_sdf_union_grid(const float *prims, int nx, int ny, int nz, const float *aabb_min,
                        const float *aabb_max, float *out, void *stream);
 
+/* ---- isoext's vertex order --------------------------------------------------
+ * The extraction entry points number vertices by grid edge (MC) or by cell
+ * (DC); isoext sorts its welded vertices by position (src/utils.cu:32-59:
+ * thrust::sort with float3_less_pred, then unique), and the faces' order is
+ * the same either way.  This pass renumbers a mesh in isoext's order, in
+ * place: vertices (device float [V, 3], distinct positions) sorted
+ * lexicographically by (x, y, z), -0 and +0 equal; faces (device int32
+ * [F, 3]) renumbered to match.  Two stable radix sorts (CUB).
+ * workspace: iso_sort_vertices_workspace_size(V) bytes. */
+size_t iso_sort_vertices_workspace_size(long long num_vertices);
+int iso_sort_vertices(float *vertices, long long num_vertices, int *faces, long long num_faces, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
 /* ---- native serving loop -------------------------------------------------
  * No counterpart in isoext.  A server keeps `slots` worker threads on the
  * current device, each with its own stream and a cache of entries: device

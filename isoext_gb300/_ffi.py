@@ -47,6 +47,9 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_set_arith.argtypes = [_i]
     lib.iso_get_arith.restype = _i
     lib.iso_axis_coords.argtypes = [_vp, _i, _f, _f, _vp]
+    lib.iso_sort_vertices_workspace_size.argtypes = [_ll]
+    lib.iso_sort_vertices_workspace_size.restype = C.c_size_t
+    lib.iso_sort_vertices.argtypes = [_vp, _ll, _vp, _ll, _vp, C.c_size_t, _vp]
     _apply(lib, _EXTRA)
 
 
@@ -117,6 +120,44 @@ def set_arithmetic(mode: str) -> None:
 def get_arithmetic() -> str:
     m = lib().iso_get_arith()
     return next(k for k, v in ARITH.items() if v == m)
+
+
+ORDERS = ("edge", "position")
+_vertex_order = "edge"
+
+
+def set_vertex_order(order: str) -> None:
+    """How extraction results number their vertices (process-wide).
+
+    ``"edge"`` (default): by grid edge (marching cubes) or by cell (dual
+    contouring), as the kernels produce them; the mesh is isoext's after
+    relabelling.  ``"position"``: sorted by position, lexicographically in
+    (x, y, z), which is isoext's own numbering, so the returned tensors equal
+    isoext's.  Faces are in isoext's order either way.  No counterpart in
+    isoext (one order only)."""
+    global _vertex_order
+    if order not in ORDERS:
+        raise ValueError(f"vertex order must be one of {ORDERS}, not {order!r}")
+    _vertex_order = order
+
+
+def get_vertex_order() -> str:
+    return _vertex_order
+
+
+def in_vertex_order(v, f):
+    """(v, f) renumbered in the current vertex order (in place when sorting)."""
+    if _vertex_order == "edge" or v is None or f is None or v.shape[0] < 2:
+        return v, f
+    import torch
+
+    v = v.contiguous()
+    f = f.contiguous()
+    ws = torch.empty(lib().iso_sort_vertices_workspace_size(v.shape[0]), dtype=torch.uint8, device=v.device)
+    with torch.cuda.device(v.device):
+        check(lib().iso_sort_vertices(v.data_ptr(), v.shape[0], f.data_ptr(), f.shape[0], ws.data_ptr(), ws.numel(),
+                                      C.c_void_p(torch.cuda.current_stream(v.device).cuda_stream)))
+    return v, f
 
 
 def fvec3(xs) -> C.Array:

@@ -48,8 +48,10 @@ __device__ __forceinline__ void cell_normal(const CellCorners& cc, const float* 
 }
 
 // Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
-// Loan, sec. 8.5), FP32.  a is destroyed; w = eigenvalues, q = eigenvectors
-// (columns).
+// Loan, sec. 8.5), FP32.  Each rotation annihilates its pair exactly (a_pr = 0,
+// a_pp -= t a_pr, a_rr += t a_pr, the third row and column rotated), so the
+// off-diagonal mass falls quadratically to zero instead of stalling at FP32
+// rounding.  a is destroyed; w = eigenvalues, q = eigenvectors (columns).
 __device__ __forceinline__ void jacobi3f(float a[3][3], float w[3], float q[3][3]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -61,29 +63,24 @@ __device__ __forceinline__ void jacobi3f(float a[3][3], float w[3], float q[3][3
         if (off <= 1e-9f * diag || off == 0.0f) break;
 #pragma unroll
         for (int pr = 0; pr < 3; ++pr) {
-            const int p = pr == 2 ? 1 : 0, r = pr == 0 ? 1 : 2;
+            const int p = pr == 2 ? 1 : 0, r = pr == 0 ? 1 : 2, k = 3 - p - r;
             const float apr = a[p][r];
             if (apr == 0.0f) continue;
             const float theta = (a[r][r] - a[p][p]) / (2.0f * apr);
             const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
             const float c = rsqrtf(t * t + 1.0f), s = t * c;
+            const float tapr = t * apr;
+            a[p][p] -= tapr;
+            a[r][r] += tapr;
+            a[p][r] = a[r][p] = 0.0f;
+            const float akp = a[k][p], akr = a[k][r];
+            a[k][p] = a[p][k] = c * akp - s * akr;
+            a[k][r] = a[r][k] = s * akp + c * akr;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float akp = a[k][p], akr = a[k][r];
-                a[k][p] = c * akp - s * akr;
-                a[k][r] = s * akp + c * akr;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float apk = a[p][k], ark = a[r][k];
-                a[p][k] = c * apk - s * ark;
-                a[r][k] = s * apk + c * ark;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float qkp = q[k][p], qkr = q[k][r];
-                q[k][p] = c * qkp - s * qkr;
-                q[k][r] = s * qkp + c * qkr;
+            for (int m = 0; m < 3; ++m) {
+                const float qmp = q[m][p], qmr = q[m][r];
+                q[m][p] = c * qmp - s * qmr;
+                q[m][r] = s * qmp + c * qmr;
             }
         }
     }

@@ -257,6 +257,234 @@ __global__ void __launch_bounds__(SP_BLOCK) sp_mc_emit(SpGrid g, const int* __re
     }
 }
 
+// --- one-call sparse MC: crossed cells compacted per CTA ------------------------
+//
+// A CTA takes SP2_CHUNK consecutive cells.  It reads every cell's 8 values once
+// for its case, compacts the crossed ones (a few percent of a band) into a list
+// in shared memory, and does the per-crossed-cell work with full warps.  The
+// emit writes each crossed cell's vertices once (the crossed edges its kept
+// triangles use, in edge order) and the triangles as indices into that list, so
+// the position weld hashes each distinct vertex about four times instead of
+// six.
+
+constexpr int SP2_THREADS = 256;
+constexpr int SP2_ROUNDS = 16;                       // cells per thread
+constexpr int SP2_CHUNK = SP2_THREADS * SP2_ROUNDS;  // cells per CTA
+
+// Kept faces of crossed cell c (case cs) and the crossed edges they use
+// (used).  Far from corners every triangle of the case is kept and every
+// crossed edge used; otherwise the positions decide, as mc_cell does (ev then
+// holds them).
+__device__ __forceinline__ uint32_t sp_cell_summary(const SpGrid& g, const int* ids, long long c, Cell8& cc,
+                                                    uint32_t cs, float (*ev)[3], uint32_t& used, bool& fast) {
+    const uint32_t est = ISO_EDGE_STATUS[cs];
+    uint32_t nf = mc_cell_fast(g, cc, cs);
+    fast = nf != ~0u;
+    if (fast) {
+        used = est;
+        return nf;
+    }
+    int x, y, z;
+    cell_xyz(g, uint32_t(ids[c]), x, y, z);
+    set_coords(g, x, y, z, cc);
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+        if ((est >> e) & 1u) edge_point(cc, e, g.level, ev[e]);
+    int ml;
+    const signed char* tr = tri_row(g.method, cs, ml);
+    used = 0;
+    nf = 0;
+    for (int k = 0; k < ml && tr[k] >= 0; k += 3) {
+        const float* a = ev[tr[k]];
+        const float* b = ev[tr[k + 1]];
+        const float* d = ev[tr[k + 2]];
+        if (eq3(a, b) || eq3(a, d) || eq3(b, d)) continue;
+        used |= (1u << tr[k]) | (1u << tr[k + 1]) | (1u << tr[k + 2]);
+        ++nf;
+    }
+    return nf;
+}
+
+__device__ __forceinline__ uint32_t sp_case(const SpGrid& g, const float* vals, long long c, Cell8& cc) {
+    load_vals(vals, c, cc);
+    uint32_t cs = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cs |= (iso::below(cc.v[k], g.level) ? 1u : 0u) << k;
+    return cs;
+}
+
+// Block sum of two counts (thread 0 gets them).
+__device__ __forceinline__ void sp_sum2(uint32_t& a, uint32_t& b, uint32_t (*sm)[SP2_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+        a += __shfl_xor_sync(~0u, a, d);
+        b += __shfl_xor_sync(~0u, b, d);
+    }
+    if (lane == 0) { sm[0][warp] = a; sm[1][warp] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = 0;
+        b = 0;
+        for (int k = 0; k < SP2_THREADS / 32; ++k) { a += sm[0][k]; b += sm[1][k]; }
+    }
+}
+
+// Per CTA: faces and vertex-list entries of its chunk -> blk[2 b], blk[2 b + 1].
+__global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
+                                                            const float* __restrict__ vals, long long n,
+                                                            unsigned long long* blk) {
+    __shared__ uint16_t list[SP2_CHUNK];
+    __shared__ uint32_t nlist;
+    __shared__ uint32_t sm[2][SP2_THREADS / 32];
+    const int lane = threadIdx.x & 31;
+    const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
+    if (threadIdx.x == 0) nlist = 0;
+    __syncthreads();
+#pragma unroll 4
+    for (int r = 0; r < SP2_ROUNDS; ++r) {
+        const int li = r * SP2_THREADS + threadIdx.x;
+        bool crossed = false;
+        if (c0 + li < n) {
+            Cell8 cc;
+            const uint32_t cs = sp_case(g, vals, c0 + li, cc);
+            crossed = cs != 0 && cs != 255;
+        }
+        const uint32_t bal = __ballot_sync(~0u, crossed);
+        uint32_t base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&nlist, uint32_t(__popc(bal)));
+        base = __shfl_sync(~0u, base, 0);
+        if (crossed) list[base + __popc(bal & ((1u << lane) - 1u))] = uint16_t(li);
+    }
+    __syncthreads();
+    uint32_t nf = 0, nv = 0;
+    for (uint32_t j = threadIdx.x; j < nlist; j += SP2_THREADS) {
+        const long long c = c0 + list[j];
+        Cell8 cc;
+        const uint32_t cs = sp_case(g, vals, c, cc);
+        float ev[12][3];
+        uint32_t used;
+        bool fast;
+        nf += sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
+        nv += __popc(used);
+    }
+    sp_sum2(nf, nv, sm);
+    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = nf; blk[2 * blockIdx.x + 1] = nv; }
+}
+
+// Per CTA: its crossed cells in cell order; each writes its used vertices at the
+// CTA's vertex-list offset plus the cells before it, and its kept triangles as
+// indices into the list at the CTA's face offset plus the cells before it.
+// dn (device): nothing is written when dn[0] == 0 (over capacity).
+__global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* __restrict__ ids,
+                                                           const float* __restrict__ vals, long long n,
+                                                           const unsigned long long* __restrict__ blk,
+                                                           float* __restrict__ vlist, int32_t* __restrict__ tri,
+                                                           const long long* __restrict__ dn) {
+    __shared__ uint16_t list[SP2_CHUNK];
+    __shared__ uint8_t cf[SP2_CHUNK], cv[SP2_CHUNK];  // per listed cell: kept faces, used vertices
+    __shared__ uint32_t wcnt[2][SP2_THREADS / 32];
+    if (dn[0] == 0) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
+    // 1. crossed cells, compacted in cell order
+    uint32_t nl = 0;
+    for (int r = 0; r < SP2_ROUNDS; ++r) {
+        const int li = r * SP2_THREADS + threadIdx.x;
+        bool crossed = false;
+        if (c0 + li < n) {
+            Cell8 cc;
+            const uint32_t cs = sp_case(g, vals, c0 + li, cc);
+            crossed = cs != 0 && cs != 255;
+        }
+        const uint32_t bal = __ballot_sync(~0u, crossed);
+        if (lane == 0) wcnt[0][warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = 0, all = 0;
+#pragma unroll
+        for (int k = 0; k < SP2_THREADS / 32; ++k) {
+            before += k < warp ? wcnt[0][k] : 0u;
+            all += wcnt[0][k];
+        }
+        if (crossed) list[nl + before + __popc(bal & ((1u << lane) - 1u))] = uint16_t(li);
+        nl += all;
+        __syncthreads();
+    }
+    // 2. each listed cell's counts, the cells spread over the threads
+    for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
+        const long long c = c0 + list[j];
+        Cell8 cc;
+        const uint32_t cs = sp_case(g, vals, c, cc);
+        float ev[12][3];
+        uint32_t used;
+        bool fast;
+        cf[j] = uint8_t(sp_cell_summary(g, ids, c, cc, cs, ev, used, fast));
+        cv[j] = uint8_t(__popc(used));
+    }
+    __syncthreads();
+    // 3. offsets in cell order: E consecutive listed cells per thread, block scan
+    const uint32_t E = (nl + SP2_THREADS - 1) / SP2_THREADS;
+    const uint32_t j0 = threadIdx.x * E;
+    uint32_t sf = 0, sv = 0;
+    for (uint32_t e = 0; e < E; ++e)
+        if (j0 + e < nl) { sf += cf[j0 + e]; sv += cv[j0 + e]; }
+    uint32_t ff = sf, vv = sv;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t a = __shfl_up_sync(~0u, ff, d), b = __shfl_up_sync(~0u, vv, d);
+        if (lane >= d) { ff += a; vv += b; }
+    }
+    if (lane == 31) { wcnt[0][warp] = ff; wcnt[1][warp] = vv; }
+    __syncthreads();
+    uint32_t bf = 0, bv = 0;
+#pragma unroll
+    for (int k = 0; k < SP2_THREADS / 32; ++k)
+        if (k < warp) { bf += wcnt[0][k]; bv += wcnt[1][k]; }
+    unsigned long long fo = blk[2 * blockIdx.x] + bf + ff - sf;
+    unsigned long long vo = blk[2 * blockIdx.x + 1] + bv + vv - sv;
+    // 4. vertices and triangles
+    for (uint32_t e = 0; e < E; ++e) {
+        const uint32_t j = j0 + e;
+        if (j >= nl) break;
+        const long long c = c0 + list[j];
+        Cell8 cc;
+        const uint32_t cs = sp_case(g, vals, c, cc);
+        float ev[12][3];
+        uint32_t used;
+        bool fast;
+        sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
+        if (fast) {  // positions of the used edges (the slow path has them all)
+            int x, y, z;
+            cell_xyz(g, uint32_t(ids[c]), x, y, z);
+            set_coords(g, x, y, z, cc);
+#pragma unroll
+            for (int q = 0; q < 12; ++q)
+                if ((used >> q) & 1u) edge_point(cc, q, g.level, ev[q]);
+        }
+        // the cell's vertices in edge order
+        uint32_t k = 0;
+#pragma unroll
+        for (int q = 0; q < 12; ++q)
+            if ((used >> q) & 1u) {
+                float* o = vlist + 3 * (vo + k);
+                o[0] = ev[q][0]; o[1] = ev[q][1]; o[2] = ev[q][2];
+                ++k;
+            }
+        int ml;
+        const signed char* tr = tri_row(g.method, cs, ml);
+        for (int t = 0; t < ml && tr[t] >= 0; t += 3) {
+            const int a = tr[t], b = tr[t + 1], d = tr[t + 2];
+            if (!fast && (eq3(ev[a], ev[b]) || eq3(ev[a], ev[d]) || eq3(ev[b], ev[d]))) continue;
+            int32_t* o = tri + 3 * fo;
+            o[0] = int32_t(vo + __popc(used & ((1u << a) - 1u)));
+            o[1] = int32_t(vo + __popc(used & ((1u << b) - 1u)));
+            o[2] = int32_t(vo + __popc(used & ((1u << d) - 1u)));
+            ++fo;
+        }
+        vo += k;
+    }
+}
+
 // --- intersections -----------------------------------------------------------
 
 // Normal at crossing point p (src/its.cu:186-268).
@@ -563,6 +791,21 @@ __global__ void sp_mc_sizes(const long long* __restrict__ tf, long long capF, lo
     counts[2] = F;
 }
 
+// The list's and the faces' sizes against the capacities: eff = (vertex-list
+// entries, 0, 3 F, vertex capacity) for the weld, all 0 when they do not fit.
+__global__ void sp_mc_sizes2(const long long* __restrict__ tot, long long capF, long long capV, long long* eff,
+                             long long* counts, int* status) {
+    const long long F = tot[0], L = tot[1];
+    const bool ok = F <= capF && L <= 3 * capF && 3 * F < 0x7fffffffll;
+    if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
+    eff[0] = ok ? L : 0;
+    eff[1] = 0;
+    eff[2] = ok ? 3 * F : 0;
+    eff[3] = capV;
+    counts[1] = ok ? F : 0;
+    counts[2] = F;
+}
+
 __global__ void sp_mc_finish(const long long* __restrict__ vtot, long long capV, long long* counts, int* status) {
     const long long V = vtot[0];
     counts[0] = V;
@@ -571,8 +814,9 @@ __global__ void sp_mc_finish(const long long* __restrict__ vtot, long long capV,
 
 struct SpMcWs {
     void* blk;
-    long long* tot;  // [0..1] F, 0  [4..7] eff  [8..9] V, 0
-    float* soup;
+    long long* tot;  // [0..1] F, vertex-list entries  [4..7] eff  [8..9] V, 0
+    float* soup;     // the vertex list (at most 3 F entries)
+    int32_t* tri;    // the triangles' indices into it [3 F]
     void* weld;
     size_t total;
 };
@@ -586,9 +830,10 @@ SpMcWs sp_mc_carve(void* ws, long long n, long long capV, long long capF) {
         o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
         return p;
     };
-    w.blk = take(size_t((n + SP_BLOCK - 1) / SP_BLOCK + 1) * 16);
+    w.blk = take(size_t((n + SP2_CHUNK - 1) / SP2_CHUNK + 1) * 16);
     w.tot = reinterpret_cast<long long*>(take(16 * 8));
     w.soup = reinterpret_cast<float*>(take(size_t(3 * capF) * 12));
+    w.tri = reinterpret_cast<int32_t*>(take(size_t(3 * capF) * 4));
     w.weld = take(weld_dev_workspace(3 * capF, capV));
     w.total = o + 256;
     return w;
@@ -743,15 +988,16 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     long long* eff = w.tot + 4;
     {
         iso::ProfScope ps("sparse_mc", st, 4);
-        sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk);
-        iso_block_scan_launch((unsigned long long*)w.blk, nb(n, SP_BLOCK), w.tot, st);
-        sp_mc_sizes<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
-        sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.soup,
-                                                         eff);
+        const unsigned chunks = nb(n, SP2_CHUNK);
+        sp_mc_count2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk);
+        iso_block_scan_launch((unsigned long long*)w.blk, chunks, w.tot, st);
+        sp_mc_sizes2<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
+        sp_mc_emit2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.soup, w.tri,
+                                                    eff);
     }
-    // the weld's table holds vertex_capacity distinct positions; more report an
-    // overflow with a vertex count that fits on the rerun
-    weld_dev_launch(w.soup, 3 * face_capacity, std::max<long long>(vertex_capacity, 1), nullptr, 3 * face_capacity,
+    // the weld of the vertex list: its table holds vertex_capacity distinct
+    // positions; more report an overflow with a vertex count that fits on the rerun
+    weld_dev_launch(w.soup, 3 * face_capacity, std::max<long long>(vertex_capacity, 1), w.tri, 3 * face_capacity,
                     eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr);
     {
         iso::ProfScope ps("sparse_mc", st);

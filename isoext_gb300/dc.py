@@ -260,9 +260,10 @@ def dual_contouring(grid, level: float = 0.0, intersection: Intersection | None 
 
     Returns (vertices float32 [V, 3], faces int32 [F, 3]) or (None, None).
     Faces follow isoext's order (quads by crossed edge, two triangles each);
-    vertices are ordered by active cell (isoext sorts them by position)."""
+    vertices are ordered by active cell, or sorted by position as isoext's after
+    set_vertex_order("position")."""
     if isinstance(grid, UniformGrid):
-        return _dc_uniform(grid, level, intersection, reg, svd_tol)
+        return _ffi.in_vertex_order(*_dc_uniform(grid, level, intersection, reg, svd_tol))
     if isinstance(grid, SparseGridBase):
-        return grid._dual_contouring(level, intersection, reg, svd_tol)
+        return _ffi.in_vertex_order(*grid._dual_contouring(level, intersection, reg, svd_tol))
     raise TypeError("grid must be a UniformGrid or SparseGrid")

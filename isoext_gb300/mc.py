@@ -146,11 +146,12 @@ def marching_cubes(grid, level: float = 0.0, method: str = "nagae"):
     Returns (vertices float32 [V, 3], faces int32 [F, 3]) CUDA tensors, or
     (None, None) when the surface is empty -- as isoext.marching_cubes.
     Faces follow isoext's order (ascending cell id, table slot order); vertices
-    are in ascending edge-key order (isoext sorts them by position).
+    are in ascending edge-key order, or sorted by position as isoext's after
+    set_vertex_order("position").
     """
     mid = method_id(method)
     if isinstance(grid, UniformGrid):
-        return _mc_uniform(grid, level, mid)
+        return _ffi.in_vertex_order(*_mc_uniform(grid, level, mid))
     if isinstance(grid, SparseGridBase):
-        return grid._marching_cubes(level, mid)
+        return _ffi.in_vertex_order(*grid._marching_cubes(level, mid))
     raise TypeError("grid must be a UniformGrid or SparseGrid")
