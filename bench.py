@@ -578,7 +578,7 @@ def run_sparse(args, wl, rank, world) -> dict | None:
     torch.cuda.synchronize()
     lib.iso_profile_enable(0)
     kt = {k: _ffi.profile_read(k) for k in ("sparse_mc", "dc_weld")}
-    kavg = {k: t / max(c, 1) for k, (c, t) in kt.items() if c}
+    kavg = {k: t / args.steps for k, (c, t) in kt.items() if c}  # per extraction (a name may time several groups)
     launches = sum(_ffi.profile_kernels(k) for k in kt)  # kernels, not timed groups
     # e2e: ids and values from pinned host memory, the mesh back
     ids_h = grid.get_cell_indices().cpu().pin_memory()

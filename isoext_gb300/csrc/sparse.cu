@@ -330,55 +330,110 @@ __device__ __forceinline__ void sp_sum2(uint32_t& a, uint32_t& b, uint32_t (*sm)
     }
 }
 
-// Per CTA: faces and vertex-list entries of its chunk -> blk[2 b], blk[2 b + 1].
-__global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
-                                                            const float* __restrict__ vals, long long n,
-                                                            unsigned long long* blk) {
-    __shared__ uint16_t list[SP2_CHUNK];
-    __shared__ uint32_t nlist;
-    __shared__ uint32_t sm[2][SP2_THREADS / 32];
-    const int lane = threadIdx.x & 31;
-    const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
-    if (threadIdx.x == 0) nlist = 0;
-    __syncthreads();
-#pragma unroll 4
-    for (int r = 0; r < SP2_ROUNDS; ++r) {
-        const int li = r * SP2_THREADS + threadIdx.x;
-        bool crossed = false;
-        if (c0 + li < n) {
-            Cell8 cc;
-            const uint32_t cs = sp_case(g, vals, c0 + li, cc);
-            crossed = cs != 0 && cs != 255;
+// Ordered compaction of a chunk's crossed cells into list[] (cell order);
+// returns their number.  The values are loaded four rounds at a time; each
+// warp keeps its 16 ballots, and one barrier gives every list position.
+__device__ __forceinline__ uint32_t sp_crossed(const SpGrid& g, const float* vals, long long n, long long c0,
+                                               uint16_t* list, uint32_t (*wcnt)[SP2_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t bal[SP2_ROUNDS];
+#pragma unroll
+    for (int r0 = 0; r0 < SP2_ROUNDS; r0 += 4) {
+        float4 va[4], vb[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long long c = c0 + (r0 + k) * SP2_THREADS + threadIdx.x;
+            if (c < n) {
+                const float4* v4 = reinterpret_cast<const float4*>(vals + 8 * c);
+                va[k] = __ldg(v4);
+                vb[k] = __ldg(v4 + 1);
+            } else {
+                va[k] = vb[k] = make_float4(g.level, g.level, g.level, g.level);
+            }
         }
-        const uint32_t bal = __ballot_sync(~0u, crossed);
-        uint32_t base = 0;
-        if (lane == 0 && bal) base = atomicAdd(&nlist, uint32_t(__popc(bal)));
-        base = __shfl_sync(~0u, base, 0);
-        if (crossed) list[base + __popc(bal & ((1u << lane) - 1u))] = uint16_t(li);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v[8] = {va[k].x, va[k].y, va[k].z, va[k].w, vb[k].x, vb[k].y, vb[k].z, vb[k].w};
+            uint32_t cs = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) cs |= (iso::below(v[q], g.level) ? 1u : 0u) << q;
+            bal[r0 + k] = __ballot_sync(~0u, cs != 0 && cs != 255);
+        }
+    }
+    if (lane < SP2_ROUNDS) {  // wcnt holds [round][warp] counts (SP2_ROUNDS x warps)
+        uint32_t mine = 0;
+#pragma unroll
+        for (int r = 0; r < SP2_ROUNDS; ++r)
+            if (r == lane) mine = __popc(bal[r]);
+        wcnt[lane][warp] = mine;
     }
     __syncthreads();
+    uint32_t base = 0;
+#pragma unroll
+    for (int r = 0; r < SP2_ROUNDS; ++r) {
+        uint32_t before = 0, all = 0;
+#pragma unroll
+        for (int k = 0; k < SP2_THREADS / 32; ++k) {
+            const uint32_t c = wcnt[r][k];
+            before += k < warp ? c : 0u;
+            all += c;
+        }
+        if ((bal[r] >> lane) & 1u)
+            list[base + before + __popc(bal[r] & ((1u << lane) - 1u))] = uint16_t(r * SP2_THREADS + threadIdx.x);
+        base += all;
+    }
+    __syncthreads();  // wcnt is reused by the caller
+    return base;
+}
+
+// Per CTA: its crossed cells in cell order and, for each, sp_pack of its
+// summary, into the chunk's slots of clist / ccnt (SP2_CHUNK each; the count
+// in clen); the chunk's totals -> blk[2 b], blk[2 b + 1].  The emit then reads
+// only the crossed cells.
+__global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
+                                                            const float* __restrict__ vals, long long n,
+                                                            unsigned long long* blk, uint16_t* __restrict__ clist,
+                                                            uint16_t* __restrict__ ccnt, uint32_t* __restrict__ clen) {
+    __shared__ uint16_t list[SP2_CHUNK];
+    __shared__ uint32_t wcnt[SP2_ROUNDS][SP2_THREADS / 32];
+    const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
+    const uint32_t nl = sp_crossed(g, vals, n, c0, list, wcnt);
+    uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
+    uint16_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
     uint32_t nf = 0, nv = 0;
-    for (uint32_t j = threadIdx.x; j < nlist; j += SP2_THREADS) {
+    for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
         const long long c = c0 + list[j];
         Cell8 cc;
         const uint32_t cs = sp_case(g, vals, c, cc);
         float ev[12][3];
         uint32_t used;
         bool fast;
-        nf += sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
-        nv += __popc(used);
+        const uint32_t f = sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
+        const uint32_t v = __popc(used);
+        gl[j] = list[j];
+        gc[j] = uint16_t(f | (v << 8));
+        nf += f;
+        nv += v;
     }
-    sp_sum2(nf, nv, sm);
-    if (threadIdx.x == 0) { blk[2 * blockIdx.x] = nf; blk[2 * blockIdx.x + 1] = nv; }
+    sp_sum2(nf, nv, wcnt);
+    if (threadIdx.x == 0) {
+        blk[2 * blockIdx.x] = nf;
+        blk[2 * blockIdx.x + 1] = nv;
+        clen[blockIdx.x] = nl;
+    }
 }
 
-// Per CTA: its crossed cells in cell order; each writes its used vertices at the
-// CTA's vertex-list offset plus the cells before it, and its kept triangles as
-// indices into the list at the CTA's face offset plus the cells before it.
-// dn (device): nothing is written when dn[0] == 0 (over capacity).
+// Per CTA: its crossed cells in cell order (from the count pass); each writes
+// its used vertices at the CTA's vertex-list offset plus the cells before it,
+// and its kept triangles as indices into the list at the CTA's face offset
+// plus the cells before it.  dn (device): nothing is written when dn[0] == 0
+// (over capacity).
 __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* __restrict__ ids,
                                                            const float* __restrict__ vals, long long n,
                                                            const unsigned long long* __restrict__ blk,
+                                                           const uint16_t* __restrict__ clist,
+                                                           const uint16_t* __restrict__ ccnt,
+                                                           const uint32_t* __restrict__ clen,
                                                            float* __restrict__ vlist, int32_t* __restrict__ tri,
                                                            const long long* __restrict__ dn) {
     __shared__ uint16_t list[SP2_CHUNK];
@@ -387,42 +442,15 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
     if (dn[0] == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
-    // 1. crossed cells, compacted in cell order
-    uint32_t nl = 0;
-    for (int r = 0; r < SP2_ROUNDS; ++r) {
-        const int li = r * SP2_THREADS + threadIdx.x;
-        bool crossed = false;
-        if (c0 + li < n) {
-            Cell8 cc;
-            const uint32_t cs = sp_case(g, vals, c0 + li, cc);
-            crossed = cs != 0 && cs != 255;
-        }
-        const uint32_t bal = __ballot_sync(~0u, crossed);
-        if (lane == 0) wcnt[0][warp] = __popc(bal);
-        __syncthreads();
-        uint32_t before = 0, all = 0;
-#pragma unroll
-        for (int k = 0; k < SP2_THREADS / 32; ++k) {
-            before += k < warp ? wcnt[0][k] : 0u;
-            all += wcnt[0][k];
-        }
-        if (crossed) list[nl + before + __popc(bal & ((1u << lane) - 1u))] = uint16_t(li);
-        nl += all;
-        __syncthreads();
-    }
-    // 2. each listed cell's counts, the cells spread over the threads
+    const uint32_t nl = clen[blockIdx.x];
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
-        const long long c = c0 + list[j];
-        Cell8 cc;
-        const uint32_t cs = sp_case(g, vals, c, cc);
-        float ev[12][3];
-        uint32_t used;
-        bool fast;
-        cf[j] = uint8_t(sp_cell_summary(g, ids, c, cc, cs, ev, used, fast));
-        cv[j] = uint8_t(__popc(used));
+        list[j] = clist[(size_t)blockIdx.x * SP2_CHUNK + j];
+        const uint32_t k = ccnt[(size_t)blockIdx.x * SP2_CHUNK + j];
+        cf[j] = uint8_t(k & 0xffu);
+        cv[j] = uint8_t(k >> 8);
     }
     __syncthreads();
-    // 3. offsets in cell order: E consecutive listed cells per thread, block scan
+    // offsets in cell order: E consecutive listed cells per thread, block scan
     const uint32_t E = (nl + SP2_THREADS - 1) / SP2_THREADS;
     const uint32_t j0 = threadIdx.x * E;
     uint32_t sf = 0, sv = 0;
@@ -442,7 +470,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
         if (k < warp) { bf += wcnt[0][k]; bv += wcnt[1][k]; }
     unsigned long long fo = blk[2 * blockIdx.x] + bf + ff - sf;
     unsigned long long vo = blk[2 * blockIdx.x + 1] + bv + vv - sv;
-    // 4. vertices and triangles
+    // vertices and triangles
     for (uint32_t e = 0; e < E; ++e) {
         const uint32_t j = j0 + e;
         if (j >= nl) break;
@@ -817,6 +845,8 @@ struct SpMcWs {
     long long* tot;  // [0..1] F, vertex-list entries  [4..7] eff  [8..9] V, 0
     float* soup;     // the vertex list (at most 3 F entries)
     int32_t* tri;    // the triangles' indices into it [3 F]
+    uint16_t *clist, *ccnt;  // per chunk: crossed cells and their counts (SP2_CHUNK slots each)
+    uint32_t* clen;          // per chunk: crossed cells
     void* weld;
     size_t total;
 };
@@ -834,6 +864,10 @@ SpMcWs sp_mc_carve(void* ws, long long n, long long capV, long long capF) {
     w.tot = reinterpret_cast<long long*>(take(16 * 8));
     w.soup = reinterpret_cast<float*>(take(size_t(3 * capF) * 12));
     w.tri = reinterpret_cast<int32_t*>(take(size_t(3 * capF) * 4));
+    const size_t chunks = size_t((n + SP2_CHUNK - 1) / SP2_CHUNK);
+    w.clist = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
+    w.ccnt = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
+    w.clen = reinterpret_cast<uint32_t*>(take(chunks * 4));
     w.weld = take(weld_dev_workspace(3 * capF, capV));
     w.total = o + 256;
     return w;
@@ -989,11 +1023,12 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     {
         iso::ProfScope ps("sparse_mc", st, 4);
         const unsigned chunks = nb(n, SP2_CHUNK);
-        sp_mc_count2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk);
+        sp_mc_count2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk, w.clist, w.ccnt,
+                                                     w.clen);
         iso_block_scan_launch((unsigned long long*)w.blk, chunks, w.tot, st);
         sp_mc_sizes2<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
-        sp_mc_emit2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.soup, w.tri,
-                                                    eff);
+        sp_mc_emit2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.clist,
+                                                    w.ccnt, w.clen, w.soup, w.tri, eff);
     }
     // the weld of the vertex list: its table holds vertex_capacity distinct
     // positions; more report an overflow with a vertex count that fits on the rerun
