@@ -386,6 +386,13 @@ __device__ __forceinline__ uint32_t sp_crossed(const SpGrid& g, const float* val
     return base;
 }
 
+// Per crossed cell, what the emit needs in 16 bits: kept faces (bits 0-2),
+// whether every triangle of the case is kept (3: no vertex near a corner),
+// the crossed edges the kept triangles use (4-15).
+__device__ __forceinline__ uint16_t sp_pack(uint32_t f, uint32_t used, bool fast) {
+    return uint16_t(f | (fast ? 8u : 0u) | (used << 4));
+}
+
 // Per CTA: its crossed cells in cell order and, for each, sp_pack of its
 // summary, into the chunk's slots of clist / ccnt (SP2_CHUNK each; the count
 // in clen); the chunk's totals -> blk[2 b], blk[2 b + 1].  The emit then reads
@@ -409,11 +416,10 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
         uint32_t used;
         bool fast;
         const uint32_t f = sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
-        const uint32_t v = __popc(used);
         gl[j] = list[j];
-        gc[j] = uint16_t(f | (v << 8));
+        gc[j] = sp_pack(f, used, fast);
         nf += f;
-        nv += v;
+        nv += __popc(used);
     }
     sp_sum2(nf, nv, wcnt);
     if (threadIdx.x == 0) {
@@ -423,11 +429,58 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
     }
 }
 
-// Per CTA: its crossed cells in cell order (from the count pass); each writes
-// its used vertices at the CTA's vertex-list offset plus the cells before it,
-// and its kept triangles as indices into the list at the CTA's face offset
-// plus the cells before it.  dn (device): nothing is written when dn[0] == 0
-// (over capacity).
+// Output staging of one emit CTA: vertex-list entries and triangles up to
+// these counts go through shared memory and leave in coalesced stores; a CTA
+// with more (a dense patch of surface) writes the rest directly.
+constexpr int SP2_STAGE_V = 2048;
+constexpr int SP2_STAGE_F = 1024;
+
+struct SpStage {
+    float* v;                  // [SP2_STAGE_V * 3]
+    int32_t* f;                // [SP2_STAGE_F * 3]
+    float* gv;                 // the CTA's part of the vertex list
+    int32_t* gf;               // the CTA's part of the triangles
+    unsigned long long vbase;  // the CTA's first vertex-list entry
+};
+
+__device__ __forceinline__ void stage_vertex(const SpStage& s, uint32_t k, float x, float y, float z) {
+    float* o = k < uint32_t(SP2_STAGE_V) ? s.v + 3 * k : s.gv + 3 * (size_t)k;
+    o[0] = x; o[1] = y; o[2] = z;
+}
+
+__device__ __forceinline__ void stage_face(const SpStage& s, uint32_t k, uint32_t a, uint32_t b, uint32_t c) {
+    int32_t* o = k < uint32_t(SP2_STAGE_F) ? s.f + 3 * k : s.gf + 3 * (size_t)k;
+    o[0] = int32_t(s.vbase + a); o[1] = int32_t(s.vbase + b); o[2] = int32_t(s.vbase + c);
+}
+
+// A cell with a vertex near a corner: its triangles are kept by position
+// (as mc_cell does), so every crossed edge's position is needed.  Its
+// position array is indexed by the triangle table and lives in local memory;
+// the common path (no vertex near a corner) never touches it.
+__device__ __forceinline__ void sp_emit_near(const SpGrid& g, const Cell8& cc, uint32_t cs, uint32_t used,
+                                          unsigned long long pk, const SpStage& s, uint32_t lv, uint32_t lf) {
+    float ev[12][3];
+    const uint32_t est = ISO_EDGE_STATUS[cs];
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+        if ((est >> e) & 1u) edge_point(cc, e, g.level, ev[e]);
+#pragma unroll
+    for (int q = 0; q < 12; ++q)
+        if ((used >> q) & 1u) stage_vertex(s, lv + __popc(used & ((1u << q) - 1u)), ev[q][0], ev[q][1], ev[q][2]);
+    const int ntc = int(pk >> 60);
+    for (int t = 0; t < ntc; ++t, pk >>= 12) {
+        const int a = int(pk & 15u), b = int((pk >> 4) & 15u), d = int((pk >> 8) & 15u);
+        if (eq3(ev[a], ev[b]) || eq3(ev[a], ev[d]) || eq3(ev[b], ev[d])) continue;
+        stage_face(s, lf++, lv + __popc(used & ((1u << a) - 1u)), lv + __popc(used & ((1u << b) - 1u)),
+                   lv + __popc(used & ((1u << d) - 1u)));
+    }
+}
+
+// Per CTA: its crossed cells in cell order (from the count pass), 256 per
+// round; a block scan of each round's (faces, vertices) gives every cell its
+// offsets in list order.  A cell writes its used vertices in edge order and
+// its kept triangles as indices into the vertex list.  dn (device): nothing
+// is written when dn[0] == 0 (over capacity).
 __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* __restrict__ ids,
                                                            const float* __restrict__ vals, long long n,
                                                            const unsigned long long* __restrict__ blk,
@@ -436,81 +489,83 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                                                            const uint32_t* __restrict__ clen,
                                                            float* __restrict__ vlist, int32_t* __restrict__ tri,
                                                            const long long* __restrict__ dn) {
-    __shared__ uint16_t list[SP2_CHUNK];
-    __shared__ uint8_t cf[SP2_CHUNK], cv[SP2_CHUNK];  // per listed cell: kept faces, used vertices
-    __shared__ uint32_t wcnt[2][SP2_THREADS / 32];
+    __shared__ unsigned long long tpk[256];  // packed triangle lists of the cases
+    __shared__ float sv[SP2_STAGE_V * 3];
+    __shared__ int32_t sf[SP2_STAGE_F * 3];
+    __shared__ uint32_t wsum[2][SP2_THREADS / 32];
     if (dn[0] == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 256; i += SP2_THREADS) tpk[i] = ISO_TRI_PACKED[g.method * 256 + i];
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
     const uint32_t nl = clen[blockIdx.x];
-    for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
-        list[j] = clist[(size_t)blockIdx.x * SP2_CHUNK + j];
-        const uint32_t k = ccnt[(size_t)blockIdx.x * SP2_CHUNK + j];
-        cf[j] = uint8_t(k & 0xffu);
-        cv[j] = uint8_t(k >> 8);
-    }
-    __syncthreads();
-    // offsets in cell order: E consecutive listed cells per thread, block scan
-    const uint32_t E = (nl + SP2_THREADS - 1) / SP2_THREADS;
-    const uint32_t j0 = threadIdx.x * E;
-    uint32_t sf = 0, sv = 0;
-    for (uint32_t e = 0; e < E; ++e)
-        if (j0 + e < nl) { sf += cf[j0 + e]; sv += cv[j0 + e]; }
-    uint32_t ff = sf, vv = sv;
+    const uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
+    const uint16_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
+    SpStage s;
+    s.v = sv;
+    s.f = sf;
+    s.vbase = blk[2 * blockIdx.x + 1];
+    s.gv = vlist + 3 * s.vbase;
+    s.gf = tri + 3 * blk[2 * blockIdx.x];
+    uint32_t accf = 0, accv = 0;  // faces and vertices of the rounds before
+    for (uint32_t r0 = 0; r0 < nl; r0 += SP2_THREADS) {
+        const uint32_t j = r0 + threadIdx.x;
+        const bool ok = j < nl;
+        const uint32_t pc = ok ? gc[j] : 0u;
+        const uint32_t cl = ok ? gl[j] : 0u;
+        const uint32_t used = pc >> 4;
+        const uint32_t mine = (pc & 7u) | (uint32_t(__popc(used)) << 16);  // faces | vertices << 16
+        uint32_t inc = mine;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t a = __shfl_up_sync(~0u, ff, d), b = __shfl_up_sync(~0u, vv, d);
-        if (lane >= d) { ff += a; vv += b; }
-    }
-    if (lane == 31) { wcnt[0][warp] = ff; wcnt[1][warp] = vv; }
-    __syncthreads();
-    uint32_t bf = 0, bv = 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(~0u, inc, d);
+            if (lane >= d) inc += o;
+        }
+        const int buf = (r0 / SP2_THREADS) & 1;  // two buffers: one barrier per round
+        if (lane == 31) wsum[buf][warp] = inc;
+        __syncthreads();  // also orders tpk's fill before its first use
+        uint32_t before = 0, all = 0;
 #pragma unroll
-    for (int k = 0; k < SP2_THREADS / 32; ++k)
-        if (k < warp) { bf += wcnt[0][k]; bv += wcnt[1][k]; }
-    unsigned long long fo = blk[2 * blockIdx.x] + bf + ff - sf;
-    unsigned long long vo = blk[2 * blockIdx.x + 1] + bv + vv - sv;
-    // vertices and triangles
-    for (uint32_t e = 0; e < E; ++e) {
-        const uint32_t j = j0 + e;
-        if (j >= nl) break;
-        const long long c = c0 + list[j];
-        Cell8 cc;
-        const uint32_t cs = sp_case(g, vals, c, cc);
-        float ev[12][3];
-        uint32_t used;
-        bool fast;
-        sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
-        if (fast) {  // positions of the used edges (the slow path has them all)
+        for (int k = 0; k < SP2_THREADS / 32; ++k) {
+            const uint32_t w = wsum[buf][k];
+            before += k < warp ? w : 0u;
+            all += w;
+        }
+        const uint32_t ex = before + inc - mine;
+        if (ok) {
+            const long long c = c0 + cl;
+            Cell8 cc;
+            const uint32_t cs = sp_case(g, vals, c, cc);
             int x, y, z;
             cell_xyz(g, uint32_t(ids[c]), x, y, z);
             set_coords(g, x, y, z, cc);
+            const uint32_t lv = accv + (ex >> 16), lf = accf + (ex & 0xffffu);
+            const unsigned long long pk = tpk[cs];
+            if (pc & 8u) {  // every triangle kept, every crossed edge used
 #pragma unroll
-            for (int q = 0; q < 12; ++q)
-                if ((used >> q) & 1u) edge_point(cc, q, g.level, ev[q]);
-        }
-        // the cell's vertices in edge order
-        uint32_t k = 0;
-#pragma unroll
-        for (int q = 0; q < 12; ++q)
-            if ((used >> q) & 1u) {
-                float* o = vlist + 3 * (vo + k);
-                o[0] = ev[q][0]; o[1] = ev[q][1]; o[2] = ev[q][2];
-                ++k;
+                for (int q = 0; q < 12; ++q)
+                    if ((used >> q) & 1u) {
+                        float p[3];
+                        edge_point(cc, q, g.level, p);
+                        stage_vertex(s, lv + __popc(used & ((1u << q) - 1u)), p[0], p[1], p[2]);
+                    }
+                unsigned long long t = pk;
+                const int ntc = int(pk >> 60);
+                for (int k = 0; k < ntc; ++k, t >>= 12) {
+                    const uint32_t a = uint32_t(t & 15u), b = uint32_t((t >> 4) & 15u), d = uint32_t((t >> 8) & 15u);
+                    stage_face(s, lf + k, lv + __popc(used & ((1u << a) - 1u)),
+                               lv + __popc(used & ((1u << b) - 1u)), lv + __popc(used & ((1u << d) - 1u)));
+                }
+            } else {
+                sp_emit_near(g, cc, cs, used, pk, s, lv, lf);
             }
-        int ml;
-        const signed char* tr = tri_row(g.method, cs, ml);
-        for (int t = 0; t < ml && tr[t] >= 0; t += 3) {
-            const int a = tr[t], b = tr[t + 1], d = tr[t + 2];
-            if (!fast && (eq3(ev[a], ev[b]) || eq3(ev[a], ev[d]) || eq3(ev[b], ev[d]))) continue;
-            int32_t* o = tri + 3 * fo;
-            o[0] = int32_t(vo + __popc(used & ((1u << a) - 1u)));
-            o[1] = int32_t(vo + __popc(used & ((1u << b) - 1u)));
-            o[2] = int32_t(vo + __popc(used & ((1u << d) - 1u)));
-            ++fo;
         }
-        vo += k;
+        accf += all & 0xffffu;
+        accv += all >> 16;
     }
+    __syncthreads();
+    const uint32_t nv = 3 * min(accv, uint32_t(SP2_STAGE_V)), nf = 3 * min(accf, uint32_t(SP2_STAGE_F));
+    for (uint32_t i = threadIdx.x; i < nv; i += SP2_THREADS) s.gv[i] = sv[i];
+    for (uint32_t i = threadIdx.x; i < nf; i += SP2_THREADS) s.gf[i] = sf[i];
 }
 
 // --- intersections -----------------------------------------------------------
