@@ -141,6 +141,19 @@ __device__ __forceinline__ uint32_t range_mask(int w, int lo, int hi) {
 }
 
 // ---------------------------------------------------------------------------
+// Exact-position welds compare positions as bit patterns with -0 read as +0
+// (float equality, except that NaNs of one pattern match each other).
+
+__device__ __forceinline__ uint32_t pos_bits(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
+__device__ __forceinline__ uint32_t pos_hash(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h;
+}
+
+// ---------------------------------------------------------------------------
 // Programmatic dependent launch: a kernel launched with launch_pdl may start
 // while the previous kernel on its stream finishes; grid_wait() blocks until
 // that kernel has completed and its writes are visible.  Every kernel launched

@@ -572,14 +572,8 @@ __global__ void __launch_bounds__(DC_BLOCK) dc_quad_emit(const uint32_t* __restr
 // ---------------------------------------------------------------------------
 // weld: exact-position dedup of the dual vertices faces use.
 
-__device__ __forceinline__ uint32_t pos_bits(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
-__device__ __forceinline__ uint32_t pos_hash(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
-    h ^= h >> 15;
-    h *= 0x2C1B3C6Du;
-    h ^= h >> 12;
-    return h;
-}
+using iso::pos_bits;
+using iso::pos_hash;
 
 __global__ void dc_mark_used(const int32_t* __restrict__ tri, long long n, uint32_t* used,
                              const long long* __restrict__ dn) {
@@ -1272,61 +1266,6 @@ __global__ void __launch_bounds__(256) dc_cell_quads(const uint8_t* __restrict__
 }
 
 }  // namespace
-
-// ---------------------------------------------------------------------------
-// Exact-position weld with device-side sizes, for the one-call paths: eff[0] =
-// points, eff[2] = triangle indices (tri == nullptr: index i is point i),
-// eff[3] = vertex capacity of vout.  vtot[0] <- V.  Grids are sized by the
-// capacities capA / capT.
-
-struct WeldDev {
-    uint32_t *rep, *newidx, *table;
-    unsigned long long* blk;
-    uint32_t hcap;
-    long long nblk;
-    size_t total;
-};
-
-WeldDev weld_dev_carve(void* ws, long long capA, long long capU) {
-    WeldDev w{};
-    const long long u = capU > 0 && capU < capA ? capU : capA;  // distinct positions the table must hold
-    w.hcap = 1024;
-    while ((long long)w.hcap < 2 * u + 1024) w.hcap <<= 1;
-    w.nblk = (capA + DC_BLOCK - 1) / DC_BLOCK;
-    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
-    size_t o = 0;
-    auto take = [&](size_t bytes) {
-        uint8_t* p = ws ? b + o : nullptr;
-        o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
-        return p;
-    };
-    w.rep = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.newidx = reinterpret_cast<uint32_t*>(take(size_t(capA) * 4));
-    w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
-    w.blk = reinterpret_cast<unsigned long long*>(take(size_t(w.nblk + 1) * 16));
-    w.total = o + 256;
-    return w;
-}
-
-size_t weld_dev_workspace(long long capA, long long capU) { return weld_dev_carve(nullptr, capA, capU).total; }
-
-void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
-                     const long long* eff, void* ws, float* vout, int32_t* fout, long long* vtot, int* status,
-                     cudaStream_t st, uint32_t* vsrc) {
-    const WeldDev w = weld_dev_carve(ws, capA, capU);
-    iso::ProfScope ps("dc_weld", st, (capT > 0 ? 1 : 0) + (capA > 0 ? 5 : 0));
-    cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
-    if (capA > 0) {  // every point is used: a point list or a triangle soup
-        dc_hash_insert<<<blocks_for(capA, 256), 256, 0, st>>>(pts, nullptr, capA, w.table, w.hcap - 1, status, eff);
-        dc_hash_lookup<<<blocks_for(capA, 256), 256, 0, st>>>(pts, nullptr, capA, w.table, w.hcap - 1, w.rep, eff);
-        dc_rep_count<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, eff);
-        dc_block_scan<<<1, 1024, 0, st>>>(w.blk, w.nblk, vtot);
-        dc_rep_write<<<unsigned(w.nblk), DC_BLOCK, 0, st>>>(w.rep, capA, w.blk, pts, w.newidx, vout, vsrc, eff);
-    } else {
-        cudaMemsetAsync(vtot, 0, 16, st);
-    }
-    if (capT > 0) dc_remap<<<blocks_for(capT, 256), 256, 0, st>>>(tri, capT, w.rep, w.newidx, fout, eff);
-}
 
 // mc_signs lives in mc_dense.cu
 #include "mc_dense.cuh"

@@ -386,28 +386,64 @@ __device__ __forceinline__ uint32_t sp_crossed(const SpGrid& g, const float* val
     return base;
 }
 
-// Per crossed cell, what the emit needs in 16 bits: kept faces (bits 0-2),
+// Per crossed cell, what the emit needs in 32 bits: kept faces (bits 0-2),
 // whether every triangle of the case is kept (3: no vertex near a corner),
-// the crossed edges the kept triangles use (4-15).
-__device__ __forceinline__ uint16_t sp_pack(uint32_t f, uint32_t used, bool fast) {
-    return uint16_t(f | (fast ? 8u : 0u) | (used << 4));
+// the crossed edges the kept triangles use (4-15), and those of its bottom
+// face whose vertex is the z-neighbour's entry (16-27; see sp_reuse).
+__device__ __forceinline__ uint32_t sp_pack(uint32_t f, uint32_t used, bool fast) {
+    return f | (fast ? 8u : 0u) | (used << 4);
+}
+__device__ __forceinline__ uint32_t sp_used(uint32_t pc) { return (pc >> 4) & 0xfffu; }
+__device__ __forceinline__ uint32_t sp_own(uint32_t pc) { return sp_used(pc) & ~(pc >> 16); }
+
+// Bottom-face edges (both corners at z) and the top-face edge of the cell
+// below with the same corners (+1 in z, same order): 3 -> 1, 7 -> 5, 8 -> 9,
+// 11 -> 10.
+constexpr uint32_t SP_BOTTOM = (1u << 3) | (1u << 7) | (1u << 8) | (1u << 11);
+__device__ __forceinline__ int sp_up(int e) { return e == 3 ? 1 : e == 7 ? 5 : e == 8 ? 9 : 10; }
+
+// Bottom-face edges of crossed cell c whose vertex equals the one its
+// z-neighbour below (cp, the list's previous crossed cell) makes: both cells
+// keep every triangle, they share a column, and the edge's two corner values
+// are the same bits in both (same t from the same operands, on the same
+// corner positions: the same position).  The global weld would merge these;
+// the emit points the cell's triangles at the neighbour's entry instead.
+__device__ __forceinline__ uint32_t sp_reuse(const SpGrid& g, const int* ids, const float* vals, long long c,
+                                             long long cp, uint32_t used) {
+    const uint32_t id = uint32_t(__ldg(ids + c)), idp = uint32_t(__ldg(ids + cp));
+    if (id != idp + 1u || id % uint32_t(g.nz - 1) == 0u) return 0u;
+    const float4* a4 = reinterpret_cast<const float4*>(vals + 8 * c);
+    const float4* b4 = reinterpret_cast<const float4*>(vals + 8 * cp);
+    const float4 a0 = __ldg(a4), a1 = __ldg(a4 + 1), b0 = __ldg(b4), b1 = __ldg(b4 + 1);
+    // corner k of the cell (z = bit 0) against corner k + 1 of the one below
+    const bool s0 = __float_as_uint(a0.x) == __float_as_uint(b0.y);  // corner 0 / 1
+    const bool s2 = __float_as_uint(a0.z) == __float_as_uint(b0.w);  // 2 / 3
+    const bool s4 = __float_as_uint(a1.x) == __float_as_uint(b1.y);  // 4 / 5
+    const bool s6 = __float_as_uint(a1.z) == __float_as_uint(b1.w);  // 6 / 7
+    uint32_t r = 0;
+    r |= (s0 && s2) ? (1u << 3) : 0u;   // corners 0, 2
+    r |= (s4 && s6) ? (1u << 7) : 0u;   // 4, 6
+    r |= (s0 && s4) ? (1u << 8) : 0u;   // 0, 4
+    r |= (s2 && s6) ? (1u << 11) : 0u;  // 2, 6
+    return r & used;
 }
 
 // Per CTA: its crossed cells in cell order and, for each, sp_pack of its
-// summary, into the chunk's slots of clist / ccnt (SP2_CHUNK each; the count
-// in clen); the chunk's totals -> blk[2 b], blk[2 b + 1].  The emit then reads
-// only the crossed cells.
+// summary with the z-neighbour entries, into the chunk's slots of clist / ccnt
+// (SP2_CHUNK each; the count in clen); the chunk's faces and vertex-list
+// entries -> blk[2 b], blk[2 b + 1].  The emit then reads only the crossed
+// cells.
 __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
                                                             const float* __restrict__ vals, long long n,
                                                             unsigned long long* blk, uint16_t* __restrict__ clist,
-                                                            uint16_t* __restrict__ ccnt, uint32_t* __restrict__ clen) {
+                                                            uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clen) {
     __shared__ uint16_t list[SP2_CHUNK];
+    __shared__ uint16_t summ[SP2_CHUNK];  // sp_pack of each listed cell (16 bits)
     __shared__ uint32_t wcnt[SP2_ROUNDS][SP2_THREADS / 32];
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
     const uint32_t nl = sp_crossed(g, vals, n, c0, list, wcnt);
     uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
-    uint16_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
-    uint32_t nf = 0, nv = 0;
+    uint32_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
         const long long c = c0 + list[j];
         Cell8 cc;
@@ -416,10 +452,19 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
         uint32_t used;
         bool fast;
         const uint32_t f = sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
-        gl[j] = list[j];
-        gc[j] = sp_pack(f, used, fast);
-        nf += f;
-        nv += __popc(used);
+        summ[j] = uint16_t(sp_pack(f, used, fast));
+    }
+    __syncthreads();
+    uint32_t nf = 0, nv = 0;
+    for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
+        uint32_t pc = summ[j];
+        const uint32_t lj = list[j];
+        if (j > 0 && (pc & 8u) && (summ[j - 1] & 8u) && list[j - 1] == lj - 1u && (sp_used(pc) & SP_BOTTOM))
+            pc |= sp_reuse(g, ids, vals, c0 + lj, c0 + lj - 1, sp_used(pc)) << 16;
+        gl[j] = uint16_t(lj);
+        gc[j] = pc;
+        nf += pc & 7u;
+        nv += __popc(sp_own(pc));
     }
     sp_sum2(nf, nv, wcnt);
     if (threadIdx.x == 0) {
@@ -435,6 +480,14 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
 constexpr int SP2_STAGE_V = 2048;
 constexpr int SP2_STAGE_F = 1024;
 
+// ent[e] for a run-time e, by selects (ent stays in registers).
+__device__ __forceinline__ uint32_t sel12(const uint32_t (&ent)[12], uint32_t e) {
+    uint32_t r = ent[0];
+#pragma unroll
+    for (int q = 1; q < 12; ++q) r = e == uint32_t(q) ? ent[q] : r;
+    return r;
+}
+
 struct SpStage {
     float* v;                  // [SP2_STAGE_V * 3]
     int32_t* f;                // [SP2_STAGE_F * 3]
@@ -448,9 +501,16 @@ __device__ __forceinline__ void stage_vertex(const SpStage& s, uint32_t k, float
     o[0] = x; o[1] = y; o[2] = z;
 }
 
+// Staged triangles hold the CTA's own entry numbers (the copy-out adds the
+// base); direct ones hold vertex-list indices.
 __device__ __forceinline__ void stage_face(const SpStage& s, uint32_t k, uint32_t a, uint32_t b, uint32_t c) {
-    int32_t* o = k < uint32_t(SP2_STAGE_F) ? s.f + 3 * k : s.gf + 3 * (size_t)k;
-    o[0] = int32_t(s.vbase + a); o[1] = int32_t(s.vbase + b); o[2] = int32_t(s.vbase + c);
+    if (k < uint32_t(SP2_STAGE_F)) {
+        int32_t* o = s.f + 3 * k;
+        o[0] = int32_t(a); o[1] = int32_t(b); o[2] = int32_t(c);
+    } else {
+        int32_t* o = s.gf + 3 * (size_t)k;
+        o[0] = int32_t(s.vbase + a); o[1] = int32_t(s.vbase + b); o[2] = int32_t(s.vbase + c);
+    }
 }
 
 // A cell with a vertex near a corner: its triangles are kept by position
@@ -485,7 +545,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                                                            const float* __restrict__ vals, long long n,
                                                            const unsigned long long* __restrict__ blk,
                                                            const uint16_t* __restrict__ clist,
-                                                           const uint16_t* __restrict__ ccnt,
+                                                           const uint32_t* __restrict__ ccnt,
                                                            const uint32_t* __restrict__ clen,
                                                            float* __restrict__ vlist, int32_t* __restrict__ tri,
                                                            const long long* __restrict__ dn) {
@@ -499,7 +559,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
     const uint32_t nl = clen[blockIdx.x];
     const uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
-    const uint16_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
+    const uint32_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
     SpStage s;
     s.v = sv;
     s.f = sf;
@@ -512,8 +572,8 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
         const bool ok = j < nl;
         const uint32_t pc = ok ? gc[j] : 0u;
         const uint32_t cl = ok ? gl[j] : 0u;
-        const uint32_t used = pc >> 4;
-        const uint32_t mine = (pc & 7u) | (uint32_t(__popc(used)) << 16);  // faces | vertices << 16
+        const uint32_t used = sp_used(pc), own = sp_own(pc);
+        const uint32_t mine = (pc & 7u) | (uint32_t(__popc(own)) << 16);  // faces | vertices << 16
         uint32_t inc = mine;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -543,18 +603,26 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
             if (pc & 8u) {  // every triangle kept, every crossed edge used
 #pragma unroll
                 for (int q = 0; q < 12; ++q)
-                    if ((used >> q) & 1u) {
+                    if ((own >> q) & 1u) {
                         float p[3];
                         edge_point(cc, q, g.level, p);
-                        stage_vertex(s, lv + __popc(used & ((1u << q) - 1u)), p[0], p[1], p[2]);
+                        stage_vertex(s, lv + __popc(own & ((1u << q) - 1u)), p[0], p[1], p[2]);
                     }
+                // entry of each edge: the cell's own, or the z-neighbour's (the
+                // list's previous cell, whose entries end where this cell's begin)
+                uint32_t ent[12];
+                const uint32_t reuse = pc >> 16;
+                const uint32_t pown = reuse ? sp_own(gc[j - 1]) : 0u;
+                const uint32_t lvp = lv - __popc(pown);
+#pragma unroll
+                for (int q = 0; q < 12; ++q)
+                    ent[q] = ((reuse >> q) & 1u) ? lvp + __popc(pown & ((1u << sp_up(q)) - 1u))
+                                                 : lv + __popc(own & ((1u << q) - 1u));
                 unsigned long long t = pk;
                 const int ntc = int(pk >> 60);
-                for (int k = 0; k < ntc; ++k, t >>= 12) {
-                    const uint32_t a = uint32_t(t & 15u), b = uint32_t((t >> 4) & 15u), d = uint32_t((t >> 8) & 15u);
-                    stage_face(s, lf + k, lv + __popc(used & ((1u << a) - 1u)),
-                               lv + __popc(used & ((1u << b) - 1u)), lv + __popc(used & ((1u << d) - 1u)));
-                }
+                for (int k = 0; k < ntc; ++k, t >>= 12)
+                    stage_face(s, lf + k, sel12(ent, uint32_t(t & 15u)), sel12(ent, uint32_t((t >> 4) & 15u)),
+                               sel12(ent, uint32_t((t >> 8) & 15u)));
             } else {
                 sp_emit_near(g, cc, cs, used, pk, s, lv, lf);
             }
@@ -565,7 +633,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
     __syncthreads();
     const uint32_t nv = 3 * min(accv, uint32_t(SP2_STAGE_V)), nf = 3 * min(accf, uint32_t(SP2_STAGE_F));
     for (uint32_t i = threadIdx.x; i < nv; i += SP2_THREADS) s.gv[i] = sv[i];
-    for (uint32_t i = threadIdx.x; i < nf; i += SP2_THREADS) s.gf[i] = sf[i];
+    for (uint32_t i = threadIdx.x; i < nf; i += SP2_THREADS) s.gf[i] = int32_t(s.vbase + sf[i]);
 }
 
 // --- intersections -----------------------------------------------------------
@@ -855,7 +923,7 @@ size_t weld_dev_workspace(long long capA, long long capU);
 void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
                      const long long* eff,
                      void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
-                     uint32_t* vsrc);
+                     uint32_t* vsrc, bool freed);
 
 namespace {
 
@@ -900,7 +968,8 @@ struct SpMcWs {
     long long* tot;  // [0..1] F, vertex-list entries  [4..7] eff  [8..9] V, 0
     float* soup;     // the vertex list (at most 3 F entries)
     int32_t* tri;    // the triangles' indices into it [3 F]
-    uint16_t *clist, *ccnt;  // per chunk: crossed cells and their counts (SP2_CHUNK slots each)
+    uint16_t* clist;  // per chunk: crossed cells (SP2_CHUNK slots each)
+    uint32_t* ccnt;   // per chunk: their summaries (sp_pack)
     uint32_t* clen;          // per chunk: crossed cells
     void* weld;
     size_t total;
@@ -921,7 +990,7 @@ SpMcWs sp_mc_carve(void* ws, long long n, long long capV, long long capF) {
     w.tri = reinterpret_cast<int32_t*>(take(size_t(3 * capF) * 4));
     const size_t chunks = size_t((n + SP2_CHUNK - 1) / SP2_CHUNK);
     w.clist = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
-    w.ccnt = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
+    w.ccnt = reinterpret_cast<uint32_t*>(take(chunks * SP2_CHUNK * 4));
     w.clen = reinterpret_cast<uint32_t*>(take(chunks * 4));
     w.weld = take(weld_dev_workspace(3 * capF, capV));
     w.total = o + 256;
@@ -1088,7 +1157,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     // the weld of the vertex list: its table holds vertex_capacity distinct
     // positions; more report an overflow with a vertex count that fits on the rerun
     weld_dev_launch(w.soup, 3 * face_capacity, std::max<long long>(vertex_capacity, 1), w.tri, 3 * face_capacity,
-                    eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr);
+                    eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr, false);
     {
         iso::ProfScope ps("sparse_mc", st);
         sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);

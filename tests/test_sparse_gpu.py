@@ -99,6 +99,42 @@ def test_sparse_mc_inconsistent_values(oracle):
         assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, method)
 
 
+def test_sparse_mc_neighbours_disagree_by_an_ulp(oracle):
+    # consistent cells, then one corner value of some cells moved by one ulp:
+    # those cells' shared edges give positions that differ from the
+    # neighbour's (or not, where the lerp rounds them together), and only
+    # exact position equality may join them
+    vals = torus((36, 40, 44), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals, extra=300, seed=5)
+    rng = np.random.default_rng(11)
+    pick = rng.random(len(ids)) < 0.15
+    corner = rng.integers(0, 8, len(ids))
+    rows = np.nonzero(pick)[0]
+    cv[rows, corner[rows]] = np.nextafter(cv[rows, corner[rows]], np.float32(np.inf))
+    g = make_sparse(vals.shape, ids, cv)
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, vals.shape, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, method)
+
+
+def test_sparse_mc_every_edge_crossed(oracle):
+    # a checkerboard field crosses all 12 edges of every cell: a chunk of the
+    # cell list then holds far more vertex entries and triangles than a CTA
+    # stages, so the direct writes (and no CTA-local weld) carry the output
+    rng = np.random.default_rng(3)
+    shape = (26, 22, 30)
+    x, y, z = np.meshgrid(*[np.arange(k) for k in shape], indexing="ij")
+    vals = np.where((x + y + z) % 2 == 0, 1.0, -1.0) * (0.5 + rng.random(shape))
+    ids, cv = sparse_from_dense(vals.astype(np.float32))
+    assert len(ids) == np.prod([k - 1 for k in shape])
+    g = make_sparse(shape, ids, cv)
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, shape, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, method)
+
+
 def test_sparse_intersection_matches_oracle(oracle):
     vals = sphere((36, 36, 36), 0.6, center=(0.02, -0.03, 0.01))
     ids, cv = sparse_from_dense(vals, extra=300, seed=3)
