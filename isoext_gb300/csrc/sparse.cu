@@ -408,18 +408,18 @@ __device__ __forceinline__ int sp_up(int e) { return e == 3 ? 1 : e == 7 ? 5 : e
 // are the same bits in both (same t from the same operands, on the same
 // corner positions: the same position).  The global weld would merge these;
 // the emit points the cell's triangles at the neighbour's entry instead.
-__device__ __forceinline__ uint32_t sp_reuse(const SpGrid& g, const int* ids, const float* vals, long long c,
-                                             long long cp, uint32_t used) {
+__device__ __forceinline__ uint32_t sp_reuse(const SpGrid& g, const int* ids, const float* vals, const Cell8& cc,
+                                             long long c, uint32_t used) {
+    const long long cp = c - 1;
     const uint32_t id = uint32_t(__ldg(ids + c)), idp = uint32_t(__ldg(ids + cp));
     if (id != idp + 1u || id % uint32_t(g.nz - 1) == 0u) return 0u;
-    const float4* a4 = reinterpret_cast<const float4*>(vals + 8 * c);
     const float4* b4 = reinterpret_cast<const float4*>(vals + 8 * cp);
-    const float4 a0 = __ldg(a4), a1 = __ldg(a4 + 1), b0 = __ldg(b4), b1 = __ldg(b4 + 1);
+    const float4 b0 = __ldg(b4), b1 = __ldg(b4 + 1);
     // corner k of the cell (z = bit 0) against corner k + 1 of the one below
-    const bool s0 = __float_as_uint(a0.x) == __float_as_uint(b0.y);  // corner 0 / 1
-    const bool s2 = __float_as_uint(a0.z) == __float_as_uint(b0.w);  // 2 / 3
-    const bool s4 = __float_as_uint(a1.x) == __float_as_uint(b1.y);  // 4 / 5
-    const bool s6 = __float_as_uint(a1.z) == __float_as_uint(b1.w);  // 6 / 7
+    const bool s0 = __float_as_uint(cc.v[0]) == __float_as_uint(b0.y);
+    const bool s2 = __float_as_uint(cc.v[2]) == __float_as_uint(b0.w);
+    const bool s4 = __float_as_uint(cc.v[4]) == __float_as_uint(b1.y);
+    const bool s6 = __float_as_uint(cc.v[6]) == __float_as_uint(b1.w);
     uint32_t r = 0;
     r |= (s0 && s2) ? (1u << 3) : 0u;   // corners 0, 2
     r |= (s4 && s6) ? (1u << 7) : 0u;   // 4, 6
@@ -439,13 +439,15 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
                                                             uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clen) {
     __shared__ uint16_t list[SP2_CHUNK];
     __shared__ uint16_t summ[SP2_CHUNK];  // sp_pack of each listed cell (16 bits)
+    __shared__ uint16_t rcand[SP2_CHUNK];  // sp_reuse, before the neighbour's own test
     __shared__ uint32_t wcnt[SP2_ROUNDS][SP2_THREADS / 32];
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
     const uint32_t nl = sp_crossed(g, vals, n, c0, list, wcnt);
     uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
     uint32_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
-        const long long c = c0 + list[j];
+        const uint32_t lj = list[j];
+        const long long c = c0 + lj;
         Cell8 cc;
         const uint32_t cs = sp_case(g, vals, c, cc);
         float ev[12][3];
@@ -453,15 +455,17 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
         bool fast;
         const uint32_t f = sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
         summ[j] = uint16_t(sp_pack(f, used, fast));
+        // the list's previous crossed cell directly before this one: maybe its z-neighbour
+        const bool cand = fast && j > 0 && list[j - 1] == lj - 1u && (used & SP_BOTTOM);
+        rcand[j] = uint16_t(cand ? sp_reuse(g, ids, vals, cc, c, used) : 0u);
     }
     __syncthreads();
     uint32_t nf = 0, nv = 0;
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
         uint32_t pc = summ[j];
-        const uint32_t lj = list[j];
-        if (j > 0 && (pc & 8u) && (summ[j - 1] & 8u) && list[j - 1] == lj - 1u && (sp_used(pc) & SP_BOTTOM))
-            pc |= sp_reuse(g, ids, vals, c0 + lj, c0 + lj - 1, sp_used(pc)) << 16;
-        gl[j] = uint16_t(lj);
+        const uint32_t r = rcand[j];
+        if (r && (summ[j - 1] & 8u)) pc |= r << 16;  // the neighbour keeps every triangle too
+        gl[j] = list[j];
         gc[j] = pc;
         nf += pc & 7u;
         nv += __popc(sp_own(pc));
@@ -479,14 +483,6 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
 // with more (a dense patch of surface) writes the rest directly.
 constexpr int SP2_STAGE_V = 2048;
 constexpr int SP2_STAGE_F = 1024;
-
-// ent[e] for a run-time e, by selects (ent stays in registers).
-__device__ __forceinline__ uint32_t sel12(const uint32_t (&ent)[12], uint32_t e) {
-    uint32_t r = ent[0];
-#pragma unroll
-    for (int q = 1; q < 12; ++q) r = e == uint32_t(q) ? ent[q] : r;
-    return r;
-}
 
 struct SpStage {
     float* v;                  // [SP2_STAGE_V * 3]
@@ -609,20 +605,25 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                         stage_vertex(s, lv + __popc(own & ((1u << q) - 1u)), p[0], p[1], p[2]);
                     }
                 // entry of each edge: the cell's own, or the z-neighbour's (the
-                // list's previous cell, whose entries end where this cell's begin)
-                uint32_t ent[12];
+                // list's previous cell, whose entries end where this cell's
+                // begin); 5-bit offsets from the neighbour's first entry
                 const uint32_t reuse = pc >> 16;
                 const uint32_t pown = reuse ? sp_own(gc[j - 1]) : 0u;
-                const uint32_t lvp = lv - __popc(pown);
+                const uint32_t np = __popc(pown), lvp = lv - np;
+                unsigned long long rel = 0;
 #pragma unroll
-                for (int q = 0; q < 12; ++q)
-                    ent[q] = ((reuse >> q) & 1u) ? lvp + __popc(pown & ((1u << sp_up(q)) - 1u))
-                                                 : lv + __popc(own & ((1u << q) - 1u));
+                for (int q = 0; q < 12; ++q) {
+                    const uint32_t o = ((reuse >> q) & 1u) ? __popc(pown & ((1u << sp_up(q)) - 1u))
+                                                           : np + __popc(own & ((1u << q) - 1u));
+                    rel |= (unsigned long long)o << (5 * q);
+                }
                 unsigned long long t = pk;
                 const int ntc = int(pk >> 60);
-                for (int k = 0; k < ntc; ++k, t >>= 12)
-                    stage_face(s, lf + k, sel12(ent, uint32_t(t & 15u)), sel12(ent, uint32_t((t >> 4) & 15u)),
-                               sel12(ent, uint32_t((t >> 8) & 15u)));
+                for (int k = 0; k < ntc; ++k, t >>= 12) {
+                    const uint32_t a = uint32_t(t & 15u), b = uint32_t((t >> 4) & 15u), d = uint32_t((t >> 8) & 15u);
+                    stage_face(s, lf + k, lvp + uint32_t((rel >> (5 * a)) & 31u), lvp + uint32_t((rel >> (5 * b)) & 31u),
+                               lvp + uint32_t((rel >> (5 * d)) & 31u));
+                }
             } else {
                 sp_emit_near(g, cc, cs, used, pk, s, lv, lf);
             }
