@@ -82,6 +82,22 @@ __device__ __forceinline__ float trilin_t(const float* cv, float tx, float ty, f
     return blend2(c0, ox, c1, tx, F);
 }
 
+// fmaxf(0.01, fminf(0.99, d / csz)), the stencil's clamped cell coordinate,
+// with the division only where its result can lie inside (0.01, 0.99).  For
+// csz >= 1e-30 (so that 0.009 csz is a normal float, rounded by at most 2^-24
+// of itself): d <= fl(0.009 csz) makes d / csz < 0.0091 before rounding, so
+// the rounded quotient is below 0.01 and the clamp gives 0.01; d >=
+// fl(0.991 csz) makes it above 0.9909, and the clamp gives 0.99.  On the two
+// axes across a crossing's edge, d is within a few ulps of 0 or of csz, so
+// those coordinates need no division.
+__device__ __forceinline__ float clamp_cell_t(float d, float csz) {
+    if (csz >= 1e-30f) {
+        if (d <= __fmul_rn(0.009f, csz)) return 0.01f;
+        if (d >= __fmul_rn(0.991f, csz)) return 0.99f;
+    }
+    return fmaxf(0.01f, fminf(0.99f, __fdiv_rn(d, csz)));
+}
+
 template <bool F>
 __device__ __forceinline__ void stencil_normal_t(const float* v, const float* lo, const float* hi, const float* p,
                                                  float* n) {
@@ -89,8 +105,7 @@ __device__ __forceinline__ void stencil_normal_t(const float* v, const float* lo
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         csz[a] = __fsub_rn(hi[a], lo[a]);
-        t[a] = __fdiv_rn(__fsub_rn(p[a], lo[a]), csz[a]);
-        t[a] = fmaxf(0.01f, fminf(0.99f, t[a]));
+        t[a] = clamp_cell_t(__fsub_rn(p[a], lo[a]), csz[a]);
     }
     const float eps = 0.02f;
     const float xp = fminf(__fadd_rn(t[0], eps), 0.99f), xm = fmaxf(__fsub_rn(t[0], eps), 0.01f);

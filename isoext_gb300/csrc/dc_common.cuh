@@ -42,6 +42,24 @@ __device__ __forceinline__ void load_cell(const float* vals, const Grid3& g, int
     }
 }
 
+// load_cell with the corner positions from a table of the grid's coordinates
+// (x, then y, then z; the same bits as coord()).
+__device__ __forceinline__ void load_cell_table(const float* vals, const Grid3& g, const float* __restrict__ gc,
+                                                int cx, int cy, int cz, CellCorners& cc) {
+    cc.fma = g.fma;
+    const float x0 = gc[cx], x1 = gc[cx + 1];
+    const float y0 = gc[g.nx + cy], y1 = gc[g.nx + cy + 1];
+    const float z0 = gc[g.nx + g.ny + cz], z1 = gc[g.nx + g.ny + cz + 1];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int x = cx + (k >> 2), y = cy + ((k >> 1) & 1), z = cz + (k & 1);
+        cc.v[k] = __ldg(vals + ((long long)x * g.ny + y) * g.nz + z);
+        cc.p[k][0] = (k >> 2) ? x1 : x0;
+        cc.p[k][1] = ((k >> 1) & 1) ? y1 : y0;
+        cc.p[k][2] = (k & 1) ? z1 : z0;
+    }
+}
+
 // Normal at crossing point p of a cell (src/its.cu:186-268).
 __device__ __forceinline__ void cell_normal(const CellCorners& cc, const float* p, float* n) {
     iso::stencil_normal(cc.v, cc.p[0], cc.p[7], p, n, cc.fma);

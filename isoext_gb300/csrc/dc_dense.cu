@@ -316,12 +316,13 @@ __device__ __forceinline__ bool cell_used(const Grid3& g, int cx, int cy, int cz
 // per cell, 0 when no face uses its dual vertex, else 1, or 3 when the vertex
 // lies on a face of the cell's box.  F: the arithmetic reading (g.fma), a
 // template argument so that each reading compiles without the other's code.
+// gc (optional): the grid's coordinates (x, y, z).
 template <bool F>
 __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ vals, Grid3 g, float level,
                                                      const uint32_t* __restrict__ cell_ids, long long A, float reg,
                                                      float svd_tol, float* __restrict__ dual,
                                                      const long long* __restrict__ dn,
-                                                     uint8_t* __restrict__ used) {
+                                                     uint8_t* __restrict__ used, const float* __restrict__ gc) {
     iso::grid_wait();
     const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (dn) A = dn[0];
@@ -332,7 +333,8 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
     const int cy = int(rr % uint32_t(g.ny - 1)), cx = int(rr / uint32_t(g.ny - 1));
     g.fma = F;
     CellCorners cc;
-    load_cell(vals, g, cx, cy, cz, cc);
+    if (gc) load_cell_table(vals, g, gc, cx, cy, cz, cc);
+    else load_cell(vals, g, cx, cy, cz, cc);
     uint32_t cs = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) cs |= uint32_t(iso::below(cc.v[j], level)) << j;
@@ -351,17 +353,21 @@ __global__ void __launch_bounds__(256) dc_cell_solve(const float* __restrict__ v
         ++K;
     }
     qef_finish(Q, K, reg, svd_tol);
-    const int ci[3] = {cx, cy, cz};
     bool face = false;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        const float lo = coord(g, q, uint32_t(ci[q])), hi = coord(g, q, uint32_t(ci[q] + 1));
+        const float lo = cc.p[0][q], hi = cc.p[7][q];  // the cell's box
         const float x = fminf(fmaxf(float(Q.x[q]), lo), hi);
         face |= x == lo || x == hi;
         dual[3 * a + q] = x;
     }
     if (used) used[a] = is_used ? (face ? 3 : 1) : 0;  // bit 1: on a face of its cell's box
 }
+
+// The solve for the call's arithmetic reading.
+using SolveFn = void (*)(const float*, Grid3, float, const uint32_t*, long long, float, float, float*,
+                         const long long*, uint8_t*, const float*);
+SolveFn solve_kernel(const Grid3& g) { return g.fma ? dc_cell_solve<true> : dc_cell_solve<false>; }
 
 // Lane whose inclusive prefix first exceeds j (prefixes nondecreasing, j < total).
 __device__ __forceinline__ int owner_lane(uint32_t incl, uint32_t j) {
@@ -843,9 +849,17 @@ __device__ __forceinline__ void store_masks(uint32_t* __restrict__ m, uint32_t p
 __global__ void __launch_bounds__(CELLS_THREADS, 4) dc_cells_count(const uint32_t* __restrict__ S, Grid3 g,
                                                                    uint32_t* __restrict__ actm,
                                                                    uint32_t* __restrict__ wsum,
-                                                                   uint32_t* __restrict__ csum) {
+                                                                   uint32_t* __restrict__ csum,
+                                                                   float* __restrict__ gc) {
     __shared__ uint32_t ws[3][CELLS_WARPS];
     iso::grid_wait();
+    // the grid's coordinates (x, then y, then z), read by the solve
+    for (uint32_t i = blockIdx.x * CELLS_THREADS + threadIdx.x; i < uint32_t(g.nx + g.ny + g.nz);
+         i += gridDim.x * CELLS_THREADS) {
+        const int axis = i < uint32_t(g.nx) ? 0 : (i < uint32_t(g.nx + g.ny) ? 1 : 2);
+        const uint32_t k = i - (axis > 0 ? uint32_t(g.nx) : 0u) - (axis > 1 ? uint32_t(g.ny) : 0u);
+        gc[i] = coord(g, axis, k);
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t gw = blockIdx.x * CELLS_WARPS + warp;
     const PwGrid p = pw_grid(g);
@@ -1384,8 +1398,8 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
     }
     iso::ProfScope ps("dc_solve", st);
     const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-    (g.fma ? dc_cell_solve<true> : dc_cell_solve<false>)<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A,
-                                                      reg, svd_tol, dual, nullptr, nullptr);
+    solve_kernel(g)<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A, reg,
+                                                    svd_tol, dual, nullptr, nullptr, nullptr);
     return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
 }
 
@@ -1538,6 +1552,7 @@ struct DcDenseWs {
     uint32_t *cells, *qoff, *vmap;
     uint8_t *used, *qbits;
     float* dual;
+    float* gc;  // grid coordinates, x then y then z
     size_t total;
 };
 
@@ -1567,6 +1582,7 @@ DcDenseWs carve_dense(void* ws, int nx, int ny, int nz, long long capA) {
     w.used = take(size_t(capA));
     w.qbits = take(size_t(capA));
     w.dual = reinterpret_cast<float*>(take(size_t(capA) * 12));
+    w.gc = reinterpret_cast<float*>(take(size_t(nx + ny + nz) * 4));
     w.total = o + 256;
     return w;
 }
@@ -1605,7 +1621,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         iso::ProfScope ps("dc_classify", st, 3);
         const uint32_t* S = w.d.S;
         iso::launch_pdl(dc_cells_count, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g, w.d.actm, w.wsum,
-                        w.csum);
+                        w.csum, w.gc);
         iso::launch_pdl(dc_cells_scan, 1u, 1024u, st, w.csum, w.ntC, capA, capQ, eff, counts,
                         reinterpret_cast<uint32_t*>(cell_offsets), status);
         iso::launch_pdl(dc_cells_write, unsigned(w.ntC), unsigned(CELLS_THREADS), st, S, g,
@@ -1617,9 +1633,9 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
         {
             iso::ProfScope ps("dc_solve", st);
             const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
-            iso::launch_pdl(g.fma ? dc_cell_solve<true> : dc_cell_solve<false>, blocks_for(capA, bt), unsigned(bt), st, values, g, level,
+            iso::launch_pdl(solve_kernel(g), blocks_for(capA, bt), unsigned(bt), st, values, g, level,
                             static_cast<const uint32_t*>(cells), capA, reg, svd_tol, w.dual,
-                            static_cast<const long long*>(eff), w.used);
+                            static_cast<const long long*>(eff), w.used, static_cast<const float*>(w.gc));
         }
         {
             iso::ProfScope ps("dc_weld", st, 3);
