@@ -388,66 +388,151 @@ __device__ __forceinline__ uint32_t sp_crossed(const SpGrid& g, const float* val
 
 // Per crossed cell, what the emit needs in 32 bits: kept faces (bits 0-2),
 // whether every triangle of the case is kept (3: no vertex near a corner),
-// the crossed edges the kept triangles use (4-15), and those of its bottom
-// face whose vertex is the z-neighbour's entry (16-27; see sp_reuse).
+// the crossed edges the kept triangles use (4-15), and for each edge an
+// earlier cell of the same x may make (sp_slot), whose entry it takes (2 bits
+// from bit 16 + 2 slot: 0 its own, 1 the z-neighbour's, 2 the y-neighbour's,
+// 3 the diagonal (y - 1, z -+ 1) neighbour's; see sp_owners).
 __device__ __forceinline__ uint32_t sp_pack(uint32_t f, uint32_t used, bool fast) {
     return f | (fast ? 8u : 0u) | (used << 4);
 }
 __device__ __forceinline__ uint32_t sp_used(uint32_t pc) { return (pc >> 4) & 0xfffu; }
-__device__ __forceinline__ uint32_t sp_own(uint32_t pc) { return sp_used(pc) & ~(pc >> 16); }
 
-// Bottom-face edges (both corners at z) and the top-face edge of the cell
-// below with the same corners (+1 in z, same order): 3 -> 1, 7 -> 5, 8 -> 9,
-// 11 -> 10.
-constexpr uint32_t SP_BOTTOM = (1u << 3) | (1u << 7) | (1u << 8) | (1u << 11);
-__device__ __forceinline__ int sp_up(int e) { return e == 3 ? 1 : e == 7 ? 5 : e == 8 ? 9 : 10; }
+// Edges whose vertex an earlier cell of the same x can make, in slot order:
+// 0, 3, 4, 7, 8, 9, 11.
+__host__ __device__ constexpr int sp_slot_edge(int s) {
+    return s == 0 ? 0 : s == 1 ? 3 : s == 2 ? 4 : s == 3 ? 7 : s == 4 ? 8 : s == 5 ? 9 : 11;
+}
+constexpr unsigned long long sp_slot_table() {
+    unsigned long long t = 0;
+    for (int e = 0; e < 12; ++e) {
+        int s = 7;
+        for (int k = 0; k < 7; ++k)
+            if (sp_slot_edge(k) == e) s = k;
+        t |= (unsigned long long)s << (3 * e);
+    }
+    return t;
+}
+constexpr unsigned long long SP_SLOT = sp_slot_table();
+__device__ __forceinline__ int sp_slot(int e) { return int((SP_SLOT >> (3 * e)) & 7ull); }
 
-// Bottom-face edges of crossed cell c whose vertex equals the one its
-// z-neighbour below (cp, the list's previous crossed cell) makes: both cells
-// keep every triangle, they share a column, and the edge's two corner values
-// are the same bits in both (same t from the same operands, on the same
-// corner positions: the same position).  The global weld would merge these;
-// the emit points the cell's triangles at the neighbour's entry instead.
-__device__ __forceinline__ uint32_t sp_reuse(const SpGrid& g, const int* ids, const float* vals, const Cell8& cc,
-                                             long long c, uint32_t used) {
-    const long long cp = c - 1;
-    const uint32_t id = uint32_t(__ldg(ids + c)), idp = uint32_t(__ldg(ids + cp));
-    if (id != idp + 1u || id % uint32_t(g.nz - 1) == 0u) return 0u;
-    const float4* b4 = reinterpret_cast<const float4*>(vals + 8 * cp);
-    const float4 b0 = __ldg(b4), b1 = __ldg(b4 + 1);
-    // corner k of the cell (z = bit 0) against corner k + 1 of the one below
-    const bool s0 = __float_as_uint(cc.v[0]) == __float_as_uint(b0.y);
-    const bool s2 = __float_as_uint(cc.v[2]) == __float_as_uint(b0.w);
-    const bool s4 = __float_as_uint(cc.v[4]) == __float_as_uint(b1.y);
-    const bool s6 = __float_as_uint(cc.v[6]) == __float_as_uint(b1.w);
-    uint32_t r = 0;
-    r |= (s0 && s2) ? (1u << 3) : 0u;   // corners 0, 2
-    r |= (s4 && s6) ? (1u << 7) : 0u;   // 4, 6
-    r |= (s0 && s4) ? (1u << 8) : 0u;   // 0, 4
-    r |= (s2 && s6) ? (1u << 11) : 0u;  // 2, 6
-    return r & used;
+// The owner's edge for slot s and owner code k (1..3), a nibble of
+// SP_SRC_{LO,HI} at 3 s + k - 1: e0 <- y e2; e3 <- z e1; e4 <- y e6;
+// e7 <- z e5; e8 <- z e9, y e11, (y - 1, z - 1) e10; e9 <- y e10,
+// (y - 1, z + 1) e11; e11 <- z e10 (the same lattice edge, corners in the
+// same order).
+constexpr int SP_SRC[21] = {0, 2, 0, 1, 0, 0, 0, 6, 0, 5, 0, 0, 9, 11, 10, 0, 10, 11, 10, 0, 0};
+constexpr unsigned long long sp_src_table(int lo) {
+    unsigned long long t = 0;
+    for (int i = 0; i < 16; ++i)
+        if (lo + i < 21) t |= (unsigned long long)SP_SRC[lo + i] << (4 * i);
+    return t;
+}
+constexpr unsigned long long SP_SRC_LO = sp_src_table(0), SP_SRC_HI = sp_src_table(16);
+__device__ __forceinline__ int sp_src_edge(int s, uint32_t k) {
+    const int i = 3 * s + int(k) - 1;
+    return int(((i < 16 ? SP_SRC_LO >> (4 * i) : SP_SRC_HI >> (4 * (i - 16)))) & 15ull);
+}
+
+// Edges whose entry is another cell's.
+__device__ __forceinline__ uint32_t sp_reused(uint32_t pc) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int s = 0; s < 7; ++s) m |= ((pc >> (16 + 2 * s)) & 3u) ? (1u << sp_slot_edge(s)) : 0u;
+    return m;
+}
+__device__ __forceinline__ uint32_t sp_own(uint32_t pc) { return sp_used(pc) & ~sp_reused(pc); }
+
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+
+__device__ __forceinline__ void load8(const float* vals, long long c, float* v) {
+    const float4* p = reinterpret_cast<const float4*>(vals + 8 * c);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// Owner codes of crossed cell c (list position j, id cid[j]) that keeps every
+// triangle.  A lattice edge of the cell's x is shared with the cells at
+// (y - 1 .. y, z - 1 .. z) around it; those of them in this chunk, earlier in
+// the list, keeping every triangle and with the edge's two corner values the
+// same bits as this cell's compute the same vertex (same operands, same corner
+// positions).  Sameness is an equivalence, so the first such cell in the list
+// makes the entry itself and every later one takes it: no chains.  The weld
+// would merge the copies anyway; the emit points the triangles at the first.
+__device__ __forceinline__ uint32_t sp_owners(const SpGrid& g, const float* vals, const uint16_t* list,
+                                              const uint16_t* summ, const uint32_t* cid, long long c0, uint32_t j,
+                                              uint32_t used, int& jy_out) {
+    const uint32_t nzc = uint32_t(g.nz - 1);
+    const uint32_t id = cid[j];
+    const uint32_t z = id % nzc, y = (id / nzc) % uint32_t(g.ny - 1);
+    int jz = -1, jy = -1, jyl = -1, jyh = -1;  // z-, y-, (y-1, z-1)-, (y-1, z+1)-neighbours
+    if (z > 0 && j > 0 && cid[j - 1] == id - 1u && (summ[j - 1] & 8u)) jz = int(j) - 1;
+    if (y > 0) {
+        const uint32_t idy = id - nzc;
+        uint32_t lo = 0, hi = j;  // first position with cid >= idy
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (cid[mid] < idy) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < j && cid[lo] == idy) {
+            jy_out = int(lo);
+            if (summ[lo] & 8u) jy = int(lo);
+            if (z > 0 && lo > 0 && cid[lo - 1] == idy - 1u && (summ[lo - 1] & 8u)) jyl = int(lo) - 1;
+            if (z + 1 < nzc && lo + 1 < j && cid[lo + 1] == idy + 1u && (summ[lo + 1] & 8u)) jyh = int(lo) + 1;
+        }
+    }
+    if (jz < 0 && jy < 0 && jyl < 0 && jyh < 0) return 0u;
+    float d[8], vz[8], vy[8], vl[8], vh[8];
+    load8(vals, c0 + list[j], d);
+    if (jz >= 0) load8(vals, c0 + list[jz], vz);
+    if (jy >= 0) load8(vals, c0 + list[jy], vy);
+    if (jyl >= 0) load8(vals, c0 + list[jyl], vl);
+    if (jyh >= 0) load8(vals, c0 + list[jyh], vh);
+    // the neighbour's corner k' holds this cell's corner k: z (k | 1), y (k | 2)
+    const bool z0 = jz >= 0 && same_bits(d[0], vz[1]), z2 = jz >= 0 && same_bits(d[2], vz[3]);
+    const bool z4 = jz >= 0 && same_bits(d[4], vz[5]), z6 = jz >= 0 && same_bits(d[6], vz[7]);
+    const bool y0 = jy >= 0 && same_bits(d[0], vy[2]), y1 = jy >= 0 && same_bits(d[1], vy[3]);
+    const bool y4 = jy >= 0 && same_bits(d[4], vy[6]), y5 = jy >= 0 && same_bits(d[5], vy[7]);
+    uint32_t k = 0;
+    if ((used & (1u << 0)) && y0 && y1) k |= 2u << 0;     // e0 (0, 1) <- y e2
+    if ((used & (1u << 3)) && z0 && z2) k |= 1u << 2;     // e3 (0, 2) <- z e1
+    if ((used & (1u << 4)) && y4 && y5) k |= 2u << 4;     // e4 (4, 5) <- y e6
+    if ((used & (1u << 7)) && z4 && z6) k |= 1u << 6;     // e7 (4, 6) <- z e5
+    if (used & (1u << 8)) {                               // e8 (0, 4), owners in list order
+        if (jyl >= 0 && same_bits(d[0], vl[3]) && same_bits(d[4], vl[7])) k |= 3u << 8;
+        else if (y0 && y4) k |= 2u << 8;
+        else if (z0 && z4) k |= 1u << 8;
+    }
+    if (used & (1u << 9)) {                               // e9 (1, 5)
+        if (y1 && y5) k |= 2u << 10;
+        else if (jyh >= 0 && same_bits(d[1], vh[2]) && same_bits(d[5], vh[6])) k |= 3u << 10;
+    }
+    if ((used & (1u << 11)) && z2 && z6) k |= 1u << 12;   // e11 (2, 6) <- z e10
+    return k;
 }
 
 // Per CTA: its crossed cells in cell order and, for each, sp_pack of its
-// summary with the z-neighbour entries, into the chunk's slots of clist / ccnt
-// (SP2_CHUNK each; the count in clen); the chunk's faces and vertex-list
-// entries -> blk[2 b], blk[2 b + 1].  The emit then reads only the crossed
-// cells.
+// summary with the owner codes, into the chunk's slots of clist / ccnt / cjy
+// (SP2_CHUNK each: cjy the y-neighbour's list position; the count in clen);
+// the chunk's faces and vertex-list entries -> blk[2 b], blk[2 b + 1].  The
+// emit then reads only the crossed cells.
 __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
                                                             const float* __restrict__ vals, long long n,
                                                             unsigned long long* blk, uint16_t* __restrict__ clist,
-                                                            uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clen) {
+                                                            uint32_t* __restrict__ ccnt, uint16_t* __restrict__ cjy,
+                                                            uint32_t* __restrict__ clen) {
     __shared__ uint16_t list[SP2_CHUNK];
     __shared__ uint16_t summ[SP2_CHUNK];  // sp_pack of each listed cell (16 bits)
-    __shared__ uint16_t rcand[SP2_CHUNK];  // sp_reuse, before the neighbour's own test
+    __shared__ uint32_t cid[SP2_CHUNK];   // their ids
     __shared__ uint32_t wcnt[SP2_ROUNDS][SP2_THREADS / 32];
     const long long c0 = (long long)blockIdx.x * SP2_CHUNK;
     const uint32_t nl = sp_crossed(g, vals, n, c0, list, wcnt);
     uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
     uint32_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
+    uint16_t* gy = cjy + (size_t)blockIdx.x * SP2_CHUNK;
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
-        const uint32_t lj = list[j];
-        const long long c = c0 + lj;
+        const long long c = c0 + list[j];
         Cell8 cc;
         const uint32_t cs = sp_case(g, vals, c, cc);
         float ev[12][3];
@@ -455,18 +540,17 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int*
         bool fast;
         const uint32_t f = sp_cell_summary(g, ids, c, cc, cs, ev, used, fast);
         summ[j] = uint16_t(sp_pack(f, used, fast));
-        // the list's previous crossed cell directly before this one: maybe its z-neighbour
-        const bool cand = fast && j > 0 && list[j - 1] == lj - 1u && (used & SP_BOTTOM);
-        rcand[j] = uint16_t(cand ? sp_reuse(g, ids, vals, cc, c, used) : 0u);
+        cid[j] = uint32_t(__ldg(ids + c));
     }
     __syncthreads();
     uint32_t nf = 0, nv = 0;
     for (uint32_t j = threadIdx.x; j < nl; j += SP2_THREADS) {
         uint32_t pc = summ[j];
-        const uint32_t r = rcand[j];
-        if (r && (summ[j - 1] & 8u)) pc |= r << 16;  // the neighbour keeps every triangle too
+        int jy = 0;
+        if (pc & 8u) pc |= sp_owners(g, vals, list, summ, cid, c0, j, sp_used(pc), jy) << 16;
         gl[j] = list[j];
         gc[j] = pc;
+        gy[j] = uint16_t(jy);
         nf += pc & 7u;
         nv += __popc(sp_own(pc));
     }
@@ -542,6 +626,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                                                            const unsigned long long* __restrict__ blk,
                                                            const uint16_t* __restrict__ clist,
                                                            const uint32_t* __restrict__ ccnt,
+                                                           const uint16_t* __restrict__ cjy,
                                                            const uint32_t* __restrict__ clen,
                                                            float* __restrict__ vlist, int32_t* __restrict__ tri,
                                                            const long long* __restrict__ dn) {
@@ -549,6 +634,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
     __shared__ float sv[SP2_STAGE_V * 3];
     __shared__ int32_t sf[SP2_STAGE_F * 3];
     __shared__ uint32_t wsum[2][SP2_THREADS / 32];
+    __shared__ uint16_t slv[SP2_CHUNK];  // each listed cell's first own entry (CTA-local)
     if (dn[0] == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < 256; i += SP2_THREADS) tpk[i] = ISO_TRI_PACKED[g.method * 256 + i];
@@ -556,6 +642,7 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
     const uint32_t nl = clen[blockIdx.x];
     const uint16_t* gl = clist + (size_t)blockIdx.x * SP2_CHUNK;
     const uint32_t* gc = ccnt + (size_t)blockIdx.x * SP2_CHUNK;
+    const uint16_t* gy = cjy + (size_t)blockIdx.x * SP2_CHUNK;
     SpStage s;
     s.v = sv;
     s.f = sf;
@@ -569,14 +656,14 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
         const uint32_t pc = ok ? gc[j] : 0u;
         const uint32_t cl = ok ? gl[j] : 0u;
         const uint32_t used = sp_used(pc), own = sp_own(pc);
-        const uint32_t mine = (pc & 7u) | (uint32_t(__popc(own)) << 16);  // faces | vertices << 16
+        const uint32_t mine = (pc & 7u) | (uint32_t(__popc(own)) << 16);  // faces | own vertices << 16
         uint32_t inc = mine;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t o = __shfl_up_sync(~0u, inc, d);
             if (lane >= d) inc += o;
         }
-        const int buf = (r0 / SP2_THREADS) & 1;  // two buffers: one barrier per round
+        const int buf = (r0 / SP2_THREADS) & 1;  // alternate buffers between rounds
         if (lane == 31) wsum[buf][warp] = inc;
         __syncthreads();  // also orders tpk's fill before its first use
         uint32_t before = 0, all = 0;
@@ -587,6 +674,9 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
             all += w;
         }
         const uint32_t ex = before + inc - mine;
+        const uint32_t lv = accv + (ex >> 16), lf = accf + (ex & 0xffffu);
+        if (ok) slv[j] = uint16_t(lv);
+        __syncthreads();  // first entries of this round's cells, for the cells that take them
         if (ok) {
             const long long c = c0 + cl;
             Cell8 cc;
@@ -594,7 +684,6 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
             int x, y, z;
             cell_xyz(g, uint32_t(ids[c]), x, y, z);
             set_coords(g, x, y, z, cc);
-            const uint32_t lv = accv + (ex >> 16), lf = accf + (ex & 0xffffu);
             const unsigned long long pk = tpk[cs];
             if (pc & 8u) {  // every triangle kept, every crossed edge used
 #pragma unroll
@@ -604,25 +693,45 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                         edge_point(cc, q, g.level, p);
                         stage_vertex(s, lv + __popc(own & ((1u << q) - 1u)), p[0], p[1], p[2]);
                     }
-                // entry of each edge: the cell's own, or the z-neighbour's (the
-                // list's previous cell, whose entries end where this cell's
-                // begin); 5-bit offsets from the neighbour's first entry
-                const uint32_t reuse = pc >> 16;
-                const uint32_t pown = reuse ? sp_own(gc[j - 1]) : 0u;
-                const uint32_t np = __popc(pown), lvp = lv - np;
-                unsigned long long rel = 0;
+                // entry of each edge: the cell's own, or its owner's (an earlier
+                // listed cell: first entry from slv, rank among the owner's own edges)
+                const uint32_t codes = pc >> 16;
+                const uint32_t lo = codes & 0x1555u, hi = (codes >> 1) & 0x1555u;
+                uint32_t oz = 0, lz = 0, oy = 0, ly = 0, ol = 0, ll = 0, oh = 0, lh = 0;
+                if (lo & ~hi) { oz = sp_own(gc[j - 1]); lz = slv[j - 1]; }
+                if (codes) {
+                    const uint32_t jy = gy[j];
+                    if (hi & ~lo) { oy = sp_own(gc[jy]); ly = slv[jy]; }
+                    if (((codes >> 8) & 3u) == 3u) { ol = sp_own(gc[jy - 1]); ll = slv[jy - 1]; }
+                    if (((codes >> 10) & 3u) == 3u) { oh = sp_own(gc[jy + 1]); lh = slv[jy + 1]; }
+                }
+                unsigned long long ent[3] = {0ull, 0ull, 0ull};  // 16 bits per edge
 #pragma unroll
                 for (int q = 0; q < 12; ++q) {
-                    const uint32_t o = ((reuse >> q) & 1u) ? __popc(pown & ((1u << sp_up(q)) - 1u))
-                                                           : np + __popc(own & ((1u << q) - 1u));
-                    rel |= (unsigned long long)o << (5 * q);
+                    const int sl = sp_slot(q);
+                    const uint32_t k = sl < 7 ? (codes >> (2 * sl)) & 3u : 0u;
+                    uint32_t e;
+                    if (k == 0u) {
+                        e = lv + __popc(own & ((1u << q) - 1u));
+                    } else {
+                        const uint32_t se = uint32_t(sp_src_edge(sl, k));
+                        const uint32_t ob = k == 1u ? oz : (k == 2u ? oy : (q == 8 ? ol : oh));
+                        const uint32_t lb = k == 1u ? lz : (k == 2u ? ly : (q == 8 ? ll : lh));
+                        e = lb + __popc(ob & ((1u << se) - 1u));
+                    }
+                    ent[q >> 2] |= (unsigned long long)(e & 0xffffu) << (16 * (q & 3));
                 }
                 unsigned long long t = pk;
                 const int ntc = int(pk >> 60);
                 for (int k = 0; k < ntc; ++k, t >>= 12) {
-                    const uint32_t a = uint32_t(t & 15u), b = uint32_t((t >> 4) & 15u), d = uint32_t((t >> 8) & 15u);
-                    stage_face(s, lf + k, lvp + uint32_t((rel >> (5 * a)) & 31u), lvp + uint32_t((rel >> (5 * b)) & 31u),
-                               lvp + uint32_t((rel >> (5 * d)) & 31u));
+                    uint32_t v3[3];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        const uint32_t e = uint32_t((t >> (4 * r)) & 15u);
+                        const unsigned long long w = e < 4u ? ent[0] : (e < 8u ? ent[1] : ent[2]);
+                        v3[r] = uint32_t((w >> (16 * (e & 3u))) & 0xffffu);
+                    }
+                    stage_face(s, lf + k, v3[0], v3[1], v3[2]);
                 }
             } else {
                 sp_emit_near(g, cc, cs, used, pk, s, lv, lf);
@@ -971,6 +1080,7 @@ struct SpMcWs {
     int32_t* tri;    // the triangles' indices into it [3 F]
     uint16_t* clist;  // per chunk: crossed cells (SP2_CHUNK slots each)
     uint32_t* ccnt;   // per chunk: their summaries (sp_pack)
+    uint16_t* cjy;    // per chunk: their y-neighbours' list positions
     uint32_t* clen;          // per chunk: crossed cells
     void* weld;
     size_t total;
@@ -992,6 +1102,7 @@ SpMcWs sp_mc_carve(void* ws, long long n, long long capV, long long capF) {
     const size_t chunks = size_t((n + SP2_CHUNK - 1) / SP2_CHUNK);
     w.clist = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
     w.ccnt = reinterpret_cast<uint32_t*>(take(chunks * SP2_CHUNK * 4));
+    w.cjy = reinterpret_cast<uint16_t*>(take(chunks * SP2_CHUNK * 2));
     w.clen = reinterpret_cast<uint32_t*>(take(chunks * 4));
     w.weld = take(weld_dev_workspace(3 * capF, capV));
     w.total = o + 256;
@@ -1149,11 +1260,11 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
         iso::ProfScope ps("sparse_mc", st, 4);
         const unsigned chunks = nb(n, SP2_CHUNK);
         sp_mc_count2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (unsigned long long*)w.blk, w.clist, w.ccnt,
-                                                     w.clen);
+                                                     w.cjy, w.clen);
         iso_block_scan_launch((unsigned long long*)w.blk, chunks, w.tot, st);
         sp_mc_sizes2<<<1, 1, 0, st>>>(w.tot, face_capacity, vertex_capacity, eff, counts, status);
         sp_mc_emit2<<<chunks, SP2_THREADS, 0, st>>>(g, ids, vals, n, (const unsigned long long*)w.blk, w.clist,
-                                                    w.ccnt, w.clen, w.soup, w.tri, eff);
+                                                    w.ccnt, w.cjy, w.clen, w.soup, w.tri, eff);
     }
     // the weld of the vertex list: its table holds vertex_capacity distinct
     // positions; more report an overflow with a vertex count that fits on the rerun
