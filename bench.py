@@ -1,7 +1,7 @@
 """Benchmark: dense 512^3 FP32 marching cubes (sphere |p| - 0.8) in Gcells/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload mc512|mc128|dc512|dc256|serve|grad|sparse1024] [--mc-only]
+                    [--workload mc512|mc128|dc512|dc256|serve|grad|sparse1024|sparse768] [--mc-only]
 
 One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
   value  device-timed throughput with the grid resident in HBM (C ABI call with
@@ -51,6 +51,9 @@ WORKLOADS = {
     "grad": dict(kind="grad", n=256, batch=8, seed=5, desc="diff_mc_dc_8x256_fourier"),
     "sparse1024": dict(kind="sparse", n=1024, brick=8, spheres=64, k=0.05, seed=3,
                        desc="sparse_mc_1024_bricks8_smoothmin64"),
+    # the same field on a 768^3 lattice (32 M cells): the case ncu section captures run on
+    "sparse768": dict(kind="sparse", n=768, brick=8, spheres=64, k=0.05, seed=3,
+                      desc="sparse_mc_768_bricks8_smoothmin64"),
 }
 METRIC = "MC/DC Gcells/s @512^3 fp32"
 
