@@ -27,34 +27,39 @@ __global__ void __launch_bounds__(256) sdf_union_grid(const float* __restrict__ 
     __syncthreads();
     for (int i = threadIdx.x; i < np * 7; i += blockDim.x) pr[i / 7][i % 7] = prims[1 + i];
     __syncthreads();
-    const long long total = (long long)nx * ny * nz;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int z = int(i % nz);
-        const long long r = i / nz;
-        const int y = int(r % ny), x = int(r / ny);
+    // a warp per grid row (x, y), its lanes along z: the row's coordinates once,
+    // consecutive lanes store consecutive values
+    const int lane = threadIdx.x & 31;
+    const long long rows = (long long)nx * ny;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < rows;
+         row += nwarps) {
+        const int y = int(row % ny), x = int(row / ny);
         const float px = iso::grid_coord(uint32_t(x), uint32_t(nx), ax, sx, fma);
         const float py = iso::grid_coord(uint32_t(y), uint32_t(ny), ay, sy, fma);
-        const float pz = iso::grid_coord(uint32_t(z), uint32_t(nz), az, sz, fma);
-        float d = 3.402823466e38f;
-        for (int k = 0; k < np; ++k) {
-            const float dx = __fsub_rn(px, pr[k][1]), dy = __fsub_rn(py, pr[k][2]), dz = __fsub_rn(pz, pr[k][3]);
-            float dk;
-            if (pr[k][0] == 0.0f) {
-                dk = __fsub_rn(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
-                                                    __fmul_rn(dz, dz))),
-                               pr[k][4]);
-            } else {
-                const float qx = __fsub_rn(fabsf(dx), pr[k][4]), qy = __fsub_rn(fabsf(dy), pr[k][5]),
-                            qz = __fsub_rn(fabsf(dz), pr[k][6]);
-                const float ox = fmaxf(qx, 0.0f), oy = fmaxf(qy, 0.0f), oz = fmaxf(qz, 0.0f);
-                const float outside =
-                    __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ox, ox), __fmul_rn(oy, oy)), __fmul_rn(oz, oz)));
-                dk = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
+        float* orow = out + row * nz;
+        for (int z = lane; z < nz; z += 32) {
+            const float pz = iso::grid_coord(uint32_t(z), uint32_t(nz), az, sz, fma);
+            float d = 3.402823466e38f;
+            for (int k = 0; k < np; ++k) {
+                const float dx = __fsub_rn(px, pr[k][1]), dy = __fsub_rn(py, pr[k][2]), dz = __fsub_rn(pz, pr[k][3]);
+                float dk;
+                if (pr[k][0] == 0.0f) {
+                    dk = __fsub_rn(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                        __fmul_rn(dz, dz))),
+                                   pr[k][4]);
+                } else {
+                    const float qx = __fsub_rn(fabsf(dx), pr[k][4]), qy = __fsub_rn(fabsf(dy), pr[k][5]),
+                                qz = __fsub_rn(fabsf(dz), pr[k][6]);
+                    const float ox = fmaxf(qx, 0.0f), oy = fmaxf(qy, 0.0f), oz = fmaxf(qz, 0.0f);
+                    const float outside =
+                        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ox, ox), __fmul_rn(oy, oy)), __fmul_rn(oz, oz)));
+                    dk = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
+                }
+                d = fminf(d, dk);
             }
-            d = fminf(d, dk);
+            orow[z] = d;
         }
-        out[i] = d;
     }
 }
 
@@ -71,11 +76,11 @@ int iso_sdf_union_grid(const float* prims, int nx, int ny, int nz, const float* 
                        float* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (nx < 1 || ny < 1 || nz < 1 || !prims || !out || !aabb_min || !aabb_max) return ISO_ERR_ARG;
-    const long long total = (long long)nx * ny * nz;
+    const long long rows = (long long)nx * ny;  // a warp each, 8 per CTA
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long grid = std::max<long long>(1, std::min<long long>((total + 255) / 256, (long long)sms * 8));
+    const long long grid = std::max<long long>(1, std::min<long long>((rows + 7) / 8, (long long)sms * 8));
     iso::ProfScope ps("sdf_union_grid", st);
     sdf_union_grid<<<unsigned(grid), 256, 0, st>>>(prims, nx, ny, nz, aabb_min[0], aabb_min[1], aabb_min[2],
                                                    aabb_max[0] - aabb_min[0], aabb_max[1] - aabb_min[1],

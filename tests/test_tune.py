@@ -45,3 +45,13 @@ def test_populate_brick_setting():
         assert tune.populate_brick() == 16
     finally:
         tune.set_populate_brick(old)
+
+
+def test_choose_keeps_the_incumbent_within_the_margin():
+    # a value within MARGIN of the fastest does not displace the one in force
+    assert tune.choose({128: 1.00, 256: 1.01}, 256) == 256
+    assert tune.choose({128: 1.00, 256: 1.00 / (1 - tune.MARGIN) + 0.01}, 256) == 128
+    # an incumbent the knob does not offer: the fastest
+    assert tune.choose({8: 2.0, 16: 1.5, 32: 1.7}, 64) == 16
+    assert tune.choose({8: 2.0, 16: 1.5, 32: 1.7}, 32) == 16
+    assert tune.choose({8: 2.0, 16: 1.69, 32: 1.7}, 32) == 32
