@@ -27,14 +27,18 @@ def _union_np(points, prims):
     return d
 
 
-@pytest.mark.parametrize("shape", [(33, 40, 47), (64, 64, 64)])
-def test_union_grid_matches_formula(shape):
+@pytest.mark.parametrize("shape,req", [((33, 40, 47), 3), ((64, 64, 64), 3)] +
+                         [((29, 31, 67), r) for r in range(8)])
+def test_union_grid_matches_formula(shape, req):
+    """Bit for bit against the formula, for unions of 1 to 16 spheres and boxes
+    (a warp per grid row, its lanes along z, rows shorter and longer than a
+    warp)."""
     import ctypes as C
 
     from isoext_gb300 import UniformGrid, _ffi
     from isoext_gb300.serve import HI, LO, prims_buffer, random_requests
 
-    prims = random_requests(4, seed=11)[3].prims
+    prims = random_requests(8, seed=11)[req].prims
     grid = UniformGrid(list(shape), LO, HI)
     dev = torch.from_numpy(prims_buffer(prims)).cuda()
     _ffi.check(_ffi.lib().iso_sdf_union_grid(C.c_void_p(dev.data_ptr()), *shape, _ffi.fvec3(LO), _ffi.fvec3(HI),
