@@ -377,3 +377,40 @@ def test_sparse_mc_retries_when_buffers_are_small():
     g._mc_sizes = {(g.get_num_cells(), 0.0, 0): (4, len(f0))}  # faces fit, vertices do not
     v2, f2 = iso.marching_cubes(g)
     assert torch.equal(v0, v2) and torch.equal(f0, f2)
+
+
+def test_sparse_mc_weld_overflow_reports_a_vertex_count_that_fits():
+    """A vertex capacity far below the mesh's: the weld's table (sized from it)
+    fills, the call reports ISO_ERR_OVERFLOW with a vertex count at least the
+    true one, and a rerun sized from that count gives the mesh."""
+    import ctypes as C
+
+    from isoext_gb300 import _ffi
+    from isoext_gb300.sparse import _p, _stream
+
+    vals = torus((40, 44, 36), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals, extra=300, seed=2)
+    g = make_sparse(vals.shape, ids, cv)
+    v0, f0 = iso.marching_cubes(g)
+    lib = _ffi.lib()
+    n = g.get_num_cells()
+    sx, sy, sz, lo, hi = g._geom()
+
+    def run(cap_v, cap_f):
+        vout = torch.empty((cap_v, 3), dtype=torch.float32, device="cuda")
+        fout = torch.empty((cap_f, 3), dtype=torch.int32, device="cuda")
+        ws = torch.empty(int(lib.iso_sparse_mc_workspace_size(n, cap_v, cap_f)), dtype=torch.uint8, device="cuda")
+        small = torch.zeros(4, dtype=torch.int64, device="cuda")
+        _ffi.check(lib.iso_sparse_mc(_p(g._ids), _p(g._values), n, sx, sy, sz, lo, hi, 0.0, 0, _p(vout), cap_v,
+                                     _p(fout), cap_f, _p(ws), ws.numel(), _p(small),
+                                     C.c_void_p(small.data_ptr() + 24), _stream(torch.device("cuda"))))
+        h = small.cpu()
+        return vout, fout, int(h[0]), int(h[1]), int(h[3] & 0xFFFFFFFF)
+
+    cap_f = len(f0) + 16
+    _, _, V, _, status = run(16, cap_f)
+    assert status == _ffi.ISO_ERR_OVERFLOW
+    assert V >= len(v0)
+    vout, fout, V1, F1, status1 = run(V, cap_f)
+    assert status1 == 0 and V1 == len(v0) and F1 == len(f0)
+    assert torch.equal(vout[:V1], v0) and torch.equal(fout[:F1], f0)
