@@ -335,6 +335,26 @@ int iso_dc_backward_src(const float *values, int nx, int ny, int nz, const float
 int iso_sdf_union_grid(const float *prims, int nx, int ny, int nz, const float *aabb_min,
                        const float *aabb_max, float *out, void *stream);
 
+/* ---- exact-position weld of a mesh -------------------------------------------
+ * isoext welds its triangle soup by exact position (src/utils.cu:32-59: sort,
+ * unique) after dropping triangles with two equal vertex positions
+ * (src/mc/nagae.cu:71).  The extraction kernels weld by grid edge, which is the
+ * same mesh while neighbouring grid coordinates are many ulps apart; on a grid
+ * whose spacing comes within a few ulps of its coordinates, vertices of
+ * distinct edges can round to one position, and this pass gives isoext's mesh:
+ * vertices with bit-equal positions (-0 and +0 equal) merge into the first of
+ * them, faces with two equal vertices are dropped, and vertices no remaining
+ * face uses are dropped; the survivors keep their order.  vertices: device
+ * float [V, 3]; faces: device int32 [F, 3]; vout / fout: device, room for V and
+ * F; vertex_source (optional): device int32 [V], each output vertex's index in
+ * the input; counts: device int64 [2] <- (V', F'); status: device int, 0 or
+ * ISO_ERR_OVERFLOW (a hash probe limit; not reached when V fits the table).
+ * workspace: iso_weld_mesh_workspace_size(V, F) bytes. */
+size_t iso_weld_mesh_workspace_size(long long num_vertices, long long num_faces);
+int iso_weld_mesh(const float *vertices, long long num_vertices, const int *faces, long long num_faces,
+                  float *vout, int *fout, int *vertex_source, long long *counts, int *status,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- isoext's vertex order --------------------------------------------------
  * The extraction entry points number vertices by grid edge (MC) or by cell
  * (DC); isoext sorts its welded vertices by position (src/utils.cu:32-59:

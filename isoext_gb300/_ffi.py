@@ -47,6 +47,9 @@ def _declare(lib: C.CDLL) -> None:
     lib.iso_set_arith.argtypes = [_i]
     lib.iso_get_arith.restype = _i
     lib.iso_axis_coords.argtypes = [_vp, _i, _f, _f, _vp]
+    lib.iso_weld_mesh_workspace_size.argtypes = [_ll, _ll]
+    lib.iso_weld_mesh_workspace_size.restype = C.c_size_t
+    lib.iso_weld_mesh.argtypes = [_vp, _ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
     lib.iso_sort_vertices_workspace_size.argtypes = [_ll]
     lib.iso_sort_vertices_workspace_size.restype = C.c_size_t
     lib.iso_sort_vertices.argtypes = [_vp, _ll, _vp, _ll, _vp, C.c_size_t, _vp]
@@ -176,3 +179,35 @@ def profile_kernels(kernel: str | None) -> int:
     n = _ll()
     check(lib().iso_profile_kernels(kernel.encode() if kernel else None, C.byref(n)))
     return n.value
+
+
+def weld_mesh(v, f, want_source: bool = False):
+    """isoext's exact-position weld of a mesh on the device (iso_weld_mesh):
+    vertices with bit-equal positions merge into the first, faces with two
+    equal vertices and vertices no face uses are dropped, order kept.  Returns
+    (vertices, faces) or (None, None) for an empty result, and with want_source
+    each output vertex's input index as a third element."""
+    import torch
+
+    V, F = len(v), len(f)
+    dev = v.device
+    vout = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    fout = torch.empty((F, 3), dtype=torch.int32, device=dev)
+    src = torch.empty(V, dtype=torch.int32, device=dev) if want_source else None
+    small = torch.zeros(3, dtype=torch.int64, device=dev)
+    ws = torch.empty(int(lib().iso_weld_mesh_workspace_size(V, F)), dtype=torch.uint8, device=dev)
+    vv, ff = v.contiguous(), f.to(torch.int32).contiguous()
+    check(lib().iso_weld_mesh(C.c_void_p(vv.data_ptr()), V, C.c_void_p(ff.data_ptr()), F,
+                              C.c_void_p(vout.data_ptr()), C.c_void_p(fout.data_ptr()),
+                              C.c_void_p(src.data_ptr()) if src is not None else None,
+                              C.c_void_p(small.data_ptr()), C.c_void_p(small.data_ptr() + 16),
+                              C.c_void_p(ws.data_ptr()), ws.numel(),
+                              C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    h = small.cpu()
+    nv, nf, status = int(h[0]), int(h[1]), int(h[2] & 0xFFFFFFFF)
+    if status:
+        raise RuntimeError(f"isoext_gb300: device error {status} in the position weld")
+    if nf == 0:
+        return (None, None, None) if want_source else (None, None)
+    out = (vout[:nv], fout[:nf])
+    return out + (src[:nv],) if want_source else out

@@ -1033,7 +1033,7 @@ size_t weld_dev_workspace(long long capA, long long capU);
 void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
                      const long long* eff,
                      void* ws, float* vout, int32_t* fout, long long* vtot, int* status, cudaStream_t st,
-                     uint32_t* vsrc, bool freed);
+                     uint32_t* vsrc);
 
 namespace {
 
@@ -1269,7 +1269,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
     // the weld of the vertex list: its table holds vertex_capacity distinct
     // positions; more report an overflow with a vertex count that fits on the rerun
     weld_dev_launch(w.soup, 3 * face_capacity, std::max<long long>(vertex_capacity, 1), w.tri, 3 * face_capacity,
-                    eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr, false);
+                    eff, w.weld, vertices, faces, w.tot + 8, status, st, nullptr);
     {
         iso::ProfScope ps("sparse_mc", st);
         sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);

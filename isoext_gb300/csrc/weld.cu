@@ -13,12 +13,10 @@
 //                 prefix over tiles by decoupled look-back, and the first
 //                 entries' new numbers and positions written out.
 //   weld_remap    triangle indices -> new numbers.
-//
-// A point whose x has the bits WELD_FREED is a free slot the producer left
-// after its own dedupe (no triangle names it); arithmetic on the GPU gives NaN
-// as 0x7fffffff, so no computed position has these bits.
 #include <algorithm>
 #include <cstdint>
+
+#include <cub/device/device_scan.cuh>
 
 #include "common.cuh"
 #include "lookback.cuh"
@@ -30,7 +28,6 @@ constexpr int WELD_THREADS = 256;
 constexpr int WELD_PER = 4;                           // entries per thread
 constexpr int WELD_TILE = WELD_THREADS * WELD_PER;    // entries per CTA
 constexpr uint32_t WELD_EMPTY = 0xffffffffu;          // a free table slot
-constexpr uint32_t WELD_FREED = 0xffffffffu;          // x bits of a freed point
 constexpr uint32_t WELD_NEW = 0x80000000u;            // rep[a]: a is a first entry; low bits its new number
 constexpr uint32_t WELD_PROBES = 512;  // the table is at most half full when the capacity holds the positions
 
@@ -75,7 +72,6 @@ __device__ __noinline__ uint32_t lookup_probe(const float* __restrict__ pts, con
     return a;  // not placed (the status says overflow)
 }
 
-template <bool kFreed>
 __global__ void __launch_bounds__(WELD_THREADS) weld_insert(const float* __restrict__ pts, long long A,
                                                             uint32_t* table, uint32_t mask, int* status,
                                                             const long long* __restrict__ dn) {
@@ -88,10 +84,7 @@ __global__ void __launch_bounds__(WELD_THREADS) weld_insert(const float* __restr
     for (int e = 0; e < WELD_PER; ++e) {
         const long long a = base + e * WELD_THREADS;
         live[e] = a < A;
-        if (live[e]) {
-            k[e] = key_of(pts, a);
-            if (kFreed && k[e].x == WELD_FREED) live[e] = false;
-        }
+        if (live[e]) k[e] = key_of(pts, a);
     }
 #pragma unroll
     for (int e = 0; e < WELD_PER; ++e)
@@ -116,11 +109,10 @@ __global__ void __launch_bounds__(WELD_THREADS) weld_insert(const float* __restr
 }
 
 // rep[a] <- WELD_NEW | new number for a first entry, else the first entry with
-// a's position (WELD_EMPTY for a freed point); vout / vsrc <- the first
+// a's position; vout / vsrc <- the first
 // entries' positions and entries (up to capV); vtot[0] <- the number of
 // distinct positions.  Tiles are taken in ticket order (ctr) and chained by
 // look-back (state, one word per tile, zeroed by the caller).
-template <bool kFreed>
 __global__ void __launch_bounds__(WELD_THREADS) weld_number(const float* __restrict__ pts, long long A,
                                                             const uint32_t* __restrict__ table, uint32_t mask,
                                                             uint32_t* __restrict__ rep, unsigned long long* state,
@@ -152,10 +144,7 @@ __global__ void __launch_bounds__(WELD_THREADS) weld_number(const float* __restr
     for (int e = 0; e < WELD_PER; ++e) {
         live[e] = a0 + e < A;
         r[e] = WELD_EMPTY;
-        if (live[e]) {
-            k[e] = key_of(pts, a0 + e);
-            if (kFreed && k[e].x == WELD_FREED) live[e] = false;
-        }
+        if (live[e]) k[e] = key_of(pts, a0 + e);
     }
 #pragma unroll
     for (int e = 0; e < WELD_PER; ++e)
@@ -209,7 +198,7 @@ __global__ void __launch_bounds__(WELD_THREADS) weld_number(const float* __restr
     for (int e = 0; e < WELD_PER; ++e) {
         if (a0 + e >= A) break;
         const uint32_t a = uint32_t(a0 + e);
-        if (live[e] && r[e] == a) {
+        if (r[e] == a) {
             rep[a] = WELD_NEW | uint32_t(no);
             if ((long long)no < capV) {  // past the capacity the caller sees V and retries
                 float* v = vout + 3 * no;
@@ -280,11 +269,10 @@ size_t weld_dev_workspace(long long capA, long long capU) { return weld_dev_carv
 
 // The weld of eff[0] points (at most capA) whose distinct positions fit capU:
 // eff[2] triangle indices (tri == nullptr: index i is point i; at most capT),
-// eff[3] vertex capacity of vout.  vtot[0] <- V.  freed: the list may hold
-// freed points.
+// eff[3] vertex capacity of vout.  vtot[0] <- V.
 void weld_dev_launch(const float* pts, long long capA, long long capU, const int32_t* tri, long long capT,
                      const long long* eff, void* ws, float* vout, int32_t* fout, long long* vtot, int* status,
-                     cudaStream_t st, uint32_t* vsrc, bool freed) {
+                     cudaStream_t st, uint32_t* vsrc) {
     const WeldDev w = weld_dev_carve(ws, capA, capU);
     iso::ProfScope ps("dc_weld", st, (capT > 0 ? 1 : 0) + (capA > 0 ? 2 : 0));
     if (capA > 0) {
@@ -292,13 +280,148 @@ void weld_dev_launch(const float* pts, long long capA, long long capU, const int
         unsigned int* ctr = reinterpret_cast<unsigned int*>(w.state + tiles);
         cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
         cudaMemsetAsync(w.state, 0, w.state_bytes, st);
-        const auto ins = freed ? weld_insert<true> : weld_insert<false>;
-        const auto num = freed ? weld_number<true> : weld_number<false>;
-        ins<<<tiles, WELD_THREADS, 0, st>>>(pts, capA, w.table, w.hcap - 1, status, eff);
-        num<<<tiles, WELD_THREADS, 0, st>>>(pts, capA, w.table, w.hcap - 1, w.rep, w.state, ctr, vout, vsrc, vtot,
-                                            status, eff);
+        weld_insert<<<tiles, WELD_THREADS, 0, st>>>(pts, capA, w.table, w.hcap - 1, status, eff);
+        weld_number<<<tiles, WELD_THREADS, 0, st>>>(pts, capA, w.table, w.hcap - 1, w.rep, w.state, ctr, vout, vsrc,
+                                                    vtot, status, eff);
     } else {
         cudaMemsetAsync(vtot, 0, 16, st);
     }
     if (capT > 0) weld_remap<<<tiles_for(capT), WELD_THREADS, 0, st>>>(tri, capT, w.rep, fout, eff);
 }
+
+// ---------------------------------------------------------------------------
+// Exact-position weld of a mesh (isoext src/utils.cu:32-59 with the degenerate
+// test of src/mc/nagae.cu:71): vertices with equal positions merge into the
+// first of them, faces with two equal vertices are dropped, and vertices no
+// remaining face uses are dropped.  The survivors keep their order (first
+// occurrence).  The marching cubes of a grid whose spacing comes within a few
+// ulps of its coordinates needs it: there, vertices of distinct grid edges can
+// round to one position.
+
+namespace {
+
+__global__ void __launch_bounds__(WELD_THREADS) mesh_lookup(const float* __restrict__ pts, long long V,
+                                                            const uint32_t* __restrict__ table, uint32_t mask,
+                                                            uint32_t* __restrict__ rep) {
+    const long long a = (long long)blockIdx.x * WELD_THREADS + threadIdx.x;
+    if (a >= V) return;
+    const Key k = key_of(pts, a);
+    uint32_t h = slot_of(k, mask);
+    const uint32_t cur = table[h];
+    if (cur != WELD_EMPTY && same(key_of(pts, cur), k)) rep[a] = cur;
+    else rep[a] = cur == WELD_EMPTY ? uint32_t(a) : lookup_probe(pts, table, mask, k, h, uint32_t(a));
+}
+
+// Faces through rep; keep[i] = no two corners at one position; used[v] = 1
+// for the corners of kept faces (stores of one value: the races are benign).
+__global__ void __launch_bounds__(WELD_THREADS) mesh_faces(const int32_t* __restrict__ f, long long F,
+                                                           const uint32_t* __restrict__ rep,
+                                                           uint32_t* __restrict__ f2, uint32_t* __restrict__ keep,
+                                                           uint32_t* __restrict__ used) {
+    const long long i = (long long)blockIdx.x * WELD_THREADS + threadIdx.x;
+    if (i >= F) return;
+    const uint32_t a = rep[f[3 * i]], b = rep[f[3 * i + 1]], c = rep[f[3 * i + 2]];
+    const bool k = a != b && a != c && b != c;
+    keep[i] = k ? 1u : 0u;
+    f2[3 * i] = a; f2[3 * i + 1] = b; f2[3 * i + 2] = c;
+    if (k) { used[a] = 1u; used[b] = 1u; used[c] = 1u; }
+}
+
+__global__ void __launch_bounds__(WELD_THREADS) mesh_write(const float* __restrict__ v, long long V, long long F,
+                                                           const uint32_t* __restrict__ used,
+                                                           const uint32_t* __restrict__ vnum,
+                                                           const uint32_t* __restrict__ keep,
+                                                           const uint32_t* __restrict__ fnum,
+                                                           const uint32_t* __restrict__ f2, float* __restrict__ vout,
+                                                           int32_t* __restrict__ fout, int32_t* __restrict__ vsrc,
+                                                           long long* counts) {
+    const long long i = (long long)blockIdx.x * WELD_THREADS + threadIdx.x;
+    if (i < V && used[i]) {
+        const uint32_t o = vnum[i];
+        vout[3ll * o] = v[3 * i]; vout[3ll * o + 1] = v[3 * i + 1]; vout[3ll * o + 2] = v[3 * i + 2];
+        if (vsrc) vsrc[o] = int32_t(i);
+    }
+    if (i < F && keep[i]) {
+        const uint32_t o = fnum[i];
+        fout[3ll * o] = int32_t(vnum[f2[3 * i]]);
+        fout[3ll * o + 1] = int32_t(vnum[f2[3 * i + 1]]);
+        fout[3ll * o + 2] = int32_t(vnum[f2[3 * i + 2]]);
+    }
+    if (i == 0) {
+        counts[0] = V ? (long long)vnum[V - 1] + used[V - 1] : 0;
+        counts[1] = F ? (long long)fnum[F - 1] + keep[F - 1] : 0;
+    }
+}
+
+struct MeshWs {
+    uint32_t *table, *rep, *used, *vnum, *f2, *keep, *fnum;
+    void* temp;
+    size_t temp_bytes, total;
+    uint32_t hcap;
+};
+
+MeshWs mesh_carve(void* ws, long long V, long long F) {
+    MeshWs w{};
+    w.hcap = 1024;
+    while ((long long)w.hcap < 2 * V + 1024) w.hcap <<= 1;
+    size_t tv = 0, tf = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tv, (const uint32_t*)nullptr, (uint32_t*)nullptr, int(std::max(V, 1ll)));
+    cub::DeviceScan::ExclusiveSum(nullptr, tf, (const uint32_t*)nullptr, (uint32_t*)nullptr, int(std::max(F, 1ll)));
+    w.temp_bytes = std::max(tv, tf);
+    uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        uint8_t* p = ws ? b + o : nullptr;
+        o = (o + std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        return p;
+    };
+    w.table = reinterpret_cast<uint32_t*>(take(size_t(w.hcap) * 4));
+    w.rep = reinterpret_cast<uint32_t*>(take(size_t(V) * 4));
+    w.used = reinterpret_cast<uint32_t*>(take(size_t(V) * 4));
+    w.vnum = reinterpret_cast<uint32_t*>(take(size_t(V) * 4));
+    w.f2 = reinterpret_cast<uint32_t*>(take(size_t(F) * 12));
+    w.keep = reinterpret_cast<uint32_t*>(take(size_t(F) * 4));
+    w.fnum = reinterpret_cast<uint32_t*>(take(size_t(F) * 4));
+    w.temp = take(w.temp_bytes);
+    w.total = o + 256;
+    return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t iso_weld_mesh_workspace_size(long long V, long long F) {
+    if (V < 0 || F < 0 || V > 0x7fffffffll || F > 0x7fffffffll) return 0;
+    return mesh_carve(nullptr, V, F).total;
+}
+
+int iso_weld_mesh(const float* vertices, long long V, const int* faces, long long F, float* vout, int* fout,
+                  int* vsrc, long long* counts, int* status, void* workspace, size_t workspace_bytes,
+                  void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (V < 0 || F < 0 || V > 0x7fffffffll || F > 0x7fffffffll || !counts || !status) return ISO_ERR_ARG;
+    if ((V && (!vertices || !vout)) || (F && (!faces || !fout))) return ISO_ERR_ARG;
+    if (workspace_bytes < iso_weld_mesh_workspace_size(V, F)) return ISO_ERR_WORKSPACE;
+    if (V == 0 || F == 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    const MeshWs w = mesh_carve(workspace, V, F);
+    iso::ProfScope ps("weld_mesh", st, 4);
+    cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
+    cudaMemsetAsync(w.used, 0, size_t(V) * 4, st);
+    weld_insert<<<tiles_for(V), WELD_THREADS, 0, st>>>(vertices, V, w.table, w.hcap - 1, status, nullptr);
+    mesh_lookup<<<unsigned((V + WELD_THREADS - 1) / WELD_THREADS), WELD_THREADS, 0, st>>>(vertices, V, w.table,
+                                                                                         w.hcap - 1, w.rep);
+    mesh_faces<<<unsigned((F + WELD_THREADS - 1) / WELD_THREADS), WELD_THREADS, 0, st>>>(
+        reinterpret_cast<const int32_t*>(faces), F, w.rep, w.f2, w.keep, w.used);
+    size_t tb = w.temp_bytes;
+    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.used, w.vnum, int(V), st) != cudaSuccess) return ISO_ERR_CUDA;
+    tb = w.temp_bytes;
+    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.keep, w.fnum, int(F), st) != cudaSuccess) return ISO_ERR_CUDA;
+    const long long n = std::max(V, F);
+    mesh_write<<<unsigned((n + WELD_THREADS - 1) / WELD_THREADS), WELD_THREADS, 0, st>>>(
+        vertices, V, F, w.used, w.vnum, w.keep, w.fnum, w.f2, vout, reinterpret_cast<int32_t*>(fout),
+        reinterpret_cast<int32_t*>(vsrc), counts);
+    return cudaGetLastError() == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -116,18 +116,11 @@ def _mc_finish(L: _Launch, h):
 
 def _weld_positions(v, f, e):
     """mc.weld_by_position, keeping for each vertex the edge of the first vertex
-    merged into it."""
-    vn = torch.where(v == 0, torch.zeros_like(v), v)
-    uniq, inv = torch.unique(vn.view(torch.int32), dim=0, return_inverse=True)
-    first = torch.full((len(uniq),), len(v), dtype=torch.int64, device=v.device)
-    first.scatter_reduce_(0, inv, torch.arange(len(v), device=v.device), reduce="amin")
-    f2 = inv[f.long()]
-    keep = (f2[:, 0] != f2[:, 1]) & (f2[:, 0] != f2[:, 2]) & (f2[:, 1] != f2[:, 2])
-    f2 = f2[keep]
-    used = torch.zeros(len(uniq), dtype=torch.bool, device=v.device)
-    used[f2.reshape(-1)] = True
-    remap = torch.cumsum(used.to(torch.int64), 0) - 1
-    return uniq[used].view(torch.float32), remap[f2].to(torch.int32), e[first[used]]
+    merged into it (iso_weld_mesh reports each survivor's input vertex)."""
+    v2, f2, src = _ffi.weld_mesh(v, f, want_source=True)
+    if v2 is None:
+        return v[:0], f[:0], e[:0]
+    return v2, f2, e[src.long()]
 
 
 def _smalls(values_list):

@@ -86,21 +86,11 @@ def weld_by_position(v: torch.Tensor, f: torch.Tensor):
     """Merge vertices with bit-identical positions (+0 and -0 equal), drop faces
     that became degenerate and vertices no face uses -- the result of isoext's
     position weld (src/utils.cu:32-59 with the degenerate test of
-    src/mc/nagae.cu:71) applied to a key-welded mesh."""
+    src/mc/nagae.cu:71) applied to a key-welded mesh.  On the device
+    (iso_weld_mesh); the survivors keep their order."""
     if v is None or len(f) == 0:
         return v, f
-    vn = torch.where(v == 0, torch.zeros_like(v), v)
-    bits = vn.view(torch.int32)
-    uniq, inv = torch.unique(bits, dim=0, return_inverse=True)
-    f2 = inv[f.long()]
-    keep = (f2[:, 0] != f2[:, 1]) & (f2[:, 0] != f2[:, 2]) & (f2[:, 1] != f2[:, 2])
-    f2 = f2[keep]
-    if len(f2) == 0:
-        return None, None
-    used = torch.zeros(len(uniq), dtype=torch.bool, device=v.device)
-    used[f2.reshape(-1)] = True
-    remap = torch.cumsum(used.to(torch.int64), 0) - 1
-    return uniq[used].view(torch.float32).contiguous(), remap[f2].to(torch.int32).contiguous()
+    return _ffi.weld_mesh(v, f)
 
 
 def _mc_uniform(grid: UniformGrid, level: float, method: int):

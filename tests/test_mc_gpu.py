@@ -272,3 +272,41 @@ def test_bounded_wait_times_out_with_a_status():
                                      ctypes.c_void_p(out.data_ptr()), None) == _ffi.ISO_ERR_ARG
     v, f = run_mc(sphere((24, 24, 24), 0.5))
     assert len(f) > 0
+
+
+def _weld_mesh_np(v, f):
+    """isoext's position weld restated: the first vertex of each position
+    (bits, -0 read as +0), faces with two equal vertices dropped, unused
+    vertices dropped, order kept."""
+    vn = np.where(v == 0, np.float32(0), v).astype(np.float32)
+    bits = vn.view(np.uint32)
+    first = {}
+    rep = np.empty(len(v), np.int64)
+    for i, key in enumerate(map(bytes, bits)):
+        rep[i] = first.setdefault(key, i)
+    f2 = rep[f]
+    keep = (f2[:, 0] != f2[:, 1]) & (f2[:, 0] != f2[:, 2]) & (f2[:, 1] != f2[:, 2])
+    f2 = f2[keep]
+    used = np.zeros(len(v), bool)
+    used[f2.ravel()] = True
+    num = np.cumsum(used) - 1
+    return v[used], num[f2].astype(np.int32), np.nonzero(used)[0]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_weld_mesh_matches_the_position_weld(seed):
+    """iso_weld_mesh (the path of grids whose spacing comes within a few ulps of
+    their coordinates) against the restated weld, with repeated positions, -0
+    against +0, faces that become degenerate and vertices no face uses."""
+    from isoext_gb300 import _ffi
+
+    rng = np.random.default_rng(seed)
+    pool = rng.integers(-3, 4, size=(400, 3)).astype(np.float32) * np.float32(0.25)
+    pool[rng.random(400) < 0.1, 0] = np.float32(-0.0)
+    v = pool[rng.integers(0, 400, size=3000)]
+    f = rng.integers(0, 3000, size=(5000, 3)).astype(np.int32)
+    vo, fo, so = _weld_mesh_np(v, f)
+    vg, fg, sg = _ffi.weld_mesh(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda(), want_source=True)
+    assert np.array_equal(vg.cpu().numpy().view(np.uint32), vo.view(np.uint32))
+    assert np.array_equal(fg.cpu().numpy(), fo)
+    assert np.array_equal(sg.cpu().numpy(), so)
