@@ -409,13 +409,22 @@ long long iso_serve_submit(IsoServer *server, const IsoServeRequest *request);
  * ISO_ERR_TIMEOUT when it runs out) and moves its result out. */
 int iso_serve_wait(IsoServer *server, long long ticket, double timeout_s, IsoServeResult *result);
 void iso_serve_free_result(IsoServeResult *result);
-/* stats[0] completed, [1] most requests running at once, [2] most device
- * bytes the server held at once (never above budget_bytes), [3] queued now. */
+/* stats[0] completed, [1] most workers running at once (a worker runs one
+ * request, or one bucket of them), [2] most device bytes the server held at
+ * once (never above budget_bytes), [3] queued now. */
 int iso_serve_stats(IsoServer *server, long long *stats);
-/* The first `count` (<= 10) of: the four above, [4] device bytes held now,
+/* The first `count` (<= 12) of: the four above, [4] device bytes held now,
  * [5] entries evicted, [6] entries cached, [7] count passes run, [8] entries
- * grown for a larger mesh, [9] the budget. */
+ * grown for a larger mesh, [9] the budget, [10] launches that ran more than
+ * one request, [11] the requests they ran. */
 int iso_serve_stats_ex(IsoServer *server, long long *stats, int count);
+/* Length buckets: a worker takes, with the request at the head of the queue,
+ * up to max_requests - 1 queued requests of the same kind, grid size, method
+ * and level, and runs them with one launch of a graph with one parallel branch
+ * per request (max_requests 1, 2, 4 or 8; with fewer matching requests the
+ * largest power of two of them runs).  1 (the default): one launch per
+ * request. */
+int iso_serve_set_bucket(IsoServer *server, int max_requests);
 /* Finishes the queued requests, then frees everything. */
 int iso_serve_destroy(IsoServer *server);
 /* Capacities of the entries built after the call, as a fraction (0, 1] of the

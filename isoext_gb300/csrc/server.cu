@@ -20,6 +20,13 @@
 // grows the entry from the exact sizes it reported, and the graph runs again.
 // Allocations come from a private stream-ordered pool, so freeing an entry does
 // not synchronise the device.  No counterpart in isoext.
+//
+// Length buckets (iso_serve_set_bucket): a worker takes, with the request at
+// the head of the queue, up to B - 1 queued requests of the same kind, grid
+// size, method and level, and runs them with one launch of a graph that holds
+// B parallel branches (fork / join over the slot's helper streams), one per
+// request, on an entry with B sets of buffers.  B is a power of two; with
+// fewer matching requests the next smaller bucket runs.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -69,13 +76,15 @@ size_t ws_bytes(int kind, int n, Caps c) {
 
 size_t al(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Device bytes of an entry's values, outputs and workspace.
-size_t entry_bytes(int kind, int n, Caps c) {
-    return al(size_t(4) * n * n * n) + al(size_t(12) * c.v) + al(size_t(12) * c.f) + al(ws_bytes(kind, n, c)) + 256;
+// Device bytes of an entry of B requests: values and sizes (kept across
+// resizes), and outputs and workspaces (resized).
+size_t entry_fixed_bytes(int B, int n) { return size_t(B) * al(size_t(4) * n * n * n) + al(size_t(64) * B) + 256; }
+size_t entry_var_bytes(int B, int kind, int n, Caps c) {
+    return size_t(B) * (al(size_t(12) * c.v) + al(size_t(12) * c.f) + al(ws_bytes(kind, n, c)));
 }
 
 // The smallest footprint of a request: its count pass.
-size_t count_pass_bytes(int kind, int n) { return entry_bytes(kind, n, Caps{1, 1}); }
+size_t count_pass_bytes(int kind, int n) { return entry_fixed_bytes(1, n) + entry_var_bytes(1, kind, n, Caps{1, 1}); }
 
 // Capacities for a mesh whose sizes a pass counted: MC counts vertices and
 // faces, DC active cells (its vertices at most) and quads (two faces each).
@@ -97,19 +106,29 @@ struct Done {
     IsoServeResult r;
 };
 
-// A cache entry: one slot's buffers for one (kind, n, method, level), and its graph.
-struct Entry {
-    int kind = 0, n = 0, method = 0;
-    float level = 0.0f;
-    int slot = 0;
-    Caps cap{0, 0};
-    size_t bytes = 0;  // counted against the budget
+constexpr int BUCKET_MAX = 8;  // requests of one launch at most
+
+// One request's buffers in an entry.
+struct Part {
     float* values = nullptr;
     float* vout = nullptr;
     int* fout = nullptr;
     void* ws = nullptr;
+    long long* small = nullptr;  // counts, status (MC at [2], DC at [6]); 8 words in the entry's block
+};
+
+// A cache entry: one slot's buffers for B requests of one (kind, n, method,
+// level), and its graph (B parallel branches).
+struct Entry {
+    int kind = 0, n = 0, method = 0;
+    float level = 0.0f;
+    int slot = 0;
+    int B = 1;
+    Caps cap{0, 0};
+    size_t bytes = 0;  // counted against the budget
     size_t wsb = 0;
-    long long* small = nullptr;  // counts, status (MC at [2], DC at [6])
+    Part part[BUCKET_MAX];
+    long long* small = nullptr;  // B blocks of 8 words, one copy to the host
     cudaGraphExec_t exec = nullptr;
     bool in_use = false;
     long long last_use = 0;
@@ -117,23 +136,46 @@ struct Entry {
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    float* prims_dev = nullptr;
-    float* prims_host = nullptr;      // pinned
-    long long* small_host = nullptr;  // pinned [8]
+    cudaStream_t fork[BUCKET_MAX - 1] = {};  // the branches of bucket graphs
+    cudaEvent_t ev_fork = nullptr, ev_join[BUCKET_MAX - 1] = {};
+    float* prims_dev = nullptr;       // BUCKET_MAX unions
+    float* prims_host = nullptr;      // pinned, BUCKET_MAX unions
+    long long* small_host = nullptr;  // pinned, BUCKET_MAX blocks of 8 words
     uint8_t* out_host = nullptr;      // pinned staging of the largest mesh
     size_t out_bytes = 0;
     std::vector<Entry*> entries;      // guarded by the server's mutex
 };
 
-int queue_extraction(const Entry& b, const float* prims_dev, cudaStream_t st) {
-    if (cudaMemsetAsync(b.small, 0, 64, st) != cudaSuccess) return ISO_ERR_CUDA;
-    int rc = iso_sdf_union_grid(prims_dev, b.n, b.n, b.n, LO, HI, b.values, st);
+// Request `i` of entry `e`: its grid from the union at prims_dev, then its
+// extraction.
+int queue_extraction(const Entry& e, int i, const float* prims_dev, cudaStream_t st) {
+    const Part& p = e.part[i];
+    if (cudaMemsetAsync(p.small, 0, 64, st) != cudaSuccess) return ISO_ERR_CUDA;
+    int rc = iso_sdf_union_grid(prims_dev, e.n, e.n, e.n, LO, HI, p.values, st);
     if (rc) return rc;
-    if (b.kind == 0)
-        return iso_mc_dense(b.values, b.n, b.n, b.n, LO, HI, b.level, b.method, b.vout, b.cap.v, b.fout, b.cap.f, b.ws,
-                            b.wsb, b.small, reinterpret_cast<int*>(b.small + 2), st);
-    return iso_dc_dense(b.values, b.n, b.n, b.n, LO, HI, b.level, DC_REG, DC_SVD_TOL, b.vout, b.cap.v, b.fout, b.cap.f,
-                        b.ws, b.wsb, b.small, reinterpret_cast<int*>(b.small + 6), st);
+    if (e.kind == 0)
+        return iso_mc_dense(p.values, e.n, e.n, e.n, LO, HI, e.level, e.method, p.vout, e.cap.v, p.fout, e.cap.f, p.ws,
+                            e.wsb, p.small, reinterpret_cast<int*>(p.small + 2), st);
+    return iso_dc_dense(p.values, e.n, e.n, e.n, LO, HI, e.level, DC_REG, DC_SVD_TOL, p.vout, e.cap.v, p.fout,
+                        e.cap.f, p.ws, e.wsb, p.small, reinterpret_cast<int*>(p.small + 6), st);
+}
+
+// Every request of entry e; with B > 1 each on its own branch (fork and join
+// over the slot's helper streams, which a capture of `st` takes in).
+int queue_entry(const Entry& e, Slot& s, cudaStream_t st) {
+    if (e.B == 1) return queue_extraction(e, 0, s.prims_dev, st);
+    if (cudaEventRecord(s.ev_fork, st) != cudaSuccess) return ISO_ERR_CUDA;
+    for (int i = 1; i < e.B; ++i)
+        if (cudaStreamWaitEvent(s.fork[i - 1], s.ev_fork, 0) != cudaSuccess) return ISO_ERR_CUDA;
+    for (int i = 0; i < e.B; ++i) {
+        const int rc = queue_extraction(e, i, s.prims_dev + size_t(i) * PRIM_FLOATS, i ? s.fork[i - 1] : st);
+        if (rc) return rc;
+    }
+    for (int i = 1; i < e.B; ++i)
+        if (cudaEventRecord(s.ev_join[i - 1], s.fork[i - 1]) != cudaSuccess ||
+            cudaStreamWaitEvent(st, s.ev_join[i - 1], 0) != cudaSuccess)
+            return ISO_ERR_CUDA;
+    return ISO_OK;
 }
 
 }  // namespace
@@ -152,21 +194,24 @@ struct IsoServer {
     long long next_ticket = 0;
     long long held = 0, max_held = 0;  // device bytes the server holds
     long long evictions = 0, count_passes = 0, grows = 0, clock = 0;
-    int running = 0, max_running = 0;
-    int waiting = 0;  // running requests blocked in acquire
+    long long buckets = 0, bucketed = 0;  // launches of more than one request, and their requests
+    int running = 0, max_running = 0;     // workers with requests in hand
+    int waiting = 0;                      // of them, blocked in acquire
     long long completed = 0;
     bool closing = false;
     double cap_scale = 1.0;  // capacities of entries built or grown from now on (tests shrink them)
+    int bucket_max = 1;      // requests per launch at most (a power of two)
 
     bool acquire(long long bytes);
     void release(long long bytes);
     void free_entry(Entry* e);
     void* alloc(size_t bytes, cudaStream_t st);
-    Entry* entry_for(int slot, const Job& job, int* err);
-    Entry* build(int slot, int kind, int n, int method, float level, const float* prims_host, bool warm, int* err);
+    Entry* entry_for(int slot, const Job& job, int B, int* err);
+    Entry* build(int slot, int kind, int n, int method, float level, const float* prims_host, bool warm, int B,
+                 int* err);
     int size_entry(Entry* e, Caps c);
     void worker(int index);
-    void run(int slot, Job& job, IsoServeResult& r);
+    void run(int slot, const std::vector<Job*>& jobs, std::vector<IsoServeResult>& res);
 };
 
 // Counts `bytes` against the budget, evicting idle entries (least recently
@@ -193,8 +238,8 @@ bool IsoServer::acquire(long long bytes) {
             lk.lock();
             continue;
         }
-        // every other running request waits for memory too: nothing can free
-        // any, so this request gives up (its result reports ISO_ERR_WORKSPACE)
+        // every other running worker waits for memory too: nothing can free
+        // any, so this one gives up (its results report ISO_ERR_WORKSPACE)
         if (waiting + 1 >= running) return false;
         ++waiting;
         cv_mem.wait(lk);
@@ -222,55 +267,64 @@ void* IsoServer::alloc(size_t bytes, cudaStream_t st) {
 void IsoServer::free_entry(Entry* e) {
     cudaStream_t st = free_stream;
     if (e->exec) cudaGraphExecDestroy(e->exec);
-    for (void* p : {(void*)e->values, (void*)e->vout, (void*)e->fout, e->ws, (void*)e->small})
-        if (p) cudaFreeAsync(p, st);
+    for (int i = 0; i < e->B; ++i)
+        for (void* p : {(void*)e->part[i].values, (void*)e->part[i].vout, (void*)e->part[i].fout, e->part[i].ws})
+            if (p) cudaFreeAsync(p, st);
+    if (e->small) cudaFreeAsync(e->small, st);
     release((long long)e->bytes);
     delete e;
 }
 
-// (Re)sizes an entry's outputs and workspace to capacities c and captures its
+// (Re)sizes an entry's outputs and workspaces to capacities c and captures its
 // graph.  The values and sizes buffers stay.  The entry is its slot's alone.
 int IsoServer::size_entry(Entry* e, Caps c) {
-    cudaStream_t st = slots[e->slot].stream;
-    const size_t old_var = e->bytes - (al(size_t(4) * e->n * e->n * e->n) + 256);
+    Slot& s = slots[e->slot];
+    cudaStream_t st = s.stream;
+    const size_t old_var = e->bytes - entry_fixed_bytes(e->B, e->n);
     if (e->exec) {
         cudaGraphExecDestroy(e->exec);
         e->exec = nullptr;
     }
-    for (void* p : {(void*)e->vout, (void*)e->fout, e->ws})
-        if (p) cudaFreeAsync(p, st);
-    e->vout = nullptr;
-    e->fout = nullptr;
-    e->ws = nullptr;
+    for (int i = 0; i < e->B; ++i) {
+        Part& p = e->part[i];
+        for (void* q : {(void*)p.vout, (void*)p.fout, p.ws})
+            if (q) cudaFreeAsync(q, st);
+        p.vout = nullptr;
+        p.fout = nullptr;
+        p.ws = nullptr;
+    }
     e->bytes -= old_var;
     release((long long)old_var);
-    const size_t wsb = ws_bytes(e->kind, e->n, c);
-    const size_t var = al(size_t(12) * c.v) + al(size_t(12) * c.f) + al(wsb);
+    const size_t var = entry_var_bytes(e->B, e->kind, e->n, c);
     if (!acquire((long long)var)) return ISO_ERR_WORKSPACE;
     e->bytes += var;
     e->cap = c;
-    e->wsb = wsb;
-    e->vout = static_cast<float*>(alloc(size_t(12) * c.v, st));
-    e->fout = static_cast<int*>(alloc(size_t(12) * c.f, st));
-    e->ws = alloc(wsb, st);
-    if (!e->vout || !e->fout || !e->ws) return ISO_ERR_CUDA;
+    e->wsb = ws_bytes(e->kind, e->n, c);
+    for (int i = 0; i < e->B; ++i) {
+        Part& p = e->part[i];
+        p.vout = static_cast<float*>(alloc(size_t(12) * c.v, st));
+        p.fout = static_cast<int*>(alloc(size_t(12) * c.f, st));
+        p.ws = alloc(e->wsb, st);
+        if (!p.vout || !p.fout || !p.ws) return ISO_ERR_CUDA;
+    }
     // once outside a graph (first-use set-up of the kernels), then the capture
-    if (queue_extraction(*e, slots[e->slot].prims_dev, st) != 0 || cudaStreamSynchronize(st) != cudaSuccess)
-        return ISO_ERR_CUDA;
+    for (int i = 0; i < e->B; ++i)
+        if (queue_extraction(*e, i, s.prims_dev + size_t(i) * PRIM_FLOATS, st) != 0) return ISO_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return ISO_ERR_CUDA;
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return ISO_ERR_CUDA;
-    const int rc = queue_extraction(*e, slots[e->slot].prims_dev, st);
+    const int rc = queue_entry(*e, s, st);
     const bool ended = cudaStreamEndCapture(st, &graph) == cudaSuccess;
     const bool ok = rc == 0 && ended && cudaGraphInstantiate(&e->exec, graph, 0) == cudaSuccess;
     if (graph) cudaGraphDestroy(graph);
     return ok ? ISO_OK : ISO_ERR_CUDA;
 }
 
-// A new entry for `slot`.  Warm entries (built before any request) take the
-// closed-surface bound; others run a count pass on the request's own union
-// (prims_host) and take its exact sizes plus headroom.
+// A new entry of B requests for `slot`.  Warm entries (built before any
+// request) take the closed-surface bound; others run a count pass on the
+// request's own union (prims_host) and take its exact sizes plus headroom.
 Entry* IsoServer::build(int slot, int kind, int n, int method, float level, const float* prims_host, bool warm,
-                        int* err) {
+                        int B, int* err) {
     Slot& s = slots[slot];
     cudaStream_t st = s.stream;
     auto* e = new Entry;
@@ -279,28 +333,35 @@ Entry* IsoServer::build(int slot, int kind, int n, int method, float level, cons
     e->method = method;
     e->level = level;
     e->slot = slot;
+    e->B = B;
     e->cap = Caps{1, 1};
     e->wsb = ws_bytes(kind, n, e->cap);
-    const size_t b0 = count_pass_bytes(kind, n);
+    const size_t b0 = entry_fixed_bytes(B, n) + entry_var_bytes(B, kind, n, e->cap);
     if (!acquire((long long)b0)) {
         delete e;
         *err = ISO_ERR_WORKSPACE;
         return nullptr;
     }
     e->bytes = b0;
-    e->values = static_cast<float*>(alloc(size_t(4) * n * n * n, st));
-    e->vout = static_cast<float*>(alloc(12, st));
-    e->fout = static_cast<int*>(alloc(12, st));
-    e->ws = alloc(e->wsb, st);
-    e->small = static_cast<long long*>(alloc(64, st));
-    int rc = (e->values && e->vout && e->fout && e->ws && e->small) ? ISO_OK : ISO_ERR_CUDA;
+    e->small = static_cast<long long*>(alloc(size_t(64) * B, st));
+    bool have = e->small != nullptr;
+    for (int i = 0; i < B; ++i) {
+        Part& p = e->part[i];
+        p.values = static_cast<float*>(alloc(size_t(4) * n * n * n, st));
+        p.vout = static_cast<float*>(alloc(12, st));
+        p.fout = static_cast<int*>(alloc(12, st));
+        p.ws = alloc(e->wsb, st);
+        p.small = e->small ? e->small + 8 * i : nullptr;
+        have = have && p.values && p.vout && p.fout && p.ws;
+    }
+    int rc = have ? ISO_OK : ISO_ERR_CUDA;
     Caps c = warm_caps(n);
     if (rc == ISO_OK && !warm) {
         // the count pass: the extraction with capacity 1 reports the exact sizes
         std::memcpy(s.prims_host, prims_host, sizeof(float) * PRIM_FLOATS);
         rc = cudaMemcpyAsync(s.prims_dev, s.prims_host, sizeof(float) * PRIM_FLOATS, cudaMemcpyHostToDevice, st) ==
-                         cudaSuccess && queue_extraction(*e, s.prims_dev, st) == 0 &&
-                     cudaMemcpyAsync(s.small_host, e->small, 64, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                         cudaSuccess && queue_extraction(*e, 0, s.prims_dev, st) == 0 &&
+                     cudaMemcpyAsync(s.small_host, e->part[0].small, 64, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
                      cudaStreamSynchronize(st) == cudaSuccess
                  ? ISO_OK
                  : ISO_ERR_CUDA;
@@ -322,20 +383,20 @@ Entry* IsoServer::build(int slot, int kind, int n, int method, float level, cons
     return e;
 }
 
-// The job's entry on `slot`, marked in use: cached, or built now.
-Entry* IsoServer::entry_for(int slot, const Job& job, int* err) {
+// The entry of B requests like `job` on `slot`, marked in use: cached, or built now.
+Entry* IsoServer::entry_for(int slot, const Job& job, int B, int* err) {
     const IsoServeRequest& q = job.req;
     const int method = q.kind == 0 ? q.method : 0;  // dual contouring has no method
     {
         std::lock_guard<std::mutex> lk(mu);
         for (Entry* e : slots[slot].entries)
-            if (e->kind == q.kind && e->n == q.n && e->method == method && e->level == q.level) {
+            if (e->kind == q.kind && e->n == q.n && e->method == method && e->level == q.level && e->B == B) {
                 e->in_use = true;
                 e->last_use = ++clock;
                 return e;
             }
     }
-    Entry* e = build(slot, q.kind, q.n, method, q.level, job.prims, false, err);
+    Entry* e = build(slot, q.kind, q.n, method, q.level, job.prims, false, B, err);
     if (!e) return nullptr;
     std::lock_guard<std::mutex> lk(mu);
     e->in_use = true;
@@ -344,94 +405,141 @@ Entry* IsoServer::entry_for(int slot, const Job& job, int* err) {
     return e;
 }
 
-void IsoServer::run(int slot, Job& job, IsoServeResult& r) {
+// Requests of one kind, size, method and level (the same entry and graph).
+bool same_key(const Job& a, const Job& b) {
+    return a.req.kind == b.req.kind && a.req.n == b.req.n && a.req.level == b.req.level &&
+           (a.req.kind != 0 || a.req.method == b.req.method);
+}
+
+void IsoServer::run(int slot, const std::vector<Job*>& jobs, std::vector<IsoServeResult>& res) {
     Slot& s = slots[slot];
+    const int B = int(jobs.size());
     int err = 0;
-    Entry* b = entry_for(slot, job, &err);
+    Entry* b = entry_for(slot, *jobs[0], B, &err);
     if (!b) {
-        r.status = err;
+        for (IsoServeResult& r : res) r.status = err;
         return;
     }
-    std::memcpy(s.prims_host, job.prims, sizeof(job.prims));
+    for (int i = 0; i < B; ++i) std::memcpy(s.prims_host + size_t(i) * PRIM_FLOATS, jobs[i]->prims, sizeof(jobs[i]->prims));
     cudaStream_t st = s.stream;
     const int at = b->kind == 0 ? 2 : 6;
-    bool ok = cudaMemcpyAsync(s.prims_dev, s.prims_host, sizeof(job.prims), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+    const size_t pbytes = sizeof(float) * PRIM_FLOATS * B;
+    bool ok = cudaMemcpyAsync(s.prims_dev, s.prims_host, pbytes, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaGraphLaunch(b->exec, st) == cudaSuccess &&
-              cudaMemcpyAsync(s.small_host, b->small, 64, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+              cudaMemcpyAsync(s.small_host, b->small, size_t(64) * B, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
               cudaStreamSynchronize(st) == cudaSuccess;
-    int status = ok ? int(s.small_host[at] & 0xffffffffll) : ISO_ERR_CUDA;
-    if (status == ISO_ERR_OVERFLOW) {
-        // larger than the entry's buffers: grow it from the exact sizes this run
-        // counted, and run again
+    bool over = false;
+    for (int i = 0; ok && i < B; ++i) over = over || int(s.small_host[8 * i + at] & 0xffffffffll) == ISO_ERR_OVERFLOW;
+    int rc = ISO_OK;
+    if (ok && over) {
+        // a mesh larger than the entry's buffers: grow every request's buffers
+        // to the largest sizes this run counted, and run again
         {
             std::lock_guard<std::mutex> lk(mu);
             ++grows;
         }
-        const int rc = size_entry(b, caps_from_counts(b->kind, s.small_host, 1.0));
-        ok = rc == ISO_OK && cudaGraphLaunch(b->exec, st) == cudaSuccess &&
-             cudaMemcpyAsync(s.small_host, b->small, 64, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-             cudaStreamSynchronize(st) == cudaSuccess;
-        status = ok ? int(s.small_host[at] & 0xffffffffll) : (rc ? rc : ISO_ERR_CUDA);
-    }
-    const long long V = s.small_host[0], F = s.small_host[1];
-    if (status == 0 && V > 0 && F > 0) {
-        r.vertices = static_cast<float*>(std::malloc(size_t(12) * V));
-        r.faces = static_cast<int*>(std::malloc(size_t(12) * F));
-        const size_t vb = size_t(12) * V, fb = size_t(12) * F;
-        if (!r.vertices || !r.faces) {
-            status = ISO_ERR_ARG;
-        } else if (vb + fb <= s.out_bytes) {
-            ok = cudaMemcpyAsync(s.out_host, b->vout, vb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-                 cudaMemcpyAsync(s.out_host + vb, b->fout, fb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-                 cudaStreamSynchronize(st) == cudaSuccess;
-            if (ok) {
-                std::memcpy(r.vertices, s.out_host, vb);
-                std::memcpy(r.faces, s.out_host + vb, fb);
-            }
-        } else {
-            ok = cudaMemcpyAsync(r.vertices, b->vout, vb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-                 cudaMemcpyAsync(r.faces, b->fout, fb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-                 cudaStreamSynchronize(st) == cudaSuccess;
+        Caps c{1, 1};
+        for (int i = 0; i < B; ++i) {
+            const Caps ci = caps_from_counts(b->kind, s.small_host + 8 * i, 1.0);
+            c.v = std::max(c.v, ci.v);
+            c.f = std::max(c.f, ci.f);
         }
-        if (!ok) status = ISO_ERR_CUDA;
-        r.num_vertices = V;
-        r.num_faces = F;
+        rc = size_entry(b, c);
+        ok = rc == ISO_OK && cudaGraphLaunch(b->exec, st) == cudaSuccess &&
+             cudaMemcpyAsync(s.small_host, b->small, size_t(64) * B, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    for (int i = 0; i < B; ++i) {
+        IsoServeResult& r = res[i];
+        const long long* sm = s.small_host + 8 * i;
+        int status = ok ? int(sm[at] & 0xffffffffll) : (rc ? rc : ISO_ERR_CUDA);
+        const long long V = sm[0], F = sm[1];
+        if (status == 0 && V > 0 && F > 0) {
+            const Part& p = b->part[i];
+            r.vertices = static_cast<float*>(std::malloc(size_t(12) * V));
+            r.faces = static_cast<int*>(std::malloc(size_t(12) * F));
+            const size_t vb = size_t(12) * V, fb = size_t(12) * F;
+            bool got = false;
+            if (!r.vertices || !r.faces) {
+                status = ISO_ERR_ARG;
+            } else if (vb + fb <= s.out_bytes) {
+                got = cudaMemcpyAsync(s.out_host, p.vout, vb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                      cudaMemcpyAsync(s.out_host + vb, p.fout, fb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                      cudaStreamSynchronize(st) == cudaSuccess;
+                if (got) {
+                    std::memcpy(r.vertices, s.out_host, vb);
+                    std::memcpy(r.faces, s.out_host + vb, fb);
+                }
+            } else {
+                got = cudaMemcpyAsync(r.vertices, p.vout, vb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                      cudaMemcpyAsync(r.faces, p.fout, fb, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                      cudaStreamSynchronize(st) == cudaSuccess;
+            }
+            if (status == 0 && !got) status = ISO_ERR_CUDA;
+            r.num_vertices = V;
+            r.num_faces = F;
+        }
+        r.status = status;
     }
     {
         std::lock_guard<std::mutex> lk(mu);
         b->in_use = false;
     }
     cv_mem.notify_all();
-    r.status = status;
 }
 
 void IsoServer::worker(int index) {
     cudaSetDevice(device);
     while (true) {
-        Job* job = nullptr;
+        std::vector<Job*> jobs;
         {
             std::unique_lock<std::mutex> lk(mu);
             cv_work.wait(lk, [&] { return !queue.empty() || closing; });
             if (queue.empty()) return;  // closing
-            job = queue.front();
+            jobs.push_back(queue.front());
             queue.pop_front();
+            if (bucket_max > 1) {
+                // the head's bucket: queued requests with its key, in queue order
+                for (auto it = queue.begin(); it != queue.end() && int(jobs.size()) < bucket_max;) {
+                    if (same_key(**it, *jobs[0])) {
+                        jobs.push_back(*it);
+                        it = queue.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+                int B = 1;
+                while (2 * B <= int(jobs.size())) B *= 2;
+                for (int i = int(jobs.size()) - 1; i >= B; --i) queue.push_front(jobs[i]);  // back, in order
+                jobs.resize(B);
+                if (B > 1) {
+                    ++buckets;
+                    bucketed += B;
+                }
+            }
             ++running;
             max_running = std::max(max_running, running);
         }
-        IsoServeResult r{};
-        r.ticket = job->ticket;
-        r.slot = index;
-        r.t_submit = job->t_submit;
-        r.t_start = now_s();
-        run(index, *job, r);
-        r.t_done = now_s();
+        std::vector<IsoServeResult> res(jobs.size());
+        const double t0 = now_s();
+        for (size_t i = 0; i < jobs.size(); ++i) {
+            res[i].ticket = jobs[i]->ticket;
+            res[i].slot = index;
+            res[i].t_submit = jobs[i]->t_submit;
+            res[i].t_start = t0;
+        }
+        run(index, jobs, res);
+        const double t1 = now_s();
         {
             std::lock_guard<std::mutex> lk(mu);
             --running;
-            ++completed;
-            done[job->ticket] = Done{r};
+            for (size_t i = 0; i < jobs.size(); ++i) {
+                res[i].t_done = t1;
+                ++completed;
+                done[jobs[i]->ticket] = Done{res[i]};
+            }
         }
-        delete job;
+        for (Job* j : jobs) delete j;
         cv_done.notify_all();
         cv_mem.notify_all();
     }
@@ -456,18 +564,24 @@ int iso_serve_create(int slots, long long budget_bytes, const int* warm_sizes, i
     props.location.id = srv->device;
     bool ok = cudaMemPoolCreate(&srv->pool, &props) == cudaSuccess &&
               cudaStreamCreateWithFlags(&srv->free_stream, cudaStreamNonBlocking) == cudaSuccess;
+    const size_t pbytes = sizeof(float) * PRIM_FLOATS * BUCKET_MAX;
     for (Slot& s : srv->slots) {
         s.out_bytes = size_t(12) * (cmax.v + cmax.f);
         ok = ok && cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) == cudaSuccess &&
-             srv->acquire(al(sizeof(float) * PRIM_FLOATS)) &&
-             (s.prims_dev = static_cast<float*>(srv->alloc(sizeof(float) * PRIM_FLOATS, s.stream))) != nullptr &&
-             cudaMallocHost(&s.prims_host, sizeof(float) * PRIM_FLOATS) == cudaSuccess &&
-             cudaMallocHost(&s.small_host, 64) == cudaSuccess && cudaMallocHost(&s.out_host, s.out_bytes) == cudaSuccess;
+             cudaEventCreateWithFlags(&s.ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+             srv->acquire(al(pbytes)) &&
+             (s.prims_dev = static_cast<float*>(srv->alloc(pbytes, s.stream))) != nullptr &&
+             cudaMallocHost(&s.prims_host, pbytes) == cudaSuccess &&
+             cudaMallocHost(&s.small_host, size_t(64) * BUCKET_MAX) == cudaSuccess &&
+             cudaMallocHost(&s.out_host, s.out_bytes) == cudaSuccess;
+        for (int i = 0; ok && i < BUCKET_MAX - 1; ++i)
+            ok = cudaStreamCreateWithFlags(&s.fork[i], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&s.ev_join[i], cudaEventDisableTiming) == cudaSuccess;
         if (ok) {
-            std::memset(s.prims_host, 0, sizeof(float) * PRIM_FLOATS);
-            s.prims_host[0] = 1.0f;  // a sphere of radius 0 until the first request
-            ok = cudaMemcpyAsync(s.prims_dev, s.prims_host, sizeof(float) * PRIM_FLOATS, cudaMemcpyHostToDevice,
-                                 s.stream) == cudaSuccess &&
+            std::memset(s.prims_host, 0, pbytes);
+            for (int i = 0; i < BUCKET_MAX; ++i)
+                s.prims_host[size_t(i) * PRIM_FLOATS] = 1.0f;  // a sphere of radius 0 until a request comes
+            ok = cudaMemcpyAsync(s.prims_dev, s.prims_host, pbytes, cudaMemcpyHostToDevice, s.stream) == cudaSuccess &&
                  cudaStreamSynchronize(s.stream) == cudaSuccess;
         }
     }
@@ -477,7 +591,7 @@ int iso_serve_create(int slots, long long budget_bytes, const int* warm_sizes, i
         for (int si = 0; ok && si < slots; ++si)
             for (int kind = 0; ok && kind < 2; ++kind) {
                 int err = 0;
-                Entry* e = srv->build(si, kind, warm_sizes[i], 0, 0.0f, nullptr, true, &err);
+                Entry* e = srv->build(si, kind, warm_sizes[i], 0, 0.0f, nullptr, true, 1, &err);
                 ok = e != nullptr;
                 if (ok) {
                     std::lock_guard<std::mutex> lk(srv->mu);
@@ -504,7 +618,7 @@ long long iso_serve_submit(IsoServer* srv, const IsoServeRequest* req) {
         return -ISO_ERR_ARG;
     // the count pass alone (values and the workspace at capacity 1) must fit
     // beside the slots' own buffers
-    const long long fixed = (long long)srv->slots.size() * (long long)al(sizeof(float) * PRIM_FLOATS);
+    const long long fixed = (long long)srv->slots.size() * (long long)al(sizeof(float) * PRIM_FLOATS * BUCKET_MAX);
     if ((long long)count_pass_bytes(req->kind, req->n) + fixed > srv->budget) return -ISO_ERR_WORKSPACE;
     auto* job = new Job;
     job->req = *req;
@@ -562,9 +676,10 @@ int iso_serve_stats_ex(IsoServer* srv, long long* stats, int count) {
     std::lock_guard<std::mutex> lk(srv->mu);
     long long entries = 0;
     for (const Slot& s : srv->slots) entries += (long long)s.entries.size();
-    const long long all[10] = {srv->completed, srv->max_running, srv->max_held, (long long)srv->queue.size(),
-                               srv->held, srv->evictions, entries, srv->count_passes, srv->grows, srv->budget};
-    for (int i = 0; i < std::min(count, 10); ++i) stats[i] = all[i];
+    const long long all[12] = {srv->completed, srv->max_running, srv->max_held, (long long)srv->queue.size(),
+                               srv->held, srv->evictions, entries, srv->count_passes, srv->grows, srv->budget,
+                               srv->buckets, srv->bucketed};
+    for (int i = 0; i < std::min(count, 12); ++i) stats[i] = all[i];
     return ISO_OK;
 }
 
@@ -588,6 +703,11 @@ int iso_serve_destroy(IsoServer* srv) {
         cudaFreeHost(s.prims_host);
         cudaFreeHost(s.small_host);
         cudaFreeHost(s.out_host);
+        for (int i = 0; i < BUCKET_MAX - 1; ++i) {
+            if (s.fork[i]) cudaStreamDestroy(s.fork[i]);
+            if (s.ev_join[i]) cudaEventDestroy(s.ev_join[i]);
+        }
+        if (s.ev_fork) cudaEventDestroy(s.ev_fork);
         if (s.stream) cudaStreamDestroy(s.stream);
     }
     if (srv->free_stream) {
@@ -596,6 +716,14 @@ int iso_serve_destroy(IsoServer* srv) {
     }
     if (srv->pool) cudaMemPoolDestroy(srv->pool);
     delete srv;
+    return ISO_OK;
+}
+
+// Requests per launch at most (1, 2, 4 or 8; 1: each request its own launch).
+int iso_serve_set_bucket(IsoServer* srv, int max_requests) {
+    if (!srv || max_requests < 1 || max_requests > BUCKET_MAX || (max_requests & (max_requests - 1))) return ISO_ERR_ARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->bucket_max = max_requests;
     return ISO_OK;
 }
 

@@ -348,6 +348,7 @@ _ffi.register({
     "iso_serve_stats_ex": ([C.c_void_p, C.POINTER(C.c_longlong), C.c_int], C.c_int),
     "iso_serve_destroy": ([C.c_void_p], C.c_int),
     "iso_serve_set_capacity_scale": ([C.c_void_p, C.c_double], C.c_int),
+    "iso_serve_set_bucket": ([C.c_void_p, C.c_int], C.c_int),
 })
 
 
@@ -373,10 +374,13 @@ class NativeServer:
     used when a new one needs room, and grown when a later mesh is larger.
 
     warm_sizes: grid sizes whose buffers and graphs are built up front (the
-    launch parameters are tuned first on the largest, as Server.warmup does)."""
+    launch parameters are tuned first on the largest, as Server.warmup does).
+    bucket: requests of one kind, grid size, method and level that one launch
+    may run together (1, 2, 4 or 8; a graph with a parallel branch per
+    request)."""
 
     def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, warm_sizes=(), tune: bool = True,
-                 device=None):
+                 device=None, bucket: int = 1):
         import torch
 
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -394,6 +398,8 @@ class NativeServer:
         _ffi.check(_ffi.lib().iso_serve_create(int(slots), int(budget_bytes), sizes, len(warm_sizes), C.byref(handle)))
         self._h = handle
         self.budget = int(budget_bytes)
+        if bucket != 1:
+            _ffi.check(_ffi.lib().iso_serve_set_bucket(self._h, int(bucket)))
 
     def submit(self, req: Request) -> _NativeFuture:
         p = np.ascontiguousarray(np.asarray(req.prims, np.float32).reshape(-1, 7))
@@ -427,11 +433,11 @@ class NativeServer:
     def stats(self) -> dict:
         """Counters of the loop.  Device bytes: every byte the server holds
         (slot buffers and cached entries) counts against the budget."""
-        s = (C.c_longlong * 10)()
-        _ffi.check(_ffi.lib().iso_serve_stats_ex(self._h, s, 10))
+        s = (C.c_longlong * 12)()
+        _ffi.check(_ffi.lib().iso_serve_stats_ex(self._h, s, 12))
         return {"completed": s[0], "max_running": s[1], "max_held_bytes": s[2], "max_admitted_bytes": s[2],
                 "queued": s[3], "held_bytes": s[4], "evictions": s[5], "entries": s[6], "count_passes": s[7],
-                "grown": s[8], "budget": s[9]}
+                "grown": s[8], "budget": s[9], "bucket_launches": s[10], "bucketed_requests": s[11]}
 
     @property
     def max_running(self) -> int:

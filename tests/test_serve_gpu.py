@@ -102,6 +102,58 @@ def test_native_server_results_equal_plain_results():
         assert _same((s.vertices, s.faces), p), (r.rid, r.kind, r.n)
 
 
+def test_native_server_buckets_equal_plain_results():
+    """Length buckets: same-key requests queued together run as parallel branches
+    of one graph launch; every result equals the plain path's, bit for bit."""
+    from isoext_gb300.serve import NativeServer, random_requests, solve_plain
+
+    reqs = random_requests(40, seed=21, sizes=(32, 48))
+    solo = [solve_plain(r) for r in reqs]
+    srv = NativeServer(slots=2, budget_bytes=1 << 30, warm_sizes=(32, 48), bucket=8)
+    futs = [srv.submit(r) for r in reqs]
+    served = [f.result(timeout=300) for f in futs]
+    stats = srv.stats()
+    srv.close()
+    assert stats["completed"] == len(reqs)
+    assert stats["bucket_launches"] > 0 and stats["bucketed_requests"] >= 2 * stats["bucket_launches"]
+    for r, s, p in zip(reqs, served, solo):
+        assert s.rid == r.rid
+        assert _same((s.vertices, s.faces), p), (r.rid, r.kind, r.n)
+
+
+def test_native_server_buckets_grow_together():
+    """A bucket whose meshes outgrow its buffers grows every branch to the
+    largest counted sizes and runs again."""
+    import ctypes
+
+    from isoext_gb300 import _ffi
+    from isoext_gb300.serve import NativeServer, random_requests, solve_plain
+
+    reqs = random_requests(16, seed=23, sizes=(40,))
+    srv = NativeServer(slots=1, budget_bytes=1 << 30, warm_sizes=(), tune=False, bucket=4)
+    assert _ffi.lib().iso_serve_set_capacity_scale(srv._h, ctypes.c_double(1e-4)) == 0
+    out = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    stats = srv.stats()
+    srv.close()
+    assert stats["grown"] > 0 and stats["bucket_launches"] > 0
+    for r, s in zip(reqs, out):
+        assert _same((s.vertices, s.faces), solve_plain(r)), (r.rid, r.kind)
+
+
+def test_native_server_bucket_sizes():
+    from isoext_gb300 import _ffi
+    from isoext_gb300.serve import NativeServer
+
+    srv = NativeServer(slots=1, budget_bytes=1 << 28, warm_sizes=(), tune=False)
+    try:
+        for b in (1, 2, 4, 8):
+            assert _ffi.lib().iso_serve_set_bucket(srv._h, b) == 0
+        for b in (0, 3, 16, -1):
+            assert _ffi.lib().iso_serve_set_bucket(srv._h, b) == _ffi.ISO_ERR_ARG
+    finally:
+        srv.close()
+
+
 def test_native_server_reruns_meshes_larger_than_its_buffers():
     import ctypes
 
