@@ -475,12 +475,14 @@ __device__ __forceinline__ uint32_t sp_owners(const SpGrid& g, const float* vals
             if (cid[mid] < idy) lo = mid + 1;
             else hi = mid;
         }
-        if (lo < j && cid[lo] == idy) {
-            jy_out = int(lo);
-            if (summ[lo] & 8u) jy = int(lo);
-            if (z > 0 && lo > 0 && cid[lo - 1] == idy - 1u && (summ[lo - 1] & 8u)) jyl = int(lo) - 1;
-            if (z + 1 < nzc && lo + 1 < j && cid[lo + 1] == idy + 1u && (summ[lo + 1] & 8u)) jyh = int(lo) + 1;
-        }
+        // the diagonal cells are looked for whether the y-neighbour is listed or
+        // not, as the cells that own through them look for them
+        const bool hasy = lo < j && cid[lo] == idy;
+        jy_out = int(lo) | (hasy ? 0x8000 : 0);
+        if (hasy && (summ[lo] & 8u)) jy = int(lo);
+        if (z > 0 && lo > 0 && cid[lo - 1] == idy - 1u && (summ[lo - 1] & 8u)) jyl = int(lo) - 1;
+        const uint32_t ph = hasy ? lo + 1 : lo;
+        if (z + 1 < nzc && ph < j && cid[ph] == idy + 1u && (summ[ph] & 8u)) jyh = int(ph);
     }
     if (jz < 0 && jy < 0 && jyl < 0 && jyh < 0) return 0u;
     float d[8], vz[8], vy[8], vl[8], vh[8];
@@ -514,7 +516,8 @@ __device__ __forceinline__ uint32_t sp_owners(const SpGrid& g, const float* vals
 
 // Per CTA: its crossed cells in cell order and, for each, sp_pack of its
 // summary with the owner codes, into the chunk's slots of clist / ccnt / cjy
-// (SP2_CHUNK each: cjy the y-neighbour's list position; the count in clen);
+// (SP2_CHUNK each: cjy where id - (nz - 1) sorts in the list, bit 15 set when
+// that cell is listed; the count in clen);
 // the chunk's faces and vertex-list entries -> blk[2 b], blk[2 b + 1].  The
 // emit then reads only the crossed cells.
 __global__ void __launch_bounds__(SP2_THREADS) sp_mc_count2(SpGrid g, const int* __restrict__ ids,
@@ -700,10 +703,15 @@ __global__ void __launch_bounds__(SP2_THREADS) sp_mc_emit2(SpGrid g, const int* 
                 uint32_t oz = 0, lz = 0, oy = 0, ly = 0, ol = 0, ll = 0, oh = 0, lh = 0;
                 if (lo & ~hi) { oz = sp_own(gc[j - 1]); lz = slv[j - 1]; }
                 if (codes) {
-                    const uint32_t jy = gy[j];
-                    if (hi & ~lo) { oy = sp_own(gc[jy]); ly = slv[jy]; }
-                    if (((codes >> 8) & 3u) == 3u) { ol = sp_own(gc[jy - 1]); ll = slv[jy - 1]; }
-                    if (((codes >> 10) & 3u) == 3u) { oh = sp_own(gc[jy + 1]); lh = slv[jy + 1]; }
+                    // where id - (nz - 1) sorts in the list, and whether that cell is listed
+                    const uint32_t py = gy[j] & 0x7fffu, hasy = gy[j] >> 15;
+                    if (hi & ~lo) { oy = sp_own(gc[py]); ly = slv[py]; }
+                    if (((codes >> 8) & 3u) == 3u) { ol = sp_own(gc[py - 1]); ll = slv[py - 1]; }
+                    if (((codes >> 10) & 3u) == 3u) {
+                        const uint32_t ph = py + hasy;
+                        oh = sp_own(gc[ph]);
+                        lh = slv[ph];
+                    }
                 }
                 unsigned long long ent[3] = {0ull, 0ull, 0ull};  // 16 bits per edge
 #pragma unroll
@@ -1080,7 +1088,7 @@ struct SpMcWs {
     int32_t* tri;    // the triangles' indices into it [3 F]
     uint16_t* clist;  // per chunk: crossed cells (SP2_CHUNK slots each)
     uint32_t* ccnt;   // per chunk: their summaries (sp_pack)
-    uint16_t* cjy;    // per chunk: their y-neighbours' list positions
+    uint16_t* cjy;    // per chunk: where their y-neighbours sort in the list (bit 15: listed)
     uint32_t* clen;          // per chunk: crossed cells
     void* weld;
     size_t total;

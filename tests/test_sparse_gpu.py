@@ -83,6 +83,61 @@ def test_sparse_mc_matches_oracle(oracle, method, extra):
     assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, f"{method} extra {extra}")
 
 
+@pytest.mark.parametrize("shape", [(30, 4, 50), (33, 31, 3), (3, 40, 40), (2, 2, 2), (25, 2, 37), (41, 23, 4)])
+def test_sparse_mc_thin_grids(oracle, shape):
+    """Grids one or two cells thick along an axis: the owner of an edge is
+    looked for at y - 1 and z +- 1 only where those cells exist (y > 0, z > 0,
+    z + 1 < nz - 1), and chunk ends cut neighbours apart."""
+    rng = np.random.default_rng(sum(shape))
+    vals = (rng.standard_normal(shape) * 0.3 + sphere(shape, 0.5)).astype(np.float32) \
+        if min(shape) > 2 else rng.uniform(-1, 1, size=shape).astype(np.float32)
+    ids, cv = sparse_from_dense(vals, extra=50, seed=1)
+    if len(ids) == 0:
+        pytest.skip("no crossed cell")
+    g = make_sparse(shape, ids, cv)
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, shape, method=method)
+        if v is None:
+            assert len(fo) == 0
+            continue
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, f"{method} {shape}")
+
+
+def test_sparse_mc_missing_neighbours(oracle):
+    """Consistent values, but a random half of the crossed cells left out: an
+    edge's earlier cells are often absent, and the first present one owns it."""
+    vals = torus((44, 40, 48), 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals)
+    keep = np.random.default_rng(4).random(len(ids)) < 0.5
+    ids, cv = ids[keep], np.ascontiguousarray(cv[keep])
+    g = make_sparse(vals.shape, ids, cv)
+    v, f = iso.marching_cubes(g)
+    vo, fo, _ = oracle.mc_sparse(ids, cv, vals.shape)
+    assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, "half the cells")
+
+
+@pytest.mark.parametrize("seed,drop,shape", [(0, 0.2, (40, 44, 36)), (1, 0.5, (36, 40, 44)),
+                                             (2, 0.8, (44, 36, 40)), (3, 0.3, (96, 90, 100))])
+def test_sparse_mc_dropped_and_perturbed_cells(oracle, seed, drop, shape):
+    """Random cells left out and one corner value in ten moved by an ulp: every
+    pattern of present, absent, compatible and incompatible cells around an
+    edge (and, on the largest grid, chunk ends through them) must give the
+    oracle's mesh."""
+    vals = torus(shape, 0.5, 0.2)
+    ids, cv = sparse_from_dense(vals, extra=200, seed=seed)
+    rng = np.random.default_rng(100 + seed)
+    keep = rng.random(len(ids)) >= drop
+    ids, cv = ids[keep], np.ascontiguousarray(cv[keep])
+    moved = rng.random(cv.shape) < 0.1
+    cv[moved] = np.nextafter(cv[moved], np.float32(np.inf))
+    g = make_sparse(shape, ids, cv)
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, shape, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, f"{method} seed {seed}")
+
+
 def test_sparse_mc_inconsistent_values(oracle):
     # independent random values per cell: shared corners disagree, so welding
     # by exact position is all that joins cells
