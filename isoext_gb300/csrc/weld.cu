@@ -5,10 +5,10 @@
 // the first entry with its position.
 //
 //   weld_insert   hash table of positions: a slot keeps the smallest entry
-//                 with its position.  Four entries per thread, their probes in
+//                 with its position.  Two entries per thread, their probes in
 //                 flight together (the kernel is bound by the latency of
 //                 dependent atomics and gathers, not by bytes).
-//   weld_number   per tile of 1024 entries: each entry's first entry (table
+//   weld_number   per tile of 512 entries: each entry's first entry (table
 //                 lookup), the tile's number of first entries, the exclusive
 //                 prefix over tiles by decoupled look-back, and the first
 //                 entries' new numbers and positions written out.
@@ -25,8 +25,9 @@
 namespace {
 
 constexpr int WELD_THREADS = 256;
-constexpr int WELD_PER = 4;                           // entries per thread
+constexpr int WELD_PER = 2;                           // entries per thread (insert, numbering)
 constexpr int WELD_TILE = WELD_THREADS * WELD_PER;    // entries per CTA
+constexpr int REMAP_PER = 4;                          // triangle indices per thread of the remap
 constexpr uint32_t WELD_EMPTY = 0xffffffffu;          // a free table slot
 constexpr uint32_t WELD_NEW = 0x80000000u;            // rep[a]: a is a first entry; low bits its new number
 constexpr uint32_t WELD_PROBES = 512;  // the table is at most half full when the capacity holds the positions
@@ -217,18 +218,18 @@ __global__ void __launch_bounds__(WELD_THREADS) weld_remap(const int32_t* __rest
                                                            const uint32_t* __restrict__ rep, int32_t* fout,
                                                            const long long* __restrict__ dn) {
     if (dn) n = dn[2];
-    const long long base = (long long)blockIdx.x * WELD_TILE + threadIdx.x;
-    uint32_t r[WELD_PER];
+    const long long base = (long long)blockIdx.x * (WELD_THREADS * REMAP_PER) + threadIdx.x;
+    uint32_t r[REMAP_PER];
 #pragma unroll
-    for (int e = 0; e < WELD_PER; ++e) {
+    for (int e = 0; e < REMAP_PER; ++e) {
         const long long i = base + e * WELD_THREADS;
         r[e] = i < n ? rep[tri ? tri[i] : int32_t(i)] : WELD_NEW;
     }
 #pragma unroll
-    for (int e = 0; e < WELD_PER; ++e)
+    for (int e = 0; e < REMAP_PER; ++e)
         if (!(r[e] & WELD_NEW)) r[e] = rep[r[e]];  // the first entry with the position: numbered
 #pragma unroll
-    for (int e = 0; e < WELD_PER; ++e) {
+    for (int e = 0; e < REMAP_PER; ++e) {
         const long long i = base + e * WELD_THREADS;
         if (i < n) fout[i] = int32_t(r[e] & ~WELD_NEW);
     }
@@ -286,7 +287,11 @@ void weld_dev_launch(const float* pts, long long capA, long long capU, const int
     } else {
         cudaMemsetAsync(vtot, 0, 16, st);
     }
-    if (capT > 0) weld_remap<<<tiles_for(capT), WELD_THREADS, 0, st>>>(tri, capT, w.rep, fout, eff);
+    if (capT > 0) {
+        const long long per = (long long)WELD_THREADS * REMAP_PER;
+        weld_remap<<<unsigned(std::max<long long>((capT + per - 1) / per, 1)), WELD_THREADS, 0, st>>>(tri, capT,
+                                                                                                     w.rep, fout, eff);
+    }
 }
 
 // ---------------------------------------------------------------------------
