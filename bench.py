@@ -14,10 +14,11 @@ One step is one extraction of the whole grid (511^3 = 133,432,831 cells).
          over the step time.
   cpu_baseline  the oracle's C restatement of the reference's algorithm on all
          host cores (x slabs on threads; rank 0 only).
-  dc512, serve  (default run on one GPU) the metric's other halves in the same
-         line: dual contouring of the same grid (value, roofline, e2e, its own
-         CPU baseline) and a short served mixed stream against the plain path
-         (req/s, p50 / p99).
+  dc512, serve, sparse1024  (default run on one GPU) the metric's other halves
+         in the same line: dual contouring of the same grid (value, roofline,
+         e2e, its own CPU baseline), a short served mixed stream against the
+         plain path (req/s, p50 / p99), and sparse marching cubes of the 1024^3
+         smooth-min band.
 --impl reference runs the reference's algorithm on the CPU (the oracle port:
 the isoext sources are not available on the GPU host) and prints the same line.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -339,6 +340,10 @@ def run_ours(args, wl, rank, world) -> dict | None:
         out["dc512"] = {k: dc[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "roofline",
                                            "kernel_ms", "gpu_launches", "clocks", "cpu_baseline") if k in dc}
         out["serve"] = serve_summary(args, dev)
+        # config 3: sparse MC of the 1024^3 smooth-min band (57.2 M cells)
+        sp = run_sparse(args, WORKLOADS["sparse1024"], rank, world)
+        out["sparse1024"] = {k: sp[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "roofline",
+                                                "kernel_ms", "gpu_launches", "clocks", "cpu_baseline") if k in sp}
     return out
 
 
