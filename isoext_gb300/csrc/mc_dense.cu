@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
     constexpr uint32_t SEG = CNT_THREADS * WPT;  // words of the segment
     __shared__ uint32_t sm[64];
     __shared__ uint32_t nfs[SEG];  // faces of each word of the segment
-    __shared__ uint32_t wcell[CNT_THREADS / 32];
+    __shared__ uint32_t wcell[CNT_THREADS / 32], wvert[CNT_THREADS / 32];
     __shared__ unsigned long long cbase_s, vbase_s;
     __shared__ uint32_t nt4[64];  // triangle counts of the 256 cases, 4 per word
     __shared__ uint32_t vmask[3 * WPT][CNT_THREADS];  // x, y, z edge masks of each thread's words
@@ -420,7 +420,8 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
             }
         quiet_all = (u == 0u || u == ~0u) && diff == 0u;
     }
-    if (!__all_sync(~0u, quiet_all)) {
+    const bool warp_quiet = __all_sync(~0u, quiet_all);
+    if (!warp_quiet) {
         // the cells of these words read their corners from here
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -458,21 +459,38 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
             }
         }
     }
-    __syncthreads();  // nfs cleared
+    // nfs cleared.  A segment whose warps are all quiet has no crossed edge and
+    // no active cell: its sums are 0, and no cell reads its words' vertex
+    // offsets (a cell's edges lie in words with crossings), so it stops here.
+    if (!__syncthreads_or(!warp_quiet)) {
+        if (threadIdx.x == 0) {
+            blk[2 * seg] = 0ull;
+            blk[2 * seg + 1] = 0ull;
+        }
+        return;
+    }
+    uint32_t sv = 0;
+#pragma unroll
+    for (int k = 0; k < WPT; ++k) sv += nv[k];
     // active cells, one per lane of the warp: triangle counts, and a cell entry
     // with the cell's face offset within its word (cells of a word come in bit
     // order: a segmented scan over the lanes plus the word's faces of earlier rounds)
     {
         const uint32_t na = __popc(act[0]) + __popc(act[1]) + __popc(act[2]) + __popc(act[3]);
-        uint32_t incl = na;
+        uint32_t incl = na, vsum = sv;
 #pragma unroll
         for (int dd = 1; dd < 32; dd <<= 1) {
             const uint32_t t = __shfl_up_sync(~0u, incl, dd);
             if (lane >= dd) incl += t;
+            vsum += __shfl_xor_sync(~0u, vsum, dd);
         }
         const uint32_t total = __shfl_sync(~0u, incl, 31);
-        // the CTA's cell entries are allocated at once: warp offsets, one atomic
-        if (lane == 0) wcell[warp] = total;
+        // the CTA's cell entries and vertex entries are allocated at once: warp
+        // offsets, one atomic each, both in flight together
+        if (lane == 0) {
+            wcell[warp] = total;
+            wvert[warp] = vsum;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             uint32_t run = 0;
@@ -482,6 +500,10 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
                 run += c;
             }
             cbase_s = run ? atomicAdd(ctr + 10, (unsigned long long)run) : 0ull;
+        } else if (threadIdx.x == 32) {
+            uint32_t run = 0;
+            for (int q = 0; q < CNT_THREADS / 32; ++q) run += wvert[q];
+            vbase_s = run ? atomicAdd(ctr, (unsigned long long)run) : 0ull;
         }
         __syncthreads();
         const unsigned long long wbase = cbase_s + wcell[warp];
@@ -546,21 +568,18 @@ __global__ void __launch_bounds__(CNT_THREADS) mc_count(const McGrid g, const fl
         }
     }
     __syncthreads();
-    uint32_t nf[WPT], sv = 0, sf = 0;
+    uint32_t nf[WPT], sf = 0;
 #pragma unroll
     for (int k = 0; k < WPT; ++k) {
         nf[k] = nfs[threadIdx.x * WPT + k];
-        sv += nv[k];
         sf += nf[k];
     }
     uint32_t ev, ef, tv, tf;
     block_scan2<CNT_THREADS>(sv, sf, ev, ef, tv, tf, sm);
-    // vertex entries: the CTA's block of entries (one atomic), each entry at the
-    // block base plus its segment-local slot (x edges, then y, then z of each
-    // word); one vertex per lane of the warp, so consecutive lanes store
+    // vertex entries: the CTA's block of entries (allocated above), each entry
+    // at the block base plus its segment-local slot (x edges, then y, then z of
+    // each word); one vertex per lane of the warp, so consecutive lanes store
     // consecutive entries
-    if (threadIdx.x == 0) vbase_s = tv ? atomicAdd(ctr, (unsigned long long)tv) : 0ull;
-    __syncthreads();
     const unsigned long long vb0 = vbase_s;
     {
         uint32_t incl = sv;
