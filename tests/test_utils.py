@@ -46,3 +46,19 @@ def test_write_obj_empty_and_missing_meshes(tmp_path):
         p.write_text("stale")
         write_obj(str(p), v, f)
         assert p.read_text() == ""
+
+
+def test_make_grid_on_the_host():
+    """tests/test_grid_utils.py:11-37 on the CPU: [X, Y, Z, 3] point coordinates,
+    corners at the box's corners, per-axis resolutions."""
+    from isoext_gb300.utils import make_grid
+
+    grid = make_grid([-1, -1, -1, 1, 1, 1], res=16, device="cpu")
+    assert grid.shape == (16, 16, 16, 3) and grid.device.type == "cpu"
+    assert torch.equal(grid[0, 0, 0], torch.tensor([-1.0, -1.0, -1.0]))
+    assert torch.allclose(grid[-1, -1, -1], torch.tensor([1.0, 1.0, 1.0]), atol=1e-5)
+    grid = make_grid([0, -2, 1, 1, 2, 3], res=[4, 5, 6], device="cpu")
+    assert grid.shape == (4, 5, 6, 3)
+    assert torch.allclose(grid[:, 0, 0, 0], torch.linspace(0, 1, 4))
+    assert torch.allclose(grid[0, :, 0, 1], torch.linspace(-2, 2, 5))
+    assert torch.allclose(grid[0, 0, :, 2], torch.linspace(1, 3, 6))
