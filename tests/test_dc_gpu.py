@@ -85,7 +85,8 @@ def test_intersection_matches_reference_fixture(name, host_arith):
     assert np.array_equal(its._offsets.cpu().numpy().astype(np.uint32), gd["its_cell_offsets"])
 
 
-@pytest.mark.parametrize("shape,r", [((32, 32, 32), 0.5), ((45, 37, 61), 0.6), ((64, 64, 64), 0.7)])
+@pytest.mark.parametrize("shape,r", [((32, 32, 32), 0.5), ((45, 37, 61), 0.6), ((64, 64, 64), 0.7),
+                                     ((16, 32, 48), 0.5), ((8, 64, 16), 0.5)])
 def test_intersection_matches_oracle(oracle, shape, r):
     vals = sphere(shape, r, center=(0.05, -0.03, 0.02))
     g = make_grid(vals)
@@ -115,7 +116,8 @@ def test_dc_cuboid_fixture(host_arith):
     assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), gd["dc_v"], gd["dc_f"], cell_h((24, 24, 24)), "cuboid")
 
 
-@pytest.mark.parametrize("shape,r", [((32, 32, 32), 0.5), ((48, 40, 56), 0.6), ((96, 96, 96), 0.7)])
+@pytest.mark.parametrize("shape,r", [((32, 32, 32), 0.5), ((48, 40, 56), 0.6), ((96, 96, 96), 0.7),
+                                     ((16, 32, 48), 0.5), ((8, 64, 16), 0.5)])
 def test_dc_sphere(oracle, shape, r):
     check_dc(oracle, sphere(shape, r, center=(0.02, 0.01, -0.03)), what=f"sphere {shape}")
 

@@ -215,6 +215,38 @@ def test_sparse_dc_matches_oracle(oracle, extra):
     assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vo, fo, cell_h(vals.shape), f"extra {extra}")
 
 
+def _populate_like_the_reference(g, sdf, level):
+    """The reference tests' population loop (tests/conftest.py:39-61): the
+    potential cells in one chunk, those whose corners straddle the level kept,
+    then every kept cell's SDF values."""
+    n = g.get_shape()
+    for chunk in g.get_potential_cell_indices(n[0] * n[1] * n[2]):
+        kept = g.filter_cell_indices(chunk, sdf(g.get_points_by_cell_indices(chunk)), level=level)
+        if len(kept) > 0:
+            g.add_cells(kept)
+    if g.get_num_cells() > 0:
+        g.set_values(sdf(g.get_points()))
+
+
+@pytest.mark.parametrize("level", [-0.1, 0.0, 0.1])
+def test_sparse_levels_match_oracle(oracle, level):
+    """tests/test_marching_cubes.py:166-180 and tests/test_dual_contouring.py's
+    sparse level sweep, each mesh against the oracle."""
+    g = iso.SparseGrid([32, 32, 32], aabb_min=[-1, -1, -1], aabb_max=[1, 1, 1])
+    _populate_like_the_reference(g, lambda p: p.norm(dim=-1) - 0.5, level)
+    assert g.get_num_cells() > 0
+    ids = g.get_cell_indices().cpu().numpy()
+    cv = g.get_values().cpu().numpy()
+    for method in ("nagae", "lorensen"):
+        v, f = iso.marching_cubes(g, level=level, method=method)
+        vo, fo, _ = oracle.mc_sparse(ids, cv, (32, 32, 32), level=level, method=method)
+        assert_same_mesh(v.cpu().numpy(), f.cpu().numpy(), vo, fo, f"{method} level {level}")
+    v, f = iso.dual_contouring(g, level=level)
+    its = oracle.intersection_sparse(ids, cv, (32, 32, 32), level=level)
+    vo, fo, _ = oracle.dc(its, (32, 32, 32), values=cv, cell_ids=ids)
+    assert_dc_match(v.cpu().numpy(), f.cpu().numpy(), vo, fo, cell_h((32, 32, 32)), f"level {level}")
+
+
 def test_sparse_dc_user_intersection(oracle):
     vals = torus((36, 36, 36), 0.5, 0.2)
     ids, cv = sparse_from_dense(vals)
