@@ -1,5 +1,5 @@
-"""The reference's integration tests (tests/test_integration.py:16-137), with the
-oracle as the checker: composite SDFs built from the sdf module's primitives and
+"""The reference's integration tests (tests/test_integration.py:16-137), compared
+with the oracle: composite SDFs built from the sdf module's primitives and
 operators, evaluated on the grid's points, then extracted by marching cubes and
 dual contouring.
 
