@@ -1045,21 +1045,6 @@ void weld_dev_launch(const float* pts, long long capA, long long capU, const int
 
 namespace {
 
-// One-call sparse MC: the soup's size against the capacities; eff = (3 F, 0,
-// 3 F, vertex capacity) for the weld, all 0 when the soup does not fit.
-__global__ void sp_mc_sizes(const long long* __restrict__ tf, long long capF, long long capV, long long* eff,
-                            long long* counts, int* status) {
-    const long long F = tf[0];
-    const bool ok = F <= capF && 3 * F < 0x7fffffffll;
-    if (!ok) atomicCAS(status, 0, int(ISO_ERR_OVERFLOW));
-    eff[0] = ok ? 3 * F : 0;
-    eff[1] = 0;
-    eff[2] = ok ? 3 * F : 0;
-    eff[3] = capV;
-    counts[1] = ok ? F : 0;
-    counts[2] = F;
-}
-
 // The list's and the faces' sizes against the capacities: eff = (vertex-list
 // entries, 0, 3 F, vertex capacity) for the weld, all 0 when they do not fit.
 __global__ void sp_mc_sizes2(const long long* __restrict__ tot, long long capF, long long capV, long long* eff,
