@@ -217,20 +217,6 @@ def _classify_quads(grid: UniformGrid, level: float):
     return ws, (A, K, Q)
 
 
-def _intersect_from(grid: UniformGrid, level: float, compute_normals: bool, ws, A: int, K: int) -> Intersection:
-    lib = _ffi.lib()
-    dev = grid._values.device
-    nx, ny, nz = grid.shape
-    points = torch.empty((K, 3), dtype=torch.float32, device=dev)
-    normals = torch.empty((K, 3), dtype=torch.float32, device=dev) if compute_normals else None
-    cells = torch.empty(A, dtype=torch.int32, device=dev)
-    offs = torch.empty(A + 1, dtype=torch.int32, device=dev)
-    _ffi.check(lib.iso_dc_intersect(_p(grid._values), nx, ny, nz, _ffi.fvec3(grid.aabb_min),
-                                    _ffi.fvec3(grid.aabb_max), float(level), _p(ws), A, K, _p(points),
-                                    _p(normals), _p(cells), _p(offs), _stream(dev)))
-    return Intersection(points, normals, cells, offs, level, _grid_key(grid))
-
-
 def weld_dual(lib, dev, dual, A, tri, st, src=None):
     """Merge the dual vertices faces use by exact position (isoext's sorted weld,
     src/utils.cu:32-59).  Both steps run before the one synchronisation that reads
