@@ -84,3 +84,68 @@ def test_library_has_no_unresolved_symbols_of_its_own():
     own = [ln.split()[-1] for ln in out.splitlines()
            if ln.strip() and "@" not in ln and not ln.split()[-1].startswith(("_ITM_", "__gmon_start__"))]
     assert not own, own
+
+
+def _prototypes():
+    """{name: [parameter declarations]} of the header's entry points."""
+    protos = {}
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        for m in re.finditer(r"\b(iso_\w+)\s*\(([^;{]*?)\)\s*;", src):
+            params = " ".join(m.group(2).split())
+            protos[m.group(1)] = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+    return protos
+
+
+def _kind_of_param(decl):
+    if "*" in decl or "[" in decl:
+        return "pointer"
+    words = decl.replace("const ", "").split()[:-1]  # drop the parameter's name
+    t = " ".join(words)
+    return {"float": "float", "double": "double", "int": "int", "unsigned": "uint", "unsigned int": "uint",
+            "long long": "longlong", "size_t": "size_t"}.get(t, t)
+
+
+def _kind_of_ctype(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, (ctypes._Pointer, ctypes.Array)):
+        return "pointer"
+    for kind, ct in (("float", ctypes.c_float), ("double", ctypes.c_double), ("int", ctypes.c_int),
+                     ("uint", ctypes.c_uint), ("longlong", ctypes.c_longlong), ("size_t", ctypes.c_size_t)):
+        if t is ct:
+            return kind
+    return t.__name__
+
+
+def test_bindings_match_the_header_prototypes():
+    """Every entry point the package binds with argtypes takes, in the header,
+    the same number of parameters of the same kinds (a mismatch would only show
+    as a wrong call on a GPU)."""
+    import importlib
+
+    import isoext_gb300
+    from isoext_gb300 import _ffi
+
+    for mod in ("mc", "dc", "sparse", "diff", "serve", "grids", "tune"):
+        try:
+            importlib.import_module(f"isoext_gb300.{mod}")
+        except ModuleNotFoundError:
+            pass
+    lib = _ffi.lib()
+    _ffi._apply(lib, _ffi._EXTRA)
+    protos = _prototypes()
+    checked, bad = 0, []
+    for name, params in sorted(protos.items()):
+        fn = getattr(lib, name, None)
+        if fn is None or fn.argtypes is None:
+            continue
+        checked += 1
+        want = [_kind_of_param(p) for p in params]
+        got = [_kind_of_ctype(t) for t in fn.argtypes]
+        if want != got:
+            bad.append((name, want, got))
+    assert checked >= 30, checked
+    assert not bad, bad
