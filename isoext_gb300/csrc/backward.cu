@@ -262,13 +262,13 @@ int iso_mc_backward(const float* values, int nx, int ny, int nz, const float* aa
                     float level, const long long* vertex_edges, long long V, const float* grad_vertices,
                     float* grad_values, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (V < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max) return ISO_ERR_ARG;
+    if (V < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max) return iso::fail_code(ISO_ERR_ARG);
     if (V == 0) return 0;
-    if (!values || !vertex_edges || !grad_vertices || !grad_values) return ISO_ERR_ARG;
+    if (!values || !vertex_edges || !grad_vertices || !grad_values) return iso::fail_code(ISO_ERR_ARG);
     const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     iso::ProfScope ps("mc_backward", st);
     mc_backward<<<blocks_for(V, 256), 256, 0, st>>>(values, g, level, vertex_edges, V, grad_vertices, grad_values);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_backward(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
@@ -276,15 +276,15 @@ int iso_dc_backward(const float* values, int nx, int ny, int nz, const float* aa
                     float svd_tol, const float* normals, const float* grad_dual, float* grad_values,
                     float* grad_normals, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (A < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max) return ISO_ERR_ARG;
+    if (A < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max) return iso::fail_code(ISO_ERR_ARG);
     if (A == 0) return 0;
-    if (!values || !cell_ids || !cell_offsets || !grad_dual || !grad_values) return ISO_ERR_ARG;
+    if (!values || !cell_ids || !cell_offsets || !grad_dual || !grad_values) return iso::fail_code(ISO_ERR_ARG);
     const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     iso::ProfScope ps("dc_backward", st);
     dc_backward<<<blocks_for(A, 128), 128, 0, st>>>(values, g, level, reinterpret_cast<const uint32_t*>(cell_ids),
                                                     reinterpret_cast<const uint32_t*>(cell_offsets), A, reg,
                                                     svd_tol, normals, grad_dual, grad_values, grad_normals);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_backward_src(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
@@ -292,11 +292,11 @@ int iso_dc_backward_src(const float* values, int nx, int ny, int nz, const float
                         float svd_tol, const int* vertex_source, long long V, const float* grad_vertices,
                         float* grad_dual_ws, float* grad_values, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (A < 0 || V < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max || !grad_values) return ISO_ERR_ARG;
-    if (cudaMemsetAsync(grad_values, 0, size_t(nx) * ny * nz * sizeof(float), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (A < 0 || V < 0 || nx < 2 || ny < 2 || nz < 2 || !aabb_min || !aabb_max || !grad_values) return iso::fail_code(ISO_ERR_ARG);
+    if (cudaMemsetAsync(grad_values, 0, size_t(nx) * ny * nz * sizeof(float), st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     if (A == 0 || V == 0) return 0;
-    if (!values || !cell_ids || !cell_offsets || !vertex_source || !grad_vertices || !grad_dual_ws) return ISO_ERR_ARG;
-    if (cudaMemsetAsync(grad_dual_ws, 0, size_t(A) * 3 * sizeof(float), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (!values || !cell_ids || !cell_offsets || !vertex_source || !grad_vertices || !grad_dual_ws) return iso::fail_code(ISO_ERR_ARG);
+    if (cudaMemsetAsync(grad_dual_ws, 0, size_t(A) * 3 * sizeof(float), st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     {
         iso::ProfScope ps("dc_backward", st);
         dc_scatter_src<<<blocks_for(V, 256), 256, 0, st>>>(vertex_source, V, grad_vertices, grad_dual_ws);

@@ -30,6 +30,19 @@ namespace iso {
 // Message iso_last_error returns on this thread (for entry points in other files).
 void set_last_error(const char* msg) { g_err = msg; }
 
+int fail_code(int code) {
+    switch (code) {
+        case ISO_ERR_ARG: g_err = "invalid argument"; break;
+        case ISO_ERR_CUDA: g_err = std::string("CUDA call failed: ") + cudaGetErrorString(cudaPeekAtLastError()); break;
+        case ISO_ERR_TIMEOUT: g_err = "a bounded wait ran out"; break;
+        case ISO_ERR_LOOKUP: g_err = "lookup failed"; break;
+        case ISO_ERR_WORKSPACE: g_err = "workspace too small"; break;
+        case ISO_ERR_OVERFLOW: g_err = "output capacity exceeded"; break;
+        default: g_err = "error " + std::to_string(code); break;
+    }
+    return code;
+}
+
 // Tunables: sign-pass CTAs per SM (MC and DC sign bitmaps), threads per block of
 // the per-active-cell DC kernels, threads per block of the MC count kernel.
 std::atomic<int> g_tune[TUNE_KEYS] = {{32}, {128}, {256}};

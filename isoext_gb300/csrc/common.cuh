@@ -201,4 +201,9 @@ int tune_get(int key);
 // true = the reference's CUDA build (fused), false = its host build.
 bool arith_fma();
 
+// An entry point's failure: sets the message iso_last_error returns on this
+// thread to the plain meaning of `code` (with CUDA's error text for
+// ISO_ERR_CUDA) and returns `code`.
+int fail_code(int code);
+
 }  // namespace iso

@@ -1345,8 +1345,8 @@ extern "C" {
 int iso_dc_classify(const float* values, int nx, int ny, int nz, float level, void* ws, size_t ws_bytes,
                     long long* counts, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
-    if (ws_bytes < iso_dc_workspace_size(nx, ny, nz)) return ISO_ERR_WORKSPACE;
+    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
+    if (ws_bytes < iso_dc_workspace_size(nx, ny, nz)) return iso::fail_code(ISO_ERR_WORKSPACE);
     DcWs w = carve(ws, nx, ny, nz);
     const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
     Grid3 g = make_grid(nx, ny, nz, amin, amax);
@@ -1357,7 +1357,7 @@ int iso_dc_classify(const float* values, int nx, int ny, int nz, float level, vo
     iso::ProfScope ps("dc_classify", st, 2);
     dc_cell_count<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.cwords, w.blkC);
     dc_block_scan<<<1, 1024, 0, st>>>(w.blkC, w.nblkC, counts);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* aabb_min,
@@ -1377,7 +1377,7 @@ int iso_dc_intersect(const float* values, int nx, int ny, int nz, const float* a
                     st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids),
                                                       reinterpret_cast<uint32_t*>(cell_offsets), A, points,
                                                       normals);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // Active cells, their crossing offsets and the dual vertices, without writing
@@ -1387,7 +1387,7 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
                            int* cell_ids, int* cell_offsets, float reg, float svd_tol, float* dual, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (nx < 2 || ny < 2 || nz < 2 || A <= 0) return 0;
-    if (!cell_ids || !cell_offsets || !dual) return ISO_ERR_ARG;
+    if (!cell_ids || !cell_offsets || !dual) return iso::fail_code(ISO_ERR_ARG);
     DcWs w = carve(ws, nx, ny, nz);
     Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     {
@@ -1400,7 +1400,7 @@ int iso_dc_intersect_solve(const float* values, int nx, int ny, int nz, const fl
     const int bt = iso::tune_get(iso::TUNE_DC_CELL_THREADS);
     solve_kernel(g)<<<blocks_for(A, bt), bt, 0, st>>>(values, g, level, reinterpret_cast<uint32_t*>(cell_ids), A, reg,
                                                     svd_tol, dual, nullptr, nullptr, nullptr);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_normals(const float* values, int nx, int ny, int nz, const float* aabb_min,
@@ -1414,7 +1414,7 @@ int iso_dc_normals(const float* values, int nx, int ny, int nz, const float* aab
                                                    reinterpret_cast<const uint32_t*>(cell_ids),
                                                    reinterpret_cast<const uint32_t*>(cell_offsets), A,
                                                    normals);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_solve(int nx, int ny, int nz, const float* aabb_min, const float* aabb_max, const float* points,
@@ -1428,7 +1428,7 @@ int iso_dc_solve(int nx, int ny, int nz, const float* aabb_min, const float* aab
     dc_solve<<<blocks_for(A, bt), bt, 0, st>>>(points, normals, reinterpret_cast<const uint32_t*>(cell_ids),
                                                  reinterpret_cast<const uint32_t*>(cell_offsets), A, g, reg,
                                                  svd_tol, dual);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // Active masks and prefixes only (when the intersection was made earlier).
@@ -1441,19 +1441,19 @@ int iso_dc_cells(const float* values, int nx, int ny, int nz, float level, void*
     iso::ProfScope ps("dc_intersect", st);
     dc_intersect<<<blocks_for(w.cwords, DC_BLOCK), DC_BLOCK, 0, st>>>(
         values, w.S, g, level, w.cwords, w.blkC, w.actm, w.offA, nullptr, nullptr, nullptr, nullptr, -1, 0, nullptr);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_quads_count(int nx, int ny, int nz, void* ws, long long* counts, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (nx < 2 || ny < 2 || nz < 2) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
     DcWs w = carve(ws, nx, ny, nz);
     const float amin[3] = {0, 0, 0}, amax[3] = {1, 1, 1};
     Grid3 g = make_grid(nx, ny, nz, amin, amax);
     iso::ProfScope ps("dc_quads", st, 2);
     dc_quad_count<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ);
     dc_block_scan<<<1, 1024, 0, st>>>(w.blkQ, w.nblkQ, counts);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_quads_emit(int nx, int ny, int nz, void* ws, const float* dual, int* tri, void* stream) {
@@ -1465,7 +1465,7 @@ int iso_dc_quads_emit(int nx, int ny, int nz, void* ws, const float* dual, int* 
     iso::ProfScope ps("dc_quads", st);
     dc_quad_emit<<<blocks_for(w.pwords, DC_BLOCK), DC_BLOCK, 0, st>>>(w.S, g, w.pwords, w.blkQ, w.actm,
                                                                      w.offA, dual, tri, nullptr);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 size_t iso_dc_weld_workspace_size(long long A) {
@@ -1479,7 +1479,7 @@ size_t iso_dc_weld_workspace_size(long long A) {
 int iso_dc_weld_count(const float* dual, long long A, const int* tri, long long ntri, void* ws,
                       size_t ws_bytes, long long* counts, int* status, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (ws_bytes < iso_dc_weld_workspace_size(A)) return ISO_ERR_WORKSPACE;
+    if (ws_bytes < iso_dc_weld_workspace_size(A)) return iso::fail_code(ISO_ERR_WORKSPACE);
     uint32_t cap = 1024;
     while ((long long)cap < 2 * A + 1024) cap <<= 1;
     uint8_t* b = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
@@ -1502,7 +1502,7 @@ int iso_dc_weld_count(const float* dual, long long A, const int* tri, long long 
     } else {
         cudaMemsetAsync(counts, 0, 16, st);
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // Weld step 2: write vertices [V, 3] and faces [ntri / 3, 3]; vertex_source
@@ -1525,7 +1525,7 @@ int iso_dc_weld_write_src(const float* dual, long long A, const int* tri, long l
         dc_rep_write<<<unsigned(nblk), DC_BLOCK, 0, st>>>(rep, A, blk, dual, newidx, vout,
                                                            reinterpret_cast<uint32_t*>(vertex_source), nullptr);
     if (ntri > 0) dc_remap<<<blocks_for(ntri, 256), 256, 0, st>>>(tri, ntri, rep, newidx, fout, nullptr);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_weld_write(const float* dual, long long A, const int* tri, long long ntri, void* ws,
@@ -1601,14 +1601,14 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
                     long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
                     int* cell_ids, int* cell_offsets, int* vertex_source, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (!counts || !status || !aabb_min || !aabb_max || vertex_capacity < 0 || face_capacity < 0) return ISO_ERR_ARG;
-    if ((long long)nx * ny * nz > 0x7fffffffll) return ISO_ERR_ARG;
+    if (!counts || !status || !aabb_min || !aabb_max || vertex_capacity < 0 || face_capacity < 0) return iso::fail_code(ISO_ERR_ARG);
+    if ((long long)nx * ny * nz > 0x7fffffffll) return iso::fail_code(ISO_ERR_ARG);
     if (nx < 2 || ny < 2 || nz < 2)
-        return cudaMemsetAsync(counts, 0, 5 * sizeof(long long), st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
-    if (!values || (vertex_capacity && !vertices) || (face_capacity && !faces)) return ISO_ERR_ARG;
+        return cudaMemsetAsync(counts, 0, 5 * sizeof(long long), st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
+    if (!values || (vertex_capacity && !vertices) || (face_capacity && !faces)) return iso::fail_code(ISO_ERR_ARG);
     const long long capA = vertex_capacity, capQ = face_capacity / 2;
     if (workspace_bytes < iso_dc_dense_workspace_size(nx, ny, nz, vertex_capacity, face_capacity))
-        return ISO_ERR_WORKSPACE;
+        return iso::fail_code(ISO_ERR_WORKSPACE);
     const DcDenseWs w = carve_dense(workspace, nx, ny, nz, capA);
     const Grid3 g = make_grid(nx, ny, nz, aabb_min, aabb_max);
     long long* eff = w.misc + 4;
@@ -1659,7 +1659,7 @@ int iso_dc_dense_ex(const float* values, int nx, int ny, int nz, const float* aa
                             static_cast<const long long*>(eff), faces);
         }
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_dc_dense(const float* values, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,

@@ -1093,7 +1093,7 @@ int launch_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStream_t 
     {
         iso::ProfScope ps("mc_emit", st);
         iso::launch_pdl(mc_emit<EMIT_THREADS>, unsigned(nbv + nbf), EMIT_THREADS, st, g, a);
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaGetLastError() != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     }
     return 0;
 }
@@ -1109,7 +1109,7 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
         iso::launch_pdl(ct == 128 ? mc_count<128> : mc_count<256>, unsigned(grid), unsigned(ct), st, g, p.amin[0],
                         p.amin[1], p.amin[2], p.asize[0], p.asize[1], p.asize[2], w.S, w.info, w.blk, w.vlist, w.clist,
                         w.foff, w.ctr, w.gc, uint32_t(nseg), p.capV, p.capF);
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaGetLastError() != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     }
     {
         iso::ProfScope ps("mc_scan", st);
@@ -1117,7 +1117,7 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
         const uint32_t nchunk = (nseg + SCAN_PER * SCAN_THREADS - 1) / (SCAN_PER * SCAN_THREADS);
         iso::launch_pdl(mc_scan, nchunk, SCAN_THREADS, st, w.blk, nseg, w.ctr, w.state, p.counts, p.status, p.capV,
                    p.capF);
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaGetLastError() != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     }
     const int block = mc_get_block();
     return block == 128 ? launch_emit<128>(p, g, w, st, sms) : launch_emit<256>(p, g, w, st, sms);
@@ -1126,7 +1126,7 @@ int launch_count_emit(const McParams& p, const McGrid& g, const McWs& w, cudaStr
 }  // namespace
 
 int mc_set_block(int threads) {
-    if (threads != 128 && threads != 256) return ISO_ERR_ARG;
+    if (threads != 128 && threads != 256) return iso::fail_code(ISO_ERR_ARG);
     std::lock_guard<std::mutex> lk(g_mu);
     g_block = threads;
     return 0;
@@ -1174,7 +1174,7 @@ size_t mc_workspace_bytes(int nx, int ny, int nz, long long capV, long long capF
 
 int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     const McWs w0 = carve(p.nx, p.ny, p.nz, p.capV, p.capF, nullptr);
-    if (ws_bytes < w0.total) return ISO_ERR_WORKSPACE;
+    if (ws_bytes < w0.total) return iso::fail_code(ISO_ERR_WORKSPACE);
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     const McWs w = carve(p.nx, p.ny, p.nz, p.capV, p.capF, base);
     McGrid g;
@@ -1189,11 +1189,11 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
     g.fma = iso::arith_fma();
     g.lgseg = iso::tune_get(iso::TUNE_MC_COUNT_THREADS) == 128 ? 9 : 10;
     g.gc = w.gc;
-    if (g.PW > 0xffffffffll) return ISO_ERR_ARG;
+    if (g.PW > 0xffffffffll) return iso::fail_code(ISO_ERR_ARG);
     {
         iso::ProfScope ps("mc_signs", st);
         mc_signs_launch(p.vals, p.nx, p.ny, p.nz, p.level, w.S, st, w.ctr, (long long)(zeroed_bytes(w.nBlk) / 8));
-        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaGetLastError() != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     }
     const int rc = launch_count_emit(p, g, w, st);
     if (rc) return rc;
@@ -1206,7 +1206,7 @@ int mc_launch(const McParams& p, void* ws, size_t ws_bytes, cudaStream_t st) {
 // ISO_ERR_TIMEOUT and the kernel returns.  spin_limit <= 2^20.
 extern "C" int iso_test_wait_timeout(unsigned spin_limit, unsigned long long* state, int* status,
                                      unsigned long long* out, void* stream) {
-    if (!state || !status || !out || spin_limit > (1u << 20)) return ISO_ERR_ARG;
+    if (!state || !status || !out || spin_limit > (1u << 20)) return iso::fail_code(ISO_ERR_ARG);
     lookback_probe<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>(state, 32u, spin_limit, status, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }

@@ -72,9 +72,9 @@ int iso_profile_read(const char* kernel, long long* launches, double* total_ms) 
     double t = 0;
     for (auto& r : g_recs) {
         if (kernel && std::strcmp(kernel, r.name) != 0) continue;
-        if (cudaEventSynchronize(r.b) != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaEventSynchronize(r.b) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
         float ms = 0;
-        if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
         ++n;
         t += ms;
     }
@@ -84,7 +84,7 @@ int iso_profile_read(const char* kernel, long long* launches, double* total_ms) 
 }
 
 int iso_profile_kernels(const char* kernel, long long* kernels) {
-    if (!kernels) return ISO_ERR_ARG;
+    if (!kernels) return iso::fail_code(ISO_ERR_ARG);
     std::lock_guard<std::mutex> lk(g_mu);
     long long n = 0;
     for (auto& r : g_recs)

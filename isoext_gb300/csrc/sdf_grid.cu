@@ -75,7 +75,7 @@ extern "C" {
 int iso_sdf_union_grid(const float* prims, int nx, int ny, int nz, const float* aabb_min, const float* aabb_max,
                        float* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (nx < 1 || ny < 1 || nz < 1 || !prims || !out || !aabb_min || !aabb_max) return ISO_ERR_ARG;
+    if (nx < 1 || ny < 1 || nz < 1 || !prims || !out || !aabb_min || !aabb_max) return iso::fail_code(ISO_ERR_ARG);
     const long long rows = (long long)nx * ny;  // a warp each, 8 per CTA
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
@@ -85,7 +85,7 @@ int iso_sdf_union_grid(const float* prims, int nx, int ny, int nz, const float* 
     sdf_union_grid<<<unsigned(grid), 256, 0, st>>>(prims, nx, ny, nz, aabb_min[0], aabb_min[1], aabb_min[2],
                                                    aabb_max[0] - aabb_min[0], aabb_max[1] - aabb_min[1],
                                                    aabb_max[2] - aabb_min[2], iso::arith_fma(), out);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 }  // extern "C"

@@ -150,7 +150,7 @@ struct Slot {
 // extraction.
 int queue_extraction(const Entry& e, int i, const float* prims_dev, cudaStream_t st) {
     const Part& p = e.part[i];
-    if (cudaMemsetAsync(p.small, 0, 64, st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cudaMemsetAsync(p.small, 0, 64, st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     int rc = iso_sdf_union_grid(prims_dev, e.n, e.n, e.n, LO, HI, p.values, st);
     if (rc) return rc;
     if (e.kind == 0)
@@ -164,9 +164,9 @@ int queue_extraction(const Entry& e, int i, const float* prims_dev, cudaStream_t
 // over the slot's helper streams, which a capture of `st` takes in).
 int queue_entry(const Entry& e, Slot& s, cudaStream_t st) {
     if (e.B == 1) return queue_extraction(e, 0, s.prims_dev, st);
-    if (cudaEventRecord(s.ev_fork, st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cudaEventRecord(s.ev_fork, st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     for (int i = 1; i < e.B; ++i)
-        if (cudaStreamWaitEvent(s.fork[i - 1], s.ev_fork, 0) != cudaSuccess) return ISO_ERR_CUDA;
+        if (cudaStreamWaitEvent(s.fork[i - 1], s.ev_fork, 0) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     for (int i = 0; i < e.B; ++i) {
         const int rc = queue_extraction(e, i, s.prims_dev + size_t(i) * PRIM_FLOATS, i ? s.fork[i - 1] : st);
         if (rc) return rc;
@@ -174,7 +174,7 @@ int queue_entry(const Entry& e, Slot& s, cudaStream_t st) {
     for (int i = 1; i < e.B; ++i)
         if (cudaEventRecord(s.ev_join[i - 1], s.fork[i - 1]) != cudaSuccess ||
             cudaStreamWaitEvent(st, s.ev_join[i - 1], 0) != cudaSuccess)
-            return ISO_ERR_CUDA;
+            return iso::fail_code(ISO_ERR_CUDA);
     return ISO_OK;
 }
 
@@ -296,7 +296,7 @@ int IsoServer::size_entry(Entry* e, Caps c) {
     e->bytes -= old_var;
     release((long long)old_var);
     const size_t var = entry_var_bytes(e->B, e->kind, e->n, c);
-    if (!acquire((long long)var)) return ISO_ERR_WORKSPACE;
+    if (!acquire((long long)var)) return iso::fail_code(ISO_ERR_WORKSPACE);
     e->bytes += var;
     e->cap = c;
     e->wsb = ws_bytes(e->kind, e->n, c);
@@ -305,19 +305,19 @@ int IsoServer::size_entry(Entry* e, Caps c) {
         p.vout = static_cast<float*>(alloc(size_t(12) * c.v, st));
         p.fout = static_cast<int*>(alloc(size_t(12) * c.f, st));
         p.ws = alloc(e->wsb, st);
-        if (!p.vout || !p.fout || !p.ws) return ISO_ERR_CUDA;
+        if (!p.vout || !p.fout || !p.ws) return iso::fail_code(ISO_ERR_CUDA);
     }
     // once outside a graph (first-use set-up of the kernels), then the capture
     for (int i = 0; i < e->B; ++i)
-        if (queue_extraction(*e, i, s.prims_dev + size_t(i) * PRIM_FLOATS, st) != 0) return ISO_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return ISO_ERR_CUDA;
+        if (queue_extraction(*e, i, s.prims_dev + size_t(i) * PRIM_FLOATS, st) != 0) return iso::fail_code(ISO_ERR_CUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     cudaGraph_t graph = nullptr;
-    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     const int rc = queue_entry(*e, s, st);
     const bool ended = cudaStreamEndCapture(st, &graph) == cudaSuccess;
     const bool ok = rc == 0 && ended && cudaGraphInstantiate(&e->exec, graph, 0) == cudaSuccess;
     if (graph) cudaGraphDestroy(graph);
-    return ok ? ISO_OK : ISO_ERR_CUDA;
+    return ok ? ISO_OK : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // A new entry of B requests for `slot`.  Warm entries (built before any
@@ -548,7 +548,7 @@ void IsoServer::worker(int index) {
 extern "C" {
 
 int iso_serve_create(int slots, long long budget_bytes, const int* warm_sizes, int num_warm_sizes, IsoServer** out) {
-    if (!out || slots < 1 || slots > 256 || budget_bytes <= 0 || num_warm_sizes < 0) return ISO_ERR_ARG;
+    if (!out || slots < 1 || slots > 256 || budget_bytes <= 0 || num_warm_sizes < 0) return iso::fail_code(ISO_ERR_ARG);
     *out = nullptr;
     auto* srv = new IsoServer;
     cudaGetDevice(&srv->device);
@@ -612,14 +612,14 @@ int iso_serve_create(int slots, long long budget_bytes, const int* warm_sizes, i
 }
 
 long long iso_serve_submit(IsoServer* srv, const IsoServeRequest* req) {
-    if (!srv || !req) return -ISO_ERR_ARG;
+    if (!srv || !req) return -iso::fail_code(ISO_ERR_ARG);
     if ((req->kind != 0 && req->kind != 1) || req->n < 2 || req->n > 1290 || req->num_prims < 1 ||
         req->num_prims > MAX_PRIMS || !req->prims || (req->kind == 0 && req->method != 0 && req->method != 1))
-        return -ISO_ERR_ARG;
+        return -iso::fail_code(ISO_ERR_ARG);
     // the count pass alone (values and the workspace at capacity 1) must fit
     // beside the slots' own buffers
     const long long fixed = (long long)srv->slots.size() * (long long)al(sizeof(float) * PRIM_FLOATS * BUCKET_MAX);
-    if ((long long)count_pass_bytes(req->kind, req->n) + fixed > srv->budget) return -ISO_ERR_WORKSPACE;
+    if ((long long)count_pass_bytes(req->kind, req->n) + fixed > srv->budget) return -iso::fail_code(ISO_ERR_WORKSPACE);
     auto* job = new Job;
     job->req = *req;
     std::memset(job->prims, 0, sizeof(job->prims));
@@ -632,7 +632,7 @@ long long iso_serve_submit(IsoServer* srv, const IsoServeRequest* req) {
         std::lock_guard<std::mutex> lk(srv->mu);
         if (srv->closing) {
             delete job;
-            return -ISO_ERR_ARG;
+            return -iso::fail_code(ISO_ERR_ARG);
         }
         ticket = job->ticket = srv->next_ticket++;
         srv->queue.push_back(job);  // a worker owns (and frees) the job from here
@@ -655,7 +655,7 @@ int iso_serve_wait(IsoServer* srv, long long ticket, double timeout_s, IsoServeR
     if (timeout_s < 0) {
         srv->cv_done.wait(lk, ready);
     } else if (!srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
-        return ISO_ERR_TIMEOUT;
+        return iso::fail_code(ISO_ERR_TIMEOUT);
     }
     auto it = srv->done.find(ticket);
     *out = it->second.r;
@@ -672,7 +672,7 @@ void iso_serve_free_result(IsoServeResult* r) {
 }
 
 int iso_serve_stats_ex(IsoServer* srv, long long* stats, int count) {
-    if (!srv || !stats || count < 0) return ISO_ERR_ARG;
+    if (!srv || !stats || count < 0) return iso::fail_code(ISO_ERR_ARG);
     std::lock_guard<std::mutex> lk(srv->mu);
     long long entries = 0;
     for (const Slot& s : srv->slots) entries += (long long)s.entries.size();
@@ -721,7 +721,7 @@ int iso_serve_destroy(IsoServer* srv) {
 
 // Requests per launch at most (1, 2, 4 or 8; 1: each request its own launch).
 int iso_serve_set_bucket(IsoServer* srv, int max_requests) {
-    if (!srv || max_requests < 1 || max_requests > BUCKET_MAX || (max_requests & (max_requests - 1))) return ISO_ERR_ARG;
+    if (!srv || max_requests < 1 || max_requests > BUCKET_MAX || (max_requests & (max_requests - 1))) return iso::fail_code(ISO_ERR_ARG);
     std::lock_guard<std::mutex> lk(srv->mu);
     srv->bucket_max = max_requests;
     return ISO_OK;
@@ -730,7 +730,7 @@ int iso_serve_set_bucket(IsoServer* srv, int max_requests) {
 // Scale of the capacities of entries built or grown after the call (tests of
 // the growth path; 1 = the counted sizes plus headroom).
 int iso_serve_set_capacity_scale(IsoServer* srv, double scale) {
-    if (!srv || !(scale > 0.0) || scale > 1.0) return ISO_ERR_ARG;
+    if (!srv || !(scale > 0.0) || scale > 1.0) return iso::fail_code(ISO_ERR_ARG);
     srv->cap_scale = scale;
     return ISO_OK;
 }

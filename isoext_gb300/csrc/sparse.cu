@@ -1113,13 +1113,13 @@ int iso_sparse_mc_count(const int* ids, const float* vals, long long n, int nx, 
                         const float* amin, const float* amax, float level, int method, void* blk,
                         long long* counts, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
-    if (method != 0 && method != 1) return ISO_ERR_ARG;
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
+    if (method != 0 && method != 1) return iso::fail_code(ISO_ERR_ARG);
     SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     iso::ProfScope ps("sparse_mc", st, 2);
     sp_mc_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_mc_emit(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
@@ -1130,19 +1130,19 @@ int iso_sparse_mc_emit(const int* ids, const float* vals, long long n, int nx, i
     SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     iso::ProfScope ps("sparse_mc", st);
     sp_mc_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, soup, nullptr);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_its_count(const float* vals, long long n, float level, void* blk, long long* counts,
                          void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
     SpGrid g{};
     g.level = level;
     iso::ProfScope ps("sparse_its", st, 2);
     sp_its_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, vals, n, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // Intersection arrays; act_sparse / act_uniform: sparse index / lattice id of
@@ -1159,7 +1159,7 @@ int iso_sparse_its_emit(const int* ids, const float* vals, long long n, int nx, 
     sp_its_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, (const unsigned long long*)blk, points,
                                                       normals, act_sparse, act_uniform, offsets,
                                                       reinterpret_cast<uint32_t*>(rank), A, K);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_normals(const int* ids, const float* vals, int nx, int ny, int nz, const float* amin,
@@ -1170,20 +1170,20 @@ int iso_sparse_normals(const int* ids, const float* vals, int nx, int ny, int nz
     SpGrid g = mk(nx, ny, nz, amin, amax, 0.0f, 0);
     iso::ProfScope ps("sparse_its", st);
     sp_normals<<<nb(A, 256), 256, 0, st>>>(g, ids, vals, act_sparse, offsets, A, points, normals);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_quads_count(const int* ids, const float* vals, long long n, int nx, int ny, int nz,
                            float level, const int* rank, void* blk, long long* counts, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (n <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
     const float z3[3] = {0, 0, 0}, o3[3] = {1, 1, 1};
     SpGrid g = mk(nx, ny, nz, z3, o3, level, 0);
     iso::ProfScope ps("sparse_quads", st, 2);
     sp_quad_count<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, reinterpret_cast<const uint32_t*>(rank),
                                                         (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(n, SP_BLOCK), counts, st);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_quads_emit(const int* ids, const float* vals, long long n, int nx, int ny, int nz, float level,
@@ -1195,7 +1195,7 @@ int iso_sparse_quads_emit(const int* ids, const float* vals, long long n, int nx
     iso::ProfScope ps("sparse_quads", st);
     sp_quad_emit<<<nb(n, SP_BLOCK), SP_BLOCK, 0, st>>>(g, ids, vals, n, reinterpret_cast<const uint32_t*>(rank),
                                                        (const unsigned long long*)blk, dual, tri);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_points(const int* ids, long long m, int nx, int ny, int nz, const float* amin,
@@ -1205,17 +1205,17 @@ int iso_sparse_points(const int* ids, long long m, int nx, int ny, int nz, const
     SpGrid g = mk(nx, ny, nz, amin, amax, 0.0f, 0);
     iso::ProfScope ps("sparse_populate", st);
     sp_points<<<nb(m * 8, 256), 256, 0, st>>>(g, ids, m, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_filter_count(const float* vals, long long m, float level, void* blk, long long* counts,
                             void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (m <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    if (m <= 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
     iso::ProfScope ps("sparse_populate", st, 2);
     sp_filter_count<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(vals, m, level, (unsigned long long*)blk);
     iso_block_scan_launch((unsigned long long*)blk, nb(m, SP_BLOCK), counts, st);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 int iso_sparse_filter_write(const int* ids, const float* vals, long long m, float level, const void* blk,
@@ -1224,7 +1224,7 @@ int iso_sparse_filter_write(const int* ids, const float* vals, long long m, floa
     if (m <= 0) return 0;
     iso::ProfScope ps("sparse_populate", st);
     sp_filter_write<<<nb(m, SP_BLOCK), SP_BLOCK, 0, st>>>(ids, vals, m, level, (const unsigned long long*)blk, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 // Sparse marching cubes in one call with no host synchronisation: the triangle
@@ -1241,11 +1241,11 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
                   long long face_capacity, void* workspace, size_t workspace_bytes, long long* counts, int* status,
                   void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (!counts || !status || !amin || !amax || n < 0 || vertex_capacity < 0 || face_capacity < 0) return ISO_ERR_ARG;
-    if (method != 0 && method != 1) return ISO_ERR_ARG;
-    if (n == 0) return cudaMemsetAsync(counts, 0, 24, st) == cudaSuccess ? 0 : ISO_ERR_CUDA;
-    if (!ids || !vals || (vertex_capacity && !vertices) || (face_capacity && !faces)) return ISO_ERR_ARG;
-    if (workspace_bytes < iso_sparse_mc_workspace_size(n, vertex_capacity, face_capacity)) return ISO_ERR_WORKSPACE;
+    if (!counts || !status || !amin || !amax || n < 0 || vertex_capacity < 0 || face_capacity < 0) return iso::fail_code(ISO_ERR_ARG);
+    if (method != 0 && method != 1) return iso::fail_code(ISO_ERR_ARG);
+    if (n == 0) return cudaMemsetAsync(counts, 0, 24, st) == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
+    if (!ids || !vals || (vertex_capacity && !vertices) || (face_capacity && !faces)) return iso::fail_code(ISO_ERR_ARG);
+    if (workspace_bytes < iso_sparse_mc_workspace_size(n, vertex_capacity, face_capacity)) return iso::fail_code(ISO_ERR_WORKSPACE);
     const SpMcWs w = sp_mc_carve(workspace, n, vertex_capacity, face_capacity);
     const SpGrid g = mk(nx, ny, nz, amin, amax, level, method);
     long long* eff = w.tot + 4;
@@ -1267,7 +1267,7 @@ int iso_sparse_mc(const int* ids, const float* vals, long long n, int nx, int ny
         iso::ProfScope ps("sparse_mc", st);
         sp_mc_finish<<<1, 1, 0, st>>>(w.tot + 8, vertex_capacity, counts, status);
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : iso::fail_code(ISO_ERR_CUDA);
 }
 
 }  // extern "C"

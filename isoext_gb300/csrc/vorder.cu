@@ -120,23 +120,23 @@ int iso_sort_vertices(float* vertices, long long num_vertices, int* faces, long 
                       size_t workspace_bytes, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const long long V = num_vertices, F = num_faces;
-    if (V < 0 || F < 0 || V > 0x7fffffffll || (V && !vertices) || (F && !faces)) return ISO_ERR_ARG;
+    if (V < 0 || F < 0 || V > 0x7fffffffll || (V && !vertices) || (F && !faces)) return iso::fail_code(ISO_ERR_ARG);
     if (V <= 1) return ISO_OK;
-    if (workspace_bytes < iso_sort_vertices_workspace_size(V) || !workspace) return ISO_ERR_WORKSPACE;
+    if (workspace_bytes < iso_sort_vertices_workspace_size(V) || !workspace) return iso::fail_code(ISO_ERR_WORKSPACE);
     VoWs w = vo_carve(workspace, V);
     iso::ProfScope ps("vertex_order", st, 7);
     vo_keys_z<<<blocks(V), 256, 0, st>>>(vertices, V, w.kz, w.i0);
     size_t tb = w.temp_bytes;
     if (cub::DeviceRadixSort::SortPairs(w.temp, tb, w.kz, w.kz2, w.i0, w.i1, int(V), 0, 32, st) != cudaSuccess)
-        return ISO_ERR_CUDA;
+        return iso::fail_code(ISO_ERR_CUDA);
     vo_keys_xy<<<blocks(V), 256, 0, st>>>(vertices, V, w.i1, w.kxy);
     tb = w.temp_bytes;
     if (cub::DeviceRadixSort::SortPairs(w.temp, tb, w.kxy, w.kxy2, w.i1, w.i0, int(V), 0, 64, st) != cudaSuccess)
-        return ISO_ERR_CUDA;
+        return iso::fail_code(ISO_ERR_CUDA);
     vo_gather<<<blocks(V), 256, 0, st>>>(vertices, V, w.i0, w.vtmp, w.newidx);
     vo_copy_back<<<blocks(3 * V), 256, 0, st>>>(w.vtmp, 3 * V, vertices);
     if (F) vo_remap<<<blocks(3 * F), 256, 0, st>>>(faces, 3 * F, w.newidx);
-    return cudaGetLastError() == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? ISO_OK : iso::fail_code(ISO_ERR_CUDA);
 }
 
 }  // extern "C"

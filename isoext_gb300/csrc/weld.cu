@@ -405,10 +405,10 @@ int iso_weld_mesh(const float* vertices, long long V, const int* faces, long lon
                   int* vsrc, long long* counts, int* status, void* workspace, size_t workspace_bytes,
                   void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (V < 0 || F < 0 || V > 0x7fffffffll || F > 0x7fffffffll || !counts || !status) return ISO_ERR_ARG;
-    if ((V && (!vertices || !vout)) || (F && (!faces || !fout))) return ISO_ERR_ARG;
-    if (workspace_bytes < iso_weld_mesh_workspace_size(V, F)) return ISO_ERR_WORKSPACE;
-    if (V == 0 || F == 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    if (V < 0 || F < 0 || V > 0x7fffffffll || F > 0x7fffffffll || !counts || !status) return iso::fail_code(ISO_ERR_ARG);
+    if ((V && (!vertices || !vout)) || (F && (!faces || !fout))) return iso::fail_code(ISO_ERR_ARG);
+    if (workspace_bytes < iso_weld_mesh_workspace_size(V, F)) return iso::fail_code(ISO_ERR_WORKSPACE);
+    if (V == 0 || F == 0) return cudaMemsetAsync(counts, 0, 16, st) == cudaSuccess ? ISO_OK : iso::fail_code(ISO_ERR_CUDA);
     const MeshWs w = mesh_carve(workspace, V, F);
     iso::ProfScope ps("weld_mesh", st, 4);
     cudaMemsetAsync(w.table, 0xff, size_t(w.hcap) * 4, st);
@@ -419,14 +419,14 @@ int iso_weld_mesh(const float* vertices, long long V, const int* faces, long lon
     mesh_faces<<<unsigned((F + WELD_THREADS - 1) / WELD_THREADS), WELD_THREADS, 0, st>>>(
         reinterpret_cast<const int32_t*>(faces), F, w.rep, w.f2, w.keep, w.used);
     size_t tb = w.temp_bytes;
-    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.used, w.vnum, int(V), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.used, w.vnum, int(V), st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     tb = w.temp_bytes;
-    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.keep, w.fnum, int(F), st) != cudaSuccess) return ISO_ERR_CUDA;
+    if (cub::DeviceScan::ExclusiveSum(w.temp, tb, w.keep, w.fnum, int(F), st) != cudaSuccess) return iso::fail_code(ISO_ERR_CUDA);
     const long long n = std::max(V, F);
     mesh_write<<<unsigned((n + WELD_THREADS - 1) / WELD_THREADS), WELD_THREADS, 0, st>>>(
         vertices, V, F, w.used, w.vnum, w.keep, w.fnum, w.f2, vout, reinterpret_cast<int32_t*>(fout),
         reinterpret_cast<int32_t*>(vsrc), counts);
-    return cudaGetLastError() == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? ISO_OK : iso::fail_code(ISO_ERR_CUDA);
 }
 
 }  // extern "C"

@@ -149,3 +149,42 @@ def test_bindings_match_the_header_prototypes():
             bad.append((name, want, got))
     assert checked >= 30, checked
     assert not bad, bad
+
+
+def test_failures_leave_a_message_of_their_own():
+    """After a failure, iso_last_error describes that failure, not an earlier one.
+    Each call here fails on its arguments or its workspace size, checked on the
+    host before any device work: the placeholder device pointers are never read."""
+    import importlib
+
+    from isoext_gb300 import _ffi
+
+    for mod in ("dc", "sparse"):
+        importlib.import_module(f"isoext_gb300.{mod}")
+    lib = _ffi.lib()
+    _ffi._apply(lib, _ffi._EXTRA)
+    lo, hi = (ctypes.c_float * 3)(-1, -1, -1), (ctypes.c_float * 3)(1, 1, 1)
+    P = 1 << 20  # a placeholder device address, 16-byte aligned, never dereferenced
+
+    def stale():
+        assert lib.iso_mc_set_config(100) == 1 and "threads" in _ffi.last_error()
+
+    stale()
+    rc = lib.iso_dc_dense_ex(P, 8, 8, 8, lo, hi, 0.0, 1e-2, 1e-6, P, 16, P, 16, P, 0, None, None, None, None, None,
+                             None)
+    assert rc == 1 and _ffi.last_error() == "invalid argument"  # counts and status are required
+    stale()
+    rc = lib.iso_dc_dense_ex(P, 8, 8, 8, lo, hi, 0.0, 1e-2, 1e-6, P, 16, P, 16, P, 0, P, P, None, None, None, None)
+    assert rc == 5 and _ffi.last_error() == "workspace too small"
+    stale()
+    rc = lib.iso_sparse_mc(P, P, 10, 8, 8, 8, lo, hi, 0.0, 7, P, 16, P, 16, P, 0, P, P, None)
+    assert rc == 1 and _ffi.last_error() == "invalid argument"  # method 7
+    stale()
+    rc = lib.iso_sparse_mc(P, P, 10, 8, 8, 8, lo, hi, 0.0, 0, P, 16, P, 16, P, 0, P, P, None)
+    assert rc == 5 and _ffi.last_error() == "workspace too small"
+    stale()
+    rc = lib.iso_weld_mesh(P, 10, P, 4, P, P, None, P, P, P, 0, None)
+    assert rc == 5 and _ffi.last_error() == "workspace too small"
+    stale()
+    rc = lib.iso_sort_vertices(P, -1, P, 4, P, 0, None)
+    assert rc == 1 and _ffi.last_error() == "invalid argument"
