@@ -188,3 +188,14 @@ def test_failures_leave_a_message_of_their_own():
     stale()
     rc = lib.iso_sort_vertices(P, -1, P, 4, P, 0, None)
     assert rc == 1 and _ffi.last_error() == "invalid argument"
+    import isoext_gb300.serve  # noqa: F401  (its bindings)
+
+    _ffi._apply(lib, _ffi._EXTRA)
+    out = ctypes.c_void_p()
+    stale()
+    assert lib.iso_serve_create(0, 1 << 30, None, 0, ctypes.byref(out)) == 1  # no slots
+    assert _ffi.last_error() == "invalid argument" and not out.value
+    stale()
+    assert lib.iso_serve_set_bucket(None, 2) == 1 and _ffi.last_error() == "invalid argument"
+    stale()
+    assert lib.iso_serve_set_capacity_scale(None, 0.5) == 1 and _ffi.last_error() == "invalid argument"
